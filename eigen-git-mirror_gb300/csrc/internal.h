@@ -1,0 +1,59 @@
+// Host-side drivers shared by the C ABI translation units (not part of the public ABI).
+#pragma once
+#include <string>
+
+#include "common.cuh"
+
+namespace gbllt {
+
+// Plain-path panel width: the diagonal block factored by one CTA and the depth of each
+// trailing update.
+constexpr int kNB = 64;
+
+// Stream-ordered factorisation of the lower triangle of the column-major n x n matrix at
+// d_a (device).  `st` is a device status word, initialised by the caller to fail_col = -1.
+template <typename T>
+int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t s);
+
+// Swap the strict lower and strict upper triangles of the n x n matrix at d_a in place
+// (A <- A^T).  Used to run the lower algorithm on an upper-stored factor, the same trick as
+// llt_inplace<Scalar,Upper> (Eigen/src/Cholesky/LLT.h:377-399).
+template <typename T>
+int transpose_inplace_dev(int64_t n, T* d_a, int64_t lda, cudaStream_t s);
+
+// Out-of-place transpose: dst (cols x rows, ldd) = src^T, src rows x cols column-major.
+template <typename T>
+int transpose_dev(int64_t rows, int64_t cols, const T* src, int64_t lds, T* dst, int64_t ldd,
+                  cudaStream_t s);
+
+// Writes the LAPACK info (0, or fail_col + 1) from the status word into *d_info (device).
+int finalize_info_dev(const DevStatus* st, int64_t* d_info, cudaStream_t s);
+
+// Stream-ordered solve L L^T X = B (upper == false; L lower column-major at d_a) or
+// U^T U X = B (upper == true; U upper column-major), B column-major n x nrhs, in place.
+template <typename T>
+int potrs_dev(bool upper, int64_t n, int64_t nrhs, const T* d_a, int64_t lda, T* d_b, int64_t ldb,
+              cudaStream_t s);
+
+// Brackets one kernel launch with profiling events when gbllt_profile_enable(1) is in effect.
+struct ProfScope {
+  int slot;
+  cudaStream_t stream;
+  ProfScope(const char* kind, cudaStream_t s, double flops, double bytes);
+  ~ProfScope();
+  ProfScope(const ProfScope&) = delete;
+  ProfScope& operator=(const ProfScope&) = delete;
+};
+
+template <typename T>
+constexpr const char* tname() {
+  return sizeof(T) == 8 ? "f64" : "f32";
+}
+
+// Validates (uplo, n, lda) the way dpotrf_ does (lapack/cholesky.cpp:17-19); returns 0 or -argpos.
+int check_uplo(char uplo);
+
+// Ensures the current device can run the sm_103a kernels; GBLLT_SUCCESS or GBLLT_ERR_NO_DEVICE.
+int ensure_device();
+
+}  // namespace gbllt

@@ -1,0 +1,261 @@
+// Plain-precision blocked Cholesky on the GPU (double for LLT<MatrixXd>, float for
+// LLT<MatrixXf>).
+//
+// The algorithm is the right-looking blocked factorisation of llt_inplace<Scalar,Lower>::blocked
+// (Eigen/src/Cholesky/LLT.h:338-368), mapped onto three kernels per panel of width kNB = 64:
+//
+//   potrf_diag_kernel   one CTA factors the 64 x 64 diagonal block A11 in shared memory
+//                       (the role of llt_inplace::unblocked, LLT.h:312-336; the pivot test is
+//                       the same `x <= 0`, LLT.h:329);
+//   trsm_panel_kernel   A21 <- A21 L11^{-T}: one thread per row of A21, the row held in
+//                       registers, L11 broadcast from shared memory (the OnTheRight solve that
+//                       LLT.h:364 issues, TriangularSolverMatrix.h:188-329);
+//   syrk_lower_kernel   A22 -= A21 A21^T on 64 x 64 tiles of the lower triangle only (the rank
+//                       update of LLT.h:365 -> GeneralMatrixMatrixTriangular.h:57-194), each
+//                       thread accumulating a 4 x 4 register block over the panel depth.
+//
+// On GB300 the FP64 pipe (DFMA and DMMA alike) delivers about 1 TFLOP/s for the whole chip,
+// i.e. under two FP64 FMAs per clock per SM, so every FP64 kernel here is bound by that pipe
+// and not by memory: a 64 x 64 x 64 tile update needs 64 KB of operands for 262144 FMAs.
+#include "internal.h"
+
+namespace gbllt {
+
+namespace {
+
+constexpr int NB = kNB;
+
+template <typename T>
+__global__ void __launch_bounds__(256) potrf_diag_kernel(T* __restrict__ a, long long lda, int k0, int bs,
+                                                         DevStatus* __restrict__ st) {
+  if (st->fail_col >= 0) return;  // an earlier panel already failed: nothing more to do
+  __shared__ T s[NB][NB + 1];    // s[j][i] = A11(i, j), lower part only
+  __shared__ int fail;
+  const int tid = threadIdx.x;
+  T* blk = a + (long long)k0 * lda + k0;
+  for (int idx = tid; idx < NB * NB; idx += 256) {
+    const int j = idx / NB, i = idx % NB;
+    if (i < bs && j < bs && i >= j) s[j][i] = blk[(long long)j * lda + i];
+  }
+  if (tid == 0) fail = -1;
+  __syncthreads();
+  const int tx = tid & 63, ty = tid >> 6;
+  int j = 0;
+  for (; j < bs; ++j) {
+    if (tid == 0) {
+      const T d = s[j][j];
+      if (d <= T(0)) fail = j;
+      else s[j][j] = sqrt(d);
+    }
+    __syncthreads();
+    if (fail >= 0) break;  // block-uniform
+    const T djj = s[j][j];
+    if (tid > j && tid < bs) s[j][tid] = s[j][tid] / djj;
+    __syncthreads();
+    for (int l = j + 1 + ty; l < bs; l += 4) {
+      const T ljl = s[j][l];
+      if (tx >= l && tx < bs) s[l][tx] = fma(-s[j][tx], ljl, s[l][tx]);
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < NB * NB; idx += 256) {
+    const int jj = idx / NB, i = idx % NB;
+    if (i < bs && jj < bs && i >= jj) blk[(long long)jj * lda + i] = s[jj][i];
+  }
+  if (tid == 0 && fail >= 0) st->fail_col = (long long)k0 + fail;
+}
+
+// A21 (rs x bs, rows k0+bs.., columns k0..) <- A21 * L11^{-T}.  One thread per row.
+template <typename T>
+__global__ void __launch_bounds__(128) trsm_panel_kernel(T* __restrict__ a, long long lda, int k0, int bs,
+                                                         long long rs, const DevStatus* __restrict__ st) {
+  if (st->fail_col >= 0) return;
+  __shared__ T L[NB][NB + 1];  // L[j][p] = L11(j, p); identity outside the bs x bs block
+  const T* l11 = a + (long long)k0 * lda + k0;
+  for (int idx = threadIdx.x; idx < NB * NB; idx += 128) {
+    const int j = idx % NB, p = idx / NB;
+    T v = (j == p) ? T(1) : T(0);
+    if (j < bs && p < bs && j >= p) v = l11[(long long)p * lda + j];
+    L[j][p] = v;
+  }
+  __syncthreads();
+  const long long r = (long long)blockIdx.x * 128 + threadIdx.x;
+  if (r >= rs) return;
+  T* row = a + (long long)k0 * lda + (k0 + bs) + r;  // element (r, p) at row[p * lda]
+  T x[NB];
+#pragma unroll
+  for (int p = 0; p < NB; ++p) x[p] = p < bs ? row[(long long)p * lda] : T(0);
+#pragma unroll
+  for (int jj = 0; jj < NB; ++jj) {
+    T v = x[jj];
+#pragma unroll
+    for (int p = 0; p < jj; ++p) v = fma(-x[p], L[jj][p], v);
+    x[jj] = v / L[jj][jj];
+  }
+#pragma unroll
+  for (int p = 0; p < NB; ++p)
+    if (p < bs) row[(long long)p * lda] = x[p];
+}
+
+// A22 (rs x rs lower) -= A21 A21^T, A21 = rs x bs.  One CTA per 64 x 64 lower tile.
+template <typename T>
+__global__ void __launch_bounds__(256) syrk_lower_kernel(T* __restrict__ a, long long lda, int k0, int bs,
+                                                         long long rs, const DevStatus* __restrict__ st) {
+  if (st->fail_col >= 0) return;
+  constexpr int KC = 32;
+  __shared__ T As[KC][64 + 1];
+  __shared__ T Bs[KC][64 + 1];
+  int ti, tj;
+  lower_tile_coords(blockIdx.x, ti, tj);
+  const long long i0 = (long long)ti * 64, j0 = (long long)tj * 64;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const T* A = a + (long long)k0 * lda + (k0 + bs);  // A21(0, 0)
+  T acc[4][4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[m][q] = T(0);
+  for (int p0 = 0; p0 < bs; p0 += KC) {
+    for (int idx = tid; idx < 64 * KC; idx += 256) {
+      const int i = idx & 63, p = idx >> 6;
+      T va = T(0), vb = T(0);
+      if (p0 + p < bs) {
+        if (i0 + i < rs) va = A[(long long)(p0 + p) * lda + i0 + i];
+        if (j0 + i < rs) vb = A[(long long)(p0 + p) * lda + j0 + i];
+      }
+      As[p][i] = va;
+      Bs[p][i] = vb;
+    }
+    __syncthreads();
+    const int pe = bs - p0 < KC ? bs - p0 : KC;
+    for (int p = 0; p < pe; ++p) {
+      T av[4], bv[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) av[m] = As[p][tx + 16 * m];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) bv[q] = Bs[p][ty + 16 * q];
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[m][q] = fma(av[m], bv[q], acc[m][q]);
+    }
+    __syncthreads();
+  }
+  T* C = a + (long long)(k0 + bs) * lda + (k0 + bs);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const long long j = j0 + ty + 16 * q;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const long long i = i0 + tx + 16 * m;
+      if (i < rs && j < rs && i >= j) C[j * lda + i] -= acc[m][q];
+    }
+  }
+}
+
+// Swap strict triangles: one CTA per pair of 32 x 32 tiles (ti, tj), (tj, ti) with ti >= tj.
+template <typename T>
+__global__ void __launch_bounds__(256) transpose_inplace_kernel(T* __restrict__ a, long long lda, long long n) {
+  __shared__ T t1[32][33];
+  __shared__ T t2[32][33];
+  int ti, tj;
+  lower_tile_coords(blockIdx.x, ti, tj);
+  const long long r1 = (long long)ti * 32, c1 = (long long)tj * 32;  // tile (ti, tj)
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int c = ty; c < 32; c += 8) {
+    const long long i = r1 + tx, j = c1 + c;  // element of tile (ti,tj)
+    if (i < n && j < n) t1[c][tx] = a[j * lda + i];
+    const long long i2 = c1 + tx, j2 = r1 + c;  // element of tile (tj,ti)
+    if (i2 < n && j2 < n) t2[c][tx] = a[j2 * lda + i2];
+  }
+  __syncthreads();
+  // tile (ti,tj)(x, c) <- tile(tj,ti)(c, x) ; tile (tj,ti)(x, c) <- tile(ti,tj)(c, x)
+  for (int c = ty; c < 32; c += 8) {
+    const long long i = r1 + tx, j = c1 + c;
+    if (i < n && j < n && i != j) a[j * lda + i] = t2[tx][c];
+    const long long i2 = c1 + tx, j2 = r1 + c;
+    if (i2 < n && j2 < n && i2 != j2) a[j2 * lda + i2] = t1[tx][c];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) transpose_kernel(long long rows, long long cols, const T* __restrict__ src,
+                                                        long long lds, T* __restrict__ dst, long long ldd) {
+  __shared__ T t[32][33];
+  const long long r0 = (long long)blockIdx.x * 32, c0 = (long long)blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int c = ty; c < 32; c += 8)
+    if (r0 + tx < rows && c0 + c < cols) t[c][tx] = src[(c0 + c) * lds + r0 + tx];
+  __syncthreads();
+  // dst(c, r) = src(r, c): dst column r0 + c, row c0 + tx
+  for (int c = ty; c < 32; c += 8)
+    if (r0 + c < rows && c0 + tx < cols) dst[(r0 + c) * ldd + c0 + tx] = t[tx][c];
+}
+
+__global__ void finalize_info_kernel(const DevStatus* __restrict__ st, int64_t* __restrict__ info) {
+  info[0] = st->fail_col >= 0 ? (int64_t)(st->fail_col + 1) : 0;
+}
+
+}  // namespace
+
+template <typename T>
+int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t s) {
+  static const std::string kd = std::string("potrf_diag_") + tname<T>();
+  static const std::string kt = std::string("trsm_panel_") + tname<T>();
+  static const std::string ks = std::string("syrk_lower_") + tname<T>();
+  const double es = sizeof(T);
+  for (int64_t k0 = 0; k0 < n; k0 += NB) {
+    const int bs = (int)(n - k0 < NB ? n - k0 : NB);
+    const int64_t rs = n - k0 - bs;
+    {
+      ProfScope ps(kd.c_str(), s, (double)bs * bs * bs / 3.0, (double)bs * (bs + 1) * es);
+      potrf_diag_kernel<T><<<1, 256, 0, s>>>(d_a, lda, (int)k0, bs, st);
+    }
+    if (rs > 0) {
+      {
+        ProfScope ps(kt.c_str(), s, (double)rs * bs * bs, (2.0 * rs * bs + 0.5 * bs * bs) * es);
+        trsm_panel_kernel<T><<<(unsigned)ceil_div(rs, 128), 128, 0, s>>>(d_a, lda, (int)k0, bs, rs, st);
+      }
+      const int64_t nt = ceil_div(rs, 64);
+      // algorithmic work: rs(rs+1)/2 lower entries, each a dot of depth bs (2 bs flops),
+      // reading A21 once and reading + writing the lower triangle of A22 once
+      ProfScope ps(ks.c_str(), s, (double)rs * (rs + 1) * bs, ((double)rs * bs + (double)rs * (rs + 1)) * es);
+      syrk_lower_kernel<T><<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(d_a, lda, (int)k0, bs, rs, st);
+    }
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+template <typename T>
+int transpose_inplace_dev(int64_t n, T* d_a, int64_t lda, cudaStream_t s) {
+  if (n <= 1) return GBLLT_SUCCESS;
+  const int64_t nt = ceil_div(n, 32);
+  transpose_inplace_kernel<T><<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(d_a, lda, n);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+template <typename T>
+int transpose_dev(int64_t rows, int64_t cols, const T* src, int64_t lds, T* dst, int64_t ldd, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return GBLLT_SUCCESS;
+  dim3 grid((unsigned)ceil_div(rows, 32), (unsigned)ceil_div(cols, 32));
+  transpose_kernel<T><<<grid, 256, 0, s>>>(rows, cols, src, lds, dst, ldd);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+int finalize_info_dev(const DevStatus* st, int64_t* d_info, cudaStream_t s) {
+  finalize_info_kernel<<<1, 1, 0, s>>>(st, d_info);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+template int potrf_lower_dev<double>(int64_t, double*, int64_t, DevStatus*, cudaStream_t);
+template int potrf_lower_dev<float>(int64_t, float*, int64_t, DevStatus*, cudaStream_t);
+template int transpose_inplace_dev<double>(int64_t, double*, int64_t, cudaStream_t);
+template int transpose_inplace_dev<float>(int64_t, float*, int64_t, cudaStream_t);
+template int transpose_dev<double>(int64_t, int64_t, const double*, int64_t, double*, int64_t, cudaStream_t);
+template int transpose_dev<float>(int64_t, int64_t, const float*, int64_t, float*, int64_t, cudaStream_t);
+
+}  // namespace gbllt

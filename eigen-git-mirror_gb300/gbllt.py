@@ -1,0 +1,172 @@
+"""ctypes binding of libgbllt.so, the C ABI declared in include/gbllt.h.
+
+This is plumbing for Python callers (the test suite and the benchmark): every call goes
+straight to the sm_103a kernels behind the C ABI.  There is no fallback; if the library is not
+built, `lib()` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "lib" / "libgbllt.so"
+HEADER = PKG_DIR.parent / "include" / "gbllt.h"
+
+SUCCESS = 0
+ERR_CUDA = -1001
+ERR_ALLOC = -1002
+ERR_TIMEOUT = -1003
+ERR_NO_DEVICE = -1004
+ERR_INTERNAL = -1005
+ERR_NOT_CONVERGED = -1006
+ROW_MAJOR = 101
+COL_MAJOR = 102
+
+_i64 = ctypes.c_int64
+_int = ctypes.c_int
+_ch = ctypes.c_char
+_vp = ctypes.c_void_p
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+# argtypes of every entry point; the test suite checks this table against include/gbllt.h
+SIGNATURES: dict[str, tuple] = {
+    "gbllt_version": (_int, []),
+    "gbllt_last_error": (ctypes.c_char_p, []),
+    "gbllt_dpotrf": (_int, [_int, _ch, _i64, _vp, _i64, _i64p]),
+    "gbllt_spotrf": (_int, [_int, _ch, _i64, _vp, _i64, _i64p]),
+    "gbllt_dpotrs": (_int, [_int, _ch, _i64, _i64, _vp, _i64, _vp, _i64]),
+    "gbllt_spotrs": (_int, [_int, _ch, _i64, _i64, _vp, _i64, _vp, _i64]),
+    "gbllt_dposv": (_int, [_int, _ch, _i64, _i64, _vp, _i64, _vp, _i64, _i64p]),
+    "gbllt_sposv": (_int, [_int, _ch, _i64, _i64, _vp, _i64, _vp, _i64, _i64p]),
+    "gbllt_dpotrf_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
+    "gbllt_spotrf_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
+    "gbllt_dpotrs_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp]),
+    "gbllt_spotrs_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp]),
+    "gbllt_profile_enable": (_int, [_int]),
+    "gbllt_profile_read": (_int, [_vp, _int, ctypes.POINTER(_int)]),
+}
+
+_lib = None
+
+
+class KernelStat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 40), ("launches", ctypes.c_int64), ("ms", ctypes.c_double),
+                ("flops", ctypes.c_double), ("bytes", ctypes.c_double)]
+
+
+class GblltError(RuntimeError):
+    def __init__(self, fn: str, rc: int):
+        msg = ""
+        if _lib is not None:
+            try:
+                msg = _lib.gbllt_last_error().decode()
+            except Exception:  # pragma: no cover
+                pass
+        super().__init__(f"{fn} returned {rc} {msg}".strip())
+        self.rc = rc
+
+
+def lib() -> ctypes.CDLL:
+    """Load libgbllt.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = ctypes.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def header_functions() -> list[str]:
+    """Names of all functions declared in include/gbllt.h."""
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbllt_\w+)\s*\(", text)))
+
+
+def check(fn: str, rc: int) -> None:
+    if rc != SUCCESS:
+        raise GblltError(fn, rc)
+
+
+def _ptr(a) -> int:
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return int(a.data_ptr())  # torch tensor
+
+
+def _uplo(u: str) -> bytes:
+    return u.encode()[:1]
+
+
+# ---- host-pointer API (numpy, Fortran order) -------------------------------------------------
+
+def potrf(a: np.ndarray, uplo: str = "L") -> int:
+    """Factor a (n x n, float64/float32, Fortran order) in place; returns LAPACK info."""
+    assert a.flags.f_contiguous and a.ndim == 2 and a.shape[0] == a.shape[1]
+    info = _i64(0)
+    fn = "gbllt_dpotrf" if a.dtype == np.float64 else "gbllt_spotrf"
+    check(fn, getattr(lib(), fn)(COL_MAJOR, _uplo(uplo), a.shape[0], _ptr(a), max(1, a.shape[0]), ctypes.byref(info)))
+    return int(info.value)
+
+
+def potrs(a: np.ndarray, b: np.ndarray, uplo: str = "L") -> None:
+    """Solve in place in b (n x k or n, Fortran order) from the factor in a."""
+    n = a.shape[0]
+    k = 1 if b.ndim == 1 else b.shape[1]
+    fn = "gbllt_dpotrs" if a.dtype == np.float64 else "gbllt_spotrs"
+    check(fn, getattr(lib(), fn)(COL_MAJOR, _uplo(uplo), n, k, _ptr(a), max(1, n), _ptr(b), max(1, n)))
+
+
+def posv(a: np.ndarray, b: np.ndarray, uplo: str = "L") -> int:
+    n = a.shape[0]
+    k = 1 if b.ndim == 1 else b.shape[1]
+    info = _i64(0)
+    fn = "gbllt_dposv" if a.dtype == np.float64 else "gbllt_sposv"
+    check(fn, getattr(lib(), fn)(COL_MAJOR, _uplo(uplo), n, k, _ptr(a), max(1, n), _ptr(b), max(1, n),
+                                 ctypes.byref(info)))
+    return int(info.value)
+
+
+# ---- device-pointer API (torch tensors on cuda, column-major = transposed row-major storage) ----
+
+def potrf_dev(a_cm, n: int, lda: int, info_dev, uplo: str = "L", stream: int = 0) -> None:
+    import torch
+    fn = "gbllt_dpotrf_dev" if a_cm.dtype == torch.float64 else "gbllt_spotrf_dev"
+    check(fn, getattr(lib(), fn)(_uplo(uplo), n, _ptr(a_cm), lda, _ptr(info_dev), stream))
+
+
+def potrs_dev(a_cm, n: int, lda: int, b_cm, nrhs: int, ldb: int, uplo: str = "L", stream: int = 0) -> None:
+    import torch
+    fn = "gbllt_dpotrs_dev" if a_cm.dtype == torch.float64 else "gbllt_spotrs_dev"
+    check(fn, getattr(lib(), fn)(_uplo(uplo), n, nrhs, _ptr(a_cm), lda, _ptr(b_cm), ldb, stream))
+
+
+# ---- diagnostics -------------------------------------------------------------------------------
+
+def profile_enable(on: bool = True) -> None:
+    check("gbllt_profile_enable", lib().gbllt_profile_enable(1 if on else 0))
+
+
+def profile_read() -> dict[str, dict]:
+    """Per-kernel-class launches, device ms and algorithmic flops / bytes since profile_enable."""
+    cap = 64
+    arr = (KernelStat * cap)()
+    cnt = _int(0)
+    check("gbllt_profile_read", lib().gbllt_profile_read(ctypes.cast(arr, _vp), cap, ctypes.byref(cnt)))
+    out = {}
+    for i in range(min(cnt.value, cap)):
+        s = arr[i]
+        out[s.name.decode()] = dict(launches=int(s.launches), ms=float(s.ms), flops=float(s.flops),
+                                    bytes=float(s.bytes))
+    return out

@@ -1,0 +1,118 @@
+/* gbllt.h -- C ABI of the GB300 (sm_103a) dense Cholesky (LLT) backend.
+ *
+ * This is the drop-in boundary for Eigen's dense Cholesky path.  Each entry point names the
+ * reference interface it replaces (paths are inside the Eigen source tree):
+ *   - the LAPACKE entry Eigen binds for its LAPACKE backend, LAPACKE_?potrf
+ *     (Eigen/src/misc/lapacke.h:2821-2827), called by lapacke_llt<T>::potrf
+ *     (Eigen/src/Cholesky/LLT_LAPACKE.h:47-61), which is the body of the explicit
+ *     specialisation llt_inplace<T,Lower|Upper>::blocked (LLT_LAPACKE.h:64-92);
+ *   - the Fortran-ABI routines Eigen itself exports, ?potrf_ / ?potrs_
+ *     (lapack/cholesky.cpp:14-36 and :41-72);
+ *   - the two triangular sweeps of LLT::_solve_impl_transposed (Eigen/src/Cholesky/LLT.h:490-498).
+ *
+ * Conventions (shared by every entry point)
+ *   - Plain pointers and sizes only; no CUDA or C++ types cross this boundary.  A `stream`
+ *     argument is a cudaStream_t passed as void* (NULL = the legacy default stream).
+ *   - Host-pointer entry points are synchronous, like LAPACKE: they copy the inputs to the GPU,
+ *     compute there, copy the results back and return.  `_dev` entry points take device
+ *     pointers, are ordered on `stream` and return before the GPU work completes.
+ *   - Storage: GBLLT_COL_MAJOR or GBLLT_ROW_MAJOR (the LAPACKE values), leading dimension
+ *     `lda`.  Only the `uplo` triangle is read or written; the other strict triangle is left
+ *     untouched (LLT.h keeps the strict upper part of m_matrix as it was).
+ *   - Return value: GBLLT_SUCCESS, or -i when argument i (1-based) is illegal (the LAPACK
+ *     convention, lapack/cholesky.cpp:17-24), or one of the GBLLT_ERR_* codes below.
+ *   - `info` follows LAPACK: 0 on success, k > 0 when the leading minor of order k is not
+ *     positive definite (the factorisation stopped at 0-based column k-1).  Eigen's
+ *     llt_inplace::blocked returns k-1 for it and -1 for success (LLT_LAPACKE.h:60).
+ *   - There is no CPU fallback: without a usable GPU every entry point returns
+ *     GBLLT_ERR_NO_DEVICE.
+ *   - Thread safety: entry points may be called from several host threads; each host thread
+ *     uses its own library stream per device for the synchronous calls.
+ */
+#ifndef GBLLT_H
+#define GBLLT_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define GBLLT_API __attribute__((visibility("default")))
+#else
+#define GBLLT_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBLLT_SUCCESS 0
+#define GBLLT_ERR_CUDA (-1001)        /* a CUDA runtime call failed (see gbllt_last_error) */
+#define GBLLT_ERR_ALLOC (-1002)       /* device or pinned memory could not be allocated */
+#define GBLLT_ERR_TIMEOUT (-1003)     /* a bounded device-side wait ran out */
+#define GBLLT_ERR_NO_DEVICE (-1004)   /* no CUDA device, or the device is not sm_103 */
+#define GBLLT_ERR_INTERNAL (-1005)
+#define GBLLT_ERR_NOT_CONVERGED (-1006) /* iterative refinement did not reach the tolerance */
+
+#define GBLLT_ROW_MAJOR 101
+#define GBLLT_COL_MAJOR 102
+
+/* Library version (major*10000 + minor*100 + patch). */
+GBLLT_API int gbllt_version(void);
+
+/* Message of the last GBLLT_ERR_CUDA seen by the calling thread ("" if none). */
+GBLLT_API const char* gbllt_last_error(void);
+
+/* Factor A = L L^T ('L') or A = U^T U ('U') in place.
+ * Replaces LAPACKE_dpotrf(matrix_layout, uplo, n, a, lda) as used by
+ * Eigen/src/Cholesky/LLT_LAPACKE.h:59 and dpotrf_ (lapack/cholesky.cpp:14-36). */
+GBLLT_API int gbllt_dpotrf(int layout, char uplo, int64_t n, double* a, int64_t lda, int64_t* info);
+/* Single-precision twin: LAPACKE_spotrf / spotrf_ (LLT<MatrixXf>). */
+GBLLT_API int gbllt_spotrf(int layout, char uplo, int64_t n, float* a, int64_t lda, int64_t* info);
+
+/* Solve A X = B in place in B from a factor produced by ?potrf.
+ * Replaces dpotrs_ (lapack/cholesky.cpp:41-72) and the two solveInPlace sweeps of
+ * LLT::_solve_impl_transposed (Eigen/src/Cholesky/LLT.h:490-498). */
+GBLLT_API int gbllt_dpotrs(int layout, char uplo, int64_t n, int64_t nrhs, const double* a, int64_t lda,
+                 double* b, int64_t ldb);
+GBLLT_API int gbllt_spotrs(int layout, char uplo, int64_t n, int64_t nrhs, const float* a, int64_t lda,
+                 float* b, int64_t ldb);
+
+/* Factor and solve in one call (LAPACK ?posv semantics): A is overwritten by its factor and
+ * B by X.  Equivalent to LLT::compute followed by LLT::solveInPlace (LLT.h:430-460, :514-522)
+ * with a single upload of A. */
+GBLLT_API int gbllt_dposv(int layout, char uplo, int64_t n, int64_t nrhs, double* a, int64_t lda, double* b,
+                int64_t ldb, int64_t* info);
+GBLLT_API int gbllt_sposv(int layout, char uplo, int64_t n, int64_t nrhs, float* a, int64_t lda, float* b,
+                int64_t ldb, int64_t* info);
+
+/* Device-pointer, stream-ordered variants (column-major).  d_info points to one int64_t in
+ * device memory that receives the LAPACK info; it is written before the call's work on `stream`
+ * completes. */
+GBLLT_API int gbllt_dpotrf_dev(char uplo, int64_t n, double* d_a, int64_t lda, int64_t* d_info, void* stream);
+GBLLT_API int gbllt_spotrf_dev(char uplo, int64_t n, float* d_a, int64_t lda, int64_t* d_info, void* stream);
+GBLLT_API int gbllt_dpotrs_dev(char uplo, int64_t n, int64_t nrhs, const double* d_a, int64_t lda, double* d_b,
+                     int64_t ldb, void* stream);
+GBLLT_API int gbllt_spotrs_dev(char uplo, int64_t n, int64_t nrhs, const float* d_a, int64_t lda, float* d_b,
+                     int64_t ldb, void* stream);
+
+/* ---- Diagnostics (no counterpart in the reference; Eigen has no built-in timers) ----------- */
+
+/* Per-kernel-class totals: launches, device time (CUDA events on the launch stream) and the
+ * algorithmic work of those launches (flops and bytes implied by the launch shapes). */
+typedef struct {
+  char name[40];
+  int64_t launches;
+  double ms;
+  double flops;
+  double bytes;
+} gbllt_kernel_stat;
+
+/* Turn per-launch event timing on (1) or off (0); either call discards earlier records. */
+GBLLT_API int gbllt_profile_enable(int on);
+/* Wait for the recorded launches and return up to max_entries classes; *n_entries = classes seen. */
+GBLLT_API int gbllt_profile_read(gbllt_kernel_stat* out, int max_entries, int* n_entries);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBLLT_H */

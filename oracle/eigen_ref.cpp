@@ -1,0 +1,62 @@
+// C shim over Eigen's own dense Cholesky, compiled against the reference headers in place
+// (oracle/Makefile, target `ref`).  TEST INFRASTRUCTURE ONLY: it produces the golden vectors
+// that pin the oracle and lets the oracle be timed against Eigen on the same machine.
+//
+// Every function goes through Eigen's public LLT API (Eigen/src/Cholesky/LLT.h):
+// LLT<Matrix,UpLo>::compute (:430-460), matrixLLT, info (:191-195) and solve (:483-498).
+#include <Eigen/Cholesky>
+#include <Eigen/Dense>
+#include <chrono>
+#include <cstdint>
+
+using namespace Eigen;
+
+template <typename T, int UpLo>
+static int64_t factor_solve(int64_t n, int64_t nrhs, T* a, int64_t lda, T* b, int64_t ldb, double* seconds) {
+  typedef Matrix<T, Dynamic, Dynamic> M;
+  Map<M, 0, OuterStride<>> A(a, n, n, OuterStride<>(lda));
+  auto t0 = std::chrono::steady_clock::now();
+  LLT<M, UpLo> llt(A);                       // copies A, L1 norm, blocked factorisation
+  auto t1 = std::chrono::steady_clock::now();
+  int64_t info = llt.info() == Success ? 0 : 1;
+  if (nrhs > 0 && info == 0) {
+    Map<M, 0, OuterStride<>> B(b, n, nrhs, OuterStride<>(ldb));
+    M X = llt.solve(B);
+    B = X;
+  }
+  auto t2 = std::chrono::steady_clock::now();
+  // write the factor back (only the UpLo triangle is meaningful)
+  A.template triangularView<UpLo>() = llt.matrixLLT().template triangularView<UpLo>();
+  if (seconds) {
+    seconds[0] = std::chrono::duration<double>(t1 - t0).count();
+    seconds[1] = std::chrono::duration<double>(t2 - t1).count();
+  }
+  return info;
+}
+
+// Failing column as returned by llt_inplace<T,UpLo>::blocked (LLT.h:338-368): -1 on success.
+template <typename T, int UpLo>
+static int64_t blocked(int64_t n, T* a, int64_t lda) {
+  typedef Matrix<T, Dynamic, Dynamic> M;
+  Map<M, 0, OuterStride<>> A(a, n, n, OuterStride<>(lda));
+  return (int64_t)internal::llt_inplace<T, UpLo>::blocked(A);
+}
+
+extern "C" {
+
+int64_t ref_dllt(char uplo, int64_t n, int64_t nrhs, double* a, int64_t lda, double* b, int64_t ldb, double* sec) {
+  return uplo == 'U' ? factor_solve<double, Upper>(n, nrhs, a, lda, b, ldb, sec)
+                     : factor_solve<double, Lower>(n, nrhs, a, lda, b, ldb, sec);
+}
+int64_t ref_sllt(char uplo, int64_t n, int64_t nrhs, float* a, int64_t lda, float* b, int64_t ldb, double* sec) {
+  return uplo == 'U' ? factor_solve<float, Upper>(n, nrhs, a, lda, b, ldb, sec)
+                     : factor_solve<float, Lower>(n, nrhs, a, lda, b, ldb, sec);
+}
+int64_t ref_dblocked(char uplo, int64_t n, double* a, int64_t lda) {
+  return uplo == 'U' ? blocked<double, Upper>(n, a, lda) : blocked<double, Lower>(n, a, lda);
+}
+int64_t ref_sblocked(char uplo, int64_t n, float* a, int64_t lda) {
+  return uplo == 'U' ? blocked<float, Upper>(n, a, lda) : blocked<float, Lower>(n, a, lda);
+}
+
+}  // extern "C"

@@ -1,0 +1,241 @@
+/* Scalar-generic body of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+ *
+ * Included twice by llt_oracle.c, once with T=double / P(x)=oracle_d##x and once with
+ * T=float / P(x)=oracle_s##x.  Every routine restates the algorithm of the Eigen source it
+ * cites; the arithmetic is done in T, like Eigen's LLT<Matrix<T,...>>.
+ *
+ * A matrix is addressed through (rs, cs) strides: element (i, j) lives at p[i*rs + j*cs].
+ * A column-major lower factor uses (1, lda); a column-major UPPER factor is the lower factor
+ * of the transpose, i.e. (lda, 1) -- the same trick as llt_inplace<Scalar,Upper> in
+ * Eigen/src/Cholesky/LLT.h:377-399, which runs the Lower algorithm on Transpose<MatrixType>.
+ */
+
+#define EL(p, i, j) (p)[(int64_t)(i) * rs + (int64_t)(j) * cs]
+
+/* Left-looking unblocked factorisation of one diagonal block.
+ * Restates llt_inplace<Scalar,Lower>::unblocked, Eigen/src/Cholesky/LLT.h:312-336:
+ *   x = a_kk - ||A10||^2 ; x <= 0 -> return k ; a_kk = sqrt(x) ;
+ *   A21 -= A20 * A10^T (a GEMV) ; A21 /= a_kk.
+ * Returns -1 on success, else the failing column. */
+int64_t P(llt_unblocked)(int64_t n, T* a, int64_t rs, int64_t cs) {
+  for (int64_t k = 0; k < n; ++k) {
+    const int64_t r = n - k - 1;
+    T x = EL(a, k, k);
+    T ss = 0;
+    for (int64_t p = 0; p < k; ++p) ss += EL(a, k, p) * EL(a, k, p);
+    x -= ss;
+    if (x <= (T)0) return k;   /* same test as LLT.h:329: a NaN pivot does not stop it */
+    x = (T)sqrt((double)x);   /* correctly rounded in T for both float and double */
+    EL(a, k, k) = x;
+    if (r > 0) {
+      /* GEMV A21 -= A20 * A10^T, column-oriented (axpy per column of A20) */
+      for (int64_t p = 0; p < k; ++p) {
+        const T akp = EL(a, k, p);
+        for (int64_t i = k + 1; i < n; ++i) EL(a, i, k) -= EL(a, i, p) * akp;
+      }
+      for (int64_t i = k + 1; i < n; ++i) EL(a, i, k) /= x;
+    }
+  }
+  return -1;
+}
+
+/* Panel triangular solve A21 <- A21 * L11^{-T}, L11 lower bs x bs, A21 m x bs.
+ * Restates the OnTheRight solve that LLT.h:364 issues
+ * (triangular_solve_matrix<...,OnTheRight,...>, Eigen/src/Core/products/TriangularSolverMatrix.h:188-329):
+ * column j of X is (A21(:,j) - sum_{p<j} X(:,p) L11(j,p)) / L11(j,j).
+ * Rows are independent, so the row range is split over threads; each element sees the same
+ * operation order whatever the thread count. */
+static void P(trsm_right_lt)(int64_t m, int64_t bs, const T* l11, int64_t lrs, int64_t lcs,
+                             T* a21, int64_t rs, int64_t cs) {
+  const int64_t RB = 256;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+  for (int64_t r0 = 0; r0 < m; r0 += RB) {
+    const int64_t r1 = r0 + RB < m ? r0 + RB : m;
+    for (int64_t j = 0; j < bs; ++j) {
+      for (int64_t p = 0; p < j; ++p) {
+        const T ljp = l11[j * lrs + p * lcs];
+        for (int64_t i = r0; i < r1; ++i) EL(a21, i, j) -= EL(a21, i, p) * ljp;
+      }
+      const T ljj = l11[j * lrs + j * lcs];
+      for (int64_t i = r0; i < r1; ++i) EL(a21, i, j) /= ljj;
+    }
+  }
+}
+
+/* Lower SYRK  C -= A * A^T  (C m x m lower, A m x k).
+ * Restates the rankUpdate issued at LLT.h:365 (SelfadjointProduct.h:82-117 ->
+ * general_matrix_matrix_triangular_product, GeneralMatrixMatrixTriangular.h:57-194):
+ * A is packed once into row strips of MR and column strips of NR (the role of
+ * gemm_pack_lhs / gemm_pack_rhs, GeneralBlockPanelKernel.h:2236+, 2524+), and an MR x NR
+ * register-blocked micro-kernel (the role of gebp_kernel, :1548+) accumulates over the full
+ * depth k before subtracting from C.  Only tiles on or below the diagonal are touched, and
+ * inside a diagonal tile only the lower half is written (the role of tribb_kernel, :138-194).
+ * Per element, the sum runs over p = 0..k-1 in order and is then subtracted: the result does not
+ * depend on the thread count. */
+#define ORC_MR 8
+#define ORC_NR 4
+static void P(syrk_lower_sub)(int64_t m, int64_t k, const T* a, int64_t ars, int64_t acs,
+                              T* c, int64_t rs, int64_t cs) {
+  if (m <= 0 || k <= 0) return;
+  const int64_t mp = (m + ORC_MR - 1) / ORC_MR * ORC_MR;
+  const int64_t np = (m + ORC_NR - 1) / ORC_NR * ORC_NR;
+  T* pa = (T*)calloc((size_t)(mp * k), sizeof(T));   /* [m/MR][k][MR] */
+  T* pb = (T*)calloc((size_t)(np * k), sizeof(T));   /* [m/NR][k][NR] */
+  for (int64_t i = 0; i < m; ++i)
+    for (int64_t p = 0; p < k; ++p) {
+      const T v = a[i * ars + p * acs];
+      pa[(i / ORC_MR) * k * ORC_MR + p * ORC_MR + (i % ORC_MR)] = v;
+      pb[(i / ORC_NR) * k * ORC_NR + p * ORC_NR + (i % ORC_NR)] = v;
+    }
+  const int64_t nstrips = np / ORC_NR;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+  for (int64_t js = 0; js < nstrips; ++js) {
+    const int64_t j0 = js * ORC_NR;
+    const T* bp = pb + js * k * ORC_NR;
+    for (int64_t i0 = (j0 / ORC_MR) * ORC_MR; i0 < m; i0 += ORC_MR) {
+      const T* ap = pa + (i0 / ORC_MR) * k * ORC_MR;
+      T acc[ORC_NR][ORC_MR];
+      for (int jj = 0; jj < ORC_NR; ++jj)
+        for (int ii = 0; ii < ORC_MR; ++ii) acc[jj][ii] = 0;
+      for (int64_t p = 0; p < k; ++p) {
+        const T* av = ap + p * ORC_MR;
+        const T* bv = bp + p * ORC_NR;
+        for (int jj = 0; jj < ORC_NR; ++jj)
+          for (int ii = 0; ii < ORC_MR; ++ii) acc[jj][ii] += av[ii] * bv[jj];
+      }
+      for (int jj = 0; jj < ORC_NR; ++jj) {
+        const int64_t j = j0 + jj;
+        if (j >= m) break;
+        for (int ii = 0; ii < ORC_MR; ++ii) {
+          const int64_t i = i0 + ii;
+          if (i >= m) break;
+          if (i >= j) EL(c, i, j) -= acc[jj][ii];
+        }
+      }
+    }
+  }
+  free(pa);
+  free(pb);
+}
+
+/* Right-looking blocked factorisation.
+ * Restates llt_inplace<Scalar,Lower>::blocked, Eigen/src/Cholesky/LLT.h:338-368:
+ * n < 32 -> unblocked; blockSize = clamp((n/8)/16*16, 8, 128); per panel:
+ * unblocked(A11), A21 <- A21 L11^{-T}, A22 -= A21 A21^T (lower).
+ * Returns -1 on success, else the failing column (k + ret, :363). */
+int64_t P(llt_blocked)(int64_t n, T* a, int64_t rs, int64_t cs) {
+  if (n < 32) return P(llt_unblocked)(n, a, rs, cs);
+  int64_t bsz = n / 8;
+  bsz = (bsz / 16) * 16;
+  if (bsz < 8) bsz = 8;
+  if (bsz > 128) bsz = 128;
+  for (int64_t k = 0; k < n; k += bsz) {
+    const int64_t bs = bsz < n - k ? bsz : n - k;
+    const int64_t r = n - k - bs;
+    T* a11 = &EL(a, k, k);
+    int64_t ret = P(llt_unblocked)(bs, a11, rs, cs);
+    if (ret >= 0) return k + ret;
+    if (r > 0) {
+      T* a21 = &EL(a, k + bs, k);
+      P(trsm_right_lt)(r, bs, a11, rs, cs, a21, rs, cs);
+      P(syrk_lower_sub)(r, bs, a21, rs, cs, &EL(a, k + bs, k + bs), rs, cs);
+    }
+  }
+  return -1;
+}
+
+/* LAPACK-shaped wrapper: the mapping lapack/cholesky.cpp:14-36 performs around
+ * llt_inplace::blocked (argument checks -1/-2/-4, then info = ret + 1).
+ * uplo 'L'/'l' or 'U'/'u'; column-major storage with leading dimension lda. */
+int P(potrf)(char uplo, int64_t n, T* a, int64_t lda, int64_t* info) {
+  const int up = (uplo == 'U' || uplo == 'u');
+  const int lo = (uplo == 'L' || uplo == 'l');
+  *info = 0;
+  if (!up && !lo) { *info = -1; return -1; }
+  if (n < 0) { *info = -2; return -2; }
+  if (lda < (n > 1 ? n : 1)) { *info = -4; return -4; }
+  if (n == 0) return 0;
+  const int64_t ret = up ? P(llt_blocked)(n, a, lda, 1) : P(llt_blocked)(n, a, 1, lda);
+  if (ret >= 0) *info = ret + 1;
+  return 0;
+}
+
+/* Solve A X = B in place in B from the factor, restating LLT::_solve_impl_transposed
+ * (Eigen/src/Cholesky/LLT.h:483-498) = matrixL().solveInPlace then matrixU().solveInPlace, and
+ * the potrs wrapper lapack/cholesky.cpp:41-72.  Both sweeps walk the columns of L, which are
+ * contiguous for a lower column-major factor (the forward sweep is an axpy per column, the
+ * backward sweep a dot per column, cf. TriangularSolverVector.h:88-142 and :30-85). */
+int P(potrs)(char uplo, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b, int64_t ldb) {
+  const int up = (uplo == 'U' || uplo == 'u');
+  const int lo = (uplo == 'L' || uplo == 'l');
+  if (!up && !lo) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < (n > 1 ? n : 1)) return -5;
+  if (ldb < (n > 1 ? n : 1)) return -7;
+  const int64_t rs = up ? lda : 1, cs = up ? 1 : lda;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+  for (int64_t c = 0; c < nrhs; ++c) {
+    T* x = b + c * ldb;
+    for (int64_t j = 0; j < n; ++j) {          /* L y = b */
+      const T yj = x[j] / EL(a, j, j);
+      x[j] = yj;
+      for (int64_t i = j + 1; i < n; ++i) x[i] -= EL(a, i, j) * yj;
+    }
+    for (int64_t j = n - 1; j >= 0; --j) {     /* L^T x = y */
+      T s = x[j];
+      for (int64_t i = j + 1; i < n; ++i) s -= EL(a, i, j) * x[i];
+      x[j] = s / EL(a, j, j);
+    }
+  }
+  return 0;
+}
+
+/* Normwise backward error ||A X - B||_F / (||A||_F ||X||_F) with A symmetric, of which only
+ * the `uplo` triangle is read (the same triangle LLT::compute reads).  The residual is
+ * accumulated in double-double (error-free TwoSum / TwoProduct via fma; Dekker 1971,
+ * Ogita-Rump-Oishi 2005), so that values around 1e-17 are resolved. */
+double P(backward_error)(char uplo, int64_t n, int64_t nrhs, const T* a, int64_t lda,
+                         const T* x, int64_t ldx, const T* b, int64_t ldb) {
+  const int up = (uplo == 'U' || uplo == 'u');
+  double na = 0, nx = 0, nr = 0;
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t i = 0; i < n; ++i) {
+      const double v = (i >= j) != up || i == j ? (double)a[i + j * lda] : (double)a[j + i * lda];
+      na += v * v;
+    }
+  for (int64_t c = 0; c < nrhs; ++c)
+    for (int64_t i = 0; i < n; ++i) nx += (double)x[i + c * ldx] * (double)x[i + c * ldx];
+#ifdef _OPENMP
+#pragma omp parallel for reduction(+ : nr) schedule(static)
+#endif
+  for (int64_t c = 0; c < nrhs; ++c) {
+    for (int64_t i = 0; i < n; ++i) {
+      double hi = -(double)b[i + c * ldb], lo = 0;
+      for (int64_t j = 0; j < n; ++j) {
+        const int lower_el = i >= j;
+        const double aij = (lower_el != up || i == j) ? (double)a[i + j * lda] : (double)a[j + i * lda];
+        const double xv = (double)x[j + c * ldx];
+        const double ph = aij * xv;
+        const double pl = fma(aij, xv, -ph);
+        const double s = hi + ph;
+        const double bb = s - hi;
+        const double e = (hi - (s - bb)) + (ph - bb);
+        hi = s;
+        lo += e + pl;
+      }
+      const double r = hi + lo;
+      nr += r * r;
+    }
+  }
+  if (na == 0 || nx == 0) return nr == 0 ? 0.0 : INFINITY;
+  return sqrt(nr) / (sqrt(na) * sqrt(nx));
+}
+
+#undef EL

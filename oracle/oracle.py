@@ -1,0 +1,224 @@
+"""ctypes wrapper of the oracle (liboracle.so) -- TEST INFRASTRUCTURE ONLY.
+
+The oracle is the checker for the GPU path: a plain-C restatement of Eigen's LLT
+(Eigen/src/Cholesky/LLT.h:312-399, lapack/cholesky.cpp:14-72) plus the seeded workload
+generators.  Only the test suite, the smoke check and the CPU legs of the benchmark use it.
+
+`eigen_ref()` loads Eigen's own LLT compiled from the reference headers (oracle/Makefile,
+target `ref`) when that library exists; it exists only where the reference sources were present
+at build time.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ORACLE_DIR = Path(__file__).resolve().parent
+LIB_PATH = ORACLE_DIR / "liboracle.so"
+REF_PATH = ORACLE_DIR / "_ref" / "libeigen_ref.so"
+
+_i64 = ctypes.c_int64
+_u64 = ctypes.c_uint64
+_dbl = ctypes.c_double
+_vp = ctypes.c_void_p
+_ch = ctypes.c_char
+
+_SIGS = {
+    "oracle_philox4x32_10": (None, [_vp, _vp, _vp]),
+    "oracle_normal": (_dbl, [_u64, _u64]),
+    "oracle_uniform": (_dbl, [_u64, _u64]),
+    "oracle_fill_normal": (None, [_u64, _u64, _i64, _vp]),
+    "oracle_fill_uniform": (None, [_u64, _u64, _i64, _vp]),
+    "oracle_gen_gram": (None, [_i64, _u64, _u64, _dbl, _vp, _i64]),
+    "oracle_spectrum": (None, [_i64, _dbl, _u64, _vp]),
+    "oracle_gen_householder": (None, [_i64, ctypes.c_int, _u64, _vp, _vp, _i64]),
+    "oracle_batch_sizes": (None, [_i64, _u64, _i64, _i64, _vp]),
+    "oracle_gen_rbf": (None, [_i64, _u64, _u64, _dbl, _dbl, _dbl, _vp, _i64]),
+    "oracle_dllt_blocked": (_i64, [_i64, _vp, _i64, _i64]),
+    "oracle_sllt_blocked": (_i64, [_i64, _vp, _i64, _i64]),
+    "oracle_dllt_unblocked": (_i64, [_i64, _vp, _i64, _i64]),
+    "oracle_dpotrf": (ctypes.c_int, [_ch, _i64, _vp, _i64, _vp]),
+    "oracle_spotrf": (ctypes.c_int, [_ch, _i64, _vp, _i64, _vp]),
+    "oracle_dpotrs": (ctypes.c_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64]),
+    "oracle_spotrs": (ctypes.c_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64]),
+    "oracle_dbackward_error": (_dbl, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64]),
+    "oracle_sbackward_error": (_dbl, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64]),
+    "oracle_dbatched_posv": (None, [_i64, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "oracle_sbatched_posv": (None, [_i64, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "oracle_num_threads": (ctypes.c_int, []),
+    "oracle_set_num_threads": (None, [ctypes.c_int]),
+}
+
+_lib = None
+_ref = None
+
+
+def build(ref: bool = True) -> None:
+    """Compile liboracle.so; also Eigen's own LLT when the reference headers are present."""
+    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "liboracle.so"], check=True)
+    eigen = os.environ.get("EIGEN_REF", "/root/reference")
+    if ref and Path(eigen, "Eigen").is_dir():
+        subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"EIGEN_REF={eigen}"], check=True)
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build(ref=False)
+        L = ctypes.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def eigen_ref():
+    """Eigen's own LLT (None when it was not built here)."""
+    global _ref
+    if _ref is None and REF_PATH.exists():
+        R = ctypes.CDLL(str(REF_PATH))
+        for nm in ("ref_dllt", "ref_sllt"):
+            getattr(R, nm).restype = _i64
+            getattr(R, nm).argtypes = [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp]
+        for nm in ("ref_dblocked", "ref_sblocked"):
+            getattr(R, nm).restype = _i64
+            getattr(R, nm).argtypes = [_ch, _i64, _vp, _i64]
+        _ref = R
+    return _ref
+
+
+def _p(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+# ---- generators --------------------------------------------------------------------------------
+
+def philox(ctr, key) -> list[int]:
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    o = (ctypes.c_uint32 * 4)()
+    lib().oracle_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def normal(seed: int, count: int, offset: int = 0) -> np.ndarray:
+    out = np.empty(count, dtype=np.float64)
+    lib().oracle_fill_normal(seed, offset, count, _p(out))
+    return out
+
+
+def uniform(seed: int, count: int, offset: int = 0) -> np.ndarray:
+    out = np.empty(count, dtype=np.float64)
+    lib().oracle_fill_uniform(seed, offset, count, _p(out))
+    return out
+
+
+def gen_gram(n: int, seed: int = 1, offset: int = 0, shift: float = 1.0) -> np.ndarray:
+    """A = G G^T / n + shift I (Fortran order)."""
+    a = np.empty((n, n), dtype=np.float64, order="F")
+    if n:
+        lib().oracle_gen_gram(n, seed, offset, shift, _p(a), n)
+    return a
+
+
+def spectrum(n: int, kappa: float, perm_seed: int = 11) -> np.ndarray:
+    lam = np.empty(n, dtype=np.float64)
+    lib().oracle_spectrum(n, kappa, perm_seed, _p(lam))
+    return lam
+
+
+def gen_householder(n: int, kappa: float, nrefl: int = 8, v_seed0: int = 3, perm_seed: int = 11) -> np.ndarray:
+    """A = Q diag(lambda) Q^T, Q = H_1 ... H_nrefl, v_i from seed v_seed0 + i."""
+    lam = spectrum(n, kappa, perm_seed)
+    a = np.empty((n, n), dtype=np.float64, order="F")
+    lib().oracle_gen_householder(n, nrefl, v_seed0, _p(lam), _p(a), n)
+    return a
+
+
+def batch_sizes(count: int, seed: int = 21, lo: int = 4, hi: int = 256) -> np.ndarray:
+    out = np.empty(count, dtype=np.int64)
+    lib().oracle_batch_sizes(count, seed, lo, hi, _p(out))
+    return out
+
+
+def gen_rbf(m: int, seed: int = 31, offset: int = 0, ell: float = 0.2, sigma2: float = 1.0,
+            noise: float = 1e-2) -> np.ndarray:
+    a = np.empty((m, m), dtype=np.float64, order="F")
+    lib().oracle_gen_rbf(m, seed, offset, ell, sigma2, noise, _p(a), m)
+    return a
+
+
+# ---- LLT restatement ---------------------------------------------------------------------------
+
+def blocked(a: np.ndarray, uplo: str = "L") -> int:
+    """llt_inplace<T,UpLo>::blocked on a (Fortran order, in place): -1 or the failing column."""
+    n = a.shape[0]
+    lda = max(1, n)
+    rs, cs = (lda, 1) if uplo == "U" else (1, lda)
+    fn = lib().oracle_dllt_blocked if a.dtype == np.float64 else lib().oracle_sllt_blocked
+    return int(fn(n, _p(a), rs, cs))
+
+
+def potrf(a: np.ndarray, uplo: str = "L") -> int:
+    info = np.zeros(1, dtype=np.int64)
+    fn = lib().oracle_dpotrf if a.dtype == np.float64 else lib().oracle_spotrf
+    rc = fn(uplo.encode(), a.shape[0], _p(a), max(1, a.shape[0]), _p(info))
+    assert rc == 0, rc
+    return int(info[0])
+
+
+def potrs(a: np.ndarray, b: np.ndarray, uplo: str = "L") -> None:
+    n = a.shape[0]
+    k = 1 if b.ndim == 1 else b.shape[1]
+    fn = lib().oracle_dpotrs if a.dtype == np.float64 else lib().oracle_spotrs
+    rc = fn(uplo.encode(), n, k, _p(a), max(1, n), _p(b), max(1, n))
+    assert rc == 0, rc
+
+
+def backward_error(a: np.ndarray, x: np.ndarray, b: np.ndarray, uplo: str = "L") -> float:
+    """||A X - B||_F / (||A||_F ||X||_F), A symmetric given by its `uplo` triangle."""
+    n = a.shape[0]
+    k = 1 if b.ndim == 1 else b.shape[1]
+    fn = lib().oracle_dbackward_error if a.dtype == np.float64 else lib().oracle_sbackward_error
+    x = np.asfortranarray(x, dtype=a.dtype)
+    b = np.asfortranarray(b, dtype=a.dtype)
+    return float(fn(uplo.encode(), n, k, _p(a), max(1, n), _p(x), max(1, n), _p(b), max(1, n)))
+
+
+def solve(a: np.ndarray, b: np.ndarray, uplo: str = "L") -> tuple[np.ndarray, np.ndarray, int]:
+    """Factor a copy of a and solve: returns (factor, X, info)."""
+    f = np.array(a, order="F", copy=True)
+    info = potrf(f, uplo)
+    x = np.array(b, order="F", copy=True)
+    if info == 0:
+        potrs(f, x, uplo)
+    return f, x, info
+
+
+def batched_posv(ns: np.ndarray, a_packed: np.ndarray, b_packed: np.ndarray):
+    """Factor + solve every system of an uneven batch in place; returns info per system."""
+    ns = np.ascontiguousarray(ns, dtype=np.int64)
+    aoff = np.zeros(len(ns), dtype=np.int64)
+    boff = np.zeros(len(ns), dtype=np.int64)
+    if len(ns):
+        aoff[1:] = np.cumsum(ns * ns)[:-1]
+        boff[1:] = np.cumsum(ns)[:-1]
+    info = np.zeros(len(ns), dtype=np.int64)
+    fn = lib().oracle_dbatched_posv if a_packed.dtype == np.float64 else lib().oracle_sbatched_posv
+    fn(len(ns), _p(ns), _p(aoff), _p(boff), _p(a_packed), _p(b_packed), _p(info))
+    return info
+
+
+def set_threads(t: int) -> None:
+    lib().oracle_set_num_threads(int(t))
+
+
+def num_threads() -> int:
+    return int(lib().oracle_num_threads())
