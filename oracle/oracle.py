@@ -58,11 +58,20 @@ _ref = None
 
 
 def build(ref: bool = True) -> None:
-    """Compile liboracle.so; also Eigen's own LLT when the reference headers are present."""
-    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "liboracle.so"], check=True)
+    """Compile liboracle.so; also Eigen's own LLT when the reference headers are present.
+    Same commands as oracle/Makefile, issued directly so that `make` is not required."""
+    src = ORACLE_DIR / "llt_oracle.c"
+    deps = [src, ORACLE_DIR / "llt_oracle_body.h"]
+    if not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < max(d.stat().st_mtime for d in deps):
+        subprocess.run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-Wall", "-o", str(LIB_PATH), str(src), "-lm"],
+                       check=True)
     eigen = os.environ.get("EIGEN_REF", "/root/reference")
     if ref and Path(eigen, "Eigen").is_dir():
-        subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"EIGEN_REF={eigen}"], check=True)
+        REF_PATH.parent.mkdir(exist_ok=True)
+        cpp = ORACLE_DIR / "eigen_ref.cpp"
+        if not REF_PATH.exists() or REF_PATH.stat().st_mtime < cpp.stat().st_mtime:
+            subprocess.run(["g++", "-O3", "-DNDEBUG", "-fopenmp", "-fPIC", "-shared", f"-I{eigen}", "-o",
+                            str(REF_PATH), str(cpp)], check=True)
 
 
 def lib() -> ctypes.CDLL:
