@@ -15,6 +15,18 @@ constexpr int kNB = 64;
 template <typename T>
 int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t s);
 
+// Kernel launchers of the blocked factorisation, shared with the mixed-precision path.
+// Diagonal 64 x 64 block at (k0, k0): storage T, arithmetic TC.
+template <typename T, typename TC>
+void launch_potrf_diag(T* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s);
+// Rows below the block: A(k0+bs.., k0..k0+bs) <- A(...) L11^{-T}, rs rows.
+template <typename T>
+void launch_trsm_panel(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, cudaStream_t s);
+// Lower update of the first ncols columns of the rs x rs trailing matrix by the bs-wide panel.
+template <typename T>
+void launch_syrk_lower(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, int64_t ncols, DevStatus* st,
+                       cudaStream_t s);
+
 // Swap the strict lower and strict upper triangles of the n x n matrix at d_a in place
 // (A <- A^T).  Used to run the lower algorithm on an upper-stored factor, the same trick as
 // llt_inplace<Scalar,Upper> (Eigen/src/Cholesky/LLT.h:377-399).
@@ -49,6 +61,10 @@ template <typename T>
 constexpr const char* tname() {
   return sizeof(T) == 8 ? "f64" : "f32";
 }
+
+// Mixed-precision solve with FP64 refinement (device pointers, column-major).
+int posv_mixed_dev(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
+                   double* x, int64_t ldx, const gbllt_mixed_opts* opts, gbllt_mixed_report* rep, cudaStream_t s);
 
 // Validates (uplo, n, lda) the way dpotrf_ does (lapack/cholesky.cpp:17-19); returns 0 or -argpos.
 int check_uplo(char uplo);

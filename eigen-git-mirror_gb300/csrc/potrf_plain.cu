@@ -25,17 +25,19 @@ namespace {
 
 constexpr int NB = kNB;
 
-template <typename T>
-__global__ void __launch_bounds__(256) potrf_diag_kernel(T* __restrict__ a, long long lda, int k0, int bs,
+// T = storage type, TC = arithmetic type (the mixed-precision path stores float and factors the
+// diagonal block in double).
+template <typename T, typename TC>
+__global__ void __launch_bounds__(256) potrf_diag_kernel(T* __restrict__ a, long long lda, long long k0, int bs,
                                                          DevStatus* __restrict__ st) {
   if (st->fail_col >= 0) return;  // an earlier panel already failed: nothing more to do
-  __shared__ T s[NB][NB + 1];    // s[j][i] = A11(i, j), lower part only
+  __shared__ TC s[NB][NB + 1];   // s[j][i] = A11(i, j), lower part only
   __shared__ int fail;
   const int tid = threadIdx.x;
-  T* blk = a + (long long)k0 * lda + k0;
+  T* blk = a + k0 * lda + k0;
   for (int idx = tid; idx < NB * NB; idx += 256) {
     const int j = idx / NB, i = idx % NB;
-    if (i < bs && j < bs && i >= j) s[j][i] = blk[(long long)j * lda + i];
+    if (i < bs && j < bs && i >= j) s[j][i] = (TC)blk[(long long)j * lda + i];
   }
   if (tid == 0) fail = -1;
   __syncthreads();
@@ -43,31 +45,31 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(T* __restrict__ a, long
   int j = 0;
   for (; j < bs; ++j) {
     if (tid == 0) {
-      const T d = s[j][j];
-      if (d <= T(0)) fail = j;
+      const TC d = s[j][j];
+      if (d <= TC(0)) fail = j;
       else s[j][j] = sqrt(d);
     }
     __syncthreads();
     if (fail >= 0) break;  // block-uniform
-    const T djj = s[j][j];
+    const TC djj = s[j][j];
     if (tid > j && tid < bs) s[j][tid] = s[j][tid] / djj;
     __syncthreads();
     for (int l = j + 1 + ty; l < bs; l += 4) {
-      const T ljl = s[j][l];
+      const TC ljl = s[j][l];
       if (tx >= l && tx < bs) s[l][tx] = fma(-s[j][tx], ljl, s[l][tx]);
     }
     __syncthreads();
   }
   for (int idx = tid; idx < NB * NB; idx += 256) {
     const int jj = idx / NB, i = idx % NB;
-    if (i < bs && jj < bs && i >= jj) blk[(long long)jj * lda + i] = s[jj][i];
+    if (i < bs && jj < bs && i >= jj) blk[(long long)jj * lda + i] = (T)s[jj][i];
   }
-  if (tid == 0 && fail >= 0) st->fail_col = (long long)k0 + fail;
+  if (tid == 0 && fail >= 0) st->fail_col = k0 + fail;
 }
 
 // A21 (rs x bs, rows k0+bs.., columns k0..) <- A21 * L11^{-T}.  One thread per row.
 template <typename T>
-__global__ void __launch_bounds__(128) trsm_panel_kernel(T* __restrict__ a, long long lda, int k0, int bs,
+__global__ void __launch_bounds__(128) trsm_panel_kernel(T* __restrict__ a, long long lda, long long k0, int bs,
                                                          long long rs, const DevStatus* __restrict__ st) {
   if (st->fail_col >= 0) return;
   __shared__ T L[NB][NB + 1];  // L[j][p] = L11(j, p); identity outside the bs x bs block
@@ -97,16 +99,28 @@ __global__ void __launch_bounds__(128) trsm_panel_kernel(T* __restrict__ a, long
     if (p < bs) row[(long long)p * lda] = x[p];
 }
 
-// A22 (rs x rs lower) -= A21 A21^T, A21 = rs x bs.  One CTA per 64 x 64 lower tile.
+// A22 (rs x rs lower) -= A21 A21^T, A21 = rs x bs.  One CTA per 64 x 64 lower tile.  Only the
+// first `ncols` columns of A22 are updated (nct = ceil(ncols / 64) column tiles): the whole lower
+// triangle when ncols = rs, or the remaining columns of the current panel when the mixed-precision
+// path factors a wide panel in 64-column steps.
 template <typename T>
-__global__ void __launch_bounds__(256) syrk_lower_kernel(T* __restrict__ a, long long lda, int k0, int bs,
-                                                         long long rs, const DevStatus* __restrict__ st) {
+__global__ void __launch_bounds__(256) syrk_lower_kernel(T* __restrict__ a, long long lda, long long k0, int bs,
+                                                         long long rs, long long ncols, int nct,
+                                                         const DevStatus* __restrict__ st) {
   if (st->fail_col >= 0) return;
   constexpr int KC = 32;
   __shared__ T As[KC][64 + 1];
   __shared__ T Bs[KC][64 + 1];
   int ti, tj;
-  lower_tile_coords(blockIdx.x, ti, tj);
+  const int mt = (int)((rs + 63) / 64);
+  if (nct >= mt) {
+    lower_tile_coords(blockIdx.x, ti, tj);
+  } else {  // column tiles 0..nct-1, each holding the row tiles tj..mt-1
+    long long t = blockIdx.x;
+    tj = 0;
+    while (t >= mt - tj) { t -= mt - tj; ++tj; }
+    ti = tj + (int)t;
+  }
   const long long i0 = (long long)ti * 64, j0 = (long long)tj * 64;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const T* A = a + (long long)k0 * lda + (k0 + bs);  // A21(0, 0)
@@ -148,7 +162,7 @@ __global__ void __launch_bounds__(256) syrk_lower_kernel(T* __restrict__ a, long
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
       const long long i = i0 + tx + 16 * m;
-      if (i < rs && j < rs && i >= j) C[j * lda + i] -= acc[m][q];
+      if (i < rs && j < ncols && i >= j) C[j * lda + i] -= acc[m][q];
     }
   }
 }
@@ -198,34 +212,53 @@ __global__ void finalize_info_kernel(const DevStatus* __restrict__ st, int64_t* 
 
 }  // namespace
 
+template <typename T, typename TC>
+void launch_potrf_diag(T* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s) {
+  static const std::string kd = std::string("potrf_diag_") + tname<TC>();
+  ProfScope ps(kd.c_str(), s, (double)bs * bs * bs / 3.0, (double)bs * (bs + 1) * sizeof(T));
+  potrf_diag_kernel<T, TC><<<1, 256, 0, s>>>(a, lda, k0, bs, st);
+}
+
+template <typename T>
+void launch_trsm_panel(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, cudaStream_t s) {
+  if (rs <= 0) return;
+  static const std::string kt = std::string("trsm_panel_") + tname<T>();
+  ProfScope ps(kt.c_str(), s, (double)rs * bs * bs, (2.0 * rs * bs + 0.5 * bs * bs) * sizeof(T));
+  trsm_panel_kernel<T><<<(unsigned)ceil_div(rs, 128), 128, 0, s>>>(a, lda, k0, bs, rs, st);
+}
+
+template <typename T>
+void launch_syrk_lower(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, int64_t ncols, DevStatus* st,
+                       cudaStream_t s) {
+  if (rs <= 0 || ncols <= 0) return;
+  static const std::string ks = std::string("syrk_lower_") + tname<T>();
+  const int64_t mt = ceil_div(rs, 64);
+  const int64_t nct = ceil_div(ncols < rs ? ncols : rs, 64);
+  const int64_t tiles = nct >= mt ? mt * (mt + 1) / 2 : nct * mt - nct * (nct - 1) / 2;
+  // algorithmic work: the updated lower entries, each a dot of depth bs (2 bs flops), reading the
+  // bs-deep operand rows once and reading + writing each updated entry once
+  const double w = (double)ncols;
+  const double entries = ncols >= rs ? (double)rs * (rs + 1) / 2.0 : w * (double)rs - w * (w - 1) / 2.0;
+  ProfScope ps(ks.c_str(), s, 2.0 * entries * bs, ((double)rs * bs + 2.0 * entries) * sizeof(T));
+  syrk_lower_kernel<T><<<(unsigned)tiles, 256, 0, s>>>(a, lda, k0, bs, rs, ncols, (int)nct, st);
+}
+
 template <typename T>
 int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t s) {
-  static const std::string kd = std::string("potrf_diag_") + tname<T>();
-  static const std::string kt = std::string("trsm_panel_") + tname<T>();
-  static const std::string ks = std::string("syrk_lower_") + tname<T>();
-  const double es = sizeof(T);
   for (int64_t k0 = 0; k0 < n; k0 += NB) {
     const int bs = (int)(n - k0 < NB ? n - k0 : NB);
     const int64_t rs = n - k0 - bs;
-    {
-      ProfScope ps(kd.c_str(), s, (double)bs * bs * bs / 3.0, (double)bs * (bs + 1) * es);
-      potrf_diag_kernel<T><<<1, 256, 0, s>>>(d_a, lda, (int)k0, bs, st);
-    }
-    if (rs > 0) {
-      {
-        ProfScope ps(kt.c_str(), s, (double)rs * bs * bs, (2.0 * rs * bs + 0.5 * bs * bs) * es);
-        trsm_panel_kernel<T><<<(unsigned)ceil_div(rs, 128), 128, 0, s>>>(d_a, lda, (int)k0, bs, rs, st);
-      }
-      const int64_t nt = ceil_div(rs, 64);
-      // algorithmic work: rs(rs+1)/2 lower entries, each a dot of depth bs (2 bs flops),
-      // reading A21 once and reading + writing the lower triangle of A22 once
-      ProfScope ps(ks.c_str(), s, (double)rs * (rs + 1) * bs, ((double)rs * bs + (double)rs * (rs + 1)) * es);
-      syrk_lower_kernel<T><<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(d_a, lda, (int)k0, bs, rs, st);
-    }
+    launch_potrf_diag<T, T>(d_a, lda, k0, bs, st, s);
+    launch_trsm_panel<T>(d_a, lda, k0, bs, rs, st, s);
+    launch_syrk_lower<T>(d_a, lda, k0, bs, rs, rs, st, s);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
 }
+
+template void launch_potrf_diag<float, double>(float*, int64_t, int64_t, int, DevStatus*, cudaStream_t);
+template void launch_trsm_panel<float>(float*, int64_t, int64_t, int, int64_t, DevStatus*, cudaStream_t);
+template void launch_syrk_lower<float>(float*, int64_t, int64_t, int, int64_t, int64_t, DevStatus*, cudaStream_t);
 
 template <typename T>
 int transpose_inplace_dev(int64_t n, T* d_a, int64_t lda, cudaStream_t s) {
