@@ -231,10 +231,80 @@ int host_posv_entry(int layout, char uplo, int64_t n, int64_t nrhs, T* a, int64_
   return host_posv<T>(true, true, layout, uplo, n, nrhs, a, lda, b, ldb, info);
 }
 
+int check_mixed_args(char uplo, int64_t n, int64_t nrhs, const void* a, int64_t lda, const void* b, int64_t ldb,
+                     const void* x, int64_t ldx, int base) {
+  // base = 0 for the _dev entry (uplo is argument 1), 1 for the host entry (layout first)
+  if (check_uplo(uplo)) return -(1 + base);
+  if (n < 0) return -(2 + base);
+  if (nrhs < 0) return -(3 + base);
+  if (n > 0 && !a) return -(4 + base);
+  if (lda < (n > 1 ? n : 1)) return -(5 + base);
+  if (n > 0 && nrhs > 0 && !b) return -(6 + base);
+  if (ldb < (n > 1 ? n : 1)) return -(7 + base);
+  if (n > 0 && nrhs > 0 && !x) return -(8 + base);
+  if (ldx < (n > 1 ? n : 1)) return -(9 + base);
+  return 0;
+}
+
 }  // namespace
 }  // namespace gbllt
 
 using namespace gbllt;
+
+extern "C" int gbllt_dposv_mixed_dev(char uplo, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
+                                     const double* d_b, int64_t ldb, double* d_x, int64_t ldx,
+                                     const gbllt_mixed_opts* opts, gbllt_mixed_report* report, void* stream) {
+  int rc = check_mixed_args(uplo, n, nrhs, d_a, lda, d_b, ldb, d_x, ldx, 0);
+  if (rc) return rc;
+  if (report) memset(report, 0, sizeof *report);
+  if (n == 0 || nrhs == 0) return GBLLT_SUCCESS;
+  if ((rc = ensure_device())) return rc;
+  return posv_mixed_dev(is_upper(uplo), n, nrhs, d_a, lda, d_b, ldb, d_x, ldx, opts, report, (cudaStream_t)stream);
+}
+
+extern "C" int gbllt_dposv_mixed(int layout, char uplo, int64_t n, int64_t nrhs, const double* a, int64_t lda,
+                                 const double* b, int64_t ldb, double* x, int64_t ldx, const gbllt_mixed_opts* opts,
+                                 gbllt_mixed_report* report) {
+  if (layout != GBLLT_ROW_MAJOR && layout != GBLLT_COL_MAJOR) return -1;
+  const bool rowmajor = layout == GBLLT_ROW_MAJOR;
+  // row-major B / X are n x nrhs with leading dimension >= nrhs
+  const int64_t ldb_chk = rowmajor ? (ldb >= (nrhs > 1 ? nrhs : 1) ? (n > 1 ? n : 1) : 0) : ldb;
+  const int64_t ldx_chk = rowmajor ? (ldx >= (nrhs > 1 ? nrhs : 1) ? (n > 1 ? n : 1) : 0) : ldx;
+  int rc = check_mixed_args(uplo, n, nrhs, a, lda, b, ldb_chk, x, ldx_chk, 1);
+  if (rc) return rc;
+  if (report) memset(report, 0, sizeof *report);
+  if (n == 0 || nrhs == 0) return GBLLT_SUCCESS;
+  if ((rc = ensure_device())) return rc;
+  const bool upper = is_upper(uplo) != rowmajor;
+  cudaStream_t s = lib_stream();
+  const size_t es = 8;
+  DevBuf work;
+  const size_t abytes = ((size_t)n * n * es + 255) / 256 * 256, bbytes = ((size_t)n * nrhs * es + 255) / 256 * 256;
+  if ((rc = alloc(work, abytes + 3 * bbytes, s))) return rc;
+  double* d_a = (double*)work.p;
+  double* d_b = (double*)((char*)work.p + abytes);
+  double* d_x = (double*)((char*)d_b + bbytes);
+  double* d_t = (double*)((char*)d_x + bbytes);
+  GB_CUDA_TRY(cudaMemcpy2DAsync(d_a, n * es, a, lda * es, n * es, n, cudaMemcpyHostToDevice, s));
+  if (!rowmajor) {
+    GB_CUDA_TRY(cudaMemcpy2DAsync(d_b, n * es, b, ldb * es, n * es, nrhs, cudaMemcpyHostToDevice, s));
+  } else {
+    GB_CUDA_TRY(cudaMemcpy2DAsync(d_t, nrhs * es, b, ldb * es, nrhs * es, n, cudaMemcpyHostToDevice, s));
+    if ((rc = transpose_dev<double>(nrhs, n, d_t, nrhs, d_b, n, s))) return rc;
+  }
+  gbllt_mixed_report local;
+  rc = posv_mixed_dev(upper, n, nrhs, d_a, n, d_b, n, d_x, n, opts, report ? report : &local, s);
+  if (rc && rc != GBLLT_ERR_NOT_CONVERGED) return rc;
+  if (!rowmajor) {
+    GB_CUDA_TRY(cudaMemcpy2DAsync(x, ldx * es, d_x, n * es, n * es, nrhs, cudaMemcpyDeviceToHost, s));
+  } else {
+    int rc2 = transpose_dev<double>(n, nrhs, d_x, n, d_t, nrhs, s);
+    if (rc2) return rc2;
+    GB_CUDA_TRY(cudaMemcpy2DAsync(x, ldx * es, d_t, nrhs * es, nrhs * es, n, cudaMemcpyDeviceToHost, s));
+  }
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return rc;
+}
 
 extern "C" {
 

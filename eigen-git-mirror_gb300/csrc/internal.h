@@ -63,6 +63,22 @@ constexpr const char* tname() {
 }
 
 // Mixed-precision solve with FP64 refinement (device pointers, column-major).
+// Workspace layout of one solve: the FP32 working matrix (ldf x n), scaling, residuals, partial
+// sums, split panel operands and the status word, in `bytes`; `fallback_bytes` more hold the FP64
+// copy used by the FP64 fallback.
+struct MixedLayout {
+  int64_t ldf, ldk;
+  int nb, zc, nparts, jpc, nsq;
+  size_t es_k, bytes, fallback_bytes;
+};
+int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* out);  // defaults; -1 if invalid
+MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o);
+// The solve on a caller-supplied workspace of ws_bytes (>= layout.bytes).  With may_allocate false
+// it creates no events and allocates nothing: the fallback then runs only if the workspace also
+// holds fallback_bytes, and the report's device times are 0.
+int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
+                    double* x, int64_t ldx, const gbllt_mixed_opts& o, gbllt_mixed_report* rep, void* ws,
+                    size_t ws_bytes, bool may_allocate, cudaStream_t s);
 int posv_mixed_dev(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
                    double* x, int64_t ldx, const gbllt_mixed_opts* opts, gbllt_mixed_report* rep, cudaStream_t s);
 

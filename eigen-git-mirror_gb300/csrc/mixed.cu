@@ -1,0 +1,534 @@
+// Mixed-precision LLT solve with FP64 iterative refinement.
+//
+// Eigen's LLT<MatrixXd> (Eigen/src/Cholesky/LLT.h:430-498) factors and solves entirely in FP64.
+// On GB300 the FP64 pipe delivers ~1 TFLOP/s while the tensor cores deliver ~1 PFLOP/s (TF32) and
+// ~2 PFLOP/s (BF16), so this path:
+//   1. scales A symmetrically to unit diagonal (D A D, D = diag(a_ii)^-1/2, Higham & Pranesh 2021)
+//      and rounds the scaled lower triangle to an FP32 working matrix;
+//   2. factors it with the blocked right-looking algorithm of llt_inplace::blocked (LLT.h:338-368)
+//      in two levels: panels of width `panel` are factored in 64-column steps (diagonal blocks in
+//      FP64 arithmetic, panel TRSM and in-panel updates on FP32 cores), and the trailing SYRK of
+//      each panel -- almost all of the n^3/3 flops -- runs on tcgen05 tensor cores in TF32 or
+//      BF16 (optionally as three split-precision products) with FP32 accumulation;
+//   3. refines in FP64: r = b - A x (FP64, reading only the stored triangle of A), solve with the
+//      FP32 factor, x += d, until ||r||_F / (||A||_F ||x||_F) <= tol (LAPACK dsposv-style
+//      refinement, with the FP64 GPU factorisation as fallback).
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+#include "tc_gemm.h"
+
+namespace gbllt {
+
+namespace {
+
+constexpr int TS = 32;  // conversion tile
+
+// Af(i, j) = d_i * A(i, j) * d_j for i >= j (A given by its lower or upper triangle), as float.
+template <bool UP>
+__global__ void __launch_bounds__(256) convert_scaled_kernel(const double* __restrict__ a, long long lda, long long n,
+                                                             const double* __restrict__ d, float* __restrict__ af,
+                                                             long long ldf) {
+  __shared__ double t[TS][TS + 1];
+  int ti, tj;
+  lower_tile_coords(blockIdx.x, ti, tj);
+  const long long i0 = (long long)ti * TS, j0 = (long long)tj * TS;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  if (!UP) {
+    for (int c = ty; c < TS; c += 8) {
+      const long long i = i0 + tx, j = j0 + c;
+      if (i < n && j < n && i >= j) af[j * ldf + i] = (float)(d[i] * a[j * lda + i] * d[j]);
+    }
+  } else {
+    // element (i, j), i >= j, lives at a[i * lda + j] (upper storage of the transpose)
+    for (int c = ty; c < TS; c += 8) {
+      const long long col = i0 + c, row = j0 + tx;  // a[col * lda + row] = A(row, col) = A(col, row)
+      if (col < n && row < n && col >= row) t[c][tx] = a[col * lda + row];
+    }
+    __syncthreads();
+    for (int c = ty; c < TS; c += 8) {
+      const long long i = i0 + tx, j = j0 + c;
+      if (i < n && j < n && i >= j) af[j * ldf + i] = (float)(d[i] * t[tx][c] * d[j]);
+    }
+  }
+}
+
+template <bool UP>
+__global__ void diag_scale_kernel(const double* __restrict__ a, long long lda, long long n, double* __restrict__ d) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const double v = a[i * lda + i];
+    d[i] = v > 0.0 ? 1.0 / sqrt(v) : 1.0;
+  }
+}
+
+// hi/lo K-major copies of the panel block Af(r0 .. r0+rows, c0 .. c0+bs):
+//   out[r * ldk + p] for p < bs;  KIND 0 = bf16, 1 = tf32 (stored as fp32 with 13 zero low bits).
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) split_panel_kernel(const float* __restrict__ af, long long ldf, long long r0,
+                                                          long long c0, long long rows, int bs, void* __restrict__ hi,
+                                                          void* __restrict__ lo, long long ldk) {
+  __shared__ float t[TS][TS + 1];
+  const long long rb = (long long)blockIdx.x * TS;
+  const int pb = blockIdx.y * TS;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int c = ty; c < TS; c += 8) {  // read along rows (contiguous)
+    const long long r = rb + tx;
+    const int p = pb + c;
+    t[c][tx] = (r < rows && p < bs) ? af[(c0 + p) * ldf + r0 + r] : 0.f;
+  }
+  __syncthreads();
+  for (int c = ty; c < TS; c += 8) {  // write along p (contiguous)
+    const long long r = rb + c;
+    const int p = pb + tx;
+    if (r < rows && p < (int)ldk) {
+      const float v = p < bs ? t[tx][c] : 0.f;
+      if (KIND == 0) {
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        ((__nv_bfloat16*)hi)[r * ldk + p] = h;
+        if (lo) ((__nv_bfloat16*)lo)[r * ldk + p] = __float2bfloat16_rn(v - __bfloat162float(h));
+      } else {
+        const float h = to_tf32(v);
+        ((float*)hi)[r * ldk + p] = h;
+        if (lo) ((float*)lo)[r * ldk + p] = to_tf32(v - h);
+      }
+    }
+  }
+}
+
+// ---- FP64 residual  R = B - A X  (A symmetric, only the `UP` triangle read) ---------------------
+
+constexpr int RB = 64;   // row block
+constexpr int RCH = 16;  // right-hand sides per CTA
+
+template <bool UP>
+__device__ __forceinline__ bool stored(long long i, long long j) {
+  return UP ? (i <= j) : (i >= j);
+}
+
+template <bool UP>
+__global__ void __launch_bounds__(256) symm_partial_kernel(const double* __restrict__ a, long long lda, long long n,
+                                                           const double* __restrict__ x, long long ldx, long long nrhs,
+                                                           int jpc, double* __restrict__ part) {
+  __shared__ double As[RB][RB + 1];  // As[p][r] = A(I + r, J + p)
+  __shared__ double Xs[RB][RCH + 1];
+  const long long I = (long long)blockIdx.x * RB;
+  const long long c0 = (long long)blockIdx.z * RCH;
+  const int nb = (int)((n + RB - 1) / RB);
+  const int jb0 = blockIdx.y * jpc;
+  const int jb1 = min(nb, jb0 + jpc);
+  const int tid = threadIdx.x, r = tid & 63, cq = tid >> 6;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int jb = jb0; jb < jb1; ++jb) {
+    const long long J = (long long)jb * RB;
+    // A(I + rr, J + p): stored at a[(J+p)*lda + I+rr] ("direct", contiguous in rr) when in the stored
+    // triangle, else at a[(I+rr)*lda + J+p] ("mirrored", contiguous in p).
+    const bool all_direct = UP ? (I + RB - 1 <= J) : (I >= J + RB - 1);
+    for (int idx = tid; idx < RB * RB; idx += 256) {
+      int rr, p;
+      if (all_direct) { rr = idx & 63; p = idx >> 6; }
+      else            { p = idx & 63; rr = idx >> 6; }
+      const long long gi = I + rr, gj = J + p;
+      double v = 0.0;
+      if (gi < n && gj < n) v = stored<UP>(gi, gj) ? a[gj * lda + gi] : a[gi * lda + gj];
+      As[p][rr] = v;
+    }
+    for (int idx = tid; idx < RB * RCH; idx += 256) {
+      const int p = idx & 63, c = idx >> 6;
+      Xs[p][c] = (J + p < n && c0 + c < nrhs) ? x[(c0 + c) * ldx + J + p] : 0.0;
+    }
+    __syncthreads();
+    for (int p = 0; p < RB; ++p) {
+      const double l = As[p][r];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[q] = fma(l, Xs[p][cq * 4 + q], acc[q]);
+    }
+    __syncthreads();
+  }
+  if (I + r < n) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const long long c = c0 + cq * 4 + q;
+      if (c < nrhs) part[((long long)blockIdx.y * nrhs + c) * n + I + r] = acc[q];
+    }
+  }
+}
+
+__global__ void residual_reduce_kernel(const double* __restrict__ part, int nparts, long long n, long long nrhs,
+                                       const double* __restrict__ b, long long ldb, double* __restrict__ r,
+                                       long long ldr) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * nrhs) return;
+  const long long c = idx / n, i = idx % n;
+  double s = 0.0;
+  for (int k = 0; k < nparts; ++k) s += part[((long long)k * nrhs + c) * n + i];
+  r[c * ldr + i] = b[c * ldb + i] - s;
+}
+
+// ---- deterministic sums of squares ------------------------------------------------------------
+
+// mode 0: column-major m x k block (ld);  mode 1/2: symmetric matrix from its lower/upper triangle
+__global__ void __launch_bounds__(256) sumsq_kernel(const double* __restrict__ a, long long ld, long long m, long long k,
+                                                    int mode, double* __restrict__ part) {
+  __shared__ double red[256];
+  double s = 0.0;
+  const long long total = m * k;
+  for (long long idx = (long long)blockIdx.x * 256 + threadIdx.x; idx < total; idx += (long long)gridDim.x * 256) {
+    const long long j = idx / m, i = idx % m;
+    const double v = a[j * ld + i];
+    if (mode == 0) s += v * v;
+    else if (mode == 1) s += (i > j ? 2.0 : i == j ? 1.0 : 0.0) * v * v;
+    else s += (i < j ? 2.0 : i == j ? 1.0 : 0.0) * v * v;
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void sum_parts_kernel(const double* __restrict__ part, int np, double* __restrict__ out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < np; i += 256) s += part[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// Rf = float(d_i * R(i, c) / scale) with scale = sqrt(*ss) (the Frobenius norm of R)
+__global__ void residual_to_f32_kernel(const double* __restrict__ r, long long ldr, long long n, long long nrhs,
+                                       const double* __restrict__ d, const double* __restrict__ ss,
+                                       float* __restrict__ rf, long long ldrf) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * nrhs) return;
+  const long long c = idx / n, i = idx % n;
+  const double sc = sqrt(*ss);
+  const double inv = sc > 0.0 ? 1.0 / sc : 0.0;
+  rf[c * ldrf + i] = (float)(d[i] * r[c * ldr + i] * inv);
+}
+
+// X(i, c) += d_i * Rf(i, c) * scale
+__global__ void update_x_kernel(const float* __restrict__ rf, long long ldrf, long long n, long long nrhs,
+                                const double* __restrict__ d, const double* __restrict__ ss, double* __restrict__ x,
+                                long long ldx, int first) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * nrhs) return;
+  const long long c = idx / n, i = idx % n;
+  const double v = d[i] * (double)rf[c * ldrf + i] * sqrt(*ss);
+  x[c * ldx + i] = first ? v : x[c * ldx + i] + v;
+}
+
+__global__ void copy_cols_kernel(const double* __restrict__ src, long long lds, long long n, long long nrhs,
+                                 double* __restrict__ dst, long long ldd) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * nrhs) return;
+  const long long c = idx / n, i = idx % n;
+  dst[c * ldd + i] = src[c * lds + i];
+}
+
+inline unsigned grid1(long long total, int bs = 256) { return (unsigned)((total + bs - 1) / bs); }
+inline int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
+
+struct Arena {
+  char* base = nullptr;
+  size_t off = 0;
+  template <typename T>
+  T* take(size_t count) {
+    off = (off + 255) & ~(size_t)255;
+    T* p = (T*)(base + off);
+    off += count * sizeof(T);
+    return p;
+  }
+};
+
+}  // namespace
+
+// Factor the scaled FP32 working matrix af (n x n lower, ldf) with tensor-core trailing updates.
+int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void* hi, void* lo, int64_t ldk,
+                    DevStatus* st, int* d_err, cudaStream_t s) {
+  static const std::string ksplit = "split_panel";
+  const int kind = (prec == GBLLT_PREC_BF16 || prec == GBLLT_PREC_BF16X3) ? kTcBF16 : kTcTF32;
+  const bool split = prec == GBLLT_PREC_TF32X3 || prec == GBLLT_PREC_BF16X3;
+  for (int64_t k0 = 0; k0 < n; k0 += panel) {
+    const int bs = (int)(n - k0 < panel ? n - k0 : panel);
+    const int64_t rs = n - k0 - bs;
+    // panel: 64-column steps; the in-panel update only touches the panel's remaining columns
+    for (int64_t j0 = k0; j0 < k0 + bs; j0 += kNB) {
+      const int jb = (int)(k0 + bs - j0 < kNB ? k0 + bs - j0 : kNB);
+      const int64_t below = n - j0 - jb;
+      launch_potrf_diag<float, double>(af, ldf, j0, jb, st, s);
+      launch_trsm_panel<float>(af, ldf, j0, jb, below, st, s);
+      const int64_t cols_left = k0 + bs - (j0 + jb);
+      if (prec == GBLLT_PREC_FP32) {
+        if (cols_left > 0 || rs > 0) launch_syrk_lower<float>(af, ldf, j0, jb, below, below, st, s);
+      } else if (cols_left > 0) {
+        launch_syrk_lower<float>(af, ldf, j0, jb, below, cols_left, st, s);
+      }
+    }
+    if (rs > 0 && prec != GBLLT_PREC_FP32) {
+      {
+        ProfScope ps(ksplit.c_str(), s, 0.0, (double)rs * bs * 4.0 + (double)rs * ldk * (kind == kTcBF16 ? 2 : 4) * (split ? 2 : 1));
+        dim3 grid((unsigned)ceil_div(rs, TS), (unsigned)ceil_div(ldk, TS));
+        if (kind == kTcBF16)
+          split_panel_kernel<0><<<grid, 256, 0, s>>>(af, ldf, k0 + bs, k0, rs, bs, hi, split ? lo : nullptr, ldk);
+        else
+          split_panel_kernel<1><<<grid, 256, 0, s>>>(af, ldf, k0 + bs, k0, rs, bs, hi, split ? lo : nullptr, ldk);
+      }
+      TcOperand op{hi, split ? lo : nullptr, rs, bs, ldk, 0};
+      // segments: hi*hi, hi*lo, lo*hi  (bit 2s = A lo, bit 2s+1 = B lo)
+      const uint32_t mask = split ? ((1u << 3) | (1u << 4)) : 0u;
+      int rc = tc_update(op, op, kind, split ? 3 : 1, mask, af + (k0 + bs) * ldf + (k0 + bs), ldf, rs, rs, true,
+                         d_err, s);
+      if (rc) return rc;
+    }
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o) {
+  memset(o, 0, sizeof *o);
+  o->precision = GBLLT_PREC_TF32X3;
+  o->max_steps = 10;
+  o->tol = 1e-14;
+  o->fallback_fp64 = 1;
+  o->panel = 256;
+  if (in) {
+    *o = *in;
+    if (o->max_steps <= 0) o->max_steps = 10;
+    if (o->max_steps > 16) o->max_steps = 16;
+    if (!(o->tol > 0)) o->tol = 1e-14;
+    if (o->panel <= 0) o->panel = 256;
+  }
+  if (o->precision < GBLLT_PREC_FP32 || o->precision > GBLLT_PREC_BF16X3) return -1;
+  if (o->panel % kNB != 0) return -1;
+  return 0;
+}
+
+MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o) {
+  MixedLayout L;
+  L.ldf = round_up(n, 32);
+  L.ldk = round_up(o.panel, 64);
+  L.nb = (int)ceil_div(n, RB);
+  L.zc = (int)ceil_div(nrhs, RCH);
+  int nparts = (int)(1216 / ((int64_t)L.nb * L.zc));
+  nparts = nparts < 1 ? 1 : (nparts > L.nb ? L.nb : nparts);
+  L.jpc = (L.nb + nparts - 1) / nparts;
+  L.nparts = (L.nb + L.jpc - 1) / L.jpc;
+  L.nsq = 512;
+  L.es_k = (o.precision == GBLLT_PREC_BF16 || o.precision == GBLLT_PREC_BF16X3) ? 2 : 4;
+  L.bytes = (size_t)L.ldf * n * 4 + (size_t)n * 8 + (size_t)n * nrhs * (8 + 4) + (size_t)L.nparts * n * nrhs * 8 +
+            (size_t)L.nsq * 8 + 64 + (size_t)(o.precision == GBLLT_PREC_FP32 ? 0 : 2 * (size_t)n * L.ldk * L.es_k) +
+            sizeof(DevStatus) + 16 * 256;
+  L.fallback_bytes = (size_t)n * n * 8 + 256;
+  return L;
+}
+
+int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
+                    double* x, int64_t ldx, const gbllt_mixed_opts& o, gbllt_mixed_report* rep, void* ws,
+                    size_t ws_bytes, bool may_allocate, cudaStream_t s) {
+  gbllt_mixed_report r;
+  memset(&r, 0, sizeof r);
+  const MixedLayout Ly = mixed_layout(n, nrhs, o);
+  if (ws_bytes < Ly.bytes) return GBLLT_ERR_ALLOC;
+  const int64_t ldf = Ly.ldf, ldk = Ly.ldk;
+  const int nb = Ly.nb, zc = Ly.zc, nparts = Ly.nparts, jpc = Ly.jpc, nsq = Ly.nsq;
+  const size_t es_k = Ly.es_k;
+  struct Free {
+    void* p;
+    cudaStream_t s;
+    ~Free() {
+      if (p) cudaFreeAsync(p, s);
+    }
+  };
+  Arena ar{(char*)ws, 0};
+  float* af = ar.take<float>((size_t)ldf * n);
+  double* dsc = ar.take<double>(n);
+  double* R = ar.take<double>((size_t)n * nrhs);
+  float* Rf = ar.take<float>((size_t)n * nrhs);
+  double* part = ar.take<double>((size_t)nparts * n * nrhs);
+  double* sq = ar.take<double>(nsq);
+  double* norms = ar.take<double>(8);  // [0] ||A||^2, [1] ||R||^2, [2] ||X||^2
+  void* hi = nullptr;
+  void* lo = nullptr;
+  if (o.precision != GBLLT_PREC_FP32) {
+    hi = ar.take<char>((size_t)n * ldk * es_k);
+    lo = ar.take<char>((size_t)n * ldk * es_k);
+  }
+  DevStatus* st = ar.take<DevStatus>(1);
+  int* d_err = (int*)&st->timeout;
+  const size_t used = ar.off;
+
+  // device-time stamps (only where creating events is allowed)
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  if (may_allocate)
+    for (auto& e : ev) GB_CUDA_TRY(cudaEventCreate(&e));
+  struct EvFree {
+    cudaEvent_t* e;
+    ~EvFree() {
+      for (int i = 0; i < 3; ++i)
+        if (e[i]) cudaEventDestroy(e[i]);
+    }
+  } evguard{ev};
+  auto stamp = [&](int i) -> int {
+    if (ev[i]) GB_CUDA_TRY(cudaEventRecord(ev[i], s));
+    return 0;
+  };
+  auto elapsed = [&](int i, int j) -> double {
+    float ms = 0.f;
+    if (ev[i] && ev[j]) cudaEventElapsedTime(&ms, ev[i], ev[j]);
+    return ms;
+  };
+
+  auto sumsq = [&](const double* p, int64_t ld, int64_t m, int64_t k, int mode, double* out) {
+    int blocks = (int)((m * k + 255) / 256);
+    blocks = blocks < 1 ? 1 : (blocks > nsq ? nsq : blocks);
+    sumsq_kernel<<<blocks, 256, 0, s>>>(p, ld, m, k, mode, sq);
+    sum_parts_kernel<<<1, 256, 0, s>>>(sq, blocks, out);
+  };
+  auto residual = [&]() {  // R = B - A X
+    dim3 grid((unsigned)nb, (unsigned)nparts, (unsigned)zc);
+    static const std::string kr = "symm_residual_f64";
+    ProfScope ps(kr.c_str(), s, 2.0 * n * n * nrhs, (double)n * n * 8.0 + 3.0 * n * nrhs * 8.0);
+    if (upper) symm_partial_kernel<true><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
+    else symm_partial_kernel<false><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
+    residual_reduce_kernel<<<grid1(n * nrhs), 256, 0, s>>>(part, nparts, n, nrhs, b, ldb, R, n);
+  };
+
+  GB_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(DevStatus), s));
+  GB_CUDA_TRY(cudaMemsetAsync(&st->fail_col, 0xFF, sizeof(long long), s));
+  int rc;
+  if ((rc = stamp(0))) return rc;
+  // 1. scale and round
+  if (upper) diag_scale_kernel<true><<<grid1(n), 256, 0, s>>>(a, lda, n, dsc);
+  else diag_scale_kernel<false><<<grid1(n), 256, 0, s>>>(a, lda, n, dsc);
+  {
+    const int64_t nt = ceil_div(n, TS);
+    if (upper) convert_scaled_kernel<true><<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(a, lda, n, dsc, af, ldf);
+    else convert_scaled_kernel<false><<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(a, lda, n, dsc, af, ldf);
+  }
+  // 2. low-precision factorisation
+  rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, hi, lo, ldk, st, d_err, s);
+  if (rc) return rc;
+  if ((rc = stamp(1))) return rc;
+  DevStatus hst;
+  GB_CUDA_TRY(cudaMemcpyAsync(&hst, st, sizeof hst, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hst.timeout) return GBLLT_ERR_TIMEOUT;
+  r.info = hst.fail_col >= 0 ? hst.fail_col + 1 : 0;
+  r.factor_ms = elapsed(0, 1);
+
+  bool ok = false;
+  if (r.info == 0) {
+    // 3. refinement: x_0 = 0, r_0 = b
+    sumsq(a, lda, n, n, upper ? 2 : 1, &norms[0]);
+    copy_cols_kernel<<<grid1(n * nrhs), 256, 0, s>>>(b, ldb, n, nrhs, R, n);
+    sumsq(R, n, n, nrhs, 0, &norms[1]);
+    double best = INFINITY;
+    for (int step = 0; step < o.max_steps; ++step) {
+      residual_to_f32_kernel<<<grid1(n * nrhs), 256, 0, s>>>(R, n, n, nrhs, dsc, &norms[1], Rf, n);
+      if ((rc = potrs_dev<float>(false, n, nrhs, af, ldf, Rf, n, s))) return rc;
+      update_x_kernel<<<grid1(n * nrhs), 256, 0, s>>>(Rf, n, n, nrhs, dsc, &norms[1], x, ldx, step == 0);
+      residual();
+      sumsq(R, n, n, nrhs, 0, &norms[1]);
+      sumsq(x, ldx, n, nrhs, 0, &norms[2]);
+      double hn[3];
+      GB_CUDA_TRY(cudaMemcpyAsync(hn, norms, sizeof hn, cudaMemcpyDeviceToHost, s));
+      GB_CUDA_TRY(cudaStreamSynchronize(s));
+      const double be =
+          (hn[0] > 0 && hn[2] > 0) ? sqrt(hn[1]) / (sqrt(hn[0]) * sqrt(hn[2])) : (hn[1] > 0 ? INFINITY : 0.0);
+      r.steps = step + 1;
+      if (step < 16) r.history[step] = be;
+      r.backward_error = be;
+      if (be <= o.tol) {
+        ok = true;
+        break;
+      }
+      if (!(be < 0.5 * best) && step >= 2) break;  // stagnation or divergence
+      if (be < best) best = be;
+    }
+  }
+  if ((rc = stamp(2))) return rc;
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  r.refine_ms = elapsed(1, 2);
+  r.converged = ok ? 1 : 0;
+
+  double* w = nullptr;
+  Free wg{nullptr, s};
+  if (!ok && o.fallback_fp64) {
+    // plain FP64 GPU factorisation of a copy of A (the LAPACK dsposv fallback)
+    if (may_allocate) {
+      if (cudaMallocAsync(&w, (size_t)n * n * 8, s) != cudaSuccess) {
+        cudaGetLastError();
+        return GBLLT_ERR_ALLOC;
+      }
+      wg.p = w;
+    } else if (ws_bytes >= ((used + 255) & ~(size_t)255) + (size_t)n * n * 8) {
+      w = (double*)((char*)ws + ((used + 255) & ~(size_t)255));
+    }
+  }
+  if (w) {
+    GB_CUDA_TRY(cudaMemcpy2DAsync(w, n * 8, a, lda * 8, n * 8, n, cudaMemcpyDeviceToDevice, s));
+    GB_CUDA_TRY(cudaMemsetAsync(&st->fail_col, 0xFF, sizeof(long long), s));
+    if (upper && (rc = transpose_inplace_dev<double>(n, w, n, s))) return rc;
+    if ((rc = potrf_lower_dev<double>(n, w, n, st, s))) return rc;
+    GB_CUDA_TRY(cudaMemcpyAsync(&hst, st, sizeof hst, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    r.used_fallback = 1;
+    if (hst.fail_col >= 0) {
+      r.info = hst.fail_col + 1;
+    } else {
+      r.info = 0;
+      copy_cols_kernel<<<grid1(n * nrhs), 256, 0, s>>>(b, ldb, n, nrhs, x, ldx);
+      if ((rc = potrs_dev<double>(false, n, nrhs, w, n, x, ldx, s))) return rc;
+      residual();
+      sumsq(R, n, n, nrhs, 0, &norms[1]);
+      sumsq(x, ldx, n, nrhs, 0, &norms[2]);
+      sumsq(a, lda, n, n, upper ? 2 : 1, &norms[0]);
+      double hn[3];
+      GB_CUDA_TRY(cudaMemcpyAsync(hn, norms, sizeof hn, cudaMemcpyDeviceToHost, s));
+      GB_CUDA_TRY(cudaStreamSynchronize(s));
+      r.backward_error = sqrt(hn[1]) / (sqrt(hn[0]) * sqrt(hn[2]));
+      r.converged = r.backward_error <= o.tol;
+      ok = true;
+    }
+  }
+  if (rep) *rep = r;
+  GB_CUDA_TRY(cudaGetLastError());
+  if (r.info != 0) return GBLLT_SUCCESS;  // caller reads report->info
+  return ok ? GBLLT_SUCCESS : GBLLT_ERR_NOT_CONVERGED;
+}
+
+int posv_mixed_dev(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
+                   double* x, int64_t ldx, const gbllt_mixed_opts* opts, gbllt_mixed_report* rep, cudaStream_t s) {
+  gbllt_mixed_opts o;
+  if (resolve_mixed_opts(opts, &o)) return -10;
+  const MixedLayout Ly = mixed_layout(n, nrhs, o);
+  void* raw = nullptr;
+  if (cudaMallocAsync(&raw, Ly.bytes, s) != cudaSuccess) {
+    cudaGetLastError();
+    return GBLLT_ERR_ALLOC;
+  }
+  const int rc = posv_mixed_core(upper, n, nrhs, a, lda, b, ldb, x, ldx, o, rep, raw, Ly.bytes, true, s);
+  cudaFreeAsync(raw, s);
+  return rc;
+}
+
+}  // namespace gbllt

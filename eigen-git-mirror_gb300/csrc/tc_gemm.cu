@@ -1,0 +1,360 @@
+// Tensor-core trailing update for the mixed-precision factorisation:
+//
+//     C (fp32, column-major) -= sum_s  A_s * B_s^T          (lower tiles only for a SYRK)
+//
+// This replaces the rank update A22 -= A21 A21^T of llt_inplace::blocked (LLT.h:365 ->
+// GeneralMatrixMatrixTriangular.h:57-194, gebp_kernel GeneralBlockPanelKernel.h:1548+) by
+// Blackwell 5th-generation tensor-core tiles:
+//   - operands are K-major (row r holds its K values contiguously) BF16 or TF32 copies of the
+//     panel, streamed by TMA (cp.async.bulk.tensor, 128-byte swizzle) into a 4-stage shared
+//     memory ring guarded by mbarriers;
+//   - one elected thread issues tcgen05.mma (M = 128, N = 128, K = 16 for bf16 / 8 for tf32),
+//     accumulating in TMEM (128 lanes x 128 fp32 columns);
+//   - four epilogue warps read the accumulator with tcgen05.ld and apply C -= acc with coalesced
+//     column-major loads and stores.
+// Split precision: the K loop runs over up to three segments, each pairing the "hi" or "lo"
+// copy of A with the "hi" or "lo" copy of B (hi = round(x), lo = round(x - hi)), so
+// hi*hi^T + hi*lo^T + lo*hi^T is accumulated in one TMEM tile (Markidis et al. 2018, Ootomo &
+// Yokota 2022: split-precision products).
+//
+// Every mbarrier wait is bounded; on timeout the kernel raises an error flag, waits (bounded)
+// for its own TMA copies, frees its TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "internal.h"
+#include "tc_gemm.h"
+
+namespace gbllt {
+
+namespace {
+
+constexpr int BM = 128;
+constexpr int BN = 128;
+constexpr int STAGES = 4;
+constexpr int ROW_BYTES = 128;                 // one swizzle atom row: 64 bf16 or 32 tf32
+constexpr int A_STAGE = BM * ROW_BYTES;        // 16 KB
+constexpr int B_STAGE = BN * ROW_BYTES;        // 16 KB
+constexpr int SMEM_BYTES = STAGES * (A_STAGE + B_STAGE) + 1024;
+constexpr long long WAIT_LIMIT = 1ll << 26;    // polls of mbarrier.try_wait before giving up
+constexpr unsigned long long WAIT_NS = 2000000000ull;  // or 2 s of wall time, whichever first
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: true when the phase completed; false once WAIT_NS of wall time (or WAIT_LIMIT
+// polls) passed, or when another role of this CTA already gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  const unsigned long long t0 = globaltimer_ns();
+  for (long long i = 0; i < WAIT_LIMIT; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255) == 255) {
+      if (*abort_flag) return false;
+      if (globaltimer_ns() - t0 > WAIT_NS) break;
+    }
+  }
+  *abort_flag = 1;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                   // leading-dimension byte offset (unused for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;         // stride-dimension byte offset
+  d |= (uint64_t)1 << 46;                   // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor: fp32 accumulate, A/B K-major, M = 128, N = BN.
+// fmt: 1 = BF16 (kind::f16), 2 = TF32 (kind::tf32).
+__host__ __device__ constexpr uint32_t instr_desc(uint32_t fmt) {
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+template <int KIND>
+__device__ __forceinline__ void mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  if (KIND == 0) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+  } else {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+  }
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%"
+      "20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct TcParams {
+  float* c;
+  long long ldc;
+  int m, n;            // C is m x n; A rows [a_row0, a_row0 + m), B rows [b_row0, b_row0 + n)
+  int a_row0, b_row0;
+  int k;               // depth of one segment (elements)
+  int nseg;            // 1..3
+  uint32_t seg_mask;   // bit 2s: segment s reads A "lo"; bit 2s+1: segment s reads B "lo"
+  int lower;           // 1: only tiles / entries with global row >= column (SYRK)
+  int mt;              // tiles along m
+  int* err;            // device error word (set to 1 on a timeout)
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(192, 1) tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi,
+                                                           const __grid_constant__ CUtensorMap tm_a_lo,
+                                                           const __grid_constant__ CUtensorMap tm_b_hi,
+                                                           const __grid_constant__ CUtensorMap tm_b_lo,
+                                                           const TcParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full_bar[STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t done_bar;
+  __shared__ uint32_t tmem_base_s;
+  __shared__ volatile int abort_s;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int ti, tj;
+  if (p.lower) lower_tile_coords(blockIdx.x, ti, tj);
+  else { ti = (int)(blockIdx.x % p.mt); tj = (int)(blockIdx.x / p.mt); }
+  const int row0 = ti * BM, col0 = tj * BN;
+
+  constexpr int KE = KIND == 0 ? 64 : 32;   // elements per 128-byte row
+  constexpr int KI = KIND == 0 ? 16 : 8;    // K of one MMA instruction
+  const int kpb = (p.k + KE - 1) / KE;      // k-blocks per segment
+  const int nk = kpb * p.nseg;
+
+  if (threadIdx.x == 0) {
+    abort_s = 0;
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(&done_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_s;
+
+  if (warp == 0 && lane == 0) {
+    // ---- TMA producer
+    int issued = 0;
+    for (int it = 0; it < nk; ++it) {
+      const int s = it % STAGES;
+      const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+      if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_s)) break;
+      const int seg = it / kpb;
+      const int kx = (it % kpb) * KE;
+      const bool alo = (p.seg_mask >> (2 * seg)) & 1u;
+      const bool blo = (p.seg_mask >> (2 * seg + 1)) & 1u;
+      uint8_t* sa = smem + s * (A_STAGE + B_STAGE);
+      uint8_t* sb = sa + A_STAGE;
+      mbar_expect_tx(&full_bar[s], A_STAGE + B_STAGE);
+      tma_load_2d(sa, alo ? &tm_a_lo : &tm_a_hi, &full_bar[s], kx, p.a_row0 + row0);
+      tma_load_2d(sb, blo ? &tm_b_lo : &tm_b_hi, &full_bar[s], kx, p.b_row0 + col0);
+      issued = it + 1;
+    }
+    if (abort_s) {
+      // let the copies this thread started land before the CTA exits (bounded)
+      for (int it = issued - STAGES < 0 ? 0 : issued - STAGES; it < issued; ++it) {
+        volatile int dummy = 0;
+        mbar_wait(&full_bar[it % STAGES], (uint32_t)(it / STAGES) & 1u, &dummy);
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer
+    constexpr uint32_t idesc = instr_desc(KIND == 0 ? 1u : 2u);
+    bool ok = true;
+    for (int it = 0; it < nk; ++it) {
+      const int s = it % STAGES;
+      const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+      if (!mbar_wait(&full_bar[s], ph, &abort_s)) { ok = false; break; }
+      tc_fence_after();
+      const uint32_t sa = smem_u32(smem + s * (A_STAGE + B_STAGE));
+      const uint64_t ad = sw128_desc(sa), bd = sw128_desc(sa + A_STAGE);
+#pragma unroll
+      for (int j = 0; j < ROW_BYTES / (KI * (KIND == 0 ? 2 : 4)); ++j) {
+        // advance 32 bytes along K inside the swizzle atom: +2 in the (addr >> 4) field
+        mma<KIND>(tmem, ad + 2 * j, bd + 2 * j, idesc, (it > 0 || j > 0) ? 1u : 0u);
+      }
+      mma_commit(&empty_bar[s]);
+    }
+    if (ok) mma_commit(&done_bar);
+  } else if (warp >= 2) {
+    // ---- epilogue: C -= acc
+    const int q = warp & 3;                 // TMEM lane quadrant this warp may access
+    const int r = q * 32 + lane;            // tile row
+    const long long gi = (long long)row0 + r;
+    const bool ok = mbar_wait(&done_bar, 0, &abort_s);
+    tc_fence_after();
+    if (ok && !abort_s) {
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+        if (gi < p.m) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const long long gj = (long long)col0 + c0 + j;
+            if (gj < p.n && (!p.lower || gi >= gj)) {
+              float* cp = p.c + gj * p.ldc + gi;
+              *cp = *cp - v[j];
+            }
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0 && abort_s) atomicExch(p.err, 1);
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+  }
+  return fn;
+}
+
+// 2-D map over a K-major operand: `rows` rows of `k` elements, `ld` elements apart.
+int make_map(CUtensorMap* m, const void* base, int kind, int64_t rows, int64_t k, int64_t ld) {
+  auto fn = encode_fn();
+  if (!fn) return GBLLT_ERR_INTERNAL;
+  const int es = kind == 0 ? 2 : 4;
+  cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * es)};
+  cuuint32_t box[2] = {(cuuint32_t)(ROW_BYTES / es), (cuuint32_t)BM};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, kind == 0 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                  const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? GBLLT_SUCCESS : GBLLT_ERR_INTERNAL;
+}
+
+}  // namespace
+
+int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32_t seg_mask, float* c, int64_t ldc,
+              int64_t m, int64_t n, bool lower, int* d_err, cudaStream_t s) {
+  if (m <= 0 || n <= 0 || a.k <= 0) return GBLLT_SUCCESS;
+  if ((a.ld * (kind == 0 ? 2 : 4)) % 16 != 0 || ((uintptr_t)a.hi & 15) || ((uintptr_t)b.hi & 15))
+    return GBLLT_ERR_INTERNAL;
+  CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo;
+  int rc;
+  if ((rc = make_map(&ma_hi, a.hi, kind, a.rows, a.k, a.ld))) return rc;
+  if ((rc = make_map(&ma_lo, a.lo ? a.lo : a.hi, kind, a.rows, a.k, a.ld))) return rc;
+  if ((rc = make_map(&mb_hi, b.hi, kind, b.rows, b.k, b.ld))) return rc;
+  if ((rc = make_map(&mb_lo, b.lo ? b.lo : b.hi, kind, b.rows, b.k, b.ld))) return rc;
+  TcParams p;
+  p.c = c;
+  p.ldc = ldc;
+  p.m = (int)m;
+  p.n = (int)n;
+  p.a_row0 = (int)a.row0;
+  p.b_row0 = (int)b.row0;
+  p.k = (int)a.k;
+  p.nseg = nseg;
+  p.seg_mask = seg_mask;
+  p.lower = lower ? 1 : 0;
+  p.mt = (int)ceil_div(m, BM);
+  p.err = d_err;
+  const int64_t nt = ceil_div(n, BN);
+  const int64_t tiles = lower ? (int64_t)p.mt * (p.mt + 1) / 2 : (int64_t)p.mt * nt;
+  static bool attr_set[2] = {false, false};
+  static const std::string kname[2] = {"tc_update_bf16", "tc_update_tf32"};
+  // algorithmic work: 2 k flops per updated entry and segment; operands read once, C read+written
+  const double entries = lower ? (double)m * (m + 1) / 2.0 : (double)m * n;
+  ProfScope ps(kname[kind].c_str(), s, 2.0 * entries * a.k * nseg,
+               ((double)(m + (lower ? 0 : n)) * a.k * nseg * (kind == 0 ? 2 : 4)) + entries * 8.0);
+  if (kind == 0) {
+    if (!attr_set[0]) {
+      GB_CUDA_TRY(cudaFuncSetAttribute(tc_update_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+      attr_set[0] = true;
+    }
+    tc_update_kernel<0><<<(unsigned)tiles, 192, SMEM_BYTES, s>>>(ma_hi, ma_lo, mb_hi, mb_lo, p);
+  } else {
+    if (!attr_set[1]) {
+      GB_CUDA_TRY(cudaFuncSetAttribute(tc_update_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+      attr_set[1] = true;
+    }
+    tc_update_kernel<1><<<(unsigned)tiles, 192, SMEM_BYTES, s>>>(ma_hi, ma_lo, mb_hi, mb_lo, p);
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+}  // namespace gbllt

@@ -48,6 +48,8 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_spotrf_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
     "gbllt_dpotrs_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp]),
     "gbllt_spotrs_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp]),
+    "gbllt_dposv_mixed_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _vp]),
+    "gbllt_dposv_mixed": (_int, [_int, _ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp]),
     "gbllt_profile_enable": (_int, [_int]),
     "gbllt_profile_read": (_int, [_vp, _int, ctypes.POINTER(_int)]),
 }
@@ -58,6 +60,32 @@ _lib = None
 class KernelStat(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 40), ("launches", ctypes.c_int64), ("ms", ctypes.c_double),
                 ("flops", ctypes.c_double), ("bytes", ctypes.c_double)]
+
+
+PREC = {"fp32": 0, "tf32": 1, "tf32x3": 2, "bf16": 3, "bf16x3": 4}
+
+
+class MixedOpts(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("max_steps", ctypes.c_int), ("tol", ctypes.c_double),
+                ("fallback_fp64", ctypes.c_int), ("panel", ctypes.c_int)]
+
+
+class MixedReport(ctypes.Structure):
+    _fields_ = [("info", ctypes.c_int64), ("steps", ctypes.c_int), ("converged", ctypes.c_int),
+                ("used_fallback", ctypes.c_int), ("backward_error", ctypes.c_double),
+                ("factor_ms", ctypes.c_double), ("refine_ms", ctypes.c_double),
+                ("history", ctypes.c_double * 16)]
+
+    def as_dict(self) -> dict:
+        return {"info": int(self.info), "steps": int(self.steps), "converged": bool(self.converged),
+                "used_fallback": bool(self.used_fallback), "backward_error": float(self.backward_error),
+                "factor_ms": float(self.factor_ms), "refine_ms": float(self.refine_ms),
+                "history": [float(self.history[i]) for i in range(min(int(self.steps), 16))]}
+
+
+def mixed_opts(precision: str = "tf32x3", max_steps: int = 10, tol: float = 1e-14, fallback: bool = True,
+               panel: int = 256) -> MixedOpts:
+    return MixedOpts(PREC[precision], max_steps, tol, 1 if fallback else 0, panel)
 
 
 class GblltError(RuntimeError):
@@ -150,6 +178,30 @@ def potrs_dev(a_cm, n: int, lda: int, b_cm, nrhs: int, ldb: int, uplo: str = "L"
     import torch
     fn = "gbllt_dpotrs_dev" if a_cm.dtype == torch.float64 else "gbllt_spotrs_dev"
     check(fn, getattr(lib(), fn)(_uplo(uplo), n, nrhs, _ptr(a_cm), lda, _ptr(b_cm), ldb, stream))
+
+
+def posv_mixed_dev(a_cm, n: int, lda: int, b_cm, ldb: int, x_cm, ldx: int, nrhs: int, opts: MixedOpts | None = None,
+                   uplo: str = "L", stream: int = 0, raise_on_error: bool = True) -> tuple[int, dict]:
+    """Mixed-precision solve with FP64 refinement on device buffers; returns (rc, report)."""
+    rep = MixedReport()
+    rc = lib().gbllt_dposv_mixed_dev(_uplo(uplo), n, nrhs, _ptr(a_cm), lda, _ptr(b_cm), ldb, _ptr(x_cm), ldx,
+                                     ctypes.byref(opts) if opts is not None else None, ctypes.byref(rep), stream)
+    if raise_on_error and rc not in (SUCCESS, ERR_NOT_CONVERGED):
+        check("gbllt_dposv_mixed_dev", rc)
+    return rc, rep.as_dict()
+
+
+def posv_mixed(a: np.ndarray, b: np.ndarray, opts: MixedOpts | None = None, uplo: str = "L") -> tuple[np.ndarray, int, dict]:
+    """Host-pointer mixed-precision solve (Fortran-order float64 arrays); returns (x, rc, report)."""
+    n = a.shape[0]
+    k = 1 if b.ndim == 1 else b.shape[1]
+    x = np.zeros_like(b, order="F")
+    rep = MixedReport()
+    rc = lib().gbllt_dposv_mixed(COL_MAJOR, _uplo(uplo), n, k, _ptr(a), max(1, n), _ptr(b), max(1, n), _ptr(x),
+                                 max(1, n), ctypes.byref(opts) if opts is not None else None, ctypes.byref(rep))
+    if rc not in (SUCCESS, ERR_NOT_CONVERGED):
+        check("gbllt_dposv_mixed", rc)
+    return x, rc, rep.as_dict()
 
 
 # ---- diagnostics -------------------------------------------------------------------------------

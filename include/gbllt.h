@@ -94,6 +94,50 @@ GBLLT_API int gbllt_dpotrs_dev(char uplo, int64_t n, int64_t nrhs, const double*
 GBLLT_API int gbllt_spotrs_dev(char uplo, int64_t n, int64_t nrhs, const float* d_a, int64_t lda, float* d_b,
                      int64_t ldb, void* stream);
 
+/* ---- Mixed precision with FP64 iterative refinement ---------------------------------------
+ * Solves A X = B to FP64 accuracy (normwise backward error <= tol) from a low-precision
+ * factorisation: A is scaled to unit diagonal and rounded to FP32, the trailing updates of the
+ * blocked factorisation run on tensor cores in the chosen precision with FP32 accumulation, the
+ * 64 x 64 diagonal blocks are factored in FP64, and residuals r = B - A X are formed in FP64 from
+ * the stored triangle of A.  Replaces LLT<MatrixXd>::compute followed by solve
+ * (Eigen/src/Cholesky/LLT.h:430-460, :483-498) for callers that need the solution, not the factor;
+ * it is the counterpart of LAPACK's dsposv.  A and B are not modified. */
+#define GBLLT_PREC_FP32 0   /* trailing update on FP32 CUDA cores (no tensor cores) */
+#define GBLLT_PREC_TF32 1   /* one TF32 product per update */
+#define GBLLT_PREC_TF32X3 2 /* three TF32 products (hi*hi + hi*lo + lo*hi): ~FP32 accuracy */
+#define GBLLT_PREC_BF16 3   /* one BF16 product per update */
+#define GBLLT_PREC_BF16X3 4 /* three BF16 products */
+
+typedef struct {
+  int precision;     /* GBLLT_PREC_*; default GBLLT_PREC_TF32X3 when opts == NULL */
+  int max_steps;     /* refinement steps (solves with the low-precision factor); <= 0 -> 10, max 16 */
+  double tol;        /* target normwise backward error; <= 0 -> 1e-14 */
+  int fallback_fp64; /* when refinement fails, solve with the plain FP64 GPU factorisation */
+  int panel;         /* outer panel width, a multiple of 64; <= 0 -> 256 */
+} gbllt_mixed_opts;
+
+typedef struct {
+  int64_t info;          /* LAPACK info of the factorisation that produced X (0 = ok) */
+  int steps;             /* refinement steps taken */
+  int converged;         /* backward error of X <= tol */
+  int used_fallback;     /* X came from the plain FP64 factorisation */
+  double backward_error; /* ||B - A X||_F / (||A||_F ||X||_F) of the returned X */
+  double factor_ms;      /* device time of scaling + low-precision factorisation */
+  double refine_ms;      /* device time of the refinement loop */
+  double history[16];    /* backward error after each refinement step */
+} gbllt_mixed_report;
+
+/* Device pointers, column-major; X is n x nrhs (ldx >= n).  Synchronises `stream` once per
+ * refinement step to test convergence.  Returns GBLLT_ERR_NOT_CONVERGED (X = last iterate) when the
+ * tolerance was not reached and no fallback was requested. */
+GBLLT_API int gbllt_dposv_mixed_dev(char uplo, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
+                                    const double* d_b, int64_t ldb, double* d_x, int64_t ldx,
+                                    const gbllt_mixed_opts* opts, gbllt_mixed_report* report, void* stream);
+/* Host pointers (LAPACKE-style layout), synchronous. */
+GBLLT_API int gbllt_dposv_mixed(int layout, char uplo, int64_t n, int64_t nrhs, const double* a, int64_t lda,
+                                const double* b, int64_t ldb, double* x, int64_t ldx, const gbllt_mixed_opts* opts,
+                                gbllt_mixed_report* report);
+
 /* ---- Diagnostics (no counterpart in the reference; Eigen has no built-in timers) ----------- */
 
 /* Per-kernel-class totals: launches, device time (CUDA events on the launch stream) and the
