@@ -21,6 +21,8 @@ void set_last_error(cudaError_t e, const char* what, const char* file, int line)
   g_last_error = buf;
 }
 
+void set_error_message(const char* msg) { g_last_error = msg; }
+
 int ensure_device() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {

@@ -29,6 +29,7 @@ struct DevStatus {
   } while (0)
 
 void set_last_error(cudaError_t e, const char* what, const char* file, int line);
+void set_error_message(const char* msg);
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

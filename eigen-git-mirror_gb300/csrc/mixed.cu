@@ -116,14 +116,18 @@ __device__ __forceinline__ bool stored(long long i, long long j) {
   return UP ? (i <= j) : (i >= j);
 }
 
-template <bool UP>
+template <bool UP, int NR>
 __global__ void __launch_bounds__(256) symm_partial_kernel(const double* __restrict__ a, long long lda, long long n,
                                                            const double* __restrict__ x, long long ldx, long long nrhs,
                                                            int jpc, double* __restrict__ part) {
+  // NR = 16: 4 thread groups x 4 right-hand sides each, every thread sums the full tile depth.
+  // NR = 1: one right-hand side; the 4 thread groups each sum a quarter of the tile depth and
+  //         the quarters are added in shared memory (no FP64 work on absent columns).
   __shared__ double As[RB][RB + 1];  // As[p][r] = A(I + r, J + p)
-  __shared__ double Xs[RB][RCH + 1];
+  __shared__ double Xs[RB][NR + 1];
+  __shared__ double red[4][RB];
   const long long I = (long long)blockIdx.x * RB;
-  const long long c0 = (long long)blockIdx.z * RCH;
+  const long long c0 = (long long)blockIdx.z * NR;
   const int nb = (int)((n + RB - 1) / RB);
   const int jb0 = blockIdx.y * jpc;
   const int jb1 = min(nb, jb0 + jpc);
@@ -143,19 +147,29 @@ __global__ void __launch_bounds__(256) symm_partial_kernel(const double* __restr
       if (gi < n && gj < n) v = stored<UP>(gi, gj) ? a[gj * lda + gi] : a[gi * lda + gj];
       As[p][rr] = v;
     }
-    for (int idx = tid; idx < RB * RCH; idx += 256) {
+    for (int idx = tid; idx < RB * NR; idx += 256) {
       const int p = idx & 63, c = idx >> 6;
       Xs[p][c] = (J + p < n && c0 + c < nrhs) ? x[(c0 + c) * ldx + J + p] : 0.0;
     }
     __syncthreads();
-    for (int p = 0; p < RB; ++p) {
-      const double l = As[p][r];
+    if (NR == 1) {
+#pragma unroll 4
+      for (int p = cq * 16; p < cq * 16 + 16; ++p) acc[0] = fma(As[p][r], Xs[p][0], acc[0]);
+    } else {
+      for (int p = 0; p < RB; ++p) {
+        const double l = As[p][r];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) acc[q] = fma(l, Xs[p][cq * 4 + q], acc[q]);
+        for (int q = 0; q < 4; ++q) acc[q] = fma(l, Xs[p][(cq * 4 + q) % NR], acc[q]);
+      }
     }
     __syncthreads();
   }
-  if (I + r < n) {
+  if (NR == 1) {
+    red[cq][r] = acc[0];
+    __syncthreads();
+    if (cq == 0 && I + r < n && c0 < nrhs)
+      part[((long long)blockIdx.y * nrhs + c0) * n + I + r] = (red[0][r] + red[1][r]) + (red[2][r] + red[3][r]);
+  } else if (I + r < n) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const long long c = c0 + cq * 4 + q;
@@ -185,10 +199,11 @@ __global__ void __launch_bounds__(256) sumsq_kernel(const double* __restrict__ a
   const long long total = m * k;
   for (long long idx = (long long)blockIdx.x * 256 + threadIdx.x; idx < total; idx += (long long)gridDim.x * 256) {
     const long long j = idx / m, i = idx % m;
+    // the triangle that is not stored is never read (it may hold anything, NaN included)
+    const bool in = mode == 0 || (mode == 1 ? i >= j : i <= j);
+    if (!in) continue;
     const double v = a[j * ld + i];
-    if (mode == 0) s += v * v;
-    else if (mode == 1) s += (i > j ? 2.0 : i == j ? 1.0 : 0.0) * v * v;
-    else s += (i < j ? 2.0 : i == j ? 1.0 : 0.0) * v * v;
+    s += (mode == 0 || i == j ? 1.0 : 2.0) * v * v;
   }
   red[threadIdx.x] = s;
   __syncthreads();
@@ -404,11 +419,17 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     sum_parts_kernel<<<1, 256, 0, s>>>(sq, blocks, out);
   };
   auto residual = [&]() {  // R = B - A X
-    dim3 grid((unsigned)nb, (unsigned)nparts, (unsigned)zc);
     static const std::string kr = "symm_residual_f64";
     ProfScope ps(kr.c_str(), s, 2.0 * n * n * nrhs, (double)n * n * 8.0 + 3.0 * n * nrhs * 8.0);
-    if (upper) symm_partial_kernel<true><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
-    else symm_partial_kernel<false><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
+    if (nrhs == 1) {
+      dim3 grid((unsigned)nb, (unsigned)nparts, 1);
+      if (upper) symm_partial_kernel<true, 1><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
+      else symm_partial_kernel<false, 1><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
+    } else {
+      dim3 grid((unsigned)nb, (unsigned)nparts, (unsigned)zc);
+      if (upper) symm_partial_kernel<true, RCH><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
+      else symm_partial_kernel<false, RCH><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
+    }
     residual_reduce_kernel<<<grid1(n * nrhs), 256, 0, s>>>(part, nparts, n, nrhs, b, ldb, R, n);
   };
 

@@ -250,21 +250,27 @@ __global__ void __launch_bounds__(192, 1) tc_update_kernel(const __grid_constant
     const int q = warp & 3;                 // TMEM lane quadrant this warp may access
     const int r = q * 32 + lane;            // tile row
     const long long gi = (long long)row0 + r;
+    // While the main loop runs, fetch this thread's row of the C tile into registers (all loads
+    // independent, so they overlap); each load is coalesced across the warp (consecutive rows).
+    float cv[BN];
+    const bool row_ok = gi < p.m;
+#pragma unroll
+    for (int j = 0; j < BN; ++j) {
+      const long long gj = (long long)col0 + j;
+      cv[j] = (row_ok && gj < p.n && (!p.lower || gi >= gj)) ? p.c[gj * p.ldc + gi] : 0.f;
+    }
     const bool ok = mbar_wait(&done_bar, 0, &abort_s);
     tc_fence_after();
     if (ok && !abort_s) {
-#pragma unroll 1
+#pragma unroll
       for (int c0 = 0; c0 < BN; c0 += 32) {
         float v[32];
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
-        if (gi < p.m) {
+        if (row_ok) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const long long gj = (long long)col0 + c0 + j;
-            if (gj < p.n && (!p.lower || gi >= gj)) {
-              float* cp = p.c + gj * p.ldc + gi;
-              *cp = *cp - v[j];
-            }
+            if (gj < p.n && (!p.lower || gi >= gj)) p.c[gj * p.ldc + gi] = cv[c0 + j] - v[j];
           }
         }
       }

@@ -1,0 +1,48 @@
+/* Test double of libgbllt for checking include/eigen_gb300/LLT_GB300.h on a machine without a GPU.
+ *
+ * TEST INFRASTRUCTURE ONLY.  It implements the four entry points the Eigen header calls by
+ * forwarding to the oracle (oracle/llt_oracle.c), applying the same layout rule as the real
+ * library (a row-major factor with uplo 'L' is a column-major one with uplo 'U'), and counts the
+ * calls so that a test can prove the specialisations were selected.  It never ships. */
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/gbllt.h"
+
+int oracle_dpotrf(char uplo, int64_t n, double* a, int64_t lda, int64_t* info);
+int oracle_spotrf(char uplo, int64_t n, float* a, int64_t lda, int64_t* info);
+int oracle_dpotrs(char uplo, int64_t n, int64_t nrhs, const double* a, int64_t lda, double* b, int64_t ldb);
+int oracle_spotrs(char uplo, int64_t n, int64_t nrhs, const float* a, int64_t lda, float* b, int64_t ldb);
+
+long fake_calls[4];
+
+static char eff_uplo(int layout, char uplo) {
+  const int up = uplo == 'U' || uplo == 'u';
+  return (layout == GBLLT_ROW_MAJOR) ? (up ? 'L' : 'U') : (up ? 'U' : 'L');
+}
+
+const char* gbllt_last_error(void) { return "fake"; }
+int gbllt_dpotrf(int layout, char uplo, int64_t n, double* a, int64_t lda, int64_t* info) {
+  ++fake_calls[0];
+  return oracle_dpotrf(eff_uplo(layout, uplo), n, a, lda, info);
+}
+int gbllt_spotrf(int layout, char uplo, int64_t n, float* a, int64_t lda, int64_t* info) {
+  ++fake_calls[1];
+  return oracle_spotrf(eff_uplo(layout, uplo), n, a, lda, info);
+}
+int gbllt_dpotrs(int layout, char uplo, int64_t n, int64_t nrhs, const double* a, int64_t lda, double* b, int64_t ldb) {
+  ++fake_calls[2];
+  if (layout != GBLLT_COL_MAJOR) return -1;
+  return oracle_dpotrs(uplo, n, nrhs, a, lda, b, ldb);
+}
+int gbllt_spotrs(int layout, char uplo, int64_t n, int64_t nrhs, const float* a, int64_t lda, float* b, int64_t ldb) {
+  ++fake_calls[3];
+  if (layout != GBLLT_COL_MAJOR) return -1;
+  return oracle_spotrs(uplo, n, nrhs, a, lda, b, ldb);
+}
+
+/* Prints the call counts at exit so that the test can check the backend was used. */
+__attribute__((destructor)) static void fake_report(void) {
+  fprintf(stderr, "fake_gbllt calls: dpotrf=%ld spotrf=%ld dpotrs=%ld spotrs=%ld\n", fake_calls[0], fake_calls[1],
+          fake_calls[2], fake_calls[3]);
+}

@@ -1,0 +1,110 @@
+"""Mixed-precision solve with FP64 iterative refinement (gbllt_dposv_mixed[_dev]) against the
+FP64 oracle.
+
+Bar: the returned X has normwise backward error ||AX-B||_F/(||A||_F ||X||_F) <= 1e-14, measured
+independently by the oracle (double-double residual), and agrees with the oracle's FP64 solution
+to within kappa * 1e-13 (relative Frobenius; the forward error of any solution with backward error
+1e-14 is bounded by a small multiple of kappa * 1e-14), where kappa is the condition number of
+the seeded Householder-spectrum matrix.  Which low precisions must converge without the FP64 fallback follows
+the usual IR condition kappa * u_factor < 1: every precision at kappa = 1e2; FP32, TF32x3, BF16x3
+and TF32 at 1e4; FP32, TF32x3 and BF16x3 at 1e6.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PRECS = ["fp32", "tf32", "tf32x3", "bf16", "bf16x3"]
+MUST_CONVERGE = {1e2: set(PRECS), 1e4: {"fp32", "tf32", "tf32x3", "bf16x3"}, 1e6: {"fp32", "tf32x3", "bf16x3"}}
+
+
+def _dev_solve(gbllt, a, b, opts, uplo="L"):
+    import torch
+    n, k = a.shape[0], b.shape[1]
+    A = torch.from_numpy(np.ascontiguousarray(a.T)).cuda()
+    B = torch.from_numpy(np.ascontiguousarray(b.T)).cuda()
+    X = torch.zeros_like(B)
+    rc, rep = gbllt.posv_mixed_dev(A, n, n, B, n, X, n, k, opts, uplo, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return rc, rep, np.asfortranarray(X.cpu().numpy().T)
+
+
+@pytest.fixture(scope="module")
+def spectra(oracle):
+    n = 1536
+    return {kappa: oracle.gen_householder(n, kappa) for kappa in (1e2, 1e4, 1e6)}
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e4, 1e6])
+@pytest.mark.parametrize("prec", PRECS)
+def test_mixed_refines_to_fp64(oracle, gbllt, spectra, kappa, prec):
+    pytest.importorskip("torch")
+    a = spectra[kappa]
+    n = a.shape[0]
+    b = np.asfortranarray(oracle.normal(12, n * 2).reshape(n, 2, order="F"))
+    _, xr, info = oracle.solve(a, b)
+    assert info == 0
+    # without fallback: the low precision alone must get there where the theory says it can
+    rc, rep, x = _dev_solve(gbllt, a, b, gbllt.mixed_opts(prec, 10, 1e-14, fallback=False))
+    if prec in MUST_CONVERGE[kappa]:
+        assert rc == gbllt.SUCCESS and rep["converged"] and not rep["used_fallback"], rep
+        assert rep["steps"] <= 10
+        assert oracle.backward_error(a, x, b) <= 1e-14
+        assert np.linalg.norm(x - xr) / np.linalg.norm(xr) <= kappa * 1e-13
+        # the first step already reflects the factor's precision (a broken tensor-core update would not)
+        first = {"fp32": 1e-7, "tf32": 1e-5, "tf32x3": 1e-7, "bf16": 1e-4, "bf16x3": 1e-7}[prec]
+        assert rep["history"][0] <= first * max(1.0, kappa / 1e2)
+    # with fallback: always FP64-accurate
+    rc, rep, x = _dev_solve(gbllt, a, b, gbllt.mixed_opts(prec, 10, 1e-14, fallback=True))
+    assert rc == gbllt.SUCCESS and rep["info"] == 0, rep
+    assert oracle.backward_error(a, x, b) <= 1e-14
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) <= kappa * 1e-13
+
+
+@pytest.mark.parametrize("n", [1, 7, 64, 200, 257, 300, 700])
+@pytest.mark.parametrize("nrhs", [1, 3, 17])
+def test_mixed_sizes(oracle, gbllt, n, nrhs):
+    pytest.importorskip("torch")
+    a = oracle.gen_gram(n, seed=60 + n)
+    b = np.asfortranarray(oracle.normal(61, n * nrhs).reshape(n, nrhs, order="F"))
+    rc, rep, x = _dev_solve(gbllt, a, b, gbllt.mixed_opts("tf32x3", 10, 1e-14, fallback=False))
+    assert rc == gbllt.SUCCESS and rep["converged"], rep
+    assert oracle.backward_error(a, x, b) <= 1e-14
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3"])
+def test_mixed_upper_and_host_api(oracle, gbllt, prec):
+    n, k = 900, 2
+    a = oracle.gen_householder(n, 1e4)
+    b = np.asfortranarray(oracle.normal(70, n * k).reshape(n, k, order="F"))
+    up = np.array(a, order="F")
+    up[np.tril_indices(n, -1)] = np.nan  # only the upper triangle may be read
+    rc, rep, x = _dev_solve(gbllt, up, b, gbllt.mixed_opts(prec, 10, 1e-14, fallback=False), uplo="U")
+    assert rc == gbllt.SUCCESS and rep["converged"], rep
+    assert oracle.backward_error(a, x, b) <= 1e-14
+    lo = np.array(a, order="F")
+    lo[np.triu_indices(n, 1)] = np.nan  # only the lower triangle may be read
+    xh, rc, rep = gbllt.posv_mixed(lo, b, gbllt.mixed_opts(prec, 10, 1e-14, fallback=False), "L")
+    assert rc == gbllt.SUCCESS and rep["converged"], rep
+    assert oracle.backward_error(a, xh, b) <= 1e-14
+    # row-major storage through the host entry point
+    arow = np.ascontiguousarray(a)
+    brow = np.ascontiguousarray(b)
+    xrow = np.zeros_like(brow)
+    r = gbllt.MixedReport()
+    opts = gbllt.mixed_opts(prec, 10, 1e-14, fallback=False)
+    rc = gbllt.lib().gbllt_dposv_mixed(gbllt.ROW_MAJOR, b"L", n, k, arow.ctypes.data, n, brow.ctypes.data, k,
+                                       xrow.ctypes.data, k, ctypes.byref(opts), ctypes.byref(r))
+    assert rc == gbllt.SUCCESS and r.converged
+    assert oracle.backward_error(a, np.asfortranarray(xrow), b) <= 1e-14
+
+
+def test_mixed_not_positive_definite(oracle, gbllt):
+    n = 500
+    a = oracle.gen_gram(n, seed=4)
+    a[123, 123] = -5.0
+    b = np.asfortranarray(oracle.normal(5, n).reshape(n, 1))
+    rc, rep, x = _dev_solve(gbllt, a, b, gbllt.mixed_opts("tf32x3", 10, 1e-14, fallback=True))
+    assert rc == gbllt.SUCCESS and rep["info"] == 124 and rep["used_fallback"]
