@@ -23,6 +23,7 @@ ERR_TIMEOUT = -1003
 ERR_NO_DEVICE = -1004
 ERR_INTERNAL = -1005
 ERR_NOT_CONVERGED = -1006
+ERR_SCRATCH_LIMIT = -1007
 ROW_MAJOR = 101
 COL_MAJOR = 102
 
@@ -50,6 +51,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_spotrs_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp]),
     "gbllt_dposv_mixed_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _vp]),
     "gbllt_dposv_mixed": (_int, [_int, _ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp]),
+    "gbllt_dposv_mixed_dev_noalloc": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _vp]),
     "gbllt_profile_enable": (_int, [_int]),
     "gbllt_profile_read": (_int, [_vp, _int, ctypes.POINTER(_int)]),
 }

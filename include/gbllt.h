@@ -138,6 +138,23 @@ GBLLT_API int gbllt_dposv_mixed(int layout, char uplo, int64_t n, int64_t nrhs, 
                                 const double* b, int64_t ldb, double* x, int64_t ldx, const gbllt_mixed_opts* opts,
                                 gbllt_mixed_report* report);
 
+/* Same solve as gbllt_dposv_mixed_dev, for callers that cannot let the library allocate device
+ * memory (their memory is owned by their own allocator or budget, or they must not allocate while
+ * a stream is being captured).  No counterpart in the reference: Eigen's LLT allocates on the host
+ * as it pleases.  This entry point calls no cudaMalloc / cudaMallocAsync / cudaFree: its scratch is a
+ * fixed 64 MiB area inside the library image, held by every GPU that loads the library until the
+ * process exits.  That is enough for n <= 2048 with up to 64 right-hand sides including the FP64
+ * fallback; larger problems are rejected with GBLLT_ERR_SCRATCH_LIMIT (gbllt_last_error() says how
+ * much scratch they need).  The first call on a device looks up the area's device address; make
+ * that first call before any stream capture.  All calls share the area: calls whose GPU work
+ * overlaps race and must be serialised by the caller.  No device times are reported
+ * (factor_ms = refine_ms = 0). */
+#define GBLLT_ERR_SCRATCH_LIMIT (-1007)
+GBLLT_API int gbllt_dposv_mixed_dev_noalloc(char uplo, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
+                                            const double* d_b, int64_t ldb, double* d_x, int64_t ldx,
+                                            const gbllt_mixed_opts* opts, gbllt_mixed_report* report,
+                                            void* stream);
+
 /* ---- Diagnostics (no counterpart in the reference; Eigen has no built-in timers) ----------- */
 
 /* Per-kernel-class totals: launches, device time (CUDA events on the launch stream) and the
