@@ -236,119 +236,207 @@ def run_reference(args, ws, rank):
 
 # ---- GPU arm ------------------------------------------------------------------------------------
 
+def measured_peaks() -> dict:
+    """Roofline denominators: HBM and BF16 from MEASURED_PEAKS.json (measured on this machine),
+    FP64 and TF32 measured here with cuBLAS (they are not in that file)."""
+    import torch
+    out = {"fp64_tflops": fp64_peak_tflops(), "source": {}}
+    out["source"]["fp64_tflops"] = "cuBLAS DGEMM 4096^3, best of 3, this run"
+    n = 8192
+    a = torch.randn(n, n, device="cuda")
+    b = torch.randn(n, n, device="cuda")
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    a @ b
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 1e9
+    for _ in range(3):
+        e0.record()
+        a @ b
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    torch.backends.cuda.matmul.allow_tf32 = old
+    out["tf32_tflops"] = 2.0 * n ** 3 / (best * 1e-3) / 1e12
+    out["source"]["tf32_tflops"] = "cuBLAS TF32 GEMM 8192^3, best of 3, this run"
+    mp = ROOT / "MEASURED_PEAKS.json"
+    if mp.exists():
+        d = json.loads(mp.read_text())
+        out["hbm_gbs"], out["bf16_tflops"] = d["hbm_gbs"], d["bf16_tflops"]
+        out["source"]["hbm_gbs"] = out["source"]["bf16_tflops"] = "of measured (MEASURED_PEAKS.json)"
+    else:
+        out["hbm_gbs"], out["bf16_tflops"] = 6800.0, 1900.0
+        out["source"]["hbm_gbs"] = out["source"]["bf16_tflops"] = "of fallback"
+    return out
+
+
+def roofline_for(name: str, st: dict, peaks: dict) -> dict:
+    """Achieved = algorithmic work of the kernel's launches / their summed device time."""
+    ms = max(st["ms"], 1e-9)
+    if name.startswith("tc_update_tf32"):
+        bound, unit, peak, src = "tensor", "TFLOP/s", peaks["tf32_tflops"], peaks["source"]["tf32_tflops"]
+        ach = st["flops"] / ms / 1e9
+    elif name.startswith("tc_update_bf16"):
+        bound, unit, peak, src = "tensor", "TFLOP/s", peaks["bf16_tflops"], peaks["source"]["bf16_tflops"]
+        ach = st["flops"] / ms / 1e9
+    elif name.endswith("_f64") and st["flops"] > 0 and not name.startswith(("trsv", "split", "transpose")):
+        bound, unit, peak, src = "tensor", "TFLOP/s", peaks["fp64_tflops"], peaks["source"]["fp64_tflops"] + \
+            " (FP64 pipe: DFMA and DMMA run at the same rate on GB300)"
+        ach = st["flops"] / ms / 1e9
+    else:
+        bound, unit, peak, src = "hbm", "GB/s", peaks["hbm_gbs"], peaks["source"]["hbm_gbs"]
+        ach = st["bytes"] / ms / 1e6
+    return {"kernel": name, "bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
+            "traffic": None, "launches": st["launches"], "per_launch_flops": st["flops"] / st["launches"],
+            "per_launch_bytes": st["bytes"] / st["launches"], "peak_source": src}
+
+
 def run_ours(args, ws, rank, local):
+    import ctypes
     import torch
     import gbllt as G
 
     torch.cuda.set_device(local)
-    cfg = CONFIGS[args.config]
+    cfg = dict(CONFIGS[args.config])
+    if args.n:
+        cfg["n"] = args.n
+        cfg["workload"] += f" (n overridden to {args.n})"
     n, k = cfg["n"], cfg["nrhs"]
+    flops = llt_flops(n, k)
     A0, B0 = make_inputs_gpu(cfg, seed=1 + rank)
     A = torch.empty_like(A0)
     B = torch.empty_like(B0)
+    X = torch.zeros_like(B0)
     info = torch.zeros(1, dtype=torch.int64, device="cuda")
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
+    opts = G.mixed_opts(args.mixed_precision, 10, 1e-14, fallback=False)
+    reports = []
 
-    def step():
+    def step_fp64():
         with torch.cuda.stream(stream):
             A.copy_(A0)
             B.copy_(B0)
             G.potrf_dev(A, n, n, info, "L", sp)
             G.potrs_dev(A, n, n, B, k, n, "L", sp)
 
-    for _ in range(max(args.warmup, 0)):
-        step()
-    stream.synchronize()
-    peak = fp64_peak_tflops()
+    def step_mixed():
+        with torch.cuda.stream(stream):
+            rc, rep = G.posv_mixed_dev(A0, n, n, B0, n, X, n, k, opts, "L", sp, raise_on_error=False)
+            reports.append((rc, rep))
 
-    clocks = ClockSampler(local)
-    barrier(ws)
-    torch.cuda.synchronize()
-    clocks.start()
-    G.profile_enable(True)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    e1.synchronize()
-    torch.cuda.synchronize()
-    barrier(ws)
-    ck = clocks.stop()
-    prof = G.profile_read()
-    G.profile_enable(False)
-    ms = e0.elapsed_time(e1)
-    ms_max = max_over_ranks(ws, ms)
-    assert int(info.item()) == 0, f"factorisation failed, info={int(info.item())}"
+    def timed(step_fn):
+        for _ in range(max(args.warmup, 0)):
+            step_fn()
+        stream.synchronize()
+        clocks = ClockSampler(local)
+        barrier(ws)
+        torch.cuda.synchronize()
+        clocks.start()
+        G.profile_enable(True)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step_fn()
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        barrier(ws)
+        ck = clocks.stop()
+        prof = G.profile_read()
+        G.profile_enable(False)
+        return max_over_ranks(ws, e0.elapsed_time(e1)), prof, ck
 
-    # backward error of the last step's solution (torch FP64 GEMM as a plain reference computation)
-    X = B.T  # n x k
-    R = A0 @ X - B0.T
-    be = float(torch.linalg.norm(R) / (torch.linalg.norm(A0) * torch.linalg.norm(X)))
+    def backward_error(Xs):  # torch FP64 GEMM as an independent check of the returned solution
+        R = A0 @ Xs.T - B0.T
+        return float(torch.linalg.norm(R) / (torch.linalg.norm(A0) * torch.linalg.norm(Xs)))
 
-    flops = llt_flops(n, k)
-    value = ws * flops * args.steps / (ms_max * 1e-3) / 1e12
-    launches = sum(v["launches"] for v in prof.values())
-    top = max(prof.items(), key=lambda kv: kv[1]["ms"])
-    top_name, top_s = top
-    achieved = top_s["flops"] / (top_s["ms"] * 1e-3) / 1e12
-    per_launch_flops = top_s["flops"] / top_s["launches"]
-    total_kernel_ms = sum(v["ms"] for v in prof.values())
+    peaks = measured_peaks()
+    run64 = args.arms in ("both", "fp64")
+    runmx = args.arms in ("both", "mixed")
+    if run64:
+        ms64, prof64, ck64 = timed(step_fp64)
+        assert int(info.item()) == 0, f"factorisation failed, info={int(info.item())}"
+        be64 = backward_error(B)
+    if runmx:
+        reports.clear()
+        msmx, profmx, ckmx = timed(step_mixed)
+        rcs = {rc for rc, _ in reports}
+        rep = reports[-1][1]
+        bemx = backward_error(X)
+        mixed_ok = rcs == {G.SUCCESS} and rep["converged"] and bemx <= 1e-14
+    else:
+        mixed_ok = False
+
+    def arm(ms, prof, be, extra):
+        top = max(prof.items(), key=lambda kv: kv[1]["ms"])
+        total = sum(v["ms"] for v in prof.values())
+        d = {"seconds_per_solve": ms / args.steps / 1e3, "tflops": ws * flops * args.steps / (ms * 1e-3) / 1e12,
+             "backward_error": be, "gpu_launches": sum(v["launches"] for v in prof.values()),
+             "roofline": dict(roofline_for(top[0], top[1], peaks), kernel_share_of_device_time=top[1]["ms"] / total),
+             "kernels": {kn: {"launches": v["launches"], "ms": v["ms"]} for kn, v in prof.items()}}
+        d.update(extra)
+        return d
+
+    fp64 = arm(ms64, prof64, be64, {"path": "plain FP64: gbllt_dpotrf_dev + gbllt_dpotrs_dev"}) if run64 else None
+    mixed = arm(msmx, profmx, bemx, {"path": f"gbllt_dposv_mixed_dev precision={args.mixed_precision}, FP64 "
+                                             f"residuals, tol 1e-14, no fallback",
+                                     "reached_1e-14": mixed_ok, "steps": rep["steps"], "history": rep["history"],
+                                     "factor_ms": rep["factor_ms"], "refine_ms": rep["refine_ms"]}) if runmx else None
+    # headline: the faster path that reached backward error <= 1e-14 (the mixed arm alone when only it ran)
+    use_mixed = runmx and (not run64 or (mixed_ok and mixed["seconds_per_solve"] < fp64["seconds_per_solve"]))
+    head = mixed if use_mixed else fp64
+    ms_head, ck = (msmx, ckmx) if use_mixed else (ms64, ck64)
 
     # end to end through the host-pointer C ABI (pinned host buffers; copies inside the timed call)
-    e2e = None
-    if rank == 0 or ws > 1:
-        hA0 = A0.cpu().pin_memory()
-        hB0 = B0.cpu().pin_memory()
-        hA = torch.empty_like(hA0).pin_memory()
-        hB = torch.empty_like(hB0).pin_memory()
-        a_np, b_np = hA.numpy(), hB.numpy()
-        import ctypes
-        e2e_steps = max(1, min(args.steps, 3))
-        tt = []
-        for i in range(1 + e2e_steps):
-            hA.copy_(hA0)
-            hB.copy_(hB0)
-            inf = ctypes.c_int64(0)
-            t0 = time.perf_counter()
+    hA0 = A0.cpu().pin_memory()
+    hB0 = B0.cpu().pin_memory()
+    hA = torch.empty(hA0.shape, dtype=hA0.dtype).pin_memory()
+    hB = torch.empty(hB0.shape, dtype=hB0.dtype).pin_memory()
+    hX = torch.zeros(hB0.shape, dtype=hB0.dtype).pin_memory()
+    a_np, b_np, x_np = hA.numpy(), hB.numpy(), hX.numpy()
+    tt = []
+    for i in range(1 + max(1, min(args.steps, 3))):
+        hA.copy_(hA0)
+        hB.copy_(hB0)
+        inf = ctypes.c_int64(0)
+        t0 = time.perf_counter()
+        if use_mixed:
+            r = G.MixedReport()
+            rc = G.lib().gbllt_dposv_mixed(G.COL_MAJOR, b"L", n, k, a_np.ctypes.data, n, b_np.ctypes.data, n,
+                                           x_np.ctypes.data, n, ctypes.byref(opts), ctypes.byref(r))
+        else:
             rc = G.lib().gbllt_dposv(G.COL_MAJOR, b"L", n, k, a_np.ctypes.data, n, b_np.ctypes.data, n,
                                      ctypes.byref(inf))
-            dt = time.perf_counter() - t0
-            G.check("gbllt_dposv", rc)
-            assert inf.value == 0
-            if i > 0:
-                tt.append(dt)
-        e2e_s = max_over_ranks(ws, sum(tt) / len(tt))
-        e2e = {"value": ws * flops / e2e_s / 1e12, "unit": "TFLOP/s", "seconds_per_step": e2e_s,
-               "h2d_bytes_per_step": int(n * n * 8 + n * k * 8), "d2h_bytes_per_step": int(n * n * 8 + n * k * 8),
-               "path": "gbllt_dposv (host pointers, pinned), wall clock"}
+        dt = time.perf_counter() - t0
+        G.check("e2e", rc)
+        if i > 0:
+            tt.append(dt)
+    e2e_s = max_over_ranks(ws, sum(tt) / len(tt))
+    bytes_io = int(n * n * 8 + n * k * 8)
+    e2e = {"value": ws * flops / e2e_s / 1e12, "unit": "TFLOP/s", "seconds_per_step": e2e_s,
+           "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": int(n * k * 8) if use_mixed else bytes_io,
+           "path": ("gbllt_dposv_mixed" if use_mixed else "gbllt_dposv") + " (host pointers, pinned), wall clock"}
 
     if rank != 0:
         return
     cpu = None if args.no_cpu_baseline or ws > 1 else cpu_sample()
     out = {
-        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "metric": METRIC, "value": ws * flops * args.steps / (ms_head * 1e-3) / 1e12, "unit": "TFLOP/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_head / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": f"{args.mixed_precision}+f64" if use_mixed else "f64", "data": "synthetic",
         "config": {"workload": cfg["workload"], "n": n, "nrhs": k, "kappa": cfg["kappa"],
-                   "path": "plain FP64 (gbllt_dpotrf_dev + gbllt_dpotrs_dev)",
-                   "l2": "inputs larger than L2 (matrix 2.1 GB vs 129 MB L2); each step restores A and B "
-                         "from a pristine device copy (included in the timed step)"},
-        "seconds_per_solve": ms_max / args.steps / 1e3,
-        "backward_error": be,
-        "roofline": {"kernel": top_name, "bound": "tensor", "achieved": achieved, "peak": peak,
-                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                     "per_launch_flops": per_launch_flops, "launches": top_s["launches"],
-                     "kernel_share_of_device_time": top_s["ms"] / total_kernel_ms,
-                     "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (FP64 peak; not in MEASURED_PEAKS.json)"},
-        "kernels": {kn: {"launches": v["launches"], "ms": v["ms"],
-                         "tflops": v["flops"] / max(v["ms"], 1e-9) / 1e9} for kn, v in prof.items()},
-        "gpu_launches": launches,
-        "e2e": e2e,
-        "cpu_baseline": cpu,
-        "clocks": ck,
+                   "headline": "mixed+refinement" if use_mixed else "plain FP64",
+                   "work_per_step_flops": flops, "accuracy": "normwise backward error <= 1e-14 (checked with a "
+                   "torch FP64 residual of the returned X)",
+                   "l2": "inputs larger than L2 (matrix 2.1 GB vs 129 MB L2)"},
+        "seconds_per_solve": head["seconds_per_solve"], "backward_error": head["backward_error"],
+        "roofline": head["roofline"], "gpu_launches": head["gpu_launches"],
+        "fp64": fp64, "mixed": mixed, "peaks": peaks,
+        "e2e": e2e, "cpu_baseline": cpu, "clocks": ck, "clocks_fp64_arm": ck64 if run64 else None,
     }
     print(json.dumps(out), flush=True)
 
@@ -361,6 +449,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", choices=sorted(CONFIGS), default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mixed-precision", default="tf32x3", choices=["fp32", "tf32", "tf32x3", "bf16", "bf16x3"])
+    ap.add_argument("--n", type=int, default=0, help="override the order n (profiling a smaller case)")
+    ap.add_argument("--arms", default="both", choices=["both", "fp64", "mixed"])
     args = ap.parse_args()
     if args.impl == "reference":
         # CPU only: under torchrun rank 0 alone runs it, the other ranks exit without work
