@@ -1,0 +1,705 @@
+// Batched factor + solve of many small SPD systems of uneven sizes in one persistent launch.
+//
+// Each system s is an independent LLT<MatrixX?>(A_s).solve(b_s) (Eigen/src/Cholesky/LLT.h:430-498):
+// A_s is n_s x n_s column-major at a + aoff[s] (lower triangle read and overwritten with L_s),
+// b_s holds n_s values at b + boff[s] and is overwritten with x_s; info[s] is the LAPACK info.
+//
+// Launch structure: a persistent grid (a multiple of the SM count) pulls systems from a device
+// work queue ordered largest-first, so the long systems start early and the short ones fill the
+// tail.  A system whose matrix fits in shared memory is staged there (lower triangle, odd leading
+// dimension), otherwise it is worked on in place in global memory (L2-resident at these sizes).
+// Per system, the blocked right-looking algorithm of llt_inplace::blocked (LLT.h:338-368) runs
+// with NBP-wide panels: warp 0 factors the panel warp-synchronously (the role of unblocked(),
+// LLT.h:312-336, with the same `x <= 0` pivot test), then all threads apply the trailing update
+// with 4 x 4 register tiles.  The solve is blocked the same way: warp 0 solves each diagonal
+// triangle, all warps apply the off-diagonal blocks (GEMV forward, warp-shuffle dot products
+// backward).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace gbllt {
+
+namespace {
+
+constexpr int kMaxBatchN = 1024;  // largest system order the batched path accepts
+
+template <typename T>
+struct BatchArgs {
+  T* a;
+  T* b;
+  int64_t* info;
+  const int* order;     // system indices, largest first
+  const int* n;         // orders
+  const int64_t* aoff;  // element offsets of each A
+  const int64_t* boff;  // element offsets of each b
+  int count;
+  int* counter;         // work-queue ticket, zeroed before each launch
+  int smem_max_n;       // systems with n <= smem_max_n are staged in shared memory
+};
+
+// Factor + solve one system held in M (leading dimension ld), right-hand side in bv (shared).
+// Returns -1 on success or the failing column.  All threads of the CTA call it.
+template <typename T, int NBP, int THREADS>
+__device__ int factor_solve(T* M, int ld, int n, T* bv, int* s_fail) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) *s_fail = -1;
+  __syncthreads();
+  for (int k0 = 0; k0 < n; k0 += NBP) {
+    const int kb = min(NBP, n - k0);
+    // ---- panel: columns k0 .. k0+kb, rows k0 .. n, by warp 0
+    if (warp == 0) {
+      for (int j = k0; j < k0 + kb; ++j) {
+        T d = M[j + (long long)j * ld];
+        if (d <= T(0)) {
+          if (lane == 0) *s_fail = j;
+          break;
+        }
+        d = sqrt(d);
+        __syncwarp();
+        if (lane == 0) M[j + (long long)j * ld] = d;
+        for (int i = j + 1 + lane; i < n; i += 32) M[i + (long long)j * ld] /= d;
+        __syncwarp();
+        for (int l = j + 1; l < k0 + kb; ++l) {
+          const T mlj = M[l + (long long)j * ld];
+          for (int i = l + lane; i < n; i += 32) M[i + (long long)l * ld] -= M[i + (long long)j * ld] * mlj;
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    if (*s_fail >= 0) return *s_fail;
+    // ---- trailing update: rows / columns r0 .. n, lower 4 x 4 tiles
+    const int r0 = k0 + kb;
+    const int m = n - r0;
+    if (m > 0) {
+      const int mt = (m + 3) >> 2;
+      for (int idx = tid; idx < mt * mt; idx += THREADS) {
+        const int ti = idx % mt, tj = idx / mt;
+        if (ti < tj) continue;
+        const int i0 = r0 + 4 * ti, j0 = r0 + 4 * tj;
+        T acc[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+        for (int p = k0; p < r0; ++p) {
+          const T* col = M + (long long)p * ld;
+          T ar[4], ac[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) ar[u] = i0 + u < n ? col[i0 + u] : T(0);
+#pragma unroll
+          for (int v = 0; v < 4; ++v) ac[v] = j0 + v < n ? col[j0 + v] : T(0);
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = fma(ar[u], ac[v], acc[u][v]);
+        }
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u, j = j0 + v;
+            if (i < n && j < n && i >= j) M[i + (long long)j * ld] -= acc[u][v];
+          }
+      }
+    }
+    __syncthreads();
+  }
+  // ---- forward sweep L y = b, blocks of 32
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int jb = min(32, n - j0);
+    if (warp == 0) {
+      for (int j = j0; j < j0 + jb; ++j) {
+        const T yj = bv[j] / M[j + (long long)j * ld];
+        __syncwarp();
+        if (lane == 0) bv[j] = yj;
+        const int i = j + 1 + lane;
+        if (i < j0 + jb) bv[i] -= M[i + (long long)j * ld] * yj;
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    for (int i = j0 + jb + tid; i < n; i += THREADS) {
+      T s = T(0);
+      for (int p = j0; p < j0 + jb; ++p) s = fma(M[i + (long long)p * ld], bv[p], s);
+      bv[i] -= s;
+    }
+    __syncthreads();
+  }
+  // ---- backward sweep L^T x = y
+  for (int j0 = ((n - 1) / 32) * 32; j0 >= 0; j0 -= 32) {
+    const int jb = min(32, n - j0);
+    // bv[c] -= sum_{r >= j0+jb} L(r, c) x_r for c in the block: one warp per column, shuffle reduction
+    for (int c = j0 + warp; c < j0 + jb; c += THREADS / 32) {
+      T s = T(0);
+      for (int r = j0 + jb + lane; r < n; r += 32) s = fma(M[r + (long long)c * ld], bv[r], s);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+      if (lane == 0) bv[c] -= s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      for (int j = j0 + jb - 1; j >= j0; --j) {
+        const T xj = bv[j] / M[j + (long long)j * ld];
+        __syncwarp();
+        if (lane == 0) bv[j] = xj;
+        const int i = j0 + lane;
+        if (i < j) bv[i] -= M[j + (long long)i * ld] * xj;
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+  }
+  return -1;
+}
+
+template <typename T, int NBP, int THREADS>
+__global__ void __launch_bounds__(THREADS) batched_posv_kernel(BatchArgs<T> p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* bv = reinterpret_cast<T*>(smem_raw);          // kMaxBatchN values
+  T* sm = bv + kMaxBatchN;                         // staged matrix
+  __shared__ int s_ticket, s_fail;
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) s_ticket = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int t = s_ticket;
+    __syncthreads();
+    if (t >= p.count) break;
+    const int sys = p.order[t];
+    const int n = p.n[sys];
+    T* A = p.a + p.aoff[sys];
+    T* B = p.b + p.boff[sys];
+    const bool staged = n <= p.smem_max_n;
+    const int ld = staged ? (n | 1) : n;
+    T* M = staged ? sm : A;
+    if (staged)
+      for (int idx = tid; idx < n * n; idx += THREADS) {
+        const int i = idx % n, j = idx / n;
+        if (i >= j) M[i + j * ld] = A[(long long)j * n + i];
+      }
+    for (int i = tid; i < n; i += THREADS) bv[i] = B[i];
+    __syncthreads();
+    const int fail = n > 0 ? factor_solve<T, NBP, THREADS>(M, ld, n, bv, &s_fail) : -1;
+    if (staged)
+      for (int idx = tid; idx < n * n; idx += THREADS) {
+        const int i = idx % n, j = idx / n;
+        if (i >= j) A[(long long)j * n + i] = M[i + j * ld];
+      }
+    if (fail < 0)
+      for (int i = tid; i < n; i += THREADS) B[i] = bv[i];
+    if (tid == 0) p.info[sys] = fail < 0 ? 0 : (int64_t)fail + 1;
+    __syncthreads();
+  }
+}
+
+// ---- variants and launch ---------------------------------------------------------------------
+
+struct Variant {
+  int nbp, threads;
+};
+constexpr Variant kVariants[] = {{16, 128}, {32, 128}, {16, 256}, {32, 256}};
+constexpr int kNumVariants = 4;
+
+template <typename T>
+size_t smem_bytes(int smem_max_n) {
+  const int ld = smem_max_n | 1;
+  return (size_t)kMaxBatchN * sizeof(T) + (size_t)ld * smem_max_n * sizeof(T);
+}
+
+template <typename T, int NBP, int THREADS>
+int launch_variant(const BatchArgs<T>& args, int grid, size_t smem, cudaStream_t s) {
+  auto kern = batched_posv_kernel<T, NBP, THREADS>;
+  GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<grid, THREADS, smem, s>>>(args);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+template <typename T>
+int launch_batched(int variant, const BatchArgs<T>& args, int grid, size_t smem, cudaStream_t s) {
+  switch (variant) {
+    case 0: return launch_variant<T, 16, 128>(args, grid, smem, s);
+    case 1: return launch_variant<T, 32, 128>(args, grid, smem, s);
+    case 2: return launch_variant<T, 16, 256>(args, grid, smem, s);
+    default: return launch_variant<T, 32, 256>(args, grid, smem, s);
+  }
+}
+
+template <typename T>
+int occupancy(int variant, size_t smem) {
+  int blocks = 0;
+  const void* f = nullptr;
+  switch (variant) {
+    case 0: f = (const void*)batched_posv_kernel<T, 16, 128>; break;
+    case 1: f = (const void*)batched_posv_kernel<T, 32, 128>; break;
+    case 2: f = (const void*)batched_posv_kernel<T, 16, 256>; break;
+    default: f = (const void*)batched_posv_kernel<T, 32, 256>; break;
+  }
+  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, f, kVariants[variant].threads, smem);
+  return blocks;
+}
+
+// Synthetic SPD systems with the plan's sizes (A = I * n + 1/(1 + |i - j|), b = 1) for timing.
+template <typename T>
+__global__ void fill_tuning_kernel(T* a, T* b, const int* n, const int64_t* aoff, const int64_t* boff, int count) {
+  const int s = blockIdx.x;
+  if (s >= count) return;
+  const int m = n[s];
+  for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+    const int i = idx % m, j = idx / m;
+    a[aoff[s] + idx] = (i == j ? T(m) : T(0)) + T(1) / T(1 + abs(i - j));
+  }
+  for (int i = threadIdx.x; i < m; i += blockDim.x) b[boff[s] + i] = T(1);
+}
+
+}  // namespace
+
+// ---- plans ------------------------------------------------------------------------------------
+
+struct BatchPlan {
+  int64_t count = 0;
+  int elem = 8;  // 8 = double, 4 = float
+  int64_t a_elems = 0, b_elems = 0;
+  int max_n = 0;
+  std::vector<int> h_n;
+  std::vector<int64_t> h_aoff, h_boff;
+  // device arrays (one allocation)
+  void* dev = nullptr;
+  int* d_order = nullptr;
+  int* d_n = nullptr;
+  int64_t* d_aoff = nullptr;
+  int64_t* d_boff = nullptr;
+  int* d_counter = nullptr;
+  int device = 0;
+  int variant = 3;
+  int smem_max_n = 0;
+  int grid = 0;
+  size_t smem = 0;
+  double tuned_ms[kNumVariants] = {0, 0, 0, 0};
+  // cached graph
+  cudaGraphExec_t exec = nullptr;
+  void* g_a = nullptr;
+  void* g_b = nullptr;
+  void* g_info = nullptr;
+  std::mutex mu;
+};
+
+namespace {
+
+template <typename T>
+void configure(BatchPlan* p) {
+  int dev = 0, sms = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  // stage in shared memory every system whose lower triangle fits (leaving room for b)
+  int nmax = std::min(p->max_n, kMaxBatchN);
+  while (nmax > 0 && smem_bytes<T>(nmax) > (size_t)optin) --nmax;
+  p->smem_max_n = nmax;
+  p->smem = smem_bytes<T>(std::max(nmax, 1));
+  const int occ = std::max(1, occupancy<T>(p->variant, p->smem));
+  p->grid = sms * occ;
+}
+
+// Algorithmic work of one batch: sum n^3/3 + 2 n^2 flops; bytes: read A-lower + b, write L + x.
+void batch_work(const BatchPlan* p, double* fl, double* by) {
+  *fl = 0;
+  *by = 0;
+  for (int v : p->h_n) {
+    *fl += (double)v * v * v / 3.0 + 2.0 * v * v;
+    *by += ((double)v * (v + 1) + 2.0 * v) * p->elem;
+  }
+}
+
+template <typename T>
+int run_plan(BatchPlan* p, T* a, T* b, int64_t* info, cudaStream_t s, bool prof) {
+  BatchArgs<T> args{a, b, info, p->d_order, p->d_n, p->d_aoff, p->d_boff, (int)p->count, p->d_counter,
+                    p->smem_max_n};
+  GB_CUDA_TRY(cudaMemsetAsync(p->d_counter, 0, sizeof(int), s));
+  static const std::string kname = std::string("batched_posv_") + tname<T>();
+  double fl = 0, by = 0;
+  if (prof) batch_work(p, &fl, &by);
+  ProfScope ps(prof ? kname.c_str() : nullptr, s, fl, by);
+  return launch_batched<T>(p->variant, args, p->grid, p->smem, s);
+}
+
+}  // namespace
+
+int batch_plan_create(int64_t count, const int64_t* n, int elem, BatchPlan** out) {
+  if (count < 0) return -1;
+  if (!n && count > 0) return -2;
+  if (elem != 4 && elem != 8) return -3;
+  if (!out) return -4;
+  for (int64_t s = 0; s < count; ++s)
+    if (n[s] < 0 || n[s] > kMaxBatchN) return -2;
+  int rc = ensure_device();
+  if (rc) return rc;
+  BatchPlan* p = new BatchPlan();
+  p->count = count;
+  p->elem = elem;
+  p->h_n.resize(count);
+  p->h_aoff.resize(count);
+  p->h_boff.resize(count);
+  int64_t ao = 0, bo = 0;
+  for (int64_t s = 0; s < count; ++s) {
+    p->h_n[s] = (int)n[s];
+    p->h_aoff[s] = ao;
+    p->h_boff[s] = bo;
+    ao += n[s] * n[s];
+    bo += n[s];
+    p->max_n = std::max(p->max_n, (int)n[s]);
+  }
+  p->a_elems = ao;
+  p->b_elems = bo;
+  std::vector<int> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return p->h_n[x] > p->h_n[y]; });
+  cudaGetDevice(&p->device);
+  const size_t bytes = (size_t)count * (4 + 4 + 8 + 8) + 256 * 4;
+  if (cudaMalloc(&p->dev, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete p;
+    return GBLLT_ERR_ALLOC;
+  }
+  char* base = (char*)p->dev;
+  p->d_aoff = (int64_t*)base;
+  p->d_boff = p->d_aoff + count;
+  p->d_order = (int*)(p->d_boff + count);
+  p->d_n = p->d_order + count;
+  p->d_counter = (int*)(((uintptr_t)(p->d_n + count) + 255) & ~(uintptr_t)255);
+  cudaMemcpy(p->d_aoff, p->h_aoff.data(), count * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->d_boff, p->h_boff.data(), count * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->d_order, order.data(), count * 4, cudaMemcpyHostToDevice);
+  if (cudaMemcpy(p->d_n, p->h_n.data(), count * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(p->dev);
+    delete p;
+    return GBLLT_ERR_CUDA;
+  }
+  if (elem == 8) configure<double>(p);
+  else configure<float>(p);
+  *out = p;
+  return GBLLT_SUCCESS;
+}
+
+void batch_plan_destroy(BatchPlan* p) {
+  if (!p) return;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->dev) cudaFree(p->dev);
+  delete p;
+}
+
+// Autotuner: times every kernel variant on synthetic SPD systems of the plan's sizes (3 runs
+// each, CUDA events) and keeps the fastest.  Returns the chosen variant.
+int batch_plan_tune(BatchPlan* p, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(p->mu);
+  const size_t es = p->elem;
+  void* buf = nullptr;
+  const size_t bytes = (size_t)p->a_elems * es + (size_t)p->b_elems * es + (size_t)p->count * 8 + 512;
+  if (cudaMalloc(&buf, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return GBLLT_ERR_ALLOC;
+  }
+  char* a = (char*)buf;
+  char* b = a + (((size_t)p->a_elems * es + 255) & ~(size_t)255);
+  int64_t* info = (int64_t*)(b + (((size_t)p->b_elems * es + 255) & ~(size_t)255));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = p->variant;
+  double best_ms = 1e30;
+  int rc = GBLLT_SUCCESS;
+  for (int v = 0; v < kNumVariants && !rc; ++v) {
+    p->variant = v;
+    if (p->elem == 8) configure<double>(p);
+    else configure<float>(p);
+    double tot = 0;
+    for (int r = 0; r < 4 && !rc; ++r) {
+      if (p->elem == 8) fill_tuning_kernel<double><<<(unsigned)std::max<int64_t>(p->count, 1), 256, 0, s>>>(
+          (double*)a, (double*)b, p->d_n, p->d_aoff, p->d_boff, (int)p->count);
+      else fill_tuning_kernel<float><<<(unsigned)std::max<int64_t>(p->count, 1), 256, 0, s>>>(
+          (float*)a, (float*)b, p->d_n, p->d_aoff, p->d_boff, (int)p->count);
+      cudaEventRecord(e0, s);
+      rc = p->elem == 8 ? run_plan<double>(p, (double*)a, (double*)b, info, s, false)
+                        : run_plan<float>(p, (float*)a, (float*)b, info, s, false);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (r > 0) tot += ms;  // first run warms up
+    }
+    p->tuned_ms[v] = tot / 3;
+    if (tot / 3 < best_ms) {
+      best_ms = tot / 3;
+      best = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  if (rc) return rc;
+  p->variant = best;
+  if (p->elem == 8) configure<double>(p);
+  else configure<float>(p);
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+  }
+  return best;
+}
+
+int batch_plan_set_variant(BatchPlan* p, int v) {
+  if (v < 0 || v >= kNumVariants) return -2;
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->variant = v;
+  if (p->elem == 8) configure<double>(p);
+  else configure<float>(p);
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+  }
+  return GBLLT_SUCCESS;
+}
+
+// Launch through a CUDA graph (memset of the queue ticket + the persistent kernel), captured once
+// per (plan, buffers) on a private stream and replayed on the caller's stream.
+template <typename T>
+int batch_run(BatchPlan* p, T* a, T* b, int64_t* info, bool use_graph, cudaStream_t s) {
+  if ((int)sizeof(T) != p->elem) return -1;
+  if (p->count == 0) return GBLLT_SUCCESS;
+  std::lock_guard<std::mutex> lk(p->mu);
+  if (!use_graph) return run_plan<T>(p, a, b, info, s, true);
+  if (!p->exec || p->g_a != a || p->g_b != b || p->g_info != info) {
+    if (p->exec) {
+      cudaGraphExecDestroy(p->exec);
+      p->exec = nullptr;
+    }
+    cudaStream_t cs;
+    GB_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    GB_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    int rc = run_plan<T>(p, a, b, info, cs, false);
+    cudaError_t e = cudaStreamEndCapture(cs, &g);
+    cudaStreamDestroy(cs);
+    if (rc) return rc;
+    GB_CUDA_TRY(e);
+    e = cudaGraphInstantiate(&p->exec, g, 0);
+    cudaGraphDestroy(g);
+    GB_CUDA_TRY(e);
+    p->g_a = a;
+    p->g_b = b;
+    p->g_info = info;
+  }
+  static const std::string kname = std::string("batched_posv_") + tname<T>();
+  double fl = 0, by = 0;
+  batch_work(p, &fl, &by);
+  ProfScope ps(kname.c_str(), s, fl, by);
+  GB_CUDA_TRY(cudaGraphLaunch(p->exec, s));
+  return GBLLT_SUCCESS;
+}
+
+template int batch_run<double>(BatchPlan*, double*, double*, int64_t*, bool, cudaStream_t);
+template int batch_run<float>(BatchPlan*, float*, float*, int64_t*, bool, cudaStream_t);
+
+}  // namespace gbllt
+
+// ---- tuning cache: a JSON object, one entry per line, keyed by dtype, count and a hash of the sizes
+namespace gbllt {
+namespace {
+
+std::string plan_signature(const BatchPlan* p) {
+  uint64_t h = 1469598103934665603ull;  // FNV-1a over the sizes
+  for (int v : p->h_n) {
+    h ^= (uint64_t)(uint32_t)v;
+    h *= 1099511628211ull;
+  }
+  char buf[96];
+  snprintf(buf, sizeof buf, "%s-%lld-%016llx", p->elem == 8 ? "f64" : "f32", (long long)p->count,
+           (unsigned long long)h);
+  return buf;
+}
+
+std::vector<std::pair<std::string, std::string>> read_cache(const char* path) {
+  std::vector<std::pair<std::string, std::string>> entries;
+  FILE* f = fopen(path, "r");
+  if (!f) return entries;
+  char line[1024];
+  while (fgets(line, sizeof line, f)) {
+    const char* q0 = strchr(line, '"');
+    if (!q0) continue;
+    const char* q1 = strchr(q0 + 1, '"');
+    const char* br = q1 ? strchr(q1, '{') : nullptr;
+    const char* be = br ? strrchr(br, '}') : nullptr;
+    if (!q1 || !br || !be) continue;
+    entries.emplace_back(std::string(q0 + 1, q1), std::string(br, be + 1));
+  }
+  fclose(f);
+  return entries;
+}
+
+int cached_variant(const char* path, const std::string& sig) {
+  for (auto& e : read_cache(path))
+    if (e.first == sig) {
+      const char* v = strstr(e.second.c_str(), "\"variant\":");
+      if (v) return atoi(v + 10);
+    }
+  return -1;
+}
+
+void write_cache(const char* path, const std::string& sig, const BatchPlan* p) {
+  auto entries = read_cache(path);
+  char body[512];
+  snprintf(body, sizeof body,
+           "{\"variant\": %d, \"panel\": %d, \"threads\": %d, \"smem_max_n\": %d, \"ms\": [%.4f, %.4f, %.4f, %.4f]}",
+           p->variant, kVariants[p->variant].nbp, kVariants[p->variant].threads, p->smem_max_n, p->tuned_ms[0],
+           p->tuned_ms[1], p->tuned_ms[2], p->tuned_ms[3]);
+  bool found = false;
+  for (auto& e : entries)
+    if (e.first == sig) {
+      e.second = body;
+      found = true;
+    }
+  if (!found) entries.emplace_back(sig, body);
+  FILE* f = fopen(path, "w");
+  if (!f) return;
+  fprintf(f, "{\n");
+  for (size_t i = 0; i < entries.size(); ++i)
+    fprintf(f, "\"%s\": %s%s\n", entries[i].first.c_str(), entries[i].second.c_str(), i + 1 < entries.size() ? "," : "");
+  fprintf(f, "}\n");
+  fclose(f);
+}
+
+}  // namespace
+}  // namespace gbllt
+
+using namespace gbllt;
+
+extern "C" {
+
+int gbllt_batch_plan_create(int64_t count, const int64_t* n, int elem_bytes, gbllt_batch_plan** plan) {
+  BatchPlan* p = nullptr;
+  int rc = batch_plan_create(count, n, elem_bytes, &p);
+  if (rc == GBLLT_SUCCESS) *plan = (gbllt_batch_plan*)p;
+  return rc;
+}
+
+int gbllt_batch_plan_destroy(gbllt_batch_plan* plan) {
+  batch_plan_destroy((BatchPlan*)plan);
+  return GBLLT_SUCCESS;
+}
+
+int gbllt_batch_plan_layout(const gbllt_batch_plan* plan, int64_t* aoff, int64_t* boff, int64_t* a_elems,
+                            int64_t* b_elems) {
+  if (!plan) return -1;
+  const BatchPlan* p = (const BatchPlan*)plan;
+  if (aoff) memcpy(aoff, p->h_aoff.data(), p->count * sizeof(int64_t));
+  if (boff) memcpy(boff, p->h_boff.data(), p->count * sizeof(int64_t));
+  if (a_elems) *a_elems = p->a_elems;
+  if (b_elems) *b_elems = p->b_elems;
+  return GBLLT_SUCCESS;
+}
+
+int gbllt_batch_plan_tune(gbllt_batch_plan* plan, const char* cache_path, void* stream) {
+  if (!plan) return -1;
+  BatchPlan* p = (BatchPlan*)plan;
+  const std::string sig = plan_signature(p);
+  if (cache_path) {
+    const int v = cached_variant(cache_path, sig);
+    if (v >= 0 && v < kNumVariants) {
+      batch_plan_set_variant(p, v);
+      return v;
+    }
+  }
+  const int v = batch_plan_tune(p, (cudaStream_t)stream);
+  if (v >= 0 && cache_path) write_cache(cache_path, sig, p);
+  return v;
+}
+
+int gbllt_batch_plan_set_variant(gbllt_batch_plan* plan, int variant) {
+  if (!plan) return -1;
+  return batch_plan_set_variant((BatchPlan*)plan, variant);
+}
+
+int gbllt_batch_plan_variant(const gbllt_batch_plan* plan, int* panel, int* threads, int* smem_max_n) {
+  if (!plan) return -1;
+  const BatchPlan* p = (const BatchPlan*)plan;
+  if (panel) *panel = kVariants[p->variant].nbp;
+  if (threads) *threads = kVariants[p->variant].threads;
+  if (smem_max_n) *smem_max_n = p->smem_max_n;
+  return p->variant;
+}
+
+int gbllt_dposv_batched_dev(gbllt_batch_plan* plan, double* d_a, double* d_b, int64_t* d_info, void* stream) {
+  if (!plan) return -1;
+  if (((BatchPlan*)plan)->elem != 8) return -1;
+  if (!d_a || !d_b) return -2;
+  if (!d_info) return -4;
+  return batch_run<double>((BatchPlan*)plan, d_a, d_b, d_info, true, (cudaStream_t)stream);
+}
+
+int gbllt_sposv_batched_dev(gbllt_batch_plan* plan, float* d_a, float* d_b, int64_t* d_info, void* stream) {
+  if (!plan) return -1;
+  if (((BatchPlan*)plan)->elem != 4) return -1;
+  if (!d_a || !d_b) return -2;
+  if (!d_info) return -4;
+  return batch_run<float>((BatchPlan*)plan, d_a, d_b, d_info, true, (cudaStream_t)stream);
+}
+
+static int host_batched(gbllt_batch_plan* plan, void* a, void* b, int64_t* info, int elem) {
+  if (!plan) return -1;
+  BatchPlan* p = (BatchPlan*)plan;
+  if (p->elem != elem) return -1;
+  if ((!a || !b) && p->count > 0) return -2;
+  if (!info && p->count > 0) return -4;
+  if (p->count == 0) return GBLLT_SUCCESS;
+  int rc = ensure_device();
+  if (rc) return rc;
+  cudaStream_t s = lib_stream();
+  const size_t ab = (size_t)p->a_elems * elem, bb = (size_t)p->b_elems * elem, ib = (size_t)p->count * 8;
+  char* d = nullptr;
+  if (cudaMallocAsync((void**)&d, ab + bb + ib + 512, s) != cudaSuccess) {
+    cudaGetLastError();
+    return GBLLT_ERR_ALLOC;
+  }
+  char* da = d;
+  char* db = d + ((ab + 255) & ~(size_t)255);
+  int64_t* di = (int64_t*)(db + ((bb + 255) & ~(size_t)255));
+  cudaMemcpyAsync(da, a, ab, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(db, b, bb, cudaMemcpyHostToDevice, s);
+  rc = elem == 8 ? batch_run<double>(p, (double*)da, (double*)db, di, false, s)
+                 : batch_run<float>(p, (float*)da, (float*)db, di, false, s);
+  if (!rc) {
+    cudaMemcpyAsync(a, da, ab, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(b, db, bb, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(info, di, ib, cudaMemcpyDeviceToHost, s);
+  }
+  cudaFreeAsync(d, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (!rc && e != cudaSuccess) {
+    set_last_error(e, "batched solve", __FILE__, __LINE__);
+    return GBLLT_ERR_CUDA;
+  }
+  return rc;
+}
+
+int gbllt_dposv_batched(gbllt_batch_plan* plan, double* a, double* b, int64_t* info) {
+  return host_batched(plan, a, b, info, 8);
+}
+
+int gbllt_sposv_batched(gbllt_batch_plan* plan, float* a, float* b, int64_t* info) {
+  return host_batched(plan, a, b, info, 4);
+}
+
+}  // extern "C"

@@ -47,7 +47,7 @@ int kind_id(const char* kind) {
 }  // namespace
 
 ProfScope::ProfScope(const char* kind, cudaStream_t s, double flops, double bytes) : slot(-1), stream(s) {
-  if (!g_prof_on.load(std::memory_order_relaxed)) return;
+  if (!kind || !g_prof_on.load(std::memory_order_relaxed)) return;
   std::lock_guard<std::mutex> lk(g_prof_mu);
   Rec r;
   r.kind = kind_id(kind);

@@ -52,6 +52,18 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_dposv_mixed_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _vp]),
     "gbllt_dposv_mixed": (_int, [_int, _ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp]),
     "gbllt_dposv_mixed_dev_noalloc": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _vp, _vp]),
+    "gbllt_batch_plan_create": (_int, [_i64, _vp, _int, ctypes.POINTER(_vp)]),
+    "gbllt_batch_plan_destroy": (_int, [_vp]),
+    "gbllt_batch_plan_layout": (_int, [_vp, _vp, _vp, _i64p, _i64p]),
+    "gbllt_batch_plan_tune": (_int, [_vp, ctypes.c_char_p, _vp]),
+    "gbllt_batch_plan_set_variant": (_int, [_vp, _int]),
+    "gbllt_batch_plan_variant": (_int, [_vp, ctypes.POINTER(_int), ctypes.POINTER(_int), ctypes.POINTER(_int)]),
+    "gbllt_dposv_batched_dev": (_int, [_vp, _vp, _vp, _vp, _vp]),
+    "gbllt_sposv_batched_dev": (_int, [_vp, _vp, _vp, _vp, _vp]),
+    "gbllt_dposv_batched": (_int, [_vp, _vp, _vp, _vp]),
+    "gbllt_sposv_batched": (_int, [_vp, _vp, _vp, _vp]),
+    "gbllt_dpotrf_adjoint_dev": (_int, [_i64, _vp, _i64, _vp, _i64, _vp]),
+    "gbllt_dpotrs_adjoint_dev": (_int, [_i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp]),
     "gbllt_profile_enable": (_int, [_int]),
     "gbllt_profile_read": (_int, [_vp, _int, ctypes.POINTER(_int)]),
 }
@@ -204,6 +216,69 @@ def posv_mixed(a: np.ndarray, b: np.ndarray, opts: MixedOpts | None = None, uplo
     if rc not in (SUCCESS, ERR_NOT_CONVERGED):
         check("gbllt_dposv_mixed", rc)
     return x, rc, rep.as_dict()
+
+
+def potrf_adjoint_dev(l_cm, n: int, ldl: int, lbar_cm, ldlb: int, stream: int = 0) -> None:
+    """In place: lbar (df/dL, lower) becomes df/dA (lower triangle of the symmetric gradient)."""
+    check("gbllt_dpotrf_adjoint_dev", lib().gbllt_dpotrf_adjoint_dev(n, _ptr(l_cm), ldl, _ptr(lbar_cm), ldlb, stream))
+
+
+def potrs_adjoint_dev(l_cm, n: int, ldl: int, x_cm, ldx: int, xbar_cm, ldxb: int, bbar_cm, ldbb: int, nrhs: int,
+                      abar_cm=None, ldab: int = 1, stream: int = 0) -> None:
+    check("gbllt_dpotrs_adjoint_dev",
+          lib().gbllt_dpotrs_adjoint_dev(n, nrhs, _ptr(l_cm), ldl, _ptr(x_cm), ldx, _ptr(xbar_cm), ldxb, _ptr(bbar_cm),
+                                         ldbb, _ptr(abar_cm) if abar_cm is not None else None, max(ldab, 1), stream))
+
+
+class BatchPlan:
+    """A batched-solve plan (gbllt_batch_plan): sizes, packed offsets and the tuned kernel variant."""
+
+    def __init__(self, sizes, dtype=np.float64):
+        self.sizes = np.ascontiguousarray(np.asarray(sizes, dtype=np.int64))
+        self.elem = 8 if np.dtype(dtype) == np.float64 else 4
+        h = _vp()
+        check("gbllt_batch_plan_create", lib().gbllt_batch_plan_create(len(self.sizes), self.sizes.ctypes.data,
+                                                                       self.elem, ctypes.byref(h)))
+        self.handle = h
+        n = len(self.sizes)
+        self.aoff = np.zeros(n, dtype=np.int64)
+        self.boff = np.zeros(n, dtype=np.int64)
+        ae, be = _i64(0), _i64(0)
+        check("gbllt_batch_plan_layout", lib().gbllt_batch_plan_layout(h, self.aoff.ctypes.data, self.boff.ctypes.data,
+                                                                       ctypes.byref(ae), ctypes.byref(be)))
+        self.a_elems, self.b_elems = int(ae.value), int(be.value)
+
+    def tune(self, cache_path: str | None = None, stream: int = 0) -> int:
+        v = lib().gbllt_batch_plan_tune(self.handle, cache_path.encode() if cache_path else None, stream)
+        if v < 0:
+            check("gbllt_batch_plan_tune", v)
+        return v
+
+    def set_variant(self, v: int) -> None:
+        check("gbllt_batch_plan_set_variant", lib().gbllt_batch_plan_set_variant(self.handle, v))
+
+    def variant(self) -> dict:
+        p, t, m = _int(0), _int(0), _int(0)
+        v = lib().gbllt_batch_plan_variant(self.handle, ctypes.byref(p), ctypes.byref(t), ctypes.byref(m))
+        return {"variant": v, "panel": p.value, "threads": t.value, "smem_max_n": m.value}
+
+    def solve_dev(self, a, b, info, stream: int = 0) -> None:
+        fn = "gbllt_dposv_batched_dev" if self.elem == 8 else "gbllt_sposv_batched_dev"
+        check(fn, getattr(lib(), fn)(self.handle, _ptr(a), _ptr(b), _ptr(info), stream))
+
+    def solve(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+        info = np.zeros(len(self.sizes), dtype=np.int64)
+        fn = "gbllt_dposv_batched" if self.elem == 8 else "gbllt_sposv_batched"
+        check(fn, getattr(lib(), fn)(self.handle, _ptr(a), _ptr(b), info.ctypes.data))
+        return info
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                lib().gbllt_batch_plan_destroy(self.handle)
+                self.handle = None
+        except Exception:  # pragma: no cover
+            pass
 
 
 # ---- diagnostics -------------------------------------------------------------------------------

@@ -155,6 +155,55 @@ GBLLT_API int gbllt_dposv_mixed_dev_noalloc(char uplo, int64_t n, int64_t nrhs, 
                                             const gbllt_mixed_opts* opts, gbllt_mixed_report* report,
                                             void* stream);
 
+/* ---- Batched factor + solve of many small systems of uneven sizes -------------------------
+ * Replaces a loop of `LLT<MatrixXd> llt(A_s); x_s = llt.solve(b_s);` (Eigen/src/Cholesky/LLT.h:430-498)
+ * over independent SPD systems, which Eigen runs one after another on the CPU.  A plan fixes the
+ * sizes n_s (0 <= n_s <= 1024) and the packed layout: A_s is n_s x n_s column-major at element
+ * offset aoff[s] = sum_{t<s} n_t^2 of one array, b_s (one right-hand side) at boff[s] =
+ * sum_{t<s} n_t of another.  The solve overwrites the lower triangle of each A_s with L_s and b_s
+ * with x_s, and writes the LAPACK info of each system.  All systems run in one persistent kernel
+ * launch that pulls them from a largest-first work queue; the _dev entry points replay it as a
+ * CUDA graph captured on first use for a given set of buffers. */
+typedef struct gbllt_batch_plan gbllt_batch_plan;
+/* elem_bytes: 8 (double) or 4 (float).  n is a host array of `count` sizes. */
+GBLLT_API int gbllt_batch_plan_create(int64_t count, const int64_t* n, int elem_bytes, gbllt_batch_plan** plan);
+GBLLT_API int gbllt_batch_plan_destroy(gbllt_batch_plan* plan);
+/* Host copies of the offsets (arrays of `count`, may be NULL) and total element counts. */
+GBLLT_API int gbllt_batch_plan_layout(const gbllt_batch_plan* plan, int64_t* aoff, int64_t* boff, int64_t* a_elems,
+                                      int64_t* b_elems);
+/* Autotuner: times each kernel variant (panel width x threads per CTA) on synthetic SPD systems
+ * of the plan's sizes and keeps the fastest; with cache_path, a previous choice for the same
+ * sizes is read from / a new one written to that JSON file.  Returns the variant index (>= 0). */
+GBLLT_API int gbllt_batch_plan_tune(gbllt_batch_plan* plan, const char* cache_path, void* stream);
+/* Use kernel variant `variant` (0..3) without tuning. */
+GBLLT_API int gbllt_batch_plan_set_variant(gbllt_batch_plan* plan, int variant);
+/* The variant in use: returns its index and its panel width, threads per CTA and the largest
+ * order staged in shared memory. */
+GBLLT_API int gbllt_batch_plan_variant(const gbllt_batch_plan* plan, int* panel, int* threads, int* smem_max_n);
+/* Device pointers, stream-ordered (graph replay; no allocation, no host synchronisation). */
+GBLLT_API int gbllt_dposv_batched_dev(gbllt_batch_plan* plan, double* d_a, double* d_b, int64_t* d_info,
+                                      void* stream);
+GBLLT_API int gbllt_sposv_batched_dev(gbllt_batch_plan* plan, float* d_a, float* d_b, int64_t* d_info,
+                                      void* stream);
+/* Host pointers, synchronous. */
+GBLLT_API int gbllt_dposv_batched(gbllt_batch_plan* plan, double* a, double* b, int64_t* info);
+GBLLT_API int gbllt_sposv_batched(gbllt_batch_plan* plan, float* a, float* b, int64_t* info);
+
+/* ---- Reverse mode (adjoints) of the factorisation and the solve, FP64, device pointers -------
+ * Eigen has no derivative of LLT; these give the gradients of any scalar function of the factor
+ * or of the solution, for A symmetric positive definite with A = L L^T (lower, column-major).
+ * Gradients with respect to A are symmetric matrices G with df = sum_ij G_ij dA_ij for symmetric
+ * dA; their lower triangle is stored. */
+/* d_lbar holds Lbar = df/dL (lower triangle) on entry and Abar = df/dA on return.  Blocked, in
+ * place, from L only (no stored intermediates): n^3/3 flops, like the factorisation itself. */
+GBLLT_API int gbllt_dpotrf_adjoint_dev(int64_t n, const double* d_l, int64_t ldl, double* d_lbar, int64_t ldlb,
+                                       void* stream);
+/* For X = A^{-1} B (n x nrhs) with its adjoint Xbar: writes Bbar = A^{-1} Xbar and, when d_abar is
+ * not NULL, accumulates Abar -= sym(Bbar X^T) into its lower triangle. */
+GBLLT_API int gbllt_dpotrs_adjoint_dev(int64_t n, int64_t nrhs, const double* d_l, int64_t ldl, const double* d_x,
+                                       int64_t ldx, const double* d_xbar, int64_t ldxb, double* d_bbar, int64_t ldbb,
+                                       double* d_abar, int64_t ldab, void* stream);
+
 /* ---- Diagnostics (no counterpart in the reference; Eigen has no built-in timers) ----------- */
 
 /* Per-kernel-class totals: launches, device time (CUDA events on the launch stream) and the

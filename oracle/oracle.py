@@ -231,3 +231,28 @@ def set_threads(t: int) -> None:
 
 def num_threads() -> int:
     return int(lib().oracle_num_threads())
+
+
+# ---- adjoint references (numpy, FP64) ---------------------------------------------------------
+
+def chol_adjoint_ref(L: np.ndarray, Lbar: np.ndarray) -> np.ndarray:
+    """Symmetric df/dA from df/dL for A = L L^T: 1/2 L^{-T} (P + P^T) L^{-1}, P = Phi(L^T Lbar),
+    Phi = lower triangle with halved diagonal (Murray 2016, arXiv:1602.07527, symbolic form)."""
+    from scipy.linalg import solve_triangular
+    L = np.tril(L)
+    P = np.tril(L.T @ np.tril(Lbar))
+    P[np.diag_indices_from(P)] *= 0.5
+    S = P + P.T
+    Y = solve_triangular(L, S, trans="T", lower=True)          # L^{-T} S
+    D = solve_triangular(L, Y.T, trans="T", lower=True).T      # (L^{-T} Y^T)^T = Y L^{-1}
+    return 0.25 * (D + D.T)  # 1/2 L^{-T} S L^{-1}, symmetrised against roundoff
+
+
+def gp_objective_ref(A: np.ndarray, y: np.ndarray):
+    """f = logdet A + y^T A^{-1} y and its gradients dA = A^{-1} - a a^T (a = A^{-1} y), dy = 2 a."""
+    L = np.linalg.cholesky(A)
+    from scipy.linalg import cho_solve
+    a = cho_solve((L, True), y)
+    f = 2.0 * np.sum(np.log(np.diag(L))) + float(y @ a)
+    Ainv = cho_solve((L, True), np.eye(A.shape[0]))
+    return f, Ainv - np.outer(a, a), 2.0 * a
