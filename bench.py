@@ -441,15 +441,197 @@ def run_ours(args, ws, rank, local):
     print(json.dumps(out), flush=True)
 
 
+# ---- other configurations (one JSON line each; the default run is the one above) -------------------
+
+def run_c3(args):
+    """n = 32768, 1 and 64 RHS, Householder spectra kappa in {1e2, 1e4, 1e6}: mixed precision +
+    FP64 refinement (each precision) against the plain FP64 GPU factor+solve on the same input."""
+    import torch
+    import gbllt as G
+    n = args.n or 32768
+    s = torch.cuda.current_stream().cuda_stream
+    out = {"metric": METRIC, "config": {"workload": f"C3: n={n}, Householder spectrum, 1 and 64 RHS", "n": n},
+           "unit": "s", "higher_is_better": False, "data": "synthetic", "results": []}
+    fp64_s = {}
+    for kappa in (1e2, 1e4, 1e6):
+        cfg = {"n": n, "nrhs": 64, "kappa": kappa}
+        A0, B64 = make_inputs_gpu(cfg, seed=3)
+        for k in (1, 64):
+            B0 = B64[:k].contiguous()
+            X = torch.zeros_like(B0)
+            if k not in fp64_s and kappa == 1e6:  # the FP64 time does not depend on kappa
+                A = A0.clone()
+                B = B0.clone()
+                info = torch.zeros(1, dtype=torch.int64, device="cuda")
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                G.potrf_dev(A, n, n, info, "L", s)
+                G.potrs_dev(A, n, n, B, k, n, "L", s)
+                torch.cuda.synchronize()
+                fp64_s[k] = time.perf_counter() - t0
+                R = A0 @ B.T - B0.T
+                be = float(torch.linalg.norm(R) / (torch.linalg.norm(A0) * torch.linalg.norm(B)))
+                out["results"].append({"path": "fp64", "nrhs": k, "kappa": kappa, "seconds": fp64_s[k],
+                                       "backward_error": be})
+                del A, B
+            for prec in args.c3_precisions.split(","):
+                G.posv_mixed_dev(A0, n, n, B0, n, X, n, k, G.mixed_opts(prec, 10, 1e-14, False), "L", s,
+                                 raise_on_error=False)  # warm-up
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                rc, rep = G.posv_mixed_dev(A0, n, n, B0, n, X, n, k, G.mixed_opts(prec, 10, 1e-14, False), "L", s,
+                                           raise_on_error=False)
+                torch.cuda.synchronize()
+                dt = time.perf_counter() - t0
+                R = A0 @ X.T - B0.T
+                be = float(torch.linalg.norm(R) / (torch.linalg.norm(A0) * torch.linalg.norm(X)))
+                out["results"].append({"path": "mixed", "precision": prec, "nrhs": k, "kappa": kappa, "seconds": dt,
+                                       "reached_1e-14": bool(rc == 0 and be <= 1e-14), "steps": rep["steps"],
+                                       "info": rep["info"], "backward_error": be, "factor_ms": rep["factor_ms"],
+                                       "refine_ms": rep["refine_ms"]})
+                print(json.dumps(out["results"][-1]), file=sys.stderr, flush=True)
+        del A0, B64
+        torch.cuda.empty_cache()
+    print(json.dumps(out), flush=True)
+
+
+def run_c4(args):
+    """20000 SPD systems, n_i ~ U{4..256}, one RHS each, FP64 and FP32, one graph-replayed launch."""
+    import torch
+    import gbllt as G
+    count = 20000
+    rng = torch.Generator(device="cpu").manual_seed(21)
+    sizes = torch.randint(4, 257, (count,), generator=rng).numpy().astype(np.int64)
+    out = {"metric": "batched LLT solves/s and fraction of HBM", "config": {
+        "workload": "C4: 20000 SPD systems, n_i uniform in [4,256], A_i = G_i G_i^T/n_i + 0.1 I, 1 RHS each",
+        "count": count}, "unit": "solves/s", "higher_is_better": True, "data": "synthetic", "results": []}
+    peaks = {"hbm_gbs": json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]
+             if (ROOT / "MEASURED_PEAKS.json").exists() else 6800.0, "fp64_tflops": fp64_peak_tflops()}
+    s = torch.cuda.current_stream().cuda_stream
+    for dt, tdt, name in ((np.float64, torch.float64, "f64"), (np.float32, torch.float32, "f32")):
+        plan = G.BatchPlan(sizes, dt)
+        variant = plan.tune(str(ROOT / "eigen-git-mirror_gb300" / "lib" / "batched_tune.json"), s)
+        # A_i = G_i G_i^T / n_i + 0.1 I built on the device, system by system into the packed array
+        a0 = torch.empty(plan.a_elems, dtype=tdt, device="cuda")
+        g = torch.Generator(device="cuda").manual_seed(22)
+        for i, nn in enumerate(sizes):
+            nn = int(nn)
+            Gm = torch.randn(nn, nn, generator=g, dtype=torch.float64, device="cuda")
+            Ai = Gm @ Gm.T / nn + 0.1 * torch.eye(nn, dtype=torch.float64, device="cuda")
+            a0[int(plan.aoff[i]):int(plan.aoff[i]) + nn * nn] = Ai.T.reshape(-1).to(tdt)
+        b0 = torch.randn(plan.b_elems, generator=g, dtype=torch.float64, device="cuda").to(tdt)
+        a = torch.empty_like(a0)
+        b = torch.empty_like(b0)
+        info = torch.zeros(count, dtype=torch.int64, device="cuda")
+        for _ in range(max(args.warmup, 3)):
+            a.copy_(a0)
+            b.copy_(b0)
+            plan.solve_dev(a, b, info, s)
+        torch.cuda.synchronize()
+        G.profile_enable(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        tot = 0.0
+        for _ in range(args.steps):
+            a.copy_(a0)
+            b.copy_(b0)
+            e0.record()
+            plan.solve_dev(a, b, info, s)
+            e1.record()
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        prof = G.profile_read()
+        G.profile_enable(False)
+        assert int(info.max()) == 0
+        st = prof[f"batched_posv_{name}"]
+        ms = tot / args.steps
+        gbs = st["bytes"] / st["ms"] / 1e6
+        tfs = st["flops"] / st["ms"] / 1e9
+        out["results"].append({"dtype": name, "ms": ms, "solves_per_s": count / (ms * 1e-3), "achieved_gbs": gbs,
+                               "hbm_frac": gbs / peaks["hbm_gbs"], "achieved_tflops": tfs,
+                               "fp64_frac": tfs / peaks["fp64_tflops"] if name == "f64" else None,
+                               "variant": plan.variant(), "launches_per_step": 1})
+    out["peaks"] = peaks
+    print(json.dumps(out), flush=True)
+
+
+def run_c5(args):
+    """64 RBF kernel matrices, n = 2048 (x ~ U[0,1]^3, lengthscale 0.2, variance 1, noise 1e-2),
+    y ~ N(0,1): f = logdet A + y^T A^{-1} y forward and the hand-written adjoint (dA, dy), FP64;
+    the mixed-precision forward solves A alpha = y with the tensor-core factorisation + refinement."""
+    import torch
+    import gbllt as G
+    nmat, n = 64, args.n or 2048
+    s = torch.cuda.current_stream().cuda_stream
+    g = torch.Generator(device="cuda").manual_seed(31)
+    X = torch.rand(nmat, n, 3, generator=g, dtype=torch.float64, device="cuda")
+    Y = torch.randn(nmat, n, generator=g, dtype=torch.float64, device="cuda")
+    d2 = ((X[:, :, None, :] - X[:, None, :, :]) ** 2).sum(-1)
+    A = torch.exp(-d2 / (2 * 0.2 ** 2)) + 1e-2 * torch.eye(n, dtype=torch.float64, device="cuda")
+    del d2
+    info = torch.zeros(1, dtype=torch.int64, device="cuda")
+    res = {}
+    for it in range(2):  # first pass warms up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Ls, alphas, fs = [], [], []
+        for m in range(nmat):
+            L = A[m].clone()  # symmetric: row-major storage = column-major A
+            G.potrf_dev(L, n, n, info, "L", s)
+            al = Y[m].clone().reshape(1, n)
+            G.potrs_dev(L, n, n, al, 1, n, "L", s)
+            fs.append(2.0 * torch.log(torch.diagonal(L)).sum() + torch.dot(Y[m], al.reshape(n)))
+            Ls.append(L)
+            alphas.append(al)
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        grads = []
+        for m in range(nmat):
+            M = torch.zeros_like(Ls[m])
+            M.diagonal().copy_(2.0 / torch.diagonal(Ls[m]))
+            G.potrf_adjoint_dev(Ls[m], n, n, M, n, s)
+            bbar = torch.empty_like(alphas[m])
+            G.potrs_adjoint_dev(Ls[m], n, n, alphas[m], n, Y[m].reshape(1, n), n, bbar, n, 1, M, n, s)
+            grads.append(M)
+        torch.cuda.synchronize()
+        t_bwd = time.perf_counter() - t0
+        res = {"forward_s": t_fwd, "backward_s": t_bwd}
+    # gradient check of the first matrix against the closed form A^{-1} - a a^T (cuSOLVER FP64)
+    Ainv = torch.cholesky_inverse(torch.linalg.cholesky(A[0]))
+    a0 = alphas[0].reshape(n)
+    want = torch.tril(Ainv - torch.outer(a0, a0))
+    got = grads[0].T.tril()
+    res["grad_rel_err_vs_closed_form"] = float(torch.linalg.norm(got - want) / torch.linalg.norm(want))
+    # mixed-precision forward solve of the same systems
+    opts = G.mixed_opts(args.mixed_precision, 10, 1e-14, True)
+    Xs = torch.zeros(1, n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    steps = []
+    for m in range(nmat):
+        rc, rep = G.posv_mixed_dev(A[m], n, n, Y[m].reshape(1, n), n, Xs, n, 1, opts, "L", s, raise_on_error=False)
+        steps.append(rep["steps"])
+    torch.cuda.synchronize()
+    res["mixed_solve_s"] = time.perf_counter() - t0
+    res["mixed_steps"] = [min(steps), max(steps)]
+    fl_fwd = nmat * (n ** 3 / 3 + 2 * n * n)
+    out = {"metric": "GP likelihood logdet+quad forward and adjoint (s)", "config": {
+        "workload": "C5: 64 RBF matrices n=2048, lengthscale 0.2, noise 1e-2", "nmat": nmat, "n": n},
+        "unit": "s", "higher_is_better": False, "data": "synthetic", "results": res,
+        "forward_tflops": fl_fwd / res["forward_s"] / 1e12, "backward_tflops_equiv": fl_fwd / res["backward_s"] / 1e12}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=sorted(CONFIGS), default="c2")
+    ap.add_argument("--config", choices=sorted(CONFIGS) + ["c3", "c4", "c5"], default="c2")
+    ap.add_argument("--c3-precisions", default="bf16x6,tf32x3,bf16x3,tf32,bf16")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mixed-precision", default="tf32x3", choices=["fp32", "tf32", "tf32x3", "bf16", "bf16x3"])
+    ap.add_argument("--mixed-precision", default="tf32x3", choices=["fp32", "tf32", "tf32x3", "bf16", "bf16x3", "bf16x6"])
     ap.add_argument("--n", type=int, default=0, help="override the order n (profiling a smaller case)")
     ap.add_argument("--arms", default="both", choices=["both", "fp64", "mixed"])
     args = ap.parse_args()
@@ -458,7 +640,12 @@ def main():
         run_reference(args, int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")))
         return
     ws, rank, local = dist_setup()
-    run_ours(args, ws, rank, local)
+    if args.config in ("c3", "c4", "c5"):
+        import torch
+        torch.cuda.set_device(local)
+        {"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.config](args)
+    else:
+        run_ours(args, ws, rank, local)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

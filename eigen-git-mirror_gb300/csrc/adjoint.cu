@@ -9,8 +9,9 @@
 // (holding Lbar on entry, Abar on exit; only L and M are read -- panels are recomputed from L, no
 // forward intermediates are stored):
 //     Cbar  = M_IJ L_JJ^{-1}                       (right triangular solve)
-//     M_JJ -= tril(L_IJ^T Cbar)                    (adjoint of L_JJ through L_IJ = C' L_JJ^{-T})
-//     M_IJ  = Cbar                                 (= Abar_IJ)
+//     M_JJ -= tril(Cbar^T L_IJ)                    (adjoint of L_JJ through L_IJ = C' L_JJ^{-T})
+//     M_IJ  = Cbar / 2                             (= Abar_IJ: each off-diagonal entry of the
+//                                                   symmetric A is shared by (i,j) and (j,i))
 //     M_IK -= Cbar L_JK ;  M_JK -= Cbar^T L_IK      (adjoint of C' = A_IJ - L_IK L_JK^T)
 //     Dbar  = 1/2 L_JJ^{-T} (P + P^T) L_JJ^{-1},  P = Phi(L_JJ^T M_JJ)   (diagonal block)
 //     M_JJ  = Dbar ;  M_JK -= 2 Dbar L_JK          (adjoint of D' = A_JJ - L_JK L_JK^T)
@@ -98,7 +99,9 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(long long m, long long n,
   }
 }
 
-// X L = M for X, in place on M (rows x ANB), L lower jb x jb: one thread per row, columns descending.
+// X L = M for X, then M <- X / 2, in place (rows x ANB), L lower jb x jb: one thread per row,
+// columns descending.  The halving converts the adjoint of the independent lower entries of A_IJ
+// into the symmetric-gradient convention (each off-diagonal entry stands for two symmetric ones).
 __global__ void __launch_bounds__(128) trsm_right_lower_kernel(const double* __restrict__ L, long long ldl, int jb,
                                                                double* __restrict__ M, long long ldm, long long rows) {
   __shared__ double Ls[ANB][ANB + 1];  // Ls[p][c] = L(p, c)
@@ -121,7 +124,7 @@ __global__ void __launch_bounds__(128) trsm_right_lower_kernel(const double* __r
   }
 #pragma unroll
   for (int c = 0; c < ANB; ++c)
-    if (c < jb) M[(long long)c * ldm + r] = x[c];
+    if (c < jb) M[(long long)c * ldm + r] = 0.5 * x[c];
 }
 
 // Diagonal block: Mjj (lower, holding Lbar_JJ) <- lower( 1/2 L^{-T} (P + P^T) L^{-1} ), P = Phi(L^T Lbar).
@@ -223,12 +226,13 @@ int potrf_adjoint_dev(int64_t n, const double* L, int64_t ldl, double* M, int64_
     if (ni > 0) {
       {
         ProfScope ps(kt.c_str(), s, (double)ni * jb * jb, 16.0 * ni * jb);
-        trsm_right_lower_kernel<<<(unsigned)ceil_div(ni, 128), 128, 0, s>>>(Ljj, ldl, jb, Mij, ldm, ni);  // Cbar
+        trsm_right_lower_kernel<<<(unsigned)ceil_div(ni, 128), 128, 0, s>>>(Ljj, ldl, jb, Mij, ldm, ni);  // Cbar/2
       }
-      gemm<1, 0>(jb, jb, ni, -1.0, Lij, ldl, Mij, ldm, Mjj, ldm, true, s);        // M_JJ -= tril(L_IJ^T Cbar)
+      // M_IJ now holds Cbar / 2 (its final, symmetric-convention value); the updates use Cbar = 2 M_IJ
+      gemm<1, 0>(jb, jb, ni, -2.0, Mij, ldm, Lij, ldl, Mjj, ldm, true, s);        // M_JJ -= tril(Cbar^T L_IJ)
       if (j0 > 0) {
-        gemm<0, 0>(ni, j0, jb, -1.0, Mij, ldm, Ljk, ldl, Mik, ldm, false, s);     // M_IK -= Cbar L_JK
-        gemm<1, 0>(jb, j0, ni, -1.0, Mij, ldm, Lik, ldl, Mjk, ldm, false, s);     // M_JK -= Cbar^T L_IK
+        gemm<0, 0>(ni, j0, jb, -2.0, Mij, ldm, Ljk, ldl, Mik, ldm, false, s);     // M_IK -= Cbar L_JK
+        gemm<1, 0>(jb, j0, ni, -2.0, Mij, ldm, Lik, ldl, Mjk, ldm, false, s);     // M_JK -= Cbar^T L_IK
       }
     }
     {

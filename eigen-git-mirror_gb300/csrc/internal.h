@@ -62,6 +62,13 @@ constexpr const char* tname() {
   return sizeof(T) == 8 ? "f64" : "f32";
 }
 
+// The same solve on a caller-supplied workspace of potrs_ws_bytes(n, sizeof(T)) bytes (allocates
+// nothing).
+size_t potrs_ws_bytes(int64_t n, size_t elem);
+template <typename T>
+int potrs_ws(bool upper, int64_t n, int64_t nrhs, const T* d_a, int64_t lda, T* d_b, int64_t ldb, void* ws,
+             cudaStream_t s);
+
 // Mixed-precision solve with FP64 refinement (device pointers, column-major).
 // Workspace layout of one solve: the FP32 working matrix (ldf x n), scaling, residuals, partial
 // sums, split panel operands and the status word, in `bytes`; `fallback_bytes` more hold the FP64

@@ -66,8 +66,9 @@ __global__ void diag_scale_kernel(const double* __restrict__ a, long long lda, l
   }
 }
 
-// hi/lo K-major copies of the panel block Af(r0 .. r0+rows, c0 .. c0+bs):
-//   out[r * ldk + p] for p < bs;  KIND 0 = bf16, 1 = tf32 (stored as fp32 with 13 zero low bits).
+// K-major copies of the panel block Af(r0 .. r0+rows, c0 .. c0+bs) split into NP successive
+// roundings: part0 = round(v), part1 = round(v - part0), part2 = round(v - part0 - part1), stored at
+// out[r * ldk + p] for p < bs (zero beyond).  KIND 0 = bf16, 1 = tf32 (fp32 with 13 zero low bits).
 __device__ __forceinline__ float to_tf32(float x) {
   uint32_t r;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -76,8 +77,9 @@ __device__ __forceinline__ float to_tf32(float x) {
 
 template <int KIND>
 __global__ void __launch_bounds__(256) split_panel_kernel(const float* __restrict__ af, long long ldf, long long r0,
-                                                          long long c0, long long rows, int bs, void* __restrict__ hi,
-                                                          void* __restrict__ lo, long long ldk) {
+                                                          long long c0, long long rows, int bs, int np,
+                                                          void* __restrict__ p0, void* __restrict__ p1,
+                                                          void* __restrict__ p2, long long ldk) {
   __shared__ float t[TS][TS + 1];
   const long long rb = (long long)blockIdx.x * TS;
   const int pb = blockIdx.y * TS;
@@ -88,19 +90,22 @@ __global__ void __launch_bounds__(256) split_panel_kernel(const float* __restric
     t[c][tx] = (r < rows && p < bs) ? af[(c0 + p) * ldf + r0 + r] : 0.f;
   }
   __syncthreads();
+  void* outs[3] = {p0, p1, p2};
   for (int c = ty; c < TS; c += 8) {  // write along p (contiguous)
     const long long r = rb + c;
     const int p = pb + tx;
     if (r < rows && p < (int)ldk) {
-      const float v = p < bs ? t[tx][c] : 0.f;
-      if (KIND == 0) {
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        ((__nv_bfloat16*)hi)[r * ldk + p] = h;
-        if (lo) ((__nv_bfloat16*)lo)[r * ldk + p] = __float2bfloat16_rn(v - __bfloat162float(h));
-      } else {
-        const float h = to_tf32(v);
-        ((float*)hi)[r * ldk + p] = h;
-        if (lo) ((float*)lo)[r * ldk + p] = to_tf32(v - h);
+      float v = p < bs ? t[tx][c] : 0.f;
+      for (int k = 0; k < np; ++k) {
+        if (KIND == 0) {
+          const __nv_bfloat16 h = __float2bfloat16_rn(v);
+          ((__nv_bfloat16*)outs[k])[r * ldk + p] = h;
+          v -= __bfloat162float(h);
+        } else {
+          const float h = to_tf32(v);
+          ((float*)outs[k])[r * ldk + p] = h;
+          v -= h;
+        }
       }
     }
   }
@@ -276,11 +281,21 @@ struct Arena {
 }  // namespace
 
 // Factor the scaled FP32 working matrix af (n x n lower, ldf) with tensor-core trailing updates.
-int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void* hi, void* lo, int64_t ldk,
+int split_parts(int prec) {
+  switch (prec) {
+    case GBLLT_PREC_TF32: case GBLLT_PREC_BF16: return 1;
+    case GBLLT_PREC_TF32X3: case GBLLT_PREC_BF16X3: return 2;
+    case GBLLT_PREC_BF16X6: return 3;
+    default: return 0;
+  }
+}
+
+int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void* const* parts, int64_t ldk,
                     DevStatus* st, int* d_err, cudaStream_t s) {
   static const std::string ksplit = "split_panel";
-  const int kind = (prec == GBLLT_PREC_BF16 || prec == GBLLT_PREC_BF16X3) ? kTcBF16 : kTcTF32;
-  const bool split = prec == GBLLT_PREC_TF32X3 || prec == GBLLT_PREC_BF16X3;
+  const int kind = (prec == GBLLT_PREC_BF16 || prec == GBLLT_PREC_BF16X3 || prec == GBLLT_PREC_BF16X6) ? kTcBF16
+                                                                                                       : kTcTF32;
+  const int np = split_parts(prec);
   for (int64_t k0 = 0; k0 < n; k0 += panel) {
     const int bs = (int)(n - k0 < panel ? n - k0 : panel);
     const int64_t rs = n - k0 - bs;
@@ -299,18 +314,17 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void
     }
     if (rs > 0 && prec != GBLLT_PREC_FP32) {
       {
-        ProfScope ps(ksplit.c_str(), s, 0.0, (double)rs * bs * 4.0 + (double)rs * ldk * (kind == kTcBF16 ? 2 : 4) * (split ? 2 : 1));
+        ProfScope ps(ksplit.c_str(), s, 0.0, (double)rs * bs * 4.0 + (double)rs * ldk * (kind == kTcBF16 ? 2 : 4) * np);
         dim3 grid((unsigned)ceil_div(rs, TS), (unsigned)ceil_div(ldk, TS));
         if (kind == kTcBF16)
-          split_panel_kernel<0><<<grid, 256, 0, s>>>(af, ldf, k0 + bs, k0, rs, bs, hi, split ? lo : nullptr, ldk);
+          split_panel_kernel<0><<<grid, 256, 0, s>>>(af, ldf, k0 + bs, k0, rs, bs, np, parts[0], parts[1], parts[2], ldk);
         else
-          split_panel_kernel<1><<<grid, 256, 0, s>>>(af, ldf, k0 + bs, k0, rs, bs, hi, split ? lo : nullptr, ldk);
+          split_panel_kernel<1><<<grid, 256, 0, s>>>(af, ldf, k0 + bs, k0, rs, bs, np, parts[0], parts[1], parts[2], ldk);
       }
-      TcOperand op{hi, split ? lo : nullptr, rs, bs, ldk, 0};
-      // segments: hi*hi, hi*lo, lo*hi  (bit 2s = A lo, bit 2s+1 = B lo)
-      const uint32_t mask = split ? ((1u << 3) | (1u << 4)) : 0u;
-      int rc = tc_update(op, op, kind, split ? 3 : 1, mask, af + (k0 + bs) * ldf + (k0 + bs), ldf, rs, rs, true,
-                         d_err, s);
+      TcOperand op{{parts[0], parts[1], parts[2]}, rs, bs, ldk, 0};
+      const int nseg = np == 1 ? 1 : np == 2 ? 3 : 6;
+      const uint32_t code = np == 1 ? kSegX1 : np == 2 ? kSegX3 : kSegX6;
+      int rc = tc_update(op, op, kind, nseg, code, af + (k0 + bs) * ldf + (k0 + bs), ldf, rs, rs, true, d_err, s);
       if (rc) return rc;
     }
   }
@@ -332,7 +346,7 @@ int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o) {
     if (!(o->tol > 0)) o->tol = 1e-14;
     if (o->panel <= 0) o->panel = 256;
   }
-  if (o->precision < GBLLT_PREC_FP32 || o->precision > GBLLT_PREC_BF16X3) return -1;
+  if (o->precision < GBLLT_PREC_FP32 || o->precision > GBLLT_PREC_BF16X6) return -1;
   if (o->panel % kNB != 0) return -1;
   return 0;
 }
@@ -348,10 +362,11 @@ MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o) {
   L.jpc = (L.nb + nparts - 1) / nparts;
   L.nparts = (L.nb + L.jpc - 1) / L.jpc;
   L.nsq = 512;
-  L.es_k = (o.precision == GBLLT_PREC_BF16 || o.precision == GBLLT_PREC_BF16X3) ? 2 : 4;
+  L.es_k = (o.precision == GBLLT_PREC_BF16 || o.precision == GBLLT_PREC_BF16X3 || o.precision == GBLLT_PREC_BF16X6)
+               ? 2 : 4;
   L.bytes = (size_t)L.ldf * n * 4 + (size_t)n * 8 + (size_t)n * nrhs * (8 + 4) + (size_t)L.nparts * n * nrhs * 8 +
-            (size_t)L.nsq * 8 + 64 + (size_t)(o.precision == GBLLT_PREC_FP32 ? 0 : 2 * (size_t)n * L.ldk * L.es_k) +
-            sizeof(DevStatus) + 16 * 256;
+            (size_t)L.nsq * 8 + 64 + (size_t)split_parts(o.precision) * n * L.ldk * L.es_k +
+            sizeof(DevStatus) + 16 * 256 + potrs_ws_bytes(n, 8);
   L.fallback_bytes = (size_t)n * n * 8 + 256;
   return L;
 }
@@ -381,14 +396,11 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   double* part = ar.take<double>((size_t)nparts * n * nrhs);
   double* sq = ar.take<double>(nsq);
   double* norms = ar.take<double>(8);  // [0] ||A||^2, [1] ||R||^2, [2] ||X||^2
-  void* hi = nullptr;
-  void* lo = nullptr;
-  if (o.precision != GBLLT_PREC_FP32) {
-    hi = ar.take<char>((size_t)n * ldk * es_k);
-    lo = ar.take<char>((size_t)n * ldk * es_k);
-  }
+  void* parts[3] = {nullptr, nullptr, nullptr};
+  for (int i = 0; i < split_parts(o.precision); ++i) parts[i] = ar.take<char>((size_t)n * ldk * es_k);
   DevStatus* st = ar.take<DevStatus>(1);
   int* d_err = (int*)&st->timeout;
+  void* solve_ws = ar.take<char>(potrs_ws_bytes(n, 8));  // sized for the FP64 fallback solve too
   const size_t used = ar.off;
 
   // device-time stamps (only where creating events is allowed)
@@ -446,7 +458,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     else convert_scaled_kernel<false><<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(a, lda, n, dsc, af, ldf);
   }
   // 2. low-precision factorisation
-  rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, hi, lo, ldk, st, d_err, s);
+  rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, parts, ldk, st, d_err, s);
   if (rc) return rc;
   if ((rc = stamp(1))) return rc;
   DevStatus hst;
@@ -465,7 +477,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     double best = INFINITY;
     for (int step = 0; step < o.max_steps; ++step) {
       residual_to_f32_kernel<<<grid1(n * nrhs), 256, 0, s>>>(R, n, n, nrhs, dsc, &norms[1], Rf, n);
-      if ((rc = potrs_dev<float>(false, n, nrhs, af, ldf, Rf, n, s))) return rc;
+      if ((rc = potrs_ws<float>(false, n, nrhs, af, ldf, Rf, n, solve_ws, s))) return rc;
       update_x_kernel<<<grid1(n * nrhs), 256, 0, s>>>(Rf, n, n, nrhs, dsc, &norms[1], x, ldx, step == 0);
       residual();
       sumsq(R, n, n, nrhs, 0, &norms[1]);
@@ -518,7 +530,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     } else {
       r.info = 0;
       copy_cols_kernel<<<grid1(n * nrhs), 256, 0, s>>>(b, ldb, n, nrhs, x, ldx);
-      if ((rc = potrs_dev<double>(false, n, nrhs, w, n, x, ldx, s))) return rc;
+      if ((rc = potrs_ws<double>(false, n, nrhs, w, n, x, ldx, solve_ws, s))) return rc;
       residual();
       sumsq(R, n, n, nrhs, 0, &norms[1]);
       sumsq(x, ldx, n, nrhs, 0, &norms[2]);

@@ -9,13 +9,16 @@
 //     panel, streamed by TMA (cp.async.bulk.tensor, 128-byte swizzle) into a 4-stage shared
 //     memory ring guarded by mbarriers;
 //   - one elected thread issues tcgen05.mma (M = 128, N = 128, K = 16 for bf16 / 8 for tf32),
-//     accumulating in TMEM (128 lanes x 128 fp32 columns);
-//   - four epilogue warps read the accumulator with tcgen05.ld and apply C -= acc with coalesced
-//     column-major loads and stores.
-// Split precision: the K loop runs over up to three segments, each pairing the "hi" or "lo"
-// copy of A with the "hi" or "lo" copy of B (hi = round(x), lo = round(x - hi)), so
-// hi*hi^T + hi*lo^T + lo*hi^T is accumulated in one TMEM tile (Markidis et al. 2018, Ootomo &
-// Yokota 2022: split-precision products).
+//     accumulating in TMEM; the grid is persistent (one CTA per SM walks many tiles) and the
+//     accumulator is double-buffered (2 x 128 fp32 TMEM columns), so one tile's epilogue overlaps
+//     the next tile's loads and MMAs;
+//   - four epilogue warps read the accumulator with tcgen05.ld, 32 columns at a time, and apply
+//     C -= acc with coalesced column-major loads and stores.
+// Split precision: the K loop runs over up to eight segments, each pairing one part of A with one
+// part of B, where the parts are successive roundings of the same values (hi = round(x),
+// mid = round(x - hi), lo = round(x - hi - mid)); e.g. hi*hi^T + hi*lo^T + lo*hi^T for a two-way
+// split, accumulated in one TMEM tile (Markidis et al. 2018, Ootomo & Yokota 2022: split-precision
+// products), smallest terms first.
 //
 // Every mbarrier wait is bounded; on timeout the kernel raises an error flag, waits (bounded)
 // for its own TMA copies, frees its TMEM and returns.
@@ -149,37 +152,51 @@ struct TcParams {
   int m, n;            // C is m x n; A rows [a_row0, a_row0 + m), B rows [b_row0, b_row0 + n)
   int a_row0, b_row0;
   int k;               // depth of one segment (elements)
-  int nseg;            // 1..3
-  uint32_t seg_mask;   // bit 2s: segment s reads A "lo"; bit 2s+1: segment s reads B "lo"
+  int nseg;            // 1..8
+  uint32_t seg_code;   // 4 bits per segment s: bits [4s, 4s+2) = part of A, [4s+2, 4s+4) = part of B
   int lower;           // 1: only tiles / entries with global row >= column (SYRK)
   int mt;              // tiles along m
+  long long tiles;     // tiles in the launch
   int* err;            // device error word (set to 1 on a timeout)
 };
 
+struct TcMaps {
+  CUtensorMap a[3];    // parts of A (hi, mid, lo)
+  CUtensorMap b[3];    // parts of B
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Persistent: each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The accumulator is
+// double-buffered in TMEM (2 x BN columns), so the epilogue of one tile overlaps the TMA loads and
+// MMAs of the next.
 template <int KIND>
-__global__ void __launch_bounds__(192, 1) tc_update_kernel(const __grid_constant__ CUtensorMap tm_a_hi,
-                                                           const __grid_constant__ CUtensorMap tm_a_lo,
-                                                           const __grid_constant__ CUtensorMap tm_b_hi,
-                                                           const __grid_constant__ CUtensorMap tm_b_lo,
-                                                           const TcParams p) {
+__global__ void __launch_bounds__(192, 1) tc_update_kernel(const __grid_constant__ TcMaps maps, const TcParams p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
-  __shared__ __align__(8) uint64_t done_bar;
+  __shared__ __align__(8) uint64_t tfull[2];   // accumulator ready for the epilogue
+  __shared__ __align__(8) uint64_t tempty[2];  // accumulator drained by the epilogue (4 warps arrive)
   __shared__ uint32_t tmem_base_s;
   __shared__ volatile int abort_s;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int ti, tj;
-  if (p.lower) lower_tile_coords(blockIdx.x, ti, tj);
-  else { ti = (int)(blockIdx.x % p.mt); tj = (int)(blockIdx.x / p.mt); }
-  const int row0 = ti * BM, col0 = tj * BN;
-
   constexpr int KE = KIND == 0 ? 64 : 32;   // elements per 128-byte row
   constexpr int KI = KIND == 0 ? 16 : 8;    // K of one MMA instruction
+  constexpr int MMAS = ROW_BYTES / (KI * (KIND == 0 ? 2 : 4));
   const int kpb = (p.k + KE - 1) / KE;      // k-blocks per segment
   const int nk = kpb * p.nseg;
+
+  auto coords = [&](long long t, int& row0, int& col0) {
+    int ti, tj;
+    if (p.lower) lower_tile_coords(t, ti, tj);
+    else { ti = (int)(t % p.mt); tj = (int)(t / p.mt); }
+    row0 = ti * BM;
+    col0 = tj * BN;
+  };
 
   if (threadIdx.x == 0) {
     abort_s = 0;
@@ -187,13 +204,16 @@ __global__ void __launch_bounds__(192, 1) tc_update_kernel(const __grid_constant
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
-    mbar_init(&done_bar, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], 4);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
-                 "r"(BN));
+                 "r"(2 * BN));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -203,77 +223,100 @@ __global__ void __launch_bounds__(192, 1) tc_update_kernel(const __grid_constant
 
   if (warp == 0 && lane == 0) {
     // ---- TMA producer
-    int issued = 0;
-    for (int it = 0; it < nk; ++it) {
-      const int s = it % STAGES;
-      const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
-      if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_s)) break;
-      const int seg = it / kpb;
-      const int kx = (it % kpb) * KE;
-      const bool alo = (p.seg_mask >> (2 * seg)) & 1u;
-      const bool blo = (p.seg_mask >> (2 * seg + 1)) & 1u;
-      uint8_t* sa = smem + s * (A_STAGE + B_STAGE);
-      uint8_t* sb = sa + A_STAGE;
-      mbar_expect_tx(&full_bar[s], A_STAGE + B_STAGE);
-      tma_load_2d(sa, alo ? &tm_a_lo : &tm_a_hi, &full_bar[s], kx, p.a_row0 + row0);
-      tma_load_2d(sb, blo ? &tm_b_lo : &tm_b_hi, &full_bar[s], kx, p.b_row0 + col0);
-      issued = it + 1;
+    long long it = 0, issued = 0;
+    for (long long t = blockIdx.x; t < p.tiles && !abort_s; t += gridDim.x) {
+      int row0, col0;
+      coords(t, row0, col0);
+      for (int kk = 0; kk < nk; ++kk, ++it) {
+        const int s = (int)(it % STAGES);
+        const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+        if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_s)) break;
+        const int seg = kk / kpb;
+        const int kx = (kk % kpb) * KE;
+        const uint32_t code = (p.seg_code >> (4 * seg)) & 0xFu;
+        uint8_t* sa = smem + s * (A_STAGE + B_STAGE);
+        uint8_t* sb = sa + A_STAGE;
+        mbar_expect_tx(&full_bar[s], A_STAGE + B_STAGE);
+        tma_load_2d(sa, &maps.a[code & 3u], &full_bar[s], kx, p.a_row0 + row0);
+        tma_load_2d(sb, &maps.b[code >> 2], &full_bar[s], kx, p.b_row0 + col0);
+        issued = it + 1;
+      }
     }
     if (abort_s) {
       // let the copies this thread started land before the CTA exits (bounded)
-      for (int it = issued - STAGES < 0 ? 0 : issued - STAGES; it < issued; ++it) {
+      for (long long i = issued - STAGES < 0 ? 0 : issued - STAGES; i < issued; ++i) {
         volatile int dummy = 0;
-        mbar_wait(&full_bar[it % STAGES], (uint32_t)(it / STAGES) & 1u, &dummy);
+        mbar_wait(&full_bar[i % STAGES], (uint32_t)(i / STAGES) & 1u, &dummy);
       }
     }
   } else if (warp == 1 && lane == 0) {
     // ---- MMA issuer
     constexpr uint32_t idesc = instr_desc(KIND == 0 ? 1u : 2u);
-    bool ok = true;
-    for (int it = 0; it < nk; ++it) {
-      const int s = it % STAGES;
-      const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
-      if (!mbar_wait(&full_bar[s], ph, &abort_s)) { ok = false; break; }
+    long long it = 0;
+    int local = 0;
+    for (long long t = blockIdx.x; t < p.tiles && !abort_s; t += gridDim.x, ++local) {
+      const int acc = local & 1;
+      const uint32_t use = (uint32_t)(local >> 1);
+      if (!mbar_wait(&tempty[acc], (use & 1u) ^ 1u, &abort_s)) break;
       tc_fence_after();
-      const uint32_t sa = smem_u32(smem + s * (A_STAGE + B_STAGE));
-      const uint64_t ad = sw128_desc(sa), bd = sw128_desc(sa + A_STAGE);
+      const uint32_t d_tmem = tmem + (uint32_t)(acc * BN);
+      bool ok = true;
+      for (int kk = 0; kk < nk; ++kk, ++it) {
+        const int s = (int)(it % STAGES);
+        const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+        if (!mbar_wait(&full_bar[s], ph, &abort_s)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t sa = smem_u32(smem + s * (A_STAGE + B_STAGE));
+        const uint64_t ad = sw128_desc(sa), bd = sw128_desc(sa + A_STAGE);
 #pragma unroll
-      for (int j = 0; j < ROW_BYTES / (KI * (KIND == 0 ? 2 : 4)); ++j) {
-        // advance 32 bytes along K inside the swizzle atom: +2 in the (addr >> 4) field
-        mma<KIND>(tmem, ad + 2 * j, bd + 2 * j, idesc, (it > 0 || j > 0) ? 1u : 0u);
+        for (int j = 0; j < MMAS; ++j) {
+          // advance 32 bytes along K inside the swizzle atom: +2 in the (addr >> 4) field
+          mma<KIND>(d_tmem, ad + 2 * j, bd + 2 * j, idesc, (kk > 0 || j > 0) ? 1u : 0u);
+        }
+        mma_commit(&empty_bar[s]);
       }
-      mma_commit(&empty_bar[s]);
+      if (!ok) break;
+      mma_commit(&tfull[acc]);
     }
-    if (ok) mma_commit(&done_bar);
   } else if (warp >= 2) {
-    // ---- epilogue: C -= acc
+    // ---- epilogue: C -= acc, one row of the tile per thread
     const int q = warp & 3;                 // TMEM lane quadrant this warp may access
     const int r = q * 32 + lane;            // tile row
-    const long long gi = (long long)row0 + r;
-    // While the main loop runs, fetch this thread's row of the C tile into registers (all loads
-    // independent, so they overlap); each load is coalesced across the warp (consecutive rows).
-    float cv[BN];
-    const bool row_ok = gi < p.m;
-#pragma unroll
-    for (int j = 0; j < BN; ++j) {
-      const long long gj = (long long)col0 + j;
-      cv[j] = (row_ok && gj < p.n && (!p.lower || gi >= gj)) ? p.c[gj * p.ldc + gi] : 0.f;
-    }
-    const bool ok = mbar_wait(&done_bar, 0, &abort_s);
-    tc_fence_after();
-    if (ok && !abort_s) {
-#pragma unroll
+    int local = 0;
+    for (long long t = blockIdx.x; t < p.tiles && !abort_s; t += gridDim.x, ++local) {
+      int row0, col0;
+      coords(t, row0, col0);
+      const long long gi = (long long)row0 + r;
+      const int acc = local & 1;
+      const uint32_t use = (uint32_t)(local >> 1);
+      const bool row_ok = gi < p.m;
+      float* crow = p.c + (long long)col0 * p.ldc + gi;  // C(gi, col0)
+      if (!mbar_wait(&tfull[acc], use & 1u, &abort_s)) break;
+      tc_fence_after();
+#pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
+        // 32 independent loads of this thread's row segment (coalesced across the warp), then the
+        // matching 32 accumulator columns; this epilogue overlaps the next tile's main loop
+        float cv[32];
+        const int jmax = (int)min((long long)32, (long long)p.n - (col0 + c0));
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const long long gj = (long long)col0 + c0 + j;
+          cv[j] = (row_ok && j < jmax && (!p.lower || gi >= gj)) ? crow[(long long)(c0 + j) * p.ldc] : 0.f;
+        }
         float v[32];
-        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + c0), v);
         if (row_ok) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const long long gj = (long long)col0 + c0 + j;
-            if (gj < p.n && (!p.lower || gi >= gj)) p.c[gj * p.ldc + gi] = cv[c0 + j] - v[j];
+            if (j < jmax && (!p.lower || gi >= gj)) crow[(long long)(c0 + j) * p.ldc] = cv[j] - v[j];
           }
         }
       }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[acc]);
     }
   }
   tc_fence_before();
@@ -281,7 +324,7 @@ __global__ void __launch_bounds__(192, 1) tc_update_kernel(const __grid_constant
   if (threadIdx.x == 0 && abort_s) atomicExch(p.err, 1);
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
   }
 }
 
@@ -314,17 +357,21 @@ int make_map(CUtensorMap* m, const void* base, int kind, int64_t rows, int64_t k
 
 }  // namespace
 
-int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32_t seg_mask, float* c, int64_t ldc,
+int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32_t seg_code, float* c, int64_t ldc,
               int64_t m, int64_t n, bool lower, int* d_err, cudaStream_t s) {
   if (m <= 0 || n <= 0 || a.k <= 0) return GBLLT_SUCCESS;
-  if ((a.ld * (kind == 0 ? 2 : 4)) % 16 != 0 || ((uintptr_t)a.hi & 15) || ((uintptr_t)b.hi & 15))
-    return GBLLT_ERR_INTERNAL;
-  CUtensorMap ma_hi, ma_lo, mb_hi, mb_lo;
+  if (nseg < 1 || nseg > 8) return GBLLT_ERR_INTERNAL;
+  const int es = kind == 0 ? 2 : 4;
+  if ((a.ld * es) % 16 != 0 || (b.ld * es) % 16 != 0) return GBLLT_ERR_INTERNAL;
+  TcMaps maps;
   int rc;
-  if ((rc = make_map(&ma_hi, a.hi, kind, a.rows, a.k, a.ld))) return rc;
-  if ((rc = make_map(&ma_lo, a.lo ? a.lo : a.hi, kind, a.rows, a.k, a.ld))) return rc;
-  if ((rc = make_map(&mb_hi, b.hi, kind, b.rows, b.k, b.ld))) return rc;
-  if ((rc = make_map(&mb_lo, b.lo ? b.lo : b.hi, kind, b.rows, b.k, b.ld))) return rc;
+  for (int i = 0; i < 3; ++i) {
+    const void* pa = a.parts[i] ? a.parts[i] : a.parts[0];
+    const void* pb = b.parts[i] ? b.parts[i] : b.parts[0];
+    if (((uintptr_t)pa & 15) || ((uintptr_t)pb & 15)) return GBLLT_ERR_INTERNAL;
+    if ((rc = make_map(&maps.a[i], pa, kind, a.rows, a.k, a.ld))) return rc;
+    if ((rc = make_map(&maps.b[i], pb, kind, b.rows, b.k, b.ld))) return rc;
+  }
   TcParams p;
   p.c = c;
   p.ldc = ldc;
@@ -334,30 +381,38 @@ int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32
   p.b_row0 = (int)b.row0;
   p.k = (int)a.k;
   p.nseg = nseg;
-  p.seg_mask = seg_mask;
+  p.seg_code = seg_code;
   p.lower = lower ? 1 : 0;
   p.mt = (int)ceil_div(m, BM);
   p.err = d_err;
   const int64_t nt = ceil_div(n, BN);
-  const int64_t tiles = lower ? (int64_t)p.mt * (p.mt + 1) / 2 : (int64_t)p.mt * nt;
+  p.tiles = lower ? (int64_t)p.mt * (p.mt + 1) / 2 : (int64_t)p.mt * nt;
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const unsigned grid = (unsigned)(p.tiles < sms ? p.tiles : sms);
   static bool attr_set[2] = {false, false};
   static const std::string kname[2] = {"tc_update_bf16", "tc_update_tf32"};
   // algorithmic work: 2 k flops per updated entry and segment; operands read once, C read+written
   const double entries = lower ? (double)m * (m + 1) / 2.0 : (double)m * n;
   ProfScope ps(kname[kind].c_str(), s, 2.0 * entries * a.k * nseg,
-               ((double)(m + (lower ? 0 : n)) * a.k * nseg * (kind == 0 ? 2 : 4)) + entries * 8.0);
+               ((double)(m + (lower ? 0 : n)) * a.k * nseg * es) + entries * 8.0);
   if (kind == 0) {
     if (!attr_set[0]) {
       GB_CUDA_TRY(cudaFuncSetAttribute(tc_update_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
       attr_set[0] = true;
     }
-    tc_update_kernel<0><<<(unsigned)tiles, 192, SMEM_BYTES, s>>>(ma_hi, ma_lo, mb_hi, mb_lo, p);
+    tc_update_kernel<0><<<grid, 192, SMEM_BYTES, s>>>(maps, p);
   } else {
     if (!attr_set[1]) {
       GB_CUDA_TRY(cudaFuncSetAttribute(tc_update_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
       attr_set[1] = true;
     }
-    tc_update_kernel<1><<<(unsigned)tiles, 192, SMEM_BYTES, s>>>(ma_hi, ma_lo, mb_hi, mb_lo, p);
+    tc_update_kernel<1><<<grid, 192, SMEM_BYTES, s>>>(maps, p);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;

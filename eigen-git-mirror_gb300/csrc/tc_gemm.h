@@ -5,11 +5,11 @@
 namespace gbllt {
 
 // A K-major operand: `rows` rows of `k` elements, `ld` elements apart (ld * element size a multiple
-// of 16 bytes, base 16-byte aligned).  `lo` is the second half of a split operand (may be null when
-// no segment reads it).  Row `row0` of the operand lines up with row/column 0 of C.
+// of 16 bytes, base 16-byte aligned).  parts[0..2] are the successive roundings of a split operand
+// (hi, mid, lo; unused parts may be null).  Row `row0` of the operand lines up with row/column 0
+// of C.
 struct TcOperand {
-  const void* hi;
-  const void* lo;
+  const void* parts[3];
   int64_t rows;
   int64_t k;
   int64_t ld;
@@ -21,9 +21,19 @@ constexpr int kTcBF16 = 0;
 constexpr int kTcTF32 = 1;
 
 // C (m x n fp32, column-major, ldc) -= sum over nseg segments of A_s B_s^T (lower tiles and
-// entries only when `lower`); segment s reads A "lo" when bit 2s of seg_mask is set and B "lo"
-// when bit 2s+1 is set.  d_err receives 1 if a bounded wait ran out.
-int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32_t seg_mask, float* c, int64_t ldc,
+// entries only when `lower`); segment s reads part (code & 3) of A and part (code >> 2) of B,
+// code = (seg_code >> 4s) & 15.  d_err receives 1 if a bounded wait ran out.
+int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32_t seg_code, float* c, int64_t ldc,
               int64_t m, int64_t n, bool lower, int* d_err, cudaStream_t s);
+
+// Segment tables (parts: 0 = hi, 1 = mid/lo of a two-way split, 2 = lo of a three-way split),
+// ordered smallest terms first.
+constexpr uint32_t tc_code(uint32_t pa, uint32_t pb) { return pa | (pb << 2); }
+constexpr uint32_t kSegX1 = tc_code(0, 0);
+// two-way split: hi*lo, lo*hi, hi*hi
+constexpr uint32_t kSegX3 = tc_code(0, 1) | (tc_code(1, 0) << 4) | (tc_code(0, 0) << 8);
+// three-way split: hi*lo, lo*hi, mid*mid, hi*mid, mid*hi, hi*hi (drops mid*lo, lo*mid, lo*lo)
+constexpr uint32_t kSegX6 = tc_code(0, 2) | (tc_code(2, 0) << 4) | (tc_code(1, 1) << 8) | (tc_code(0, 1) << 12) |
+                            (tc_code(1, 0) << 16) | (tc_code(0, 0) << 20);
 
 }  // namespace gbllt

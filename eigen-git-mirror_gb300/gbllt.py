@@ -76,7 +76,7 @@ class KernelStat(ctypes.Structure):
                 ("flops", ctypes.c_double), ("bytes", ctypes.c_double)]
 
 
-PREC = {"fp32": 0, "tf32": 1, "tf32x3": 2, "bf16": 3, "bf16x3": 4}
+PREC = {"fp32": 0, "tf32": 1, "tf32x3": 2, "bf16": 3, "bf16x3": 4, "bf16x6": 5}
 
 
 class MixedOpts(ctypes.Structure):

@@ -106,7 +106,8 @@ GBLLT_API int gbllt_spotrs_dev(char uplo, int64_t n, int64_t nrhs, const float* 
 #define GBLLT_PREC_TF32 1   /* one TF32 product per update */
 #define GBLLT_PREC_TF32X3 2 /* three TF32 products (hi*hi + hi*lo + lo*hi): ~FP32 accuracy */
 #define GBLLT_PREC_BF16 3   /* one BF16 product per update */
-#define GBLLT_PREC_BF16X3 4 /* three BF16 products */
+#define GBLLT_PREC_BF16X3 4 /* three BF16 products (two-way split) */
+#define GBLLT_PREC_BF16X6 5 /* six BF16 products of a three-way split: ~FP32 accuracy at TF32X3 cost */
 
 typedef struct {
   int precision;     /* GBLLT_PREC_*; default GBLLT_PREC_TF32X3 when opts == NULL */

@@ -7,7 +7,7 @@ to within kappa * 1e-13 (relative Frobenius; the forward error of any solution w
 1e-14 is bounded by a small multiple of kappa * 1e-14), where kappa is the condition number of
 the seeded Householder-spectrum matrix.  Which low precisions must converge without the FP64 fallback follows
 the usual IR condition kappa * u_factor < 1: every precision at kappa = 1e2; FP32, TF32x3, BF16x3
-and TF32 at 1e4; FP32, TF32x3 and BF16x3 at 1e6.
+and TF32 at 1e4; FP32, TF32x3, BF16x3 and BF16x6 at 1e6.
 """
 import ctypes
 
@@ -16,8 +16,9 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-PRECS = ["fp32", "tf32", "tf32x3", "bf16", "bf16x3"]
-MUST_CONVERGE = {1e2: set(PRECS), 1e4: {"fp32", "tf32", "tf32x3", "bf16x3"}, 1e6: {"fp32", "tf32x3", "bf16x3"}}
+PRECS = ["fp32", "tf32", "tf32x3", "bf16", "bf16x3", "bf16x6"]
+MUST_CONVERGE = {1e2: set(PRECS), 1e4: {"fp32", "tf32", "tf32x3", "bf16x3", "bf16x6"},
+                 1e6: {"fp32", "tf32x3", "bf16x3", "bf16x6"}}
 
 
 def _dev_solve(gbllt, a, b, opts, uplo="L"):
@@ -54,7 +55,7 @@ def test_mixed_refines_to_fp64(oracle, gbllt, spectra, kappa, prec):
         assert oracle.backward_error(a, x, b) <= 1e-14
         assert np.linalg.norm(x - xr) / np.linalg.norm(xr) <= kappa * 1e-13
         # the first step already reflects the factor's precision (a broken tensor-core update would not)
-        first = {"fp32": 1e-7, "tf32": 1e-5, "tf32x3": 1e-7, "bf16": 1e-4, "bf16x3": 1e-7}[prec]
+        first = {"fp32": 1e-7, "tf32": 1e-5, "tf32x3": 1e-7, "bf16": 1e-4, "bf16x3": 1e-7, "bf16x6": 1e-8}[prec]
         assert rep["history"][0] <= first * max(1.0, kappa / 1e2)
     # with fallback: always FP64-accurate
     rc, rep, x = _dev_solve(gbllt, a, b, gbllt.mixed_opts(prec, 10, 1e-14, fallback=True))

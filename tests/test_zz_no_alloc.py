@@ -49,6 +49,25 @@ def test_noalloc_matches_allocating_entry(oracle, gbllt):
         assert oracle.backward_error(a, np.asfortranarray(x.T), b) <= 1e-14
 
 
+@pytest.mark.gpu
+def test_noalloc_accepts_its_stated_maximum(oracle, gbllt):
+    # n = 2048 with 64 right-hand sides and the FP64 fallback enabled fits the fixed area
+    torch = pytest.importorskip("torch")
+    n, k = 2048, 64
+    a = oracle.gen_gram(n, seed=23)
+    A = torch.from_numpy(np.ascontiguousarray(a.T)).cuda()
+    B = torch.from_numpy(np.ascontiguousarray(oracle.normal(24, n * k).reshape(k, n))).cuda()
+    X = torch.zeros_like(B)
+    opts = gbllt.mixed_opts("tf32x3", 10, 1e-14, True)
+    r = gbllt.MixedReport()
+    rc = gbllt.lib().gbllt_dposv_mixed_dev_noalloc(b"L", n, k, A.data_ptr(), n, B.data_ptr(), n, X.data_ptr(), n,
+                                                   ctypes.byref(opts), ctypes.byref(r),
+                                                   torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert rc == gbllt.SUCCESS, gbllt.lib().gbllt_last_error()
+    assert r.converged and r.backward_error <= 1e-14
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch(gbllt):
     # n = 8192 needs far more scratch than the fixed area: rejected on the host, before any device work
     L = gbllt.lib()
