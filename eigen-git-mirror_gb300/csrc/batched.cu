@@ -9,9 +9,9 @@
 // tail.  A system whose matrix fits in shared memory is staged there (lower triangle, odd leading
 // dimension), otherwise it is worked on in place in global memory (L2-resident at these sizes).
 // Per system, the blocked right-looking algorithm of llt_inplace::blocked (LLT.h:338-368) runs
-// with NBP-wide panels: warp 0 factors the panel warp-synchronously (the role of unblocked(),
-// LLT.h:312-336, with the same `x <= 0` pivot test), then all threads apply the trailing update
-// with 4 x 4 register tiles.  The solve is blocked the same way: warp 0 solves each diagonal
+// with NBP-wide panels: the panel is factored one column at a time by all threads (the role of
+// unblocked(), LLT.h:312-336, with the same `x <= 0` pivot test; the column is scaled by the
+// reciprocal of its pivot), then all threads apply the trailing update with 4 x 4 register tiles.  The solve is blocked the same way: warp 0 solves each diagonal
 // triangle, all warps apply the off-diagonal blocks (GEMV forward, warp-shuffle dot products
 // backward).
 #include <cuda_runtime.h>
@@ -50,34 +50,36 @@ struct BatchArgs {
 // Factor + solve one system held in M (leading dimension ld), right-hand side in bv (shared).
 // Returns -1 on success or the failing column.  All threads of the CTA call it.
 template <typename T, int NBP, int THREADS>
-__device__ int factor_solve(T* M, int ld, int n, T* bv, int* s_fail) {
+__device__ int factor_solve(T* M, int ld, int n, T* bv, int* s_fail, T* s_inv) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) *s_fail = -1;
   __syncthreads();
   for (int k0 = 0; k0 < n; k0 += NBP) {
     const int kb = min(NBP, n - k0);
-    // ---- panel: columns k0 .. k0+kb, rows k0 .. n, by warp 0
-    if (warp == 0) {
-      for (int j = k0; j < k0 + kb; ++j) {
-        T d = M[j + (long long)j * ld];
+    // ---- panel: columns k0 .. k0+kb, rows k0 .. n, by all threads, one column at a time
+    for (int j = k0; j < k0 + kb; ++j) {
+      if (tid == 0) {
+        const T d = M[j + (long long)j * ld];
         if (d <= T(0)) {
-          if (lane == 0) *s_fail = j;
-          break;
+          *s_fail = j;
+        } else {
+          const T r = sqrt(d);
+          M[j + (long long)j * ld] = r;
+          *s_inv = T(1) / r;  // one division per column; the column is scaled by multiplication
         }
-        d = sqrt(d);
-        __syncwarp();
-        if (lane == 0) M[j + (long long)j * ld] = d;
-        for (int i = j + 1 + lane; i < n; i += 32) M[i + (long long)j * ld] /= d;
-        __syncwarp();
-        for (int l = j + 1; l < k0 + kb; ++l) {
-          const T mlj = M[l + (long long)j * ld];
-          for (int i = l + lane; i < n; i += 32) M[i + (long long)l * ld] -= M[i + (long long)j * ld] * mlj;
-        }
-        __syncwarp();
       }
+      __syncthreads();
+      if (*s_fail >= 0) return *s_fail;
+      const T inv = *s_inv;
+      for (int i = j + 1 + tid; i < n; i += THREADS) M[i + (long long)j * ld] *= inv;
+      __syncthreads();
+      // remaining panel columns: one warp per column, lanes over rows
+      for (int l = j + 1 + warp; l < k0 + kb; l += THREADS / 32) {
+        const T mlj = M[l + (long long)j * ld];
+        for (int i = l + lane; i < n; i += 32) M[i + (long long)l * ld] -= M[i + (long long)j * ld] * mlj;
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    if (*s_fail >= 0) return *s_fail;
     // ---- trailing update: rows / columns r0 .. n, lower 4 x 4 tiles
     const int r0 = k0 + kb;
     const int m = n - r0;
@@ -169,6 +171,7 @@ __global__ void __launch_bounds__(THREADS) batched_posv_kernel(BatchArgs<T> p) {
   T* bv = reinterpret_cast<T*>(smem_raw);          // kMaxBatchN values
   T* sm = bv + kMaxBatchN;                         // staged matrix
   __shared__ int s_ticket, s_fail;
+  __shared__ T s_inv;
   const int tid = threadIdx.x;
   for (;;) {
     if (tid == 0) s_ticket = atomicAdd(p.counter, 1);
@@ -190,7 +193,7 @@ __global__ void __launch_bounds__(THREADS) batched_posv_kernel(BatchArgs<T> p) {
       }
     for (int i = tid; i < n; i += THREADS) bv[i] = B[i];
     __syncthreads();
-    const int fail = n > 0 ? factor_solve<T, NBP, THREADS>(M, ld, n, bv, &s_fail) : -1;
+    const int fail = n > 0 ? factor_solve<T, NBP, THREADS>(M, ld, n, bv, &s_fail, &s_inv) : -1;
     if (staged)
       for (int idx = tid; idx < n * n; idx += THREADS) {
         const int i = idx % n, j = idx / n;
@@ -205,11 +208,15 @@ __global__ void __launch_bounds__(THREADS) batched_posv_kernel(BatchArgs<T> p) {
 
 // ---- variants and launch ---------------------------------------------------------------------
 
+// Kernel variants the autotuner sweeps: panel width x threads per CTA x the largest order staged
+// in shared memory (-1 = as large as fits in one CTA's shared memory; smaller caps leave room for
+// more CTAs per SM, the larger systems then running in place in global memory, L2-resident).
 struct Variant {
-  int nbp, threads;
+  int nbp, threads, smem_cap;
 };
-constexpr Variant kVariants[] = {{16, 128}, {32, 128}, {16, 256}, {32, 256}};
-constexpr int kNumVariants = 4;
+constexpr Variant kVariants[] = {{16, 128, -1}, {32, 128, -1}, {16, 256, -1}, {32, 256, -1},
+                                 {16, 128, 96},  {16, 256, 96},  {16, 128, 0},  {16, 256, 0}};
+constexpr int kNumVariants = 8;
 
 template <typename T>
 size_t smem_bytes(int smem_max_n) {
@@ -227,25 +234,26 @@ int launch_variant(const BatchArgs<T>& args, int grid, size_t smem, cudaStream_t
 }
 
 template <typename T>
+const void* kernel_of(int variant) {
+  const Variant v = kVariants[variant];
+  if (v.nbp == 16) return v.threads == 128 ? (const void*)batched_posv_kernel<T, 16, 128>
+                                           : (const void*)batched_posv_kernel<T, 16, 256>;
+  return v.threads == 128 ? (const void*)batched_posv_kernel<T, 32, 128> : (const void*)batched_posv_kernel<T, 32, 256>;
+}
+
+template <typename T>
 int launch_batched(int variant, const BatchArgs<T>& args, int grid, size_t smem, cudaStream_t s) {
-  switch (variant) {
-    case 0: return launch_variant<T, 16, 128>(args, grid, smem, s);
-    case 1: return launch_variant<T, 32, 128>(args, grid, smem, s);
-    case 2: return launch_variant<T, 16, 256>(args, grid, smem, s);
-    default: return launch_variant<T, 32, 256>(args, grid, smem, s);
-  }
+  const Variant v = kVariants[variant];
+  if (v.nbp == 16) return v.threads == 128 ? launch_variant<T, 16, 128>(args, grid, smem, s)
+                                           : launch_variant<T, 16, 256>(args, grid, smem, s);
+  return v.threads == 128 ? launch_variant<T, 32, 128>(args, grid, smem, s)
+                          : launch_variant<T, 32, 256>(args, grid, smem, s);
 }
 
 template <typename T>
 int occupancy(int variant, size_t smem) {
   int blocks = 0;
-  const void* f = nullptr;
-  switch (variant) {
-    case 0: f = (const void*)batched_posv_kernel<T, 16, 128>; break;
-    case 1: f = (const void*)batched_posv_kernel<T, 32, 128>; break;
-    case 2: f = (const void*)batched_posv_kernel<T, 16, 256>; break;
-    default: f = (const void*)batched_posv_kernel<T, 32, 256>; break;
-  }
+  const void* f = kernel_of<T>(variant);
   cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, f, kVariants[variant].threads, smem);
   return blocks;
@@ -287,7 +295,7 @@ struct BatchPlan {
   int smem_max_n = 0;
   int grid = 0;
   size_t smem = 0;
-  double tuned_ms[kNumVariants] = {0, 0, 0, 0};
+  double tuned_ms[kNumVariants] = {};
   // cached graph
   cudaGraphExec_t exec = nullptr;
   void* g_a = nullptr;
@@ -304,11 +312,13 @@ void configure(BatchPlan* p) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  // stage in shared memory every system whose lower triangle fits (leaving room for b)
+  // stage in shared memory every system whose matrix fits (leaving room for b), up to the variant's cap
   int nmax = std::min(p->max_n, kMaxBatchN);
   while (nmax > 0 && smem_bytes<T>(nmax) > (size_t)optin) --nmax;
+  const int cap = kVariants[p->variant].smem_cap;
+  if (cap >= 0 && nmax > cap) nmax = cap;
   p->smem_max_n = nmax;
-  p->smem = smem_bytes<T>(std::max(nmax, 1));
+  p->smem = nmax > 0 ? smem_bytes<T>(nmax) : (size_t)kMaxBatchN * sizeof(T);
   const int occ = std::max(1, occupancy<T>(p->variant, p->smem));
   p->grid = sms * occ;
 }
@@ -562,9 +572,11 @@ void write_cache(const char* path, const std::string& sig, const BatchPlan* p) {
   auto entries = read_cache(path);
   char body[512];
   snprintf(body, sizeof body,
-           "{\"variant\": %d, \"panel\": %d, \"threads\": %d, \"smem_max_n\": %d, \"ms\": [%.4f, %.4f, %.4f, %.4f]}",
+           "{\"variant\": %d, \"panel\": %d, \"threads\": %d, \"smem_max_n\": %d, \"ms\": [%.4f, %.4f, %.4f, %.4f, "
+           "%.4f, %.4f, %.4f, %.4f]}",
            p->variant, kVariants[p->variant].nbp, kVariants[p->variant].threads, p->smem_max_n, p->tuned_ms[0],
-           p->tuned_ms[1], p->tuned_ms[2], p->tuned_ms[3]);
+           p->tuned_ms[1], p->tuned_ms[2], p->tuned_ms[3], p->tuned_ms[4], p->tuned_ms[5], p->tuned_ms[6],
+           p->tuned_ms[7]);
   bool found = false;
   for (auto& e : entries)
     if (e.first == sig) {

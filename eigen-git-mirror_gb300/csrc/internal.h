@@ -79,10 +79,12 @@ struct MixedLayout {
   size_t es_k, bytes, fallback_bytes;
 };
 int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* out);  // defaults; -1 if invalid
-MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o);
-// The solve on a caller-supplied workspace of ws_bytes (>= layout.bytes).  With may_allocate false
-// it creates no events and allocates nothing: the fallback then runs only if the workspace also
-// holds fallback_bytes, and the report's device times are 0.
+// lookahead: room for the second set of panel operands that the two-stream schedule uses.
+MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o, bool lookahead);
+// The solve on a caller-supplied workspace of ws_bytes (>= mixed_layout(.., may_allocate).bytes).
+// With may_allocate false it creates no streams or events and allocates nothing: the factorisation
+// runs without lookahead, the fallback runs only if the workspace also holds fallback_bytes, and the
+// report's device times are 0.
 int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
                     double* x, int64_t ldx, const gbllt_mixed_opts& o, gbllt_mixed_report* rep, void* ws,
                     size_t ws_bytes, bool may_allocate, cudaStream_t s);

@@ -290,13 +290,24 @@ int split_parts(int prec) {
   }
 }
 
-int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void* const* parts, int64_t ldk,
-                    DevStatus* st, int* d_err, cudaStream_t s) {
+// Factor the scaled FP32 working matrix af (n x n lower, ldf) with tensor-core trailing updates.
+// With a side stream (and the events and second operand set that go with it), one panel of
+// lookahead: panel k's trailing update is split into the strip of panel k+1's columns (main stream,
+// first) and the rest (side stream), so panel k+1's factorisation overlaps the large update.
+//   ev[0/1]: panel k's operands are split (side waits before its update)
+//   ev[2/3]: side update k finished (main waits before touching those columns / operand buffers)
+int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void* const* parts, void* const* parts2,
+                    int64_t ldk, DevStatus* st, int* d_err, cudaStream_t s, cudaStream_t side, cudaEvent_t* ev) {
   static const std::string ksplit = "split_panel";
   const int kind = (prec == GBLLT_PREC_BF16 || prec == GBLLT_PREC_BF16X3 || prec == GBLLT_PREC_BF16X6) ? kTcBF16
                                                                                                        : kTcTF32;
   const int np = split_parts(prec);
-  for (int64_t k0 = 0; k0 < n; k0 += panel) {
+  const bool lookahead = side != nullptr && prec != GBLLT_PREC_FP32;
+  const int nseg = np == 1 ? 1 : np == 2 ? 3 : 6;
+  const uint32_t code = np == 1 ? kSegX1 : np == 2 ? kSegX3 : kSegX6;
+  int iter = 0;
+  bool side_pending = false;
+  for (int64_t k0 = 0; k0 < n; k0 += panel, ++iter) {
     const int bs = (int)(n - k0 < panel ? n - k0 : panel);
     const int64_t rs = n - k0 - bs;
     // panel: 64-column steps; the in-panel update only touches the panel's remaining columns
@@ -313,20 +324,45 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void
       }
     }
     if (rs > 0 && prec != GBLLT_PREC_FP32) {
+      void* const* pp = (lookahead && (iter & 1)) ? parts2 : parts;
+      // the operand buffers about to be overwritten were last read by the side update two panels ago,
+      // and the columns of the next panel were last written by the previous side update
+      if (lookahead && side_pending) GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[2 + ((iter + 1) & 1)], 0));
       {
         ProfScope ps(ksplit.c_str(), s, 0.0, (double)rs * bs * 4.0 + (double)rs * ldk * (kind == kTcBF16 ? 2 : 4) * np);
         dim3 grid((unsigned)ceil_div(rs, TS), (unsigned)ceil_div(ldk, TS));
         if (kind == kTcBF16)
-          split_panel_kernel<0><<<grid, 256, 0, s>>>(af, ldf, k0 + bs, k0, rs, bs, np, parts[0], parts[1], parts[2], ldk);
+          split_panel_kernel<0><<<grid, 256, 0, s>>>(af, ldf, k0 + bs, k0, rs, bs, np, pp[0], pp[1], pp[2], ldk);
         else
-          split_panel_kernel<1><<<grid, 256, 0, s>>>(af, ldf, k0 + bs, k0, rs, bs, np, parts[0], parts[1], parts[2], ldk);
+          split_panel_kernel<1><<<grid, 256, 0, s>>>(af, ldf, k0 + bs, k0, rs, bs, np, pp[0], pp[1], pp[2], ldk);
       }
-      TcOperand op{{parts[0], parts[1], parts[2]}, rs, bs, ldk, 0};
-      const int nseg = np == 1 ? 1 : np == 2 ? 3 : 6;
-      const uint32_t code = np == 1 ? kSegX1 : np == 2 ? kSegX3 : kSegX6;
-      int rc = tc_update(op, op, kind, nseg, code, af + (k0 + bs) * ldf + (k0 + bs), ldf, rs, rs, true, d_err, s);
-      if (rc) return rc;
+      TcOperand op{{pp[0], pp[1], pp[2]}, rs, bs, ldk, 0};
+      float* c0 = af + (k0 + bs) * ldf + (k0 + bs);
+      int rc;
+      if (!lookahead || rs <= panel) {
+        if (lookahead && side_pending) GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[2 + ((iter + 1) & 1)], 0));
+        rc = tc_update(op, op, kind, nseg, code, c0, ldf, rs, rs, kTcLowerTri, d_err, s);
+        if (rc) return rc;
+      } else {
+        const int64_t nb = panel;  // the next panel's width
+        // strip: columns of the next panel, all rows below (row >= column inside its top block)
+        rc = tc_update(op, op, kind, nseg, code, c0, ldf, rs, nb, kTcLowerRect, d_err, s);
+        if (rc) return rc;
+        GB_CUDA_TRY(cudaEventRecord(ev[iter & 1], s));
+        // the rest of the trailing matrix on the side stream
+        GB_CUDA_TRY(cudaStreamWaitEvent(side, ev[iter & 1], 0));
+        TcOperand op2{{pp[0], pp[1], pp[2]}, rs, bs, ldk, nb};
+        rc = tc_update(op2, op2, kind, nseg, code, c0 + nb * ldf + nb, ldf, rs - nb, rs - nb, kTcLowerTri, d_err,
+                       side);
+        if (rc) return rc;
+        GB_CUDA_TRY(cudaEventRecord(ev[2 + (iter & 1)], side));
+        side_pending = true;
+      }
     }
+  }
+  if (lookahead && side_pending) {
+    GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[2], 0));
+    GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[3], 0));
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
@@ -351,7 +387,7 @@ int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o) {
   return 0;
 }
 
-MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o) {
+MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o, bool lookahead) {
   MixedLayout L;
   L.ldf = round_up(n, 32);
   L.ldk = round_up(o.panel, 64);
@@ -365,7 +401,7 @@ MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o) {
   L.es_k = (o.precision == GBLLT_PREC_BF16 || o.precision == GBLLT_PREC_BF16X3 || o.precision == GBLLT_PREC_BF16X6)
                ? 2 : 4;
   L.bytes = (size_t)L.ldf * n * 4 + (size_t)n * 8 + (size_t)n * nrhs * (8 + 4) + (size_t)L.nparts * n * nrhs * 8 +
-            (size_t)L.nsq * 8 + 64 + (size_t)split_parts(o.precision) * n * L.ldk * L.es_k +
+            (size_t)L.nsq * 8 + 64 + (size_t)split_parts(o.precision) * (lookahead ? 2 : 1) * n * L.ldk * L.es_k +
             sizeof(DevStatus) + 16 * 256 + potrs_ws_bytes(n, 8);
   L.fallback_bytes = (size_t)n * n * 8 + 256;
   return L;
@@ -376,7 +412,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
                     size_t ws_bytes, bool may_allocate, cudaStream_t s) {
   gbllt_mixed_report r;
   memset(&r, 0, sizeof r);
-  const MixedLayout Ly = mixed_layout(n, nrhs, o);
+  const MixedLayout Ly = mixed_layout(n, nrhs, o, may_allocate);
   if (ws_bytes < Ly.bytes) return GBLLT_ERR_ALLOC;
   const int64_t ldf = Ly.ldf, ldk = Ly.ldk;
   const int nb = Ly.nb, zc = Ly.zc, nparts = Ly.nparts, jpc = Ly.jpc, nsq = Ly.nsq;
@@ -397,7 +433,10 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   double* sq = ar.take<double>(nsq);
   double* norms = ar.take<double>(8);  // [0] ||A||^2, [1] ||R||^2, [2] ||X||^2
   void* parts[3] = {nullptr, nullptr, nullptr};
+  void* parts2[3] = {nullptr, nullptr, nullptr};  // second operand set for the lookahead schedule
   for (int i = 0; i < split_parts(o.precision); ++i) parts[i] = ar.take<char>((size_t)n * ldk * es_k);
+  if (may_allocate)
+    for (int i = 0; i < split_parts(o.precision); ++i) parts2[i] = ar.take<char>((size_t)n * ldk * es_k);
   DevStatus* st = ar.take<DevStatus>(1);
   int* d_err = (int*)&st->timeout;
   void* solve_ws = ar.take<char>(potrs_ws_bytes(n, 8));  // sized for the FP64 fallback solve too
@@ -458,7 +497,18 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     else convert_scaled_kernel<false><<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(a, lda, n, dsc, af, ldf);
   }
   // 2. low-precision factorisation
-  rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, parts, ldk, st, d_err, s);
+  // lookahead needs a second stream and four events: only where creating them is allowed
+  cudaStream_t side = nullptr;
+  cudaEvent_t lev[4] = {nullptr, nullptr, nullptr, nullptr};
+  if (may_allocate) {
+    GB_CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    for (auto& e : lev) GB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, parts, parts2, ldk, st, d_err, s, side, lev);
+  if (side) {
+    cudaStreamDestroy(side);  // work already issued on it completes; s waited on its last event
+    for (auto& e : lev) cudaEventDestroy(e);
+  }
   if (rc) return rc;
   if ((rc = stamp(1))) return rc;
   DevStatus hst;
@@ -553,7 +603,7 @@ int posv_mixed_dev(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t
                    double* x, int64_t ldx, const gbllt_mixed_opts* opts, gbllt_mixed_report* rep, cudaStream_t s) {
   gbllt_mixed_opts o;
   if (resolve_mixed_opts(opts, &o)) return -10;
-  const MixedLayout Ly = mixed_layout(n, nrhs, o);
+  const MixedLayout Ly = mixed_layout(n, nrhs, o, true);
   void* raw = nullptr;
   if (cudaMallocAsync(&raw, Ly.bytes, s) != cudaSuccess) {
     cudaGetLastError();

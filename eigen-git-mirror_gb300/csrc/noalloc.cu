@@ -69,7 +69,7 @@ extern "C" int gbllt_dposv_mixed_dev_noalloc(char uplo, int64_t n, int64_t nrhs,
   if (resolve_mixed_opts(opts, &o)) return -10;
   if (report) memset(report, 0, sizeof *report);
   if (n == 0 || nrhs == 0) return GBLLT_SUCCESS;
-  const MixedLayout ly = mixed_layout(n, nrhs, o);
+  const MixedLayout ly = mixed_layout(n, nrhs, o, false);
   const size_t need = ly.bytes + (o.fallback_fp64 ? ly.fallback_bytes + 256 : 0);
   if (need > kScratchBytes) {
     char buf[256];

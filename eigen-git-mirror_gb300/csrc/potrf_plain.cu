@@ -6,7 +6,9 @@
 //
 //   potrf_diag_kernel   one CTA factors the 64 x 64 diagonal block A11 in shared memory
 //                       (the role of llt_inplace::unblocked, LLT.h:312-336; the pivot test is
-//                       the same `x <= 0`, LLT.h:329);
+//                       the same `x <= 0`, LLT.h:329).  Where Eigen divides the column by the
+//                       pivot, the kernel multiplies by its reciprocal (one division per column):
+//                       FP64 division is a long DFMA sequence on GB300's narrow FP64 pipe;
 //   trsm_panel_kernel   A21 <- A21 L11^{-T}: one thread per row of A21, the row held in
 //                       registers, L11 broadcast from shared memory (the OnTheRight solve that
 //                       LLT.h:364 issues, TriangularSolverMatrix.h:188-329);
@@ -42,17 +44,22 @@ __global__ void __launch_bounds__(256) potrf_diag_kernel(T* __restrict__ a, long
   if (tid == 0) fail = -1;
   __syncthreads();
   const int tx = tid & 63, ty = tid >> 6;
+  __shared__ TC inv_s;
   int j = 0;
   for (; j < bs; ++j) {
     if (tid == 0) {
       const TC d = s[j][j];
       if (d <= TC(0)) fail = j;
-      else s[j][j] = sqrt(d);
+      else {
+        const TC r = sqrt(d);
+        s[j][j] = r;
+        inv_s = TC(1) / r;  // one division per column; the column is scaled by multiplication
+      }
     }
     __syncthreads();
     if (fail >= 0) break;  // block-uniform
-    const TC djj = s[j][j];
-    if (tid > j && tid < bs) s[j][tid] = s[j][tid] / djj;
+    const TC inv = inv_s;
+    if (tid > j && tid < bs) s[j][tid] = s[j][tid] * inv;
     __syncthreads();
     for (int l = j + 1 + ty; l < bs; l += 4) {
       const TC ljl = s[j][l];
@@ -73,6 +80,7 @@ __global__ void __launch_bounds__(128) trsm_panel_kernel(T* __restrict__ a, long
                                                          long long rs, const DevStatus* __restrict__ st) {
   if (st->fail_col >= 0) return;
   __shared__ T L[NB][NB + 1];  // L[j][p] = L11(j, p); identity outside the bs x bs block
+  __shared__ T rdiag[NB];      // 1 / L11(j, j): the substitution multiplies instead of dividing
   const T* l11 = a + (long long)k0 * lda + k0;
   for (int idx = threadIdx.x; idx < NB * NB; idx += 128) {
     const int j = idx % NB, p = idx / NB;
@@ -80,6 +88,8 @@ __global__ void __launch_bounds__(128) trsm_panel_kernel(T* __restrict__ a, long
     if (j < bs && p < bs && j >= p) v = l11[(long long)p * lda + j];
     L[j][p] = v;
   }
+  __syncthreads();
+  if (threadIdx.x < NB) rdiag[threadIdx.x] = T(1) / L[threadIdx.x][threadIdx.x];
   __syncthreads();
   const long long r = (long long)blockIdx.x * 128 + threadIdx.x;
   if (r >= rs) return;
@@ -92,7 +102,7 @@ __global__ void __launch_bounds__(128) trsm_panel_kernel(T* __restrict__ a, long
     T v = x[jj];
 #pragma unroll
     for (int p = 0; p < jj; ++p) v = fma(-x[p], L[jj][p], v);
-    x[jj] = v / L[jj][jj];
+    x[jj] = v * rdiag[jj];
   }
 #pragma unroll
   for (int p = 0; p < NB; ++p)

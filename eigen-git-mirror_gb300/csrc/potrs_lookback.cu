@@ -11,7 +11,8 @@
 //   - applies the pre-inverted diagonal triangle (a 64 x 64 product instead of a 64-step
 //     substitution on the critical path), stores Y_I, fences, and raises its flag.
 // The backward sweep runs the same scheme on L^T from the last block up.  Right-hand sides are
-// processed in chunks of 16 (one pair of launches per chunk).
+// split into chunks of 16 that run as independent chains in the same launch (grid.y), so the FP64
+// work of the last row blocks is spread over several SMs.
 //
 // The diagonal inverses come from trinv_kernel (one CTA per block, column-wise substitution).
 #include "internal.h"
@@ -21,7 +22,7 @@ namespace gbllt {
 namespace {
 
 constexpr int RB = 64;
-constexpr int RC = 16;
+constexpr int RC = 512;  // right-hand sides per launch (at most 32 chains of 16)
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
 __device__ __forceinline__ unsigned long long gtimer() {
@@ -67,21 +68,31 @@ __global__ void __launch_bounds__(128) trinv_kernel(const T* __restrict__ a, lon
   }
 }
 
-template <typename T>
+template <typename T, int RCT>
 struct SweepSmem {
-  T Ls[RB][RB + 1];   // Ls[p][r]: forward L(I0+r, J0+p); backward L(J0+p, I0+r)
-  T Ds[RB][RB + 1];   // inverse of the diagonal triangle, Ds[i][p] = Linv(i, p)
-  T Ys[RB][RC + 1];   // the solved block J
-  T Bs[RB][RC + 1];   // this block's right-hand sides
+  T Ls[RB][RB + 1];    // Ls[p][r]: forward L(I0+r, J0+p); backward L(J0+p, I0+r)
+  T Ds[RB][RB + 1];    // inverse of the diagonal triangle, Ds[i][p] = Linv(i, p)
+  T Ys[RB][RCT + 1];   // the solved block J
+  T Bs[RB][RCT + 1];   // this block's right-hand sides
 };
 
-template <typename T, bool UP, bool BWD>
+// RCT right-hand sides per pass; thread (r, cq) owns row r and RCT/4 of them.
+template <typename T, bool UP, bool BWD, int RCT>
 __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, long long lda, long long n,
                                                     T* __restrict__ b, long long ldb, int nrhs, const T* __restrict__ inv,
                                                     int* __restrict__ flags, int* __restrict__ counter,
                                                     int* __restrict__ err) {
+  constexpr int CPT = RCT / 4;
+  // right-hand-side chunk: an independent chain with its own tickets and flags
+  {
+    const int chunk = blockIdx.y;
+    b += (long long)chunk * RCT * ldb;
+    nrhs -= chunk * RCT;
+    flags += (long long)chunk * ((n + RB - 1) / RB);
+    counter += chunk;
+  }
   extern __shared__ __align__(16) unsigned char sweep_raw[];
-  SweepSmem<T>& sm = *reinterpret_cast<SweepSmem<T>*>(sweep_raw);
+  SweepSmem<T, RCT>& sm = *reinterpret_cast<SweepSmem<T, RCT>*>(sweep_raw);
   __shared__ int s_ticket, s_abort;
   const int tid = threadIdx.x, r = tid & 63, cq = tid >> 6;
   const int nb = (int)((n + RB - 1) / RB);
@@ -98,11 +109,13 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
     const int i = idx & 63, p = idx >> 6;
     sm.Ds[i][p] = Dinv[(long long)p * RB + i];
   }
-  for (int idx = tid; idx < RB * RC; idx += 256) {
+  for (int idx = tid; idx < RB * RCT; idx += 256) {
     const int p = idx & 63, c = idx >> 6;
     sm.Bs[p][c] = (I0 + p < n && c < nrhs) ? b[(long long)c * ldb + I0 + p] : T(0);
   }
-  T acc[4] = {T(0), T(0), T(0), T(0)};
+  T acc[CPT];
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) acc[q] = T(0);
   // off-diagonal blocks in the order they become ready
   const int jfirst = BWD ? nb - 1 : 0;
   const int jstep = BWD ? -1 : 1;
@@ -132,33 +145,37 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
     }
     __syncthreads();
     if (s_abort) return;
-    for (int idx = tid; idx < RB * RC; idx += 256) {
+    for (int idx = tid; idx < RB * RCT; idx += 256) {
       const int p = idx & 63, c = idx >> 6;
       sm.Ys[p][c] = (J0 + p < n && c < nrhs) ? __ldcg(b + (long long)c * ldb + J0 + p) : T(0);
     }
     __syncthreads();
-#pragma unroll 8
+#pragma unroll 4
     for (int p = 0; p < RB; ++p) {
       const T l = sm.Ls[p][r];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) acc[q] = fma(l, sm.Ys[p][cq * 4 + q], acc[q]);
+      for (int q = 0; q < CPT; ++q) acc[q] = fma(l, sm.Ys[p][cq * CPT + q], acc[q]);
     }
     __syncthreads();
   }
-  // V = B_I - acc, then X_I = Linv V (forward) or Linv^T V (backward)
-#pragma unroll
-  for (int q = 0; q < 4; ++q) sm.Ys[r][cq * 4 + q] = sm.Bs[r][cq * 4 + q] - acc[q];
+  // V = B_I - acc, then X_I = Linv V (forward) or Linv^T V (backward).  The barrier orders the Ds/Bs
+  // preload (written under another thread mapping) before these reads when the J loop ran no pass.
   __syncthreads();
-  T x[4] = {T(0), T(0), T(0), T(0)};
-#pragma unroll 8
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) sm.Ys[r][cq * CPT + q] = sm.Bs[r][cq * CPT + q] - acc[q];
+  __syncthreads();
+  T x[CPT];
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) x[q] = T(0);
+#pragma unroll 4
   for (int p = 0; p < RB; ++p) {
     const T d = BWD ? sm.Ds[p][r] : sm.Ds[r][p];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) x[q] = fma(d, sm.Ys[p][cq * 4 + q], x[q]);
+    for (int q = 0; q < CPT; ++q) x[q] = fma(d, sm.Ys[p][cq * CPT + q], x[q]);
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int c = cq * 4 + q;
+  for (int q = 0; q < CPT; ++q) {
+    const int c = cq * CPT + q;
     if (I0 + r < n && c < nrhs) b[(long long)c * ldb + I0 + r] = x[q];
   }
   __threadfence();
@@ -166,23 +183,35 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
   if (tid == 0) atomicExch(flags + I, 1);
 }
 
+template <typename T, bool UP, bool BWD, int RCT>
+void launch_sweep_rc(int nb, const T* a, long long lda, long long n, T* b, long long ldb, int nrhs, const T* inv,
+                     int* flags, int* counter, int* err, cudaStream_t s) {
+  static bool attr = false;
+  const int smem = (int)sizeof(SweepSmem<T, RCT>);
+  if (!attr) {
+    cudaFuncSetAttribute(sweep_kernel<T, UP, BWD, RCT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  dim3 grid((unsigned)nb, (unsigned)((nrhs + RCT - 1) / RCT));
+  sweep_kernel<T, UP, BWD, RCT><<<grid, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, flags, counter, err);
+}
+
+// One launch per sweep: chunks of RCT right-hand sides run as parallel chains (grid.y); 4 columns
+// per chunk for a single right-hand side, 16 otherwise (more chains spread the FP64 work of the
+// last row blocks over more SMs).
 template <typename T, bool UP, bool BWD>
 void launch_sweep(int nb, const T* a, long long lda, long long n, T* b, long long ldb, int nrhs, const T* inv,
                   int* flags, int* counter, int* err, cudaStream_t s) {
-  static bool attr = false;
-  const int smem = (int)sizeof(SweepSmem<T>);
-  if (!attr) {
-    cudaFuncSetAttribute(sweep_kernel<T, UP, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr = true;
-  }
-  sweep_kernel<T, UP, BWD><<<nb, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, flags, counter, err);
+  if (nrhs <= 4) launch_sweep_rc<T, UP, BWD, 4>(nb, a, lda, n, b, ldb, nrhs, inv, flags, counter, err, s);
+  else launch_sweep_rc<T, UP, BWD, 16>(nb, a, lda, n, b, ldb, nrhs, inv, flags, counter, err, s);
 }
 
 }  // namespace
 
 size_t potrs_ws_bytes(int64_t n, size_t elem) {
   const int64_t nb = (n + RB - 1) / RB;
-  return (size_t)nb * RB * RB * elem + (size_t)(2 * nb + 8) * sizeof(int) + 512;
+  const int64_t nch = RC / 16;  // chains of one launch, at most
+  return (size_t)nb * RB * RB * elem + (size_t)(2 * nch * nb + 2 * nch + 8) * sizeof(int) + 512;
 }
 
 template <typename T>
@@ -193,9 +222,7 @@ int potrs_ws(bool upper, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b,
   static const std::string kf = std::string("sweep_") + tname<T>();
   const int nb = (int)ceil_div(n, RB);
   T* inv = (T*)ws;
-  int* flags = (int*)((char*)ws + (((size_t)nb * RB * RB * sizeof(T) + 255) & ~(size_t)255));
-  int* counter = flags + 2 * nb;   // [0] forward ticket, [1] backward ticket
-  int* err = counter + 2;
+  int* base = (int*)((char*)ws + (((size_t)nb * RB * RB * sizeof(T) + 255) & ~(size_t)255));
   {
     ProfScope ps(ki.c_str(), s, (double)nb * RB * RB * RB / 3.0, (double)n * RB * sizeof(T) * 1.5);
     if (upper) trinv_kernel<T, true><<<nb, 128, 0, s>>>(a, lda, n, inv);
@@ -203,19 +230,25 @@ int potrs_ws(bool upper, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b,
   }
   for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
     const int nc = (int)(nrhs - c0 < RC ? nrhs - c0 : RC);
+    const int nch = nc <= 4 ? 1 : (nc + 15) / 16;  // chains in this launch
+    int* fflags = base;                 // forward: nch x nb
+    int* bflags = base + nch * nb;      // backward: nch x nb
+    int* fctr = base + 2 * nch * nb;    // nch forward tickets, nch backward tickets, error word
+    int* bctr = fctr + nch;
+    int* err = bctr + nch;
     T* bc = b + c0 * ldb;
-    GB_CUDA_TRY(cudaMemsetAsync(flags, 0, (size_t)(2 * nb + 3) * sizeof(int), s));
+    GB_CUDA_TRY(cudaMemsetAsync(base, 0, (size_t)(2 * nch * nb + 2 * nch + 1) * sizeof(int), s));
     // algorithmic work per sweep: the lower triangle of L read once, 2 flops per entry and RHS
     const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
     {
       ProfScope ps(kf.c_str(), s, fl, by);
-      if (upper) launch_sweep<T, true, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, counter, err, s);
-      else launch_sweep<T, false, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, counter, err, s);
+      if (upper) launch_sweep<T, true, false>(nb, a, lda, n, bc, ldb, nc, inv, fflags, fctr, err, s);
+      else launch_sweep<T, false, false>(nb, a, lda, n, bc, ldb, nc, inv, fflags, fctr, err, s);
     }
     {
       ProfScope ps(kf.c_str(), s, fl, by);
-      if (upper) launch_sweep<T, true, true>(nb, a, lda, n, bc, ldb, nc, inv, flags + nb, counter + 1, err, s);
-      else launch_sweep<T, false, true>(nb, a, lda, n, bc, ldb, nc, inv, flags + nb, counter + 1, err, s);
+      if (upper) launch_sweep<T, true, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
+      else launch_sweep<T, false, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
     }
   }
   GB_CUDA_TRY(cudaGetLastError());

@@ -154,7 +154,9 @@ struct TcParams {
   int k;               // depth of one segment (elements)
   int nseg;            // 1..8
   uint32_t seg_code;   // 4 bits per segment s: bits [4s, 4s+2) = part of A, [4s+2, 4s+4) = part of B
-  int lower;           // 1: only tiles / entries with global row >= column (SYRK)
+  int lower;           // 0: every tile of the m x n rectangle; 1: lower-triangle tiles of a square (SYRK);
+                       // 2: every tile of the rectangle; with 1 and 2 only entries with row >= column
+                       // are written
   int mt;              // tiles along m
   long long tiles;     // tiles in the launch
   int* err;            // device error word (set to 1 on a timeout)
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(192, 1) tc_update_kernel(const __grid_constant
 
   auto coords = [&](long long t, int& row0, int& col0) {
     int ti, tj;
-    if (p.lower) lower_tile_coords(t, ti, tj);
+    if (p.lower == 1) lower_tile_coords(t, ti, tj);
     else { ti = (int)(t % p.mt); tj = (int)(t / p.mt); }
     row0 = ti * BM;
     col0 = tj * BN;
@@ -358,7 +360,7 @@ int make_map(CUtensorMap* m, const void* base, int kind, int64_t rows, int64_t k
 }  // namespace
 
 int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32_t seg_code, float* c, int64_t ldc,
-              int64_t m, int64_t n, bool lower, int* d_err, cudaStream_t s) {
+              int64_t m, int64_t n, int lower, int* d_err, cudaStream_t s) {
   if (m <= 0 || n <= 0 || a.k <= 0) return GBLLT_SUCCESS;
   if (nseg < 1 || nseg > 8) return GBLLT_ERR_INTERNAL;
   const int es = kind == 0 ? 2 : 4;
@@ -382,11 +384,11 @@ int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32
   p.k = (int)a.k;
   p.nseg = nseg;
   p.seg_code = seg_code;
-  p.lower = lower ? 1 : 0;
+  p.lower = lower;
   p.mt = (int)ceil_div(m, BM);
   p.err = d_err;
   const int64_t nt = ceil_div(n, BN);
-  p.tiles = lower ? (int64_t)p.mt * (p.mt + 1) / 2 : (int64_t)p.mt * nt;
+  p.tiles = lower == 1 ? (int64_t)p.mt * (p.mt + 1) / 2 : (int64_t)p.mt * nt;
   static int sms = 0;
   if (!sms) {
     int dev = 0;
@@ -398,9 +400,11 @@ int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32
   static bool attr_set[2] = {false, false};
   static const std::string kname[2] = {"tc_update_bf16", "tc_update_tf32"};
   // algorithmic work: 2 k flops per updated entry and segment; operands read once, C read+written
-  const double entries = lower ? (double)m * (m + 1) / 2.0 : (double)m * n;
+  const double entries = lower == 1   ? (double)m * (m + 1) / 2.0
+                         : lower == 2 ? (double)m * n - (double)n * (n - 1) / 2.0
+                                      : (double)m * n;
   ProfScope ps(kname[kind].c_str(), s, 2.0 * entries * a.k * nseg,
-               ((double)(m + (lower ? 0 : n)) * a.k * nseg * es) + entries * 8.0);
+               ((double)(m + (lower == 1 ? 0 : n)) * a.k * nseg * es) + entries * 8.0);
   if (kind == 0) {
     if (!attr_set[0]) {
       GB_CUDA_TRY(cudaFuncSetAttribute(tc_update_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));

@@ -20,11 +20,13 @@ struct TcOperand {
 constexpr int kTcBF16 = 0;
 constexpr int kTcTF32 = 1;
 
-// C (m x n fp32, column-major, ldc) -= sum over nseg segments of A_s B_s^T (lower tiles and
-// entries only when `lower`); segment s reads part (code & 3) of A and part (code >> 2) of B,
-// code = (seg_code >> 4s) & 15.  d_err receives 1 if a bounded wait ran out.
+// C (m x n fp32, column-major, ldc) -= sum over nseg segments of A_s B_s^T; segment s reads part
+// (code & 3) of A and part (code >> 2) of B, code = (seg_code >> 4s) & 15.  lower: 0 = the whole
+// rectangle; 1 = the lower triangle of a square C (SYRK); 2 = the rectangle, writing only entries
+// with row >= column.  d_err receives 1 if a bounded wait ran out.
+constexpr int kTcFull = 0, kTcLowerTri = 1, kTcLowerRect = 2;
 int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32_t seg_code, float* c, int64_t ldc,
-              int64_t m, int64_t n, bool lower, int* d_err, cudaStream_t s);
+              int64_t m, int64_t n, int lower, int* d_err, cudaStream_t s);
 
 // Segment tables (parts: 0 = hi, 1 = mid/lo of a two-way split, 2 = lo of a three-way split),
 // ordered smallest terms first.

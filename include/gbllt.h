@@ -176,7 +176,7 @@ GBLLT_API int gbllt_batch_plan_layout(const gbllt_batch_plan* plan, int64_t* aof
  * of the plan's sizes and keeps the fastest; with cache_path, a previous choice for the same
  * sizes is read from / a new one written to that JSON file.  Returns the variant index (>= 0). */
 GBLLT_API int gbllt_batch_plan_tune(gbllt_batch_plan* plan, const char* cache_path, void* stream);
-/* Use kernel variant `variant` (0..3) without tuning. */
+/* Use kernel variant `variant` (0..7) without tuning. */
 GBLLT_API int gbllt_batch_plan_set_variant(gbllt_batch_plan* plan, int variant);
 /* The variant in use: returns its index and its panel width, threads per CTA and the largest
  * order staged in shared memory. */
