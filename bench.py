@@ -568,34 +568,41 @@ def run_c5(args):
     d2 = ((X[:, :, None, :] - X[:, None, :, :]) ** 2).sum(-1)
     A = torch.exp(-d2 / (2 * 0.2 ** 2)) + 1e-2 * torch.eye(n, dtype=torch.float64, device="cuda")
     del d2
-    info = torch.zeros(1, dtype=torch.int64, device="cuda")
+    # the 64 independent problems run on NSTREAM concurrent streams (matrix m on stream m % NSTREAM)
+    nstream = 8
+    streams = [torch.cuda.Stream() for _ in range(nstream)]
+    infos = [torch.zeros(1, dtype=torch.int64, device="cuda") for _ in range(nstream)]
     res = {}
     for it in range(2):  # first pass warms up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        Ls, alphas, fs = [], [], []
+        Ls, alphas, fs = [None] * nmat, [None] * nmat, [None] * nmat
         for m in range(nmat):
-            L = A[m].clone()  # symmetric: row-major storage = column-major A
-            G.potrf_dev(L, n, n, info, "L", s)
-            al = Y[m].clone().reshape(1, n)
-            G.potrs_dev(L, n, n, al, 1, n, "L", s)
-            fs.append(2.0 * torch.log(torch.diagonal(L)).sum() + torch.dot(Y[m], al.reshape(n)))
-            Ls.append(L)
-            alphas.append(al)
+            st = streams[m % nstream]
+            with torch.cuda.stream(st):
+                L = A[m].clone()  # symmetric: row-major storage = column-major A
+                G.potrf_dev(L, n, n, infos[m % nstream], "L", st.cuda_stream)
+                al = Y[m].clone().reshape(1, n)
+                G.potrs_dev(L, n, n, al, 1, n, "L", st.cuda_stream)
+                fs[m] = 2.0 * torch.log(torch.diagonal(L)).sum() + torch.dot(Y[m], al.reshape(n))
+                Ls[m], alphas[m] = L, al
         torch.cuda.synchronize()
         t_fwd = time.perf_counter() - t0
         t0 = time.perf_counter()
-        grads = []
+        grads = [None] * nmat
         for m in range(nmat):
-            M = torch.zeros_like(Ls[m])
-            M.diagonal().copy_(2.0 / torch.diagonal(Ls[m]))
-            G.potrf_adjoint_dev(Ls[m], n, n, M, n, s)
-            bbar = torch.empty_like(alphas[m])
-            G.potrs_adjoint_dev(Ls[m], n, n, alphas[m], n, Y[m].reshape(1, n), n, bbar, n, 1, M, n, s)
-            grads.append(M)
+            st = streams[m % nstream]
+            with torch.cuda.stream(st):
+                M = torch.zeros_like(Ls[m])
+                M.diagonal().copy_(2.0 / torch.diagonal(Ls[m]))
+                G.potrf_adjoint_dev(Ls[m], n, n, M, n, st.cuda_stream)
+                bbar = torch.empty_like(alphas[m])
+                G.potrs_adjoint_dev(Ls[m], n, n, alphas[m], n, Y[m].reshape(1, n), n, bbar, n, 1, M, n,
+                                    st.cuda_stream)
+                grads[m] = M
         torch.cuda.synchronize()
         t_bwd = time.perf_counter() - t0
-        res = {"forward_s": t_fwd, "backward_s": t_bwd}
+        res = {"forward_s": t_fwd, "backward_s": t_bwd, "streams": nstream}
     # gradient check of the first matrix against the closed form A^{-1} - a a^T (cuSOLVER FP64)
     Ainv = torch.cholesky_inverse(torch.linalg.cholesky(A[0]))
     a0 = alphas[0].reshape(n)
@@ -604,13 +611,26 @@ def run_c5(args):
     res["grad_rel_err_vs_closed_form"] = float(torch.linalg.norm(got - want) / torch.linalg.norm(want))
     # mixed-precision forward solve of the same systems
     opts = G.mixed_opts(args.mixed_precision, 10, 1e-14, True)
-    Xs = torch.zeros(1, n, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
+    Xs = [torch.zeros(1, n, dtype=torch.float64, device="cuda") for _ in range(nmat)]
+    # each mixed solve reads its convergence test on the host, so the streams are driven by one host
+    # thread each (ctypes releases the GIL during the call)
+    from concurrent.futures import ThreadPoolExecutor
+
+    def mixed_chain(t):
+        st = streams[t]
+        torch.cuda.set_device(0)
+        got = []
+        with torch.cuda.stream(st):
+            for m in range(t, nmat, nstream):
+                rc, rep = G.posv_mixed_dev(A[m], n, n, Y[m].reshape(1, n), n, Xs[m], n, 1, opts, "L",
+                                           st.cuda_stream, raise_on_error=False)
+                got.append(rep["steps"])
+        return got
+
     t0 = time.perf_counter()
-    steps = []
-    for m in range(nmat):
-        rc, rep = G.posv_mixed_dev(A[m], n, n, Y[m].reshape(1, n), n, Xs, n, 1, opts, "L", s, raise_on_error=False)
-        steps.append(rep["steps"])
+    with ThreadPoolExecutor(nstream) as pool:
+        steps = [v for chain in pool.map(mixed_chain, range(nstream)) for v in chain]
     torch.cuda.synchronize()
     res["mixed_solve_s"] = time.perf_counter() - t0
     res["mixed_steps"] = [min(steps), max(steps)]

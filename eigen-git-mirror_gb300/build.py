@@ -17,6 +17,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "lib" / "libgbllt.so"
+LAPACK_LIB = PKG / "lib" / "libgbllt_lapack.so"  # Fortran-ABI dpotrf_/dpotrs_/spotrf_/spotrs_ shim
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -51,6 +52,21 @@ def _compile(src: Path, verbose_ptxas: bool) -> Path:
     return obj
 
 
+def build_lapack_shim(force: bool = False) -> Path:
+    """libgbllt_lapack.so: the Fortran-ABI Cholesky routines (C, gcc) linked against libgbllt.so."""
+    src = CSRC / "lapack_shim.c"
+    deps = [src, LIB, INCLUDE / "gbllt.h", INCLUDE / "gbllt_lapack.h"]
+    if not force and LAPACK_LIB.exists() and LAPACK_LIB.stat().st_mtime > max(d.stat().st_mtime for d in deps):
+        return LAPACK_LIB
+    cc = os.environ.get("CC") or shutil.which("gcc") or "cc"
+    cmd = [cc, "-O2", "-fPIC", "-shared", "-fvisibility=hidden", "-I", str(INCLUDE), str(src), "-o", str(LAPACK_LIB),
+           "-L", str(LIB.parent), "-lgbllt", "-Wl,-rpath,$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"LAPACK shim build failed:\n{res.stdout}\n{res.stderr}")
+    return LAPACK_LIB
+
+
 def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIB.parent.mkdir(exist_ok=True)
@@ -60,14 +76,14 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), srcs))
-    if LIB.exists() and LIB.stat().st_mtime > max(o.stat().st_mtime for o in objs) and not force:
-        return LIB
-    # libcuda is not linked: driver entry points (tensor-map encoding) are fetched at run time
-    # through cudaGetDriverEntryPoint, so the library also loads on a machine without a driver.
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0:
-        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    if force or not LIB.exists() or LIB.stat().st_mtime <= max(o.stat().st_mtime for o in objs):
+        # libcuda is not linked: driver entry points (tensor-map encoding) are fetched at run time
+        # through cudaGetDriverEntryPoint, so the library also loads on a machine without a driver.
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    build_lapack_shim(force)
     return LIB
 
 

@@ -19,9 +19,12 @@
 // with df = sum_ij Abar_ij dA_ij for symmetric perturbations dA (its lower triangle is stored).
 // The symbolic form of the same result, Abar = 1/2 L^{-T} (P + P^T) L^{-1} with P = Phi(L^T Lbar),
 // is Murray 2016 ("Differentiation of the Cholesky decomposition", arXiv:1602.07527); the blocked
-// in-place order above has the flop count of the forward factorisation (n^3/3 in GEMMs).
+// in-place order above does about 2n^3/3 flops (twice the forward factorisation), nearly all of them
+// in the two products with the panel below each block (M_IK and M_JK updates).
 //
 // Reverse of the solve X = A^{-1} B:  Bbar = A^{-1} Xbar,  Abar -= sym(Bbar X^T).
+#include <algorithm>
+
 #include "internal.h"
 
 namespace gbllt {
@@ -34,30 +37,37 @@ constexpr int ANB = 32;  // block size of the adjoint
 // opA: 0 = A (m x k), 1 = A^T (A stored k x m), 2 = A symmetric m x m stored in its lower triangle.
 // opB: 0 = B (k x n), 1 = B^T (B stored n x k).
 // lower_only: write only entries with global row >= column (row/col offsets applied by the caller).
-template <int OPA, int OPB>
-__global__ void __launch_bounds__(256) gemm_f64_kernel(long long m, long long n, long long k, double alpha,
+// Tiles of TM x 64 (TM = 32 for the 32-row products of the block adjoint, else 64).  Split K: with
+// gridDim.z > 1, CTA z covers k in [z*kc, (z+1)*kc) and stores alpha * its partial product densely
+// in part[z] (m x n, leading dimension m); split_reduce_kernel then adds the partials into C in a
+// fixed order, so the result does not depend on scheduling.
+template <int OPA, int OPB, int TM>
+__global__ void __launch_bounds__(256) gemm_f64_kernel(long long m, long long n, long long k, long long kc, double alpha,
                                                        const double* __restrict__ A, long long lda,
                                                        const double* __restrict__ B, long long ldb,
-                                                       double* __restrict__ C, long long ldc, int lower_only) {
-  constexpr int KC = 32;
-  __shared__ double As[KC][64 + 1];  // As[p][i] = op(A)(i0 + i, p0 + p)
+                                                       double* __restrict__ C, long long ldc, int lower_only,
+                                                       double* __restrict__ part) {
+  constexpr int KC = 32, RT = TM / 16;
+  __shared__ double As[KC][TM + 1];  // As[p][i] = op(A)(i0 + i, p0 + p)
   __shared__ double Bs[KC][64 + 1];  // Bs[p][j] = op(B)(p0 + p, j0 + j)
-  const long long i0 = (long long)blockIdx.x * 64, j0 = (long long)blockIdx.y * 64;
-  if (lower_only && i0 + 63 < j0) return;  // tile strictly above the diagonal
+  const long long i0 = (long long)blockIdx.x * TM, j0 = (long long)blockIdx.y * 64;
+  if (lower_only && i0 + TM - 1 < j0) return;  // tile strictly above the diagonal
+  const long long kb = (long long)blockIdx.z * kc;
+  const long long ke = kb + kc < k ? kb + kc : k;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  double acc[4][4];
+  double acc[RT][4];
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < RT; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) acc[u][v] = 0.0;
-  for (long long p0 = 0; p0 < k; p0 += KC) {
-    for (int idx = tid; idx < 64 * KC; idx += 256) {
+  for (long long p0 = kb; p0 < ke; p0 += KC) {
+    for (int idx = tid; idx < TM * KC; idx += 256) {
       int i, p;
       if (OPA == 1) { p = idx & 31; i = idx >> 5; }   // A^T: contiguous along p
-      else          { i = idx & 63; p = idx >> 6; }   // A: contiguous along i
+      else          { i = idx % TM; p = idx / TM; }   // A: contiguous along i
       const long long gi = i0 + i, gp = p0 + p;
       double v = 0.0;
-      if (gi < m && gp < k) {
+      if (gi < m && gp < ke) {
         if (OPA == 0) v = A[gp * lda + gi];
         else if (OPA == 1) v = A[gi * lda + gp];
         else v = gi >= gp ? A[gp * lda + gi] : A[gi * lda + gp];
@@ -70,47 +80,63 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(long long m, long long n,
       else          { j = idx & 63; p = idx >> 6; }   // B^T: contiguous along j
       const long long gj = j0 + j, gp = p0 + p;
       double v = 0.0;
-      if (gj < n && gp < k) v = OPB == 0 ? B[gj * ldb + gp] : B[gp * ldb + gj];
+      if (gj < n && gp < ke) v = OPB == 0 ? B[gj * ldb + gp] : B[gp * ldb + gj];
       Bs[p][j] = v;
     }
     __syncthreads();
-    const int pe = (int)(k - p0 < KC ? k - p0 : KC);
+    const int pe = (int)(ke - p0 < KC ? ke - p0 : KC);
     for (int p = 0; p < pe; ++p) {
-      double av[4], bv[4];
+      double av[RT], bv[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) av[u] = As[p][tx + 16 * u];
+      for (int u = 0; u < RT; ++u) av[u] = As[p][tx + 16 * u];
 #pragma unroll
       for (int v = 0; v < 4; ++v) bv[v] = Bs[p][ty + 16 * v];
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < RT; ++u)
 #pragma unroll
         for (int v = 0; v < 4; ++v) acc[u][v] = fma(av[u], bv[v], acc[u][v]);
     }
     __syncthreads();
   }
+  double* P = part ? part + (long long)blockIdx.z * m * n : nullptr;
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
     const long long j = j0 + ty + 16 * v;
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < RT; ++u) {
       const long long i = i0 + tx + 16 * u;
-      if (i < m && j < n && (!lower_only || i >= j)) C[j * ldc + i] += alpha * acc[u][v];
+      if (i < m && j < n && (!lower_only || i >= j)) {
+        if (P) P[j * m + i] = alpha * acc[u][v];
+        else C[j * ldc + i] += alpha * acc[u][v];
+      }
     }
   }
+}
+
+// C(i, j) += sum_z part[z](i, j) over the nz partials, z ascending.
+__global__ void split_reduce_kernel(long long m, long long n, int nz, const double* __restrict__ part,
+                                    double* __restrict__ C, long long ldc, int lower_only) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= m * n) return;
+  const long long i = idx % m, j = idx / m;
+  if (lower_only && i < j) return;
+  double s = 0.0;
+  for (int z = 0; z < nz; ++z) s += part[(long long)z * m * n + idx];
+  C[j * ldc + i] += s;
 }
 
 // X L = M for X, then M <- X / 2, in place (rows x ANB), L lower jb x jb: one thread per row,
 // columns descending.  The halving converts the adjoint of the independent lower entries of A_IJ
 // into the symmetric-gradient convention (each off-diagonal entry stands for two symmetric ones).
-__global__ void __launch_bounds__(128) trsm_right_lower_kernel(const double* __restrict__ L, long long ldl, int jb,
+__global__ void __launch_bounds__(64) trsm_right_lower_kernel(const double* __restrict__ L, long long ldl, int jb,
                                                                double* __restrict__ M, long long ldm, long long rows) {
   __shared__ double Ls[ANB][ANB + 1];  // Ls[p][c] = L(p, c)
-  for (int idx = threadIdx.x; idx < ANB * ANB; idx += 128) {
+  for (int idx = threadIdx.x; idx < ANB * ANB; idx += 64) {
     const int p = idx % ANB, c = idx / ANB;
     Ls[p][c] = (p < jb && c < jb && p >= c) ? L[(long long)c * ldl + p] : (p == c ? 1.0 : 0.0);
   }
   __syncthreads();
-  const long long r = (long long)blockIdx.x * 128 + threadIdx.x;
+  const long long r = (long long)blockIdx.x * 64 + threadIdx.x;
   if (r >= rows) return;
   double x[ANB];
 #pragma unroll
@@ -183,14 +209,33 @@ __global__ void __launch_bounds__(256) chol_adjoint_diag_kernel(const double* __
   }
 }
 
+// Split-K scratch: partial products of at most kSplitElems doubles.
+constexpr long long kSplitElems = 1ll << 21;  // 16 MiB
+constexpr int kTargetCtas = 2 * 152;          // two waves of CTAs over the 152 SMs
+
 template <int OPA, int OPB>
 void gemm(long long m, long long n, long long k, double alpha, const double* A, long long lda, const double* B,
-          long long ldb, double* C, long long ldc, bool lower_only, cudaStream_t s) {
+          long long ldb, double* C, long long ldc, bool lower_only, double* part, cudaStream_t s) {
   if (m <= 0 || n <= 0 || k <= 0) return;
   static const std::string kname = "adjoint_gemm_f64";
   ProfScope ps(kname.c_str(), s, 2.0 * m * n * k * (lower_only ? 0.5 : 1.0), 8.0 * (m * k + k * n + 2 * m * n));
-  dim3 grid((unsigned)ceil_div(m, 64), (unsigned)ceil_div(n, 64));
-  gemm_f64_kernel<OPA, OPB><<<grid, 256, 0, s>>>(m, n, k, alpha, A, lda, B, ldb, C, ldc, lower_only ? 1 : 0);
+  const int tm = m <= 32 ? 32 : 64;
+  const long long tiles = ceil_div(m, tm) * ceil_div(n, 64);
+  // split K when the output alone gives too few CTAs and each split keeps >= 64 of K
+  long long nz = 1;
+  if (part && tiles < kTargetCtas) {
+    nz = std::min<long long>(kTargetCtas / tiles, k / 64);
+    while (nz > 1 && nz * m * n > kSplitElems) --nz;
+    if (nz < 1) nz = 1;
+  }
+  const long long kc = nz > 1 ? ceil_div(ceil_div(k, nz), 32) * 32 : k;
+  nz = ceil_div(k, kc);
+  double* P = nz > 1 ? part : nullptr;
+  dim3 grid((unsigned)ceil_div(m, tm), (unsigned)ceil_div(n, 64), (unsigned)nz);
+  const int lo = lower_only ? 1 : 0;
+  if (tm == 32) gemm_f64_kernel<OPA, OPB, 32><<<grid, 256, 0, s>>>(m, n, k, kc, alpha, A, lda, B, ldb, C, ldc, lo, P);
+  else gemm_f64_kernel<OPA, OPB, 64><<<grid, 256, 0, s>>>(m, n, k, kc, alpha, A, lda, B, ldb, C, ldc, lo, P);
+  if (P) split_reduce_kernel<<<(unsigned)ceil_div(m * n, 256), 256, 0, s>>>(m, n, (int)nz, P, C, ldc, lo);
 }
 
 __global__ void sym_rank_update_kernel(long long n, long long nrhs, const double* __restrict__ X, long long ldx,
@@ -211,6 +256,13 @@ __global__ void sym_rank_update_kernel(long long n, long long nrhs, const double
 
 int potrf_adjoint_dev(int64_t n, const double* L, int64_t ldl, double* M, int64_t ldm, cudaStream_t s) {
   static const std::string kt = "adjoint_trsm_f64", kd = "adjoint_diag_f64";
+  // split-K partials of the long, narrow products (stream-ordered, from the pool)
+  double* part = nullptr;
+  if (cudaMallocAsync((void**)&part, (size_t)kSplitElems * sizeof(double), s) != cudaSuccess) {
+    cudaGetLastError();
+    set_error_message("gbllt_dpotrf_adjoint_dev: cudaMallocAsync of the split-K scratch failed");
+    return GBLLT_ERR_ALLOC;
+  }
   const int64_t last = ((n - 1) / ANB) * ANB;
   for (int64_t j0 = last; j0 >= 0; j0 -= ANB) {
     const int jb = (int)(n - j0 < ANB ? n - j0 : ANB);
@@ -226,21 +278,22 @@ int potrf_adjoint_dev(int64_t n, const double* L, int64_t ldl, double* M, int64_
     if (ni > 0) {
       {
         ProfScope ps(kt.c_str(), s, (double)ni * jb * jb, 16.0 * ni * jb);
-        trsm_right_lower_kernel<<<(unsigned)ceil_div(ni, 128), 128, 0, s>>>(Ljj, ldl, jb, Mij, ldm, ni);  // Cbar/2
+        trsm_right_lower_kernel<<<(unsigned)ceil_div(ni, 64), 64, 0, s>>>(Ljj, ldl, jb, Mij, ldm, ni);  // Cbar/2
       }
       // M_IJ now holds Cbar / 2 (its final, symmetric-convention value); the updates use Cbar = 2 M_IJ
-      gemm<1, 0>(jb, jb, ni, -2.0, Mij, ldm, Lij, ldl, Mjj, ldm, true, s);        // M_JJ -= tril(Cbar^T L_IJ)
+      gemm<1, 0>(jb, jb, ni, -2.0, Mij, ldm, Lij, ldl, Mjj, ldm, true, part, s);        // M_JJ -= tril(Cbar^T L_IJ)
       if (j0 > 0) {
-        gemm<0, 0>(ni, j0, jb, -2.0, Mij, ldm, Ljk, ldl, Mik, ldm, false, s);     // M_IK -= Cbar L_JK
-        gemm<1, 0>(jb, j0, ni, -2.0, Mij, ldm, Lik, ldl, Mjk, ldm, false, s);     // M_JK -= Cbar^T L_IK
+        gemm<0, 0>(ni, j0, jb, -2.0, Mij, ldm, Ljk, ldl, Mik, ldm, false, part, s);     // M_IK -= Cbar L_JK
+        gemm<1, 0>(jb, j0, ni, -2.0, Mij, ldm, Lik, ldl, Mjk, ldm, false, part, s);     // M_JK -= Cbar^T L_IK
       }
     }
     {
       ProfScope ps(kd.c_str(), s, 4.0 * jb * jb * jb, 24.0 * jb * jb);
       chol_adjoint_diag_kernel<<<1, 256, 0, s>>>(Ljj, ldl, jb, Mjj, ldm);          // Dbar
     }
-    if (j0 > 0) gemm<2, 0>(jb, j0, jb, -2.0, Mjj, ldm, Ljk, ldl, Mjk, ldm, false, s);  // M_JK -= 2 Dbar L_JK
+    if (j0 > 0) gemm<2, 0>(jb, j0, jb, -2.0, Mjj, ldm, Ljk, ldl, Mjk, ldm, false, part, s);  // M_JK -= 2 Dbar L_JK
   }
+  cudaFreeAsync(part, s);
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
 }

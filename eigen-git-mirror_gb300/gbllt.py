@@ -64,6 +64,12 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_sposv_batched": (_int, [_vp, _vp, _vp, _vp]),
     "gbllt_dpotrf_adjoint_dev": (_int, [_i64, _vp, _i64, _vp, _i64, _vp]),
     "gbllt_dpotrs_adjoint_dev": (_int, [_i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp]),
+    "gbllt_dlansy_l1_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
+    "gbllt_slansy_l1_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
+    "gbllt_dpocon_dev": (_int, [_ch, _i64, _vp, _i64, ctypes.c_double, _dp, _vp]),
+    "gbllt_spocon_dev": (_int, [_ch, _i64, _vp, _i64, ctypes.c_float, _fp, _vp]),
+    "gbllt_dpocon": (_int, [_int, _ch, _i64, _vp, _i64, ctypes.c_double, _dp]),
+    "gbllt_spocon": (_int, [_int, _ch, _i64, _vp, _i64, ctypes.c_float, _fp]),
     "gbllt_profile_enable": (_int, [_int]),
     "gbllt_profile_read": (_int, [_vp, _int, ctypes.POINTER(_int)]),
 }
@@ -127,6 +133,70 @@ def lib() -> ctypes.CDLL:
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+LAPACK_PATH = PKG_DIR / "lib" / "libgbllt_lapack.so"
+_lapack = None
+_I = ctypes.POINTER(ctypes.c_int)
+_C = ctypes.c_char_p
+_D = ctypes.POINTER(ctypes.c_double)
+_F = ctypes.POINTER(ctypes.c_float)
+LAPACK_SIGNATURES = {
+    "dpotrf_": (ctypes.c_int, [_C, _I, _D, _I, _I]),
+    "spotrf_": (ctypes.c_int, [_C, _I, _F, _I, _I]),
+    "dpotrs_": (ctypes.c_int, [_C, _I, _I, _D, _I, _D, _I, _I]),
+    "spotrs_": (ctypes.c_int, [_C, _I, _I, _F, _I, _F, _I, _I]),
+}
+
+
+def lapack() -> ctypes.CDLL:
+    """Load libgbllt_lapack.so, the Fortran-ABI dpotrf_/dpotrs_/spotrf_/spotrs_ routines."""
+    global _lapack
+    if _lapack is None:
+        lib()  # the shim resolves its gbllt_* calls against libgbllt.so
+        if not LAPACK_PATH.exists():
+            raise RuntimeError(f"{LAPACK_PATH} is missing: build it with __graft_entry__.build()")
+        L = ctypes.CDLL(str(LAPACK_PATH))
+        for name, (res, args) in LAPACK_SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lapack = L
+    return _lapack
+
+
+def _cptr(a: np.ndarray, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def lapack_potrf(a: np.ndarray, uplo: str = "L", lda: int | None = None, n: int | None = None) -> int:
+    """?potrf_ through the Fortran ABI on a Fortran-order array; returns info."""
+    L = lapack()
+    dbl = a.dtype == np.float64
+    fn = L.dpotrf_ if dbl else L.spotrf_
+    n_ = ctypes.c_int(a.shape[0] if n is None else n)
+    lda_ = ctypes.c_int(a.shape[0] if lda is None else lda)
+    info = ctypes.c_int(0)
+    fn(uplo.encode(), ctypes.byref(n_), _cptr(a, ctypes.c_double if dbl else ctypes.c_float), ctypes.byref(lda_),
+       ctypes.byref(info))
+    return info.value
+
+
+def lapack_potrs(a: np.ndarray, b: np.ndarray, uplo: str = "L", nrhs: int | None = None, ldb: int | None = None,
+                 n: int | None = None, lda: int | None = None) -> int:
+    """?potrs_ through the Fortran ABI (b overwritten with the solution); returns info."""
+    L = lapack()
+    dbl = a.dtype == np.float64
+    ct = ctypes.c_double if dbl else ctypes.c_float
+    fn = L.dpotrs_ if dbl else L.spotrs_
+    n_ = ctypes.c_int(a.shape[0] if n is None else n)
+    k_ = ctypes.c_int((b.shape[1] if b.ndim == 2 else 1) if nrhs is None else nrhs)
+    lda_ = ctypes.c_int(a.shape[0] if lda is None else lda)
+    ldb_ = ctypes.c_int(b.shape[0] if ldb is None else ldb)
+    info = ctypes.c_int(0)
+    fn(uplo.encode(), ctypes.byref(n_), ctypes.byref(k_), _cptr(a, ct), ctypes.byref(lda_), _cptr(b, ct),
+       ctypes.byref(ldb_), ctypes.byref(info))
+    return info.value
 
 
 def header_functions() -> list[str]:
@@ -285,6 +355,32 @@ class BatchPlan:
 
 def profile_enable(on: bool = True) -> None:
     check("gbllt_profile_enable", lib().gbllt_profile_enable(1 if on else 0))
+
+
+def pocon(l: np.ndarray, anorm: float, uplo: str = "L") -> float:
+    """Reciprocal condition estimate from a host factor (Fortran-order float64/float32 array)."""
+    dbl = l.dtype == np.float64
+    out = ctypes.c_double(0.0) if dbl else ctypes.c_float(0.0)
+    fn = lib().gbllt_dpocon if dbl else lib().gbllt_spocon
+    n = l.shape[0]
+    check("gbllt_?pocon", fn(COL_MAJOR, uplo.encode(), n, l.ctypes.data if n else None, max(n, 1), anorm,
+                            ctypes.byref(out)))
+    return out.value
+
+
+def pocon_dev(d_l, n: int, ldl: int, anorm: float, uplo: str = "L", stream=None, dtype=np.float64) -> float:
+    """Device-pointer form: d_l is a device tensor holding the factor."""
+    dbl = dtype == np.float64
+    out = ctypes.c_double(0.0) if dbl else ctypes.c_float(0.0)
+    fn = lib().gbllt_dpocon_dev if dbl else lib().gbllt_spocon_dev
+    check("gbllt_?pocon_dev", fn(uplo.encode(), n, _ptr(d_l), ldl, anorm, ctypes.byref(out), stream))
+    return out.value
+
+
+def lansy_l1_dev(d_a, n: int, lda: int, d_norm, uplo: str = "L", stream=None, dtype=np.float64) -> None:
+    """1-norm of the symmetric matrix stored in one triangle of d_a, written to the device scalar d_norm."""
+    fn = lib().gbllt_dlansy_l1_dev if dtype == np.float64 else lib().gbllt_slansy_l1_dev
+    check("gbllt_?lansy_l1_dev", fn(uplo.encode(), n, _ptr(d_a), lda, _ptr(d_norm), stream))
 
 
 def profile_read() -> dict[str, dict]:

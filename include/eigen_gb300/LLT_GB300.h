@@ -15,8 +15,12 @@
 //     (dst = llt.solve(b), Solve.h:137-149) and internal::evaluator<Solve<LLT<...>, Rhs>>
 //     (dst += / -= / noalias, Solve.h:114-131) call gbllt_?potrs on the current host factor
 //     (matrixLLT()), so a modified factor changes the result as Eigen's own solve does.
+//   - the condition estimate: explicit specialisations of internal::rcond_estimate_helper for the
+//     dynamic-size LLTs (called by LLT::rcond, LLT.h:166-171) call gbllt_?pocon, which runs
+//     Eigen's estimator (ConditionEstimator.h:56-171) with the factor resident on the device.
 // What stays on Eigen's CPU code: LLT::solveInPlace (LLT.h:514-522) calls the triangular views
-// directly and bypasses Solve<>; rankUpdate; rcond's L1 norm (its solves go to the GPU).
+// directly and bypasses Solve<>; rankUpdate; the L1 norm that LLT::compute keeps for rcond
+// (LLT.h:443-453; gbllt_?lansy_l1_dev is its device form for callers outside Eigen).
 //
 // Errors: a failing library call (no usable GPU, CUDA error) trips eigen_assert; with assertions
 // disabled the factorisation reports NumericalIssue and a solve leaves NaN in its result.
@@ -154,6 +158,36 @@ EIGEN_GB300_SOLVE(double)
 EIGEN_GB300_SOLVE(float)
 
 #undef EIGEN_GB300_SOLVE
+
+// llt.rcond(): LLT::rcond (LLT.h:166-171) returns rcond_estimate_helper(m_l1_norm, *this)
+// (ConditionEstimator.h:161-171), whose estimator runs up to 11 solves.  These explicit
+// specialisations for the dynamic-size double/float LLTs hand the whole estimate to gbllt_?pocon,
+// which copies the factor to the device once and runs the same algorithm there.
+#define EIGEN_GB300_RCOND(EIGTYPE, POCON, OPT, UPLO)                                                    \
+  template <>                                                                                          \
+  inline EIGTYPE rcond_estimate_helper<LLT<Matrix<EIGTYPE, Dynamic, Dynamic, OPT>, UPLO> >(             \
+      EIGTYPE matrix_norm, const LLT<Matrix<EIGTYPE, Dynamic, Dynamic, OPT>, UPLO>& dec) {              \
+    eigen_assert(dec.rows() == dec.cols());                                                            \
+    const int64_t n = (int64_t)dec.rows();                                                             \
+    const auto& f = dec.matrixLLT();                                                                   \
+    const int layout = (OPT & RowMajor) ? GBLLT_ROW_MAJOR : GBLLT_COL_MAJOR;                          \
+    EIGTYPE r = 0;                                                                                     \
+    const int rc = POCON(layout, UPLO == Lower ? 'L' : 'U', n, n ? f.data() : nullptr,                 \
+                         n ? (int64_t)f.outerStride() : 1, matrix_norm, &r);                            \
+    if (!gb300_check(#POCON, rc)) return std::numeric_limits<EIGTYPE>::quiet_NaN();                   \
+    return r;                                                                                          \
+  }
+
+EIGEN_GB300_RCOND(double, gbllt_dpocon, ColMajor, Lower)
+EIGEN_GB300_RCOND(double, gbllt_dpocon, ColMajor, Upper)
+EIGEN_GB300_RCOND(double, gbllt_dpocon, RowMajor, Lower)
+EIGEN_GB300_RCOND(double, gbllt_dpocon, RowMajor, Upper)
+EIGEN_GB300_RCOND(float, gbllt_spocon, ColMajor, Lower)
+EIGEN_GB300_RCOND(float, gbllt_spocon, ColMajor, Upper)
+EIGEN_GB300_RCOND(float, gbllt_spocon, RowMajor, Lower)
+EIGEN_GB300_RCOND(float, gbllt_spocon, RowMajor, Upper)
+
+#undef EIGEN_GB300_RCOND
 
 }  // namespace internal
 }  // namespace Eigen

@@ -205,6 +205,27 @@ GBLLT_API int gbllt_dpotrs_adjoint_dev(int64_t n, int64_t nrhs, const double* d_
                                        int64_t ldx, const double* d_xbar, int64_t ldxb, double* d_bbar, int64_t ldbb,
                                        double* d_abar, int64_t ldab, void* stream);
 
+/* ---- Condition estimate (LLT::rcond, Eigen/src/Cholesky/LLT.h:166-171) ---------------------- */
+
+/* 1-norm (max absolute column sum) of the symmetric n x n matrix stored in the `uplo` triangle of
+ * the column-major d_a: the m_l1_norm loop of LLT::compute (LLT.h:443-453).  The result is written
+ * to *d_norm (device), stream-ordered. */
+GBLLT_API int gbllt_dlansy_l1_dev(char uplo, int64_t n, const double* d_a, int64_t lda, double* d_norm,
+                                  void* stream);
+GBLLT_API int gbllt_slansy_l1_dev(char uplo, int64_t n, const float* d_a, int64_t lda, float* d_norm, void* stream);
+/* Reciprocal 1-norm condition estimate from a factor produced by ?potrf and anorm = ||A||_1:
+ * rcond_estimate_helper + rcond_invmatrix_L1_norm_estimate (Eigen/src/Core/ConditionEstimator.h:
+ * 56-171) with every solve on the device; the same role as LAPACK dpocon.  Returns after the
+ * estimate is known (*rcond is host memory): +inf for n = 0, 0 for anorm = 0, 1 for n = 1. */
+GBLLT_API int gbllt_dpocon_dev(char uplo, int64_t n, const double* d_l, int64_t ldl, double anorm, double* rcond,
+                               void* stream);
+GBLLT_API int gbllt_spocon_dev(char uplo, int64_t n, const float* d_l, int64_t ldl, float anorm, float* rcond,
+                               void* stream);
+/* Host-pointer form (the factor is copied to the device once for all the solves). */
+GBLLT_API int gbllt_dpocon(int layout, char uplo, int64_t n, const double* l, int64_t ldl, double anorm,
+                           double* rcond);
+GBLLT_API int gbllt_spocon(int layout, char uplo, int64_t n, const float* l, int64_t ldl, float anorm, float* rcond);
+
 /* ---- Diagnostics (no counterpart in the reference; Eigen has no built-in timers) ----------- */
 
 /* Per-kernel-class totals: launches, device time (CUDA events on the launch stream) and the

@@ -42,7 +42,24 @@ static int64_t blocked(int64_t n, T* a, int64_t lda) {
   return (int64_t)internal::llt_inplace<T, UpLo>::blocked(A);
 }
 
+// LLT<Matrix,UpLo>(A).rcond() (LLT.h:166-171): Eigen's own 1-norm and condition estimate.
+template <typename T, int UpLo>
+static double rcond(int64_t n, const T* a, int64_t lda) {
+  typedef Matrix<T, Dynamic, Dynamic> M;
+  Map<const M, 0, OuterStride<>> A(a, n, n, OuterStride<>(lda));
+  LLT<M, UpLo> llt(A);
+  if (llt.info() != Success) return -1.0;
+  return (double)llt.rcond();
+}
+
 extern "C" {
+
+double ref_drcond(char uplo, int64_t n, const double* a, int64_t lda) {
+  return uplo == 'U' ? rcond<double, Upper>(n, a, lda) : rcond<double, Lower>(n, a, lda);
+}
+double ref_srcond(char uplo, int64_t n, const float* a, int64_t lda) {
+  return uplo == 'U' ? rcond<float, Upper>(n, a, lda) : rcond<float, Lower>(n, a, lda);
+}
 
 int64_t ref_dllt(char uplo, int64_t n, int64_t nrhs, double* a, int64_t lda, double* b, int64_t ldb, double* sec) {
   return uplo == 'U' ? factor_solve<double, Upper>(n, nrhs, a, lda, b, ldb, sec)

@@ -239,3 +239,81 @@ double P(backward_error)(char uplo, int64_t n, int64_t nrhs, const T* a, int64_t
 }
 
 #undef EL
+
+/* 1-norm of the symmetric matrix of which only the `uplo` triangle of the column-major a is read:
+ * the m_l1_norm loop of LLT::compute (Eigen/src/Cholesky/LLT.h:443-453), column by column, the
+ * stored part of column j plus the stored part of row j. */
+T P(sym_l1_norm)(char uplo, int64_t n, const T* a, int64_t lda) {
+  const int up = (uplo == 'U' || uplo == 'u');
+  T best = 0;
+  for (int64_t j = 0; j < n; ++j) {
+    T s = 0;
+    if (!up) {
+      for (int64_t i = j; i < n; ++i) s += (T)fabs((double)a[i + j * lda]);   /* col(j).tail(n-j) */
+      for (int64_t k = 0; k < j; ++k) s += (T)fabs((double)a[j + k * lda]);   /* row(j).head(j)   */
+    } else {
+      for (int64_t i = 0; i < j; ++i) s += (T)fabs((double)a[i + j * lda]);   /* col(j).head(j)   */
+      for (int64_t k = j; k < n; ++k) s += (T)fabs((double)a[j + k * lda]);   /* row(j).tail(n-j) */
+    }
+    if (s > best) best = s;
+  }
+  return best;
+}
+
+static T P(vec_l1)(int64_t n, const T* v) {
+  T s = 0;
+  for (int64_t i = 0; i < n; ++i) s += (T)fabs((double)v[i]);
+  return s;
+}
+
+/* Reciprocal condition estimate from the factor: rcond_estimate_helper and
+ * rcond_invmatrix_L1_norm_estimate (Eigen/src/Core/ConditionEstimator.h:56-171), restated step by
+ * step over this oracle's potrs (the LLT solve; A is symmetric, so dec.adjoint().solve is the same
+ * solve).  Returns +inf for n = 0, 0 for anorm = 0, 1 for n = 1 (:165-167). */
+double P(rcond)(char uplo, int64_t n, const T* l, int64_t ldl, double anorm) {
+  if (n == 0) return INFINITY;
+  if (anorm == 0) return 0.0;
+  if (n == 1) return 1.0;
+  T* v = (T*)malloc(sizeof(T) * n);
+  T* sign = (T*)malloc(sizeof(T) * n);
+  T* old_sign = (T*)malloc(sizeof(T) * n);
+  for (int64_t i = 0; i < n; ++i) v[i] = (T)1 / (T)n;                 /* :79 */
+  P(potrs)(uplo, n, 1, l, ldl, v, n);
+  T lower = P(vec_l1)(n, v);                                            /* :88 */
+  T old_lower = lower;
+  int64_t old_idx = -1;
+  for (int k = 0; k < 4; ++k) {                                         /* :100-128 */
+    int same = k > 0;
+    for (int64_t i = 0; i < n; ++i) {
+      sign[i] = v[i] < (T)0 ? (T)-1 : (T)1;                            /* :29-35 */
+      if (k > 0 && sign[i] != old_sign[i]) same = 0;
+    }
+    if (k > 0 && same) break;
+    for (int64_t i = 0; i < n; ++i) v[i] = sign[i];
+    P(potrs)(uplo, n, 1, l, ldl, v, n);
+    int64_t idx = 0;                                                    /* first max |v| */
+    T mx = (T)fabs((double)v[0]);
+    for (int64_t i = 1; i < n; ++i)
+      if ((T)fabs((double)v[i]) > mx) { mx = (T)fabs((double)v[i]); idx = i; }
+    if (idx == old_idx) break;
+    for (int64_t i = 0; i < n; ++i) v[i] = (T)(i == idx ? 1 : 0);
+    P(potrs)(uplo, n, 1, l, ldl, v, n);
+    lower = P(vec_l1)(n, v);
+    if (lower <= old_lower) break;
+    for (int64_t i = 0; i < n; ++i) old_sign[i] = sign[i];
+    old_idx = idx;
+    old_lower = lower;
+  }
+  T alt_sign = (T)1;                                                    /* :141-147 */
+  for (int64_t i = 0; i < n; ++i) {
+    v[i] = alt_sign * ((T)1 + (T)i / (T)(n - 1));
+    alt_sign = -alt_sign;
+  }
+  P(potrs)(uplo, n, 1, l, ldl, v, n);
+  const T alt = ((T)2 * P(vec_l1)(n, v)) / ((T)3 * (T)n);
+  const T est = lower > alt ? lower : alt;
+  free(v);
+  free(sign);
+  free(old_sign);
+  return est == (T)0 ? 0.0 : ((double)((T)1 / est) / anorm);
+}

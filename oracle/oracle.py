@@ -28,6 +28,10 @@ _vp = ctypes.c_void_p
 _ch = ctypes.c_char
 
 _SIGS = {
+    "oracle_dsym_l1_norm": (_dbl, [_ch, _i64, _vp, _i64]),
+    "oracle_ssym_l1_norm": (ctypes.c_float, [_ch, _i64, _vp, _i64]),
+    "oracle_drcond": (_dbl, [_ch, _i64, _vp, _i64, _dbl]),
+    "oracle_srcond": (_dbl, [_ch, _i64, _vp, _i64, _dbl]),
     "oracle_philox4x32_10": (None, [_vp, _vp, _vp]),
     "oracle_normal": (_dbl, [_u64, _u64]),
     "oracle_uniform": (_dbl, [_u64, _u64]),
@@ -98,6 +102,9 @@ def eigen_ref():
             getattr(R, nm).argtypes = [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp]
         for nm in ("ref_dblocked", "ref_sblocked"):
             getattr(R, nm).restype = _i64
+            getattr(R, nm).argtypes = [_ch, _i64, _vp, _i64]
+        for nm in ("ref_drcond", "ref_srcond"):
+            getattr(R, nm).restype = _dbl
             getattr(R, nm).argtypes = [_ch, _i64, _vp, _i64]
         _ref = R
     return _ref
@@ -189,6 +196,20 @@ def potrs(a: np.ndarray, b: np.ndarray, uplo: str = "L") -> None:
     fn = lib().oracle_dpotrs if a.dtype == np.float64 else lib().oracle_spotrs
     rc = fn(uplo.encode(), n, k, _p(a), max(1, n), _p(b), max(1, n))
     assert rc == 0, rc
+
+
+def sym_l1_norm(a: np.ndarray, uplo: str = "L") -> float:
+    """1-norm of the symmetric matrix stored in the `uplo` triangle (LLT.h:443-453)."""
+    n = a.shape[0]
+    fn = lib().oracle_dsym_l1_norm if a.dtype == np.float64 else lib().oracle_ssym_l1_norm
+    return float(fn(uplo.encode(), n, _p(a), max(1, n)))
+
+
+def rcond(l: np.ndarray, anorm: float, uplo: str = "L") -> float:
+    """Reciprocal condition estimate from a factor (ConditionEstimator.h:56-171 over potrs)."""
+    n = l.shape[0]
+    fn = lib().oracle_drcond if l.dtype == np.float64 else lib().oracle_srcond
+    return float(fn(uplo.encode(), n, _p(l) if n else None, max(1, n), float(anorm)))
 
 
 def backward_error(a: np.ndarray, x: np.ndarray, b: np.ndarray, uplo: str = "L") -> float:

@@ -1,6 +1,6 @@
 /* Test double of libgbllt for checking include/eigen_gb300/LLT_GB300.h on a machine without a GPU.
  *
- * TEST INFRASTRUCTURE ONLY.  It implements the four entry points the Eigen header calls by
+ * TEST INFRASTRUCTURE ONLY.  It implements the entry points the Eigen header calls by
  * forwarding to the oracle (oracle/llt_oracle.c), applying the same layout rule as the real
  * library (a row-major factor with uplo 'L' is a column-major one with uplo 'U'), and counts the
  * calls so that a test can prove the specialisations were selected.  It never ships. */
@@ -13,8 +13,10 @@ int oracle_dpotrf(char uplo, int64_t n, double* a, int64_t lda, int64_t* info);
 int oracle_spotrf(char uplo, int64_t n, float* a, int64_t lda, int64_t* info);
 int oracle_dpotrs(char uplo, int64_t n, int64_t nrhs, const double* a, int64_t lda, double* b, int64_t ldb);
 int oracle_spotrs(char uplo, int64_t n, int64_t nrhs, const float* a, int64_t lda, float* b, int64_t ldb);
+double oracle_drcond(char uplo, int64_t n, const double* l, int64_t ldl, double anorm);
+double oracle_srcond(char uplo, int64_t n, const float* l, int64_t ldl, double anorm);
 
-long fake_calls[4];
+long fake_calls[6];
 
 static char eff_uplo(int layout, char uplo) {
   const int up = uplo == 'U' || uplo == 'u';
@@ -41,8 +43,19 @@ int gbllt_spotrs(int layout, char uplo, int64_t n, int64_t nrhs, const float* a,
   return oracle_spotrs(uplo, n, nrhs, a, lda, b, ldb);
 }
 
+int gbllt_dpocon(int layout, char uplo, int64_t n, const double* l, int64_t ldl, double anorm, double* rcond) {
+  ++fake_calls[4];
+  *rcond = oracle_drcond(eff_uplo(layout, uplo), n, l, ldl, anorm);
+  return 0;
+}
+int gbllt_spocon(int layout, char uplo, int64_t n, const float* l, int64_t ldl, float anorm, float* rcond) {
+  ++fake_calls[5];
+  *rcond = (float)oracle_srcond(eff_uplo(layout, uplo), n, l, ldl, anorm);
+  return 0;
+}
+
 /* Prints the call counts at exit so that the test can check the backend was used. */
 __attribute__((destructor)) static void fake_report(void) {
-  fprintf(stderr, "fake_gbllt calls: dpotrf=%ld spotrf=%ld dpotrs=%ld spotrs=%ld\n", fake_calls[0], fake_calls[1],
-          fake_calls[2], fake_calls[3]);
+  fprintf(stderr, "fake_gbllt calls: dpotrf=%ld spotrf=%ld dpotrs=%ld spotrs=%ld dpocon=%ld spocon=%ld\n",
+          fake_calls[0], fake_calls[1], fake_calls[2], fake_calls[3], fake_calls[4], fake_calls[5]);
 }

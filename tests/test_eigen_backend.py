@@ -47,17 +47,19 @@ def _build_and_run(objs, test_name):
     subprocess.run(cmd, check=True, capture_output=True)
     res = subprocess.run([str(exe), "r3", "s1234"], capture_output=True, text=True, timeout=600)
     assert res.returncode == 0, res.stdout[-2000:] + res.stderr[-2000:]
-    m = re.search(r"fake_gbllt calls: dpotrf=(\d+) spotrf=(\d+) dpotrs=(\d+) spotrs=(\d+)", res.stderr)
+    m = re.search(r"fake_gbllt calls: dpotrf=(\d+) spotrf=(\d+) dpotrs=(\d+) spotrs=(\d+) dpocon=(\d+) "
+                  r"spocon=(\d+)", res.stderr)
     assert m, res.stderr[-2000:]
     return [int(v) for v in m.groups()]
 
 
 def test_eigen_cholesky_suite_through_backend(objs):
-    dpotrf, spotrf, dpotrs, _ = _build_and_run(objs, "cholesky")
-    # MatrixXd factorisations and solves, and fixed-size float ones, went through the C ABI
-    assert dpotrf > 0 and dpotrs > 0 and spotrf > 0
+    dpotrf, spotrf, dpotrs, _, dpocon, _ = _build_and_run(objs, "cholesky")
+    # MatrixXd factorisations, solves and condition estimates, and fixed-size float factorisations,
+    # went through the C ABI (the rcond checks of test/cholesky.cpp:94-115 ran on gbllt_dpocon)
+    assert dpotrf > 0 and dpotrs > 0 and spotrf > 0 and dpocon > 0
 
 
 def test_eigen_inplace_decomposition_through_backend(objs):
-    dpotrf, _, _, _ = _build_and_run(objs, "inplace_decomposition")
+    dpotrf, _, _, _, _, _ = _build_and_run(objs, "inplace_decomposition")
     assert dpotrf > 0
