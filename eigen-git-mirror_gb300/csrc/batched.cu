@@ -45,7 +45,57 @@ struct BatchArgs {
   int count;
   int* counter;         // work-queue ticket, zeroed before each launch
   int smem_max_n;       // systems with n <= smem_max_n are staged in shared memory
+  int psld;             // algo 1: leading dimension of the shared panel copy (round_up(max n, 4))
 };
+
+// The two sweeps of the solve (LLT.h:483-498) on the factored system: blocks of 32, warp 0
+// substitutes inside each diagonal block, all warps apply the off-diagonal blocks.
+template <typename T, int THREADS>
+__device__ void solve_sweeps(const T* M, int ld, int n, T* bv) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int jb = min(32, n - j0);
+    if (warp == 0) {
+      for (int j = j0; j < j0 + jb; ++j) {
+        const T yj = bv[j] / M[j + (long long)j * ld];
+        __syncwarp();
+        if (lane == 0) bv[j] = yj;
+        const int i = j + 1 + lane;
+        if (i < j0 + jb) bv[i] -= M[i + (long long)j * ld] * yj;
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    for (int i = j0 + jb + tid; i < n; i += THREADS) {
+      T s = T(0);
+      for (int p = j0; p < j0 + jb; ++p) s = fma(M[i + (long long)p * ld], bv[p], s);
+      bv[i] -= s;
+    }
+    __syncthreads();
+  }
+  for (int j0 = ((n - 1) / 32) * 32; j0 >= 0; j0 -= 32) {
+    const int jb = min(32, n - j0);
+    for (int c = j0 + warp; c < j0 + jb; c += THREADS / 32) {
+      T s = T(0);
+      for (int r = j0 + jb + lane; r < n; r += 32) s = fma(M[r + (long long)c * ld], bv[r], s);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+      if (lane == 0) bv[c] -= s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      for (int j = j0 + jb - 1; j >= j0; --j) {
+        const T xj = bv[j] / M[j + (long long)j * ld];
+        __syncwarp();
+        if (lane == 0) bv[j] = xj;
+        const int i = j0 + lane;
+        if (i < j) bv[i] -= M[j + (long long)i * ld] * xj;
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+  }
+}
 
 // Factor + solve one system held in M (leading dimension ld), right-hand side in bv (shared).
 // Returns -1 on success or the failing column.  All threads of the CTA call it.
@@ -117,47 +167,132 @@ __device__ int factor_solve(T* M, int ld, int n, T* bv, int* s_fail, T* s_inv) {
     }
     __syncthreads();
   }
-  // ---- forward sweep L y = b, blocks of 32
-  for (int j0 = 0; j0 < n; j0 += 32) {
-    const int jb = min(32, n - j0);
+  solve_sweeps<T, THREADS>(M, ld, n, bv);
+  return -1;
+}
+
+// Four consecutive values from 16-byte aligned (float) / 32-byte aligned (double) shared memory.
+__device__ __forceinline__ void load4(const float* p, float* o) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+__device__ __forceinline__ void load4(const double* p, double* o) {
+  const double2 a = *reinterpret_cast<const double2*>(p);
+  const double2 b = *reinterpret_cast<const double2*>(p + 2);
+  o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+
+// Panel-blocked factorisation (the kernel variants with algo = 1).  Per NBP-wide panel at k0:
+//   1. warp 0 factors the kb x kb diagonal block in shared memory (Ds), one column per step with
+//      the rows spread over the lanes and only warp-level synchronisation: unblocked() of
+//      LLT.h:312-336 with its `x <= 0` test, so the failing column is the same;
+//   2. every thread solves whole rows below the block against it (L21 = A21 L11^{-T}, the row's
+//      kb values in registers, no synchronisation inside), storing them to M and to the
+//      shared panel copy Ps (Ps[p * psld + r] = L(r0 + r, k0 + p));
+//   3. the trailing update A22 -= L21 L21^T reads L21 from Ps only: 4 x 4 register tiles over the
+//      lower tiles in column-major order, so the lanes of a warp share the tile column (its 4
+//      panel values are a shared-memory broadcast) and cover consecutive rows of M (coalesced).
+// Four CTA barriers per panel instead of three per column.
+template <typename T, int NBP, int THREADS>
+__device__ int factor_blk(T* M, int ld, int n, T* Ds, T* Dinv, T* Ps, int psld, int* s_fail) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr int DLD = NBP + 1;
+  if (tid == 0) *s_fail = -1;
+  for (int k0 = 0; k0 < n; k0 += NBP) {
+    const int kb = min(NBP, n - k0);
+    for (int idx = tid; idx < kb * kb; idx += THREADS) {
+      const int r = idx % kb, c = idx / kb;
+      if (r >= c) Ds[r * DLD + c] = M[(k0 + r) + (long long)(k0 + c) * ld];
+    }
+    __syncthreads();
     if (warp == 0) {
-      for (int j = j0; j < j0 + jb; ++j) {
-        const T yj = bv[j] / M[j + (long long)j * ld];
-        __syncwarp();
-        if (lane == 0) bv[j] = yj;
+      for (int j = 0; j < kb; ++j) {
+        const T d = Ds[j * DLD + j];
+        if (d <= T(0)) {  // the `x <= 0` test of LLT.h:328 (a NaN pivot passes it)
+          if (lane == 0) *s_fail = k0 + j;
+          break;
+        }
+        const T rt = sqrt(d), inv = T(1) / rt;
         const int i = j + 1 + lane;
-        if (i < j0 + jb) bv[i] -= M[i + (long long)j * ld] * yj;
+        T lij = T(0);
+        if (i < kb) {
+          lij = Ds[i * DLD + j] * inv;
+          Ds[i * DLD + j] = lij;
+        }
+        __syncwarp();
+        if (i < kb)
+          for (int l = j + 1; l <= i; ++l) Ds[i * DLD + l] -= lij * Ds[l * DLD + j];
+        if (lane == 0) {
+          Ds[j * DLD + j] = rt;
+          Dinv[j] = inv;
+        }
         __syncwarp();
       }
     }
     __syncthreads();
-    for (int i = j0 + jb + tid; i < n; i += THREADS) {
-      T s = T(0);
-      for (int p = j0; p < j0 + jb; ++p) s = fma(M[i + (long long)p * ld], bv[p], s);
-      bv[i] -= s;
+    if (*s_fail >= 0) return *s_fail;
+    // the factored diagonal block back to M; rows below: L21 = A21 L11^{-T}, one thread per row
+    for (int idx = tid; idx < kb * kb; idx += THREADS) {
+      const int r = idx % kb, c = idx / kb;
+      if (r >= c) M[(k0 + r) + (long long)(k0 + c) * ld] = Ds[r * DLD + c];
     }
-    __syncthreads();
-  }
-  // ---- backward sweep L^T x = y
-  for (int j0 = ((n - 1) / 32) * 32; j0 >= 0; j0 -= 32) {
-    const int jb = min(32, n - j0);
-    // bv[c] -= sum_{r >= j0+jb} L(r, c) x_r for c in the block: one warp per column, shuffle reduction
-    for (int c = j0 + warp; c < j0 + jb; c += THREADS / 32) {
-      T s = T(0);
-      for (int r = j0 + jb + lane; r < n; r += 32) s = fma(M[r + (long long)c * ld], bv[r], s);
+    const int r0 = k0 + kb;
+    const int m = n - r0;
+    for (int r = tid; r < m; r += THREADS) {
+      T x[NBP];
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-      if (lane == 0) bv[c] -= s;
+      for (int c = 0; c < NBP; ++c) x[c] = c < kb ? M[(r0 + r) + (long long)(k0 + c) * ld] : T(0);
+#pragma unroll
+      for (int c = 0; c < NBP; ++c) {
+        if (c < kb) {
+          T v = x[c];
+#pragma unroll
+          for (int q = 0; q < c; ++q) v = fma(-x[q], Ds[c * DLD + q], v);
+          x[c] = v * Dinv[c];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NBP; ++c)
+        if (c < kb) {
+          M[(r0 + r) + (long long)(k0 + c) * ld] = x[c];
+          Ps[c * psld + r] = x[c];
+        }
     }
     __syncthreads();
-    if (warp == 0) {
-      for (int j = j0 + jb - 1; j >= j0; --j) {
-        const T xj = bv[j] / M[j + (long long)j * ld];
-        __syncwarp();
-        if (lane == 0) bv[j] = xj;
-        const int i = j0 + lane;
-        if (i < j) bv[i] -= M[j + (long long)i * ld] * xj;
-        __syncwarp();
+    if (m > 0) {
+      // lower 4 x 4 tiles of the m x m trailing matrix, column-major: tile t -> (tile column tj,
+      // offset o = ti - tj), advanced incrementally by THREADS
+      const int mt = (m + 3) >> 2;
+      const int ntile = mt * (mt + 1) / 2;
+      int tj = 0, o = tid;
+      while (tj < mt && o >= mt - tj) { o -= mt - tj; ++tj; }
+      for (int t = tid; t < ntile; t += THREADS) {
+        const int ti = tj + o;
+        const int i0 = 4 * ti, j0 = 4 * tj;
+        T acc[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+        for (int p = 0; p < kb; ++p) {
+          const T* pr = Ps + p * psld;
+          T ar[4], ac[4];
+          load4(pr + i0, ar);
+          load4(pr + j0, ac);
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = fma(ar[u], ac[v], acc[u][v]);
+        }
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u, j = j0 + v;
+            if (i < m && j < m && i >= j) M[(r0 + i) + (long long)(r0 + j) * ld] -= acc[u][v];
+          }
+        o += THREADS;
+        while (tj < mt && o >= mt - tj) { o -= mt - tj; ++tj; }
       }
     }
     __syncthreads();
@@ -165,11 +300,21 @@ __device__ int factor_solve(T* M, int ld, int n, T* bv, int* s_fail, T* s_inv) {
   return -1;
 }
 
-template <typename T, int NBP, int THREADS>
+// Shared-memory carve-up of the kernels: [bv: kMaxBatchN][Ds: NBP(NBP+1)][Dinv: NBP][Ps: NBP psld]
+// [staged matrix], the middle three only for algo 1; every part starts on a multiple of 4 elements.
+template <typename T>
+__host__ __device__ constexpr size_t blk_elems(int nbp, int psld) {
+  return (size_t)nbp * (nbp + 1) + (size_t)nbp + (size_t)nbp * psld;
+}
+
+template <typename T, int NBP, int THREADS, int ALGO>
 __global__ void __launch_bounds__(THREADS) batched_posv_kernel(BatchArgs<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* bv = reinterpret_cast<T*>(smem_raw);          // kMaxBatchN values
-  T* sm = bv + kMaxBatchN;                         // staged matrix
+  T* Ds = bv + kMaxBatchN;                         // algo 1: diagonal block, its inverse pivots, panel
+  T* Dinv = Ds + NBP * (NBP + 1);
+  T* Ps = Dinv + NBP;
+  T* sm = ALGO == 1 ? bv + kMaxBatchN + blk_elems<T>(NBP, p.psld) : bv + kMaxBatchN;  // staged matrix
   __shared__ int s_ticket, s_fail;
   __shared__ T s_inv;
   const int tid = threadIdx.x;
@@ -193,7 +338,15 @@ __global__ void __launch_bounds__(THREADS) batched_posv_kernel(BatchArgs<T> p) {
       }
     for (int i = tid; i < n; i += THREADS) bv[i] = B[i];
     __syncthreads();
-    const int fail = n > 0 ? factor_solve<T, NBP, THREADS>(M, ld, n, bv, &s_fail, &s_inv) : -1;
+    int fail = -1;
+    if (n > 0) {
+      if (ALGO == 0) {
+        fail = factor_solve<T, NBP, THREADS>(M, ld, n, bv, &s_fail, &s_inv);
+      } else {
+        fail = factor_blk<T, NBP, THREADS>(M, ld, n, Ds, Dinv, Ps, p.psld, &s_fail);
+        if (fail < 0) solve_sweeps<T, THREADS>(M, ld, n, bv);
+      }
+    }
     if (staged)
       for (int idx = tid; idx < n * n; idx += THREADS) {
         const int i = idx % n, j = idx / n;
@@ -208,52 +361,58 @@ __global__ void __launch_bounds__(THREADS) batched_posv_kernel(BatchArgs<T> p) {
 
 // ---- variants and launch ---------------------------------------------------------------------
 
-// Kernel variants the autotuner sweeps: panel width x threads per CTA x the largest order staged
-// in shared memory (-1 = as large as fits in one CTA's shared memory; smaller caps leave room for
-// more CTAs per SM, the larger systems then running in place in global memory, L2-resident).
+// Kernel variants the autotuner sweeps: algorithm (0: column at a time, 1: panel-blocked) x panel
+// width x threads per CTA x the largest order staged in shared memory (-1 = as large as fits in one
+// CTA's shared memory; smaller caps leave room for more CTAs per SM, the larger systems then running
+// in place in global memory, L2-resident).
 struct Variant {
-  int nbp, threads, smem_cap;
+  int algo, nbp, threads, smem_cap;
 };
-constexpr Variant kVariants[] = {{16, 128, -1}, {32, 128, -1}, {16, 256, -1}, {32, 256, -1},
-                                 {16, 128, 96},  {16, 256, 96},  {16, 128, 0},  {16, 256, 0}};
-constexpr int kNumVariants = 8;
+constexpr Variant kVariants[] = {{0, 16, 128, -1}, {0, 32, 128, -1}, {0, 16, 256, -1}, {0, 32, 256, -1},
+                                 {0, 16, 128, 96},  {0, 16, 256, 96},  {0, 16, 128, 0},  {0, 16, 256, 0},
+                                 {1, 16, 128, 0},   {1, 16, 256, 0},   {1, 32, 128, 0},  {1, 32, 256, 0},
+                                 {1, 16, 128, -1},  {1, 16, 256, 96}};
+constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+static_assert(kNumVariants == GBLLT_BATCH_VARIANTS, "gbllt.h states the number of batched kernel variants");
 
 template <typename T>
-size_t smem_bytes(int smem_max_n) {
-  const int ld = smem_max_n | 1;
-  return (size_t)kMaxBatchN * sizeof(T) + (size_t)ld * smem_max_n * sizeof(T);
+using BatchKernel = void (*)(BatchArgs<T>);
+
+// kernel of each variant, in the order of kVariants
+template <typename T>
+BatchKernel<T> kernel_of(int v) {
+  static const BatchKernel<T> table[] = {
+      batched_posv_kernel<T, 16, 128, 0>, batched_posv_kernel<T, 32, 128, 0>, batched_posv_kernel<T, 16, 256, 0>,
+      batched_posv_kernel<T, 32, 256, 0>, batched_posv_kernel<T, 16, 128, 0>, batched_posv_kernel<T, 16, 256, 0>,
+      batched_posv_kernel<T, 16, 128, 0>, batched_posv_kernel<T, 16, 256, 0>, batched_posv_kernel<T, 16, 128, 1>,
+      batched_posv_kernel<T, 16, 256, 1>, batched_posv_kernel<T, 32, 128, 1>, batched_posv_kernel<T, 32, 256, 1>,
+      batched_posv_kernel<T, 16, 128, 1>, batched_posv_kernel<T, 16, 256, 1>};
+  static_assert(sizeof(table) / sizeof(table[0]) == kNumVariants, "one kernel per variant");
+  return table[v];
 }
 
-template <typename T, int NBP, int THREADS>
-int launch_variant(const BatchArgs<T>& args, int grid, size_t smem, cudaStream_t s) {
-  auto kern = batched_posv_kernel<T, NBP, THREADS>;
+// Dynamic shared memory of a variant: b, the algo-1 panel buffers, and the staged matrix.
+template <typename T>
+size_t smem_bytes(int variant, int smem_max_n, int psld) {
+  const Variant v = kVariants[variant];
+  size_t e = (size_t)kMaxBatchN + (v.algo == 1 ? blk_elems<T>(v.nbp, psld) : 0);
+  if (smem_max_n > 0) e += (size_t)(smem_max_n | 1) * smem_max_n;
+  return e * sizeof(T);
+}
+
+template <typename T>
+int launch_batched(int variant, const BatchArgs<T>& args, int grid, size_t smem, cudaStream_t s) {
+  const BatchKernel<T> kern = kernel_of<T>(variant);
   GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<grid, THREADS, smem, s>>>(args);
+  kern<<<grid, kVariants[variant].threads, smem, s>>>(args);
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
 }
 
 template <typename T>
-const void* kernel_of(int variant) {
-  const Variant v = kVariants[variant];
-  if (v.nbp == 16) return v.threads == 128 ? (const void*)batched_posv_kernel<T, 16, 128>
-                                           : (const void*)batched_posv_kernel<T, 16, 256>;
-  return v.threads == 128 ? (const void*)batched_posv_kernel<T, 32, 128> : (const void*)batched_posv_kernel<T, 32, 256>;
-}
-
-template <typename T>
-int launch_batched(int variant, const BatchArgs<T>& args, int grid, size_t smem, cudaStream_t s) {
-  const Variant v = kVariants[variant];
-  if (v.nbp == 16) return v.threads == 128 ? launch_variant<T, 16, 128>(args, grid, smem, s)
-                                           : launch_variant<T, 16, 256>(args, grid, smem, s);
-  return v.threads == 128 ? launch_variant<T, 32, 128>(args, grid, smem, s)
-                          : launch_variant<T, 32, 256>(args, grid, smem, s);
-}
-
-template <typename T>
 int occupancy(int variant, size_t smem) {
   int blocks = 0;
-  const void* f = kernel_of<T>(variant);
+  const BatchKernel<T> f = kernel_of<T>(variant);
   cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, f, kVariants[variant].threads, smem);
   return blocks;
@@ -293,6 +452,7 @@ struct BatchPlan {
   int device = 0;
   int variant = 3;
   int smem_max_n = 0;
+  int psld = 4;  // algo-1 panel copy: round_up(max_n, 4)
   int grid = 0;
   size_t smem = 0;
   double tuned_ms[kNumVariants] = {};
@@ -312,13 +472,15 @@ void configure(BatchPlan* p) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  // stage in shared memory every system whose matrix fits (leaving room for b), up to the variant's cap
+  // stage in shared memory every system whose matrix fits (leaving room for b and the panel
+  // buffers), up to the variant's cap
+  p->psld = std::max(4, (p->max_n + 3) / 4 * 4);
   int nmax = std::min(p->max_n, kMaxBatchN);
-  while (nmax > 0 && smem_bytes<T>(nmax) > (size_t)optin) --nmax;
+  while (nmax > 0 && smem_bytes<T>(p->variant, nmax, p->psld) > (size_t)optin) --nmax;
   const int cap = kVariants[p->variant].smem_cap;
   if (cap >= 0 && nmax > cap) nmax = cap;
   p->smem_max_n = nmax;
-  p->smem = nmax > 0 ? smem_bytes<T>(nmax) : (size_t)kMaxBatchN * sizeof(T);
+  p->smem = smem_bytes<T>(p->variant, nmax, p->psld);
   const int occ = std::max(1, occupancy<T>(p->variant, p->smem));
   p->grid = sms * occ;
 }
@@ -336,7 +498,7 @@ void batch_work(const BatchPlan* p, double* fl, double* by) {
 template <typename T>
 int run_plan(BatchPlan* p, T* a, T* b, int64_t* info, cudaStream_t s, bool prof) {
   BatchArgs<T> args{a, b, info, p->d_order, p->d_n, p->d_aoff, p->d_boff, (int)p->count, p->d_counter,
-                    p->smem_max_n};
+                    p->smem_max_n, p->psld};
   GB_CUDA_TRY(cudaMemsetAsync(p->d_counter, 0, sizeof(int), s));
   static const std::string kname = std::string("batched_posv_") + tname<T>();
   double fl = 0, by = 0;
@@ -570,13 +732,17 @@ int cached_variant(const char* path, const std::string& sig) {
 
 void write_cache(const char* path, const std::string& sig, const BatchPlan* p) {
   auto entries = read_cache(path);
-  char body[512];
-  snprintf(body, sizeof body,
-           "{\"variant\": %d, \"panel\": %d, \"threads\": %d, \"smem_max_n\": %d, \"ms\": [%.4f, %.4f, %.4f, %.4f, "
-           "%.4f, %.4f, %.4f, %.4f]}",
-           p->variant, kVariants[p->variant].nbp, kVariants[p->variant].threads, p->smem_max_n, p->tuned_ms[0],
-           p->tuned_ms[1], p->tuned_ms[2], p->tuned_ms[3], p->tuned_ms[4], p->tuned_ms[5], p->tuned_ms[6],
-           p->tuned_ms[7]);
+  std::string body = "{\"variant\": " + std::to_string(p->variant) +
+                     ", \"algo\": " + std::to_string(kVariants[p->variant].algo) +
+                     ", \"panel\": " + std::to_string(kVariants[p->variant].nbp) +
+                     ", \"threads\": " + std::to_string(kVariants[p->variant].threads) +
+                     ", \"smem_max_n\": " + std::to_string(p->smem_max_n) + ", \"ms\": [";
+  for (int v = 0; v < kNumVariants; ++v) {
+    char num[32];
+    snprintf(num, sizeof num, "%s%.4f", v ? ", " : "", p->tuned_ms[v]);
+    body += num;
+  }
+  body += "]}";
   bool found = false;
   for (auto& e : entries)
     if (e.first == sig) {

@@ -135,6 +135,8 @@ def lib() -> ctypes.CDLL:
     return _lib
 
 
+BATCH_VARIANTS = 14  # GBLLT_BATCH_VARIANTS of include/gbllt.h
+
 LAPACK_PATH = PKG_DIR / "lib" / "libgbllt_lapack.so"
 _lapack = None
 _I = ctypes.POINTER(ctypes.c_int)

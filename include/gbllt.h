@@ -172,11 +172,14 @@ GBLLT_API int gbllt_batch_plan_destroy(gbllt_batch_plan* plan);
 /* Host copies of the offsets (arrays of `count`, may be NULL) and total element counts. */
 GBLLT_API int gbllt_batch_plan_layout(const gbllt_batch_plan* plan, int64_t* aoff, int64_t* boff, int64_t* a_elems,
                                       int64_t* b_elems);
-/* Autotuner: times each kernel variant (panel width x threads per CTA) on synthetic SPD systems
- * of the plan's sizes and keeps the fastest; with cache_path, a previous choice for the same
- * sizes is read from / a new one written to that JSON file.  Returns the variant index (>= 0). */
+/* Number of batched kernel variants: algorithm (column at a time / panel-blocked) x panel width x
+ * threads per CTA x the largest order staged in shared memory. */
+#define GBLLT_BATCH_VARIANTS 14
+/* Autotuner: times each kernel variant on synthetic SPD systems of the plan's sizes and keeps the
+ * fastest; with cache_path, a previous choice for the same sizes is read from / a new one written
+ * to that JSON file.  Returns the variant index (>= 0). */
 GBLLT_API int gbllt_batch_plan_tune(gbllt_batch_plan* plan, const char* cache_path, void* stream);
-/* Use kernel variant `variant` (0..7) without tuning. */
+/* Use kernel variant `variant` (0 .. GBLLT_BATCH_VARIANTS - 1) without tuning. */
 GBLLT_API int gbllt_batch_plan_set_variant(gbllt_batch_plan* plan, int variant);
 /* The variant in use: returns its index and its panel width, threads per CTA and the largest
  * order staged in shared memory. */

@@ -57,12 +57,14 @@ def test_batched_host_matches_oracle(oracle, gbllt, dtype):
     _check(oracle, sizes, a, b, a2, b2, info, dtype)
 
 
-@pytest.mark.parametrize("variant", list(range(8)))
-def test_batched_every_variant_graph_replay(oracle, gbllt, variant):
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("variant", list(range(14)))
+def test_batched_every_variant_graph_replay(oracle, gbllt, variant, dtype):
     torch = pytest.importorskip("torch")
-    sizes = list(oracle.batch_sizes(120, seed=22, lo=4, hi=256)) + [1, 33, 170, 255]
-    _, a, b = _batch(oracle, sizes, np.float64, seed=300)
-    plan = gbllt.BatchPlan(sizes, np.float64)
+    assert gbllt.BATCH_VARIANTS == 14
+    sizes = list(oracle.batch_sizes(120, seed=22, lo=4, hi=256)) + [1, 2, 4, 5, 16, 17, 33, 170, 255, 256]
+    _, a, b = _batch(oracle, sizes, dtype, seed=300)
+    plan = gbllt.BatchPlan(sizes, dtype)
     plan.set_variant(variant)
     da = torch.from_numpy(a).cuda()
     db = torch.from_numpy(b).cuda()
@@ -70,16 +72,17 @@ def test_batched_every_variant_graph_replay(oracle, gbllt, variant):
     s = torch.cuda.current_stream().cuda_stream
     plan.solve_dev(da, db, di, s)           # captures the graph
     torch.cuda.synchronize()
-    _check(oracle, sizes, a, b, da.cpu().numpy(), db.cpu().numpy(), di.cpu().numpy(), np.float64)
+    _check(oracle, sizes, a, b, da.cpu().numpy(), db.cpu().numpy(), di.cpu().numpy(), dtype)
     # replay the same graph on fresh inputs in the same buffers
     da.copy_(torch.from_numpy(a))
     db.copy_(torch.from_numpy(b))
     plan.solve_dev(da, db, di, s)
     torch.cuda.synchronize()
-    _check(oracle, sizes, a, b, da.cpu().numpy(), db.cpu().numpy(), di.cpu().numpy(), np.float64)
+    _check(oracle, sizes, a, b, da.cpu().numpy(), db.cpu().numpy(), di.cpu().numpy(), dtype)
 
 
-def test_batched_failing_systems(oracle, gbllt):
+@pytest.mark.parametrize("variant", [3, 7, 8, 11, 12])
+def test_batched_failing_systems(oracle, gbllt, variant):
     sizes = [10, 70, 200, 40]
     mats, _, _ = _batch(oracle, sizes, np.float64, seed=500)
     mats[1][0, 0] = -1.0       # fails at column 0
@@ -87,6 +90,7 @@ def test_batched_failing_systems(oracle, gbllt):
     a = np.concatenate([m.ravel(order="F") for m in mats])
     b = np.concatenate([oracle.normal(9 + i, n) for i, n in enumerate(sizes)])
     plan = gbllt.BatchPlan(sizes, np.float64)
+    plan.set_variant(variant)
     a2, b2 = a.copy(), b.copy()
     info = plan.solve(a2, b2)
     assert list(info) == [0, 1, 151, 0]
@@ -98,11 +102,11 @@ def test_batched_autotuner_cache(oracle, gbllt, tmp_path):
     cache = tmp_path / "tune.json"
     plan = gbllt.BatchPlan(sizes, np.float32)
     v = plan.tune(str(cache))
-    assert 0 <= v <= 7
+    assert 0 <= v < gbllt.BATCH_VARIANTS
     entries = json.loads(cache.read_text())
     assert len(entries) == 1
     (entry,) = entries.values()
-    assert entry["variant"] == v and len(entry["ms"]) == 8 and min(entry["ms"]) > 0
+    assert entry["variant"] == v and len(entry["ms"]) == gbllt.BATCH_VARIANTS and min(entry["ms"]) > 0
     plan2 = gbllt.BatchPlan(sizes, np.float32)
     assert plan2.tune(str(cache)) == v  # read back, no new sweep
     _, a, b = _batch(oracle, sizes, np.float32, seed=700)
