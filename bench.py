@@ -271,7 +271,21 @@ def measured_peaks() -> dict:
     return out
 
 
-def roofline_for(name: str, st: dict, peaks: dict) -> dict:
+# DRAM bytes (read + write) per launch from ncu captures of the kernel on a smaller case, and the
+# law that scales them to this run's launch (profiles/ holds the summaries with the commands):
+#   symm_residual_f64 (NR = 16 kernel): 1.628 GB at n = 8192, 64 RHS; A's stored tiles are read
+#     once per 16-column chunk of right-hand sides, so traffic grows as n^2 * ceil(k / 16).
+NCU_TRAFFIC = {"symm_residual_f64": (8192, 64, 1.628e9)}
+
+
+def ncu_traffic(name: str, n: int, k: int):
+    if name not in NCU_TRAFFIC or k < 16:
+        return None
+    n0, k0, by = NCU_TRAFFIC[name]
+    return by * (n / n0) ** 2 * (-(-k // 16)) / (-(-k0 // 16))
+
+
+def roofline_for(name: str, st: dict, peaks: dict, n: int = 0, k: int = 0) -> dict:
     """Achieved = algorithmic work of the kernel's launches / their summed device time."""
     ms = max(st["ms"], 1e-9)
     if name.startswith("tc_update_tf32"):
@@ -287,9 +301,12 @@ def roofline_for(name: str, st: dict, peaks: dict) -> dict:
     else:
         bound, unit, peak, src = "hbm", "GB/s", peaks["hbm_gbs"], peaks["source"]["hbm_gbs"]
         ach = st["bytes"] / ms / 1e6
+    traffic = ncu_traffic(name, n, k)
     return {"kernel": name, "bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
-            "traffic": None, "launches": st["launches"], "per_launch_flops": st["flops"] / st["launches"],
-            "per_launch_bytes": st["bytes"] / st["launches"], "peak_source": src}
+            "traffic": traffic, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at n=8192, "
+            "64 RHS, scaled by n^2 ceil(k/16)" if traffic else None, "launches": st["launches"],
+            "per_launch_flops": st["flops"] / st["launches"], "per_launch_bytes": st["bytes"] / st["launches"],
+            "peak_source": src}
 
 
 def run_ours(args, ws, rank, local):
@@ -375,7 +392,8 @@ def run_ours(args, ws, rank, local):
         total = sum(v["ms"] for v in prof.values())
         d = {"seconds_per_solve": ms / args.steps / 1e3, "tflops": ws * flops * args.steps / (ms * 1e-3) / 1e12,
              "backward_error": be, "gpu_launches": sum(v["launches"] for v in prof.values()),
-             "roofline": dict(roofline_for(top[0], top[1], peaks), kernel_share_of_device_time=top[1]["ms"] / total),
+             "roofline": dict(roofline_for(top[0], top[1], peaks, cfg["n"], cfg["nrhs"]),
+                              kernel_share_of_device_time=top[1]["ms"] / total),
              "kernels": {kn: {"launches": v["launches"], "ms": v["ms"]} for kn, v in prof.items()}}
         d.update(extra)
         return d
@@ -495,16 +513,23 @@ def run_c3(args):
     print(json.dumps(out), flush=True)
 
 
-def run_c4(args):
-    """20000 SPD systems, n_i ~ U{4..256}, one RHS each, FP64 and FP32, one graph-replayed launch."""
+def run_c4(args, ws: int = 1, rank: int = 0):
+    """20000 SPD systems, n_i ~ U{4..256}, one RHS each, FP64 and FP32, one graph-replayed launch.
+    With N ranks the systems are sharded by cost (shard.partition, no data-path collective): each
+    rank solves its share, the step time is the maximum over ranks, and the value counts all
+    20000 systems (fixed total work: strong scaling)."""
     import torch
     import gbllt as G
-    count = 20000
+    import shard
+    count_all = 20000
     rng = torch.Generator(device="cpu").manual_seed(21)
-    sizes = torch.randint(4, 257, (count,), generator=rng).numpy().astype(np.int64)
+    sizes_all = torch.randint(4, 257, (count_all,), generator=rng).numpy().astype(np.int64)
+    sizes = sizes_all[shard.partition(sizes_all, ws)[rank]] if ws > 1 else sizes_all
+    count = len(sizes)
     out = {"metric": "batched LLT solves/s and fraction of HBM", "config": {
         "workload": "C4: 20000 SPD systems, n_i uniform in [4,256], A_i = G_i G_i^T/n_i + 0.1 I, 1 RHS each",
-        "count": count}, "unit": "solves/s", "higher_is_better": True, "data": "synthetic", "results": []}
+        "count": count_all, "ranks": ws}, "unit": "solves/s", "higher_is_better": True, "data": "synthetic",
+        "n_gpus": ws, "scaling": "strong", "results": []}
     peaks = {"hbm_gbs": json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]
              if (ROOT / "MEASURED_PEAKS.json").exists() else 6800.0, "fp64_tflops": fp64_peak_tflops()}
     s = torch.cuda.current_stream().cuda_stream
@@ -534,11 +559,13 @@ def run_c4(args):
         for _ in range(args.steps):
             a.copy_(a0)
             b.copy_(b0)
+            barrier(ws)
+            torch.cuda.synchronize()
             e0.record()
             plan.solve_dev(a, b, info, s)
             e1.record()
             e1.synchronize()
-            tot += e0.elapsed_time(e1)
+            tot += max_over_ranks(ws, e0.elapsed_time(e1))
         prof = G.profile_read()
         G.profile_enable(False)
         assert int(info.max()) == 0
@@ -546,12 +573,14 @@ def run_c4(args):
         ms = tot / args.steps
         gbs = st["bytes"] / st["ms"] / 1e6
         tfs = st["flops"] / st["ms"] / 1e9
-        out["results"].append({"dtype": name, "ms": ms, "solves_per_s": count / (ms * 1e-3), "achieved_gbs": gbs,
-                               "hbm_frac": gbs / peaks["hbm_gbs"], "achieved_tflops": tfs,
+        out["results"].append({"dtype": name, "ms": ms, "solves_per_s": count_all / (ms * 1e-3),
+                               "achieved_gbs": gbs, "hbm_frac": gbs / peaks["hbm_gbs"], "achieved_tflops": tfs,
                                "fp64_frac": tfs / peaks["fp64_tflops"] if name == "f64" else None,
-                               "variant": plan.variant(), "launches_per_step": 1})
+                               "variant": plan.variant(), "launches_per_step": 1,
+                               "per_rank_note": "achieved_* are rank 0's kernel on its shard" if ws > 1 else None})
     out["peaks"] = peaks
-    print(json.dumps(out), flush=True)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
 
 
 def run_c5(args):
@@ -663,7 +692,10 @@ def main():
     if args.config in ("c3", "c4", "c5"):
         import torch
         torch.cuda.set_device(local)
-        {"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.config](args)
+        if args.config == "c4":
+            run_c4(args, ws, rank)
+        else:
+            {"c3": run_c3, "c5": run_c5}[args.config](args)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

@@ -30,7 +30,8 @@ def test_partition_covers_every_system_once_and_is_balanced(oracle):
         cost = S.system_cost(sizes)
         # LPT makespan bound: at most the average load plus the largest single system
         assert ld.max() <= cost.sum() / ws + cost.max() + 1e-6
-        assert parts == S.partition(sizes, ws) or all(np.array_equal(x, y) for x, y in zip(parts, S.partition(sizes, ws)))
+        # deterministic: every rank computes the same partition without communicating
+        assert all(np.array_equal(x, y) for x, y in zip(parts, S.partition(sizes, ws)))
 
 
 def test_partition_more_ranks_than_systems():
