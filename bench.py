@@ -343,6 +343,12 @@ def run_ours(args, ws, rank, local):
             rc, rep = G.posv_mixed_dev(A0, n, n, B0, n, X, n, k, opts, "L", sp, raise_on_error=False)
             reports.append((rc, rep))
 
+    # L2 hygiene: a matrix smaller than 4 x L2 (129 MB) gets a 512 MB write between timed steps
+    l2_bytes = 129 << 20
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda") if n * n * 8 < 4 * l2_bytes else None
+    l2_note = (f"inputs larger than L2 (matrix {n * n * 8 / 1e9:.1f} GB vs 129 MB L2)" if flush is None else
+               f"L2 flushed before each timed step (512 MB write; matrix {n * n * 8 / 1e6:.0f} MB)")
+
     def timed(step_fn):
         for _ in range(max(args.warmup, 0)):
             step_fn()
@@ -354,17 +360,29 @@ def run_ours(args, ws, rank, local):
         G.profile_enable(True)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            step_fn()
-        e1.record(stream)
-        e1.synchronize()
+        if flush is None:  # inputs larger than L2: one timed region over all steps
+            e0.record(stream)
+            for _ in range(args.steps):
+                step_fn()
+            e1.record(stream)
+            e1.synchronize()
+            total_ms = e0.elapsed_time(e1)
+        else:  # small inputs: L2 flushed (a write larger than L2) before each step, outside its timing
+            total_ms = 0.0
+            for _ in range(args.steps):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                e0.record(stream)
+                step_fn()
+                e1.record(stream)
+                e1.synchronize()
+                total_ms += e0.elapsed_time(e1)
         torch.cuda.synchronize()
         barrier(ws)
         ck = clocks.stop()
         prof = G.profile_read()
         G.profile_enable(False)
-        return max_over_ranks(ws, e0.elapsed_time(e1)), prof, ck
+        return max_over_ranks(ws, total_ms), prof, ck
 
     def backward_error(Xs):  # torch FP64 GEMM as an independent check of the returned solution
         R = A0 @ Xs.T - B0.T
@@ -450,7 +468,7 @@ def run_ours(args, ws, rank, local):
                    "headline": "mixed+refinement" if use_mixed else "plain FP64",
                    "work_per_step_flops": flops, "accuracy": "normwise backward error <= 1e-14 (checked with a "
                    "torch FP64 residual of the returned X)",
-                   "l2": "inputs larger than L2 (matrix 2.1 GB vs 129 MB L2)"},
+                   "l2": l2_note},
         "seconds_per_solve": head["seconds_per_solve"], "backward_error": head["backward_error"],
         "roofline": head["roofline"], "gpu_launches": head["gpu_launches"],
         "fp64": fp64, "mixed": mixed, "peaks": peaks,
@@ -654,15 +672,17 @@ def run_c5(args):
             for m in range(t, nmat, nstream):
                 rc, rep = G.posv_mixed_dev(A[m], n, n, Y[m].reshape(1, n), n, Xs[m], n, 1, opts, "L",
                                            st.cuda_stream, raise_on_error=False)
-                got.append(rep["steps"])
+                got.append((rc, rep["steps"]))
         return got
 
     t0 = time.perf_counter()
     with ThreadPoolExecutor(nstream) as pool:
-        steps = [v for chain in pool.map(mixed_chain, range(nstream)) for v in chain]
+        got = [v for chain in pool.map(mixed_chain, range(nstream)) for v in chain]
     torch.cuda.synchronize()
     res["mixed_solve_s"] = time.perf_counter() - t0
+    steps = [st_ for _, st_ in got]
     res["mixed_steps"] = [min(steps), max(steps)]
+    res["mixed_return_codes"] = sorted({rc for rc, _ in got})
     fl_fwd = nmat * (n ** 3 / 3 + 2 * n * n)
     out = {"metric": "GP likelihood logdet+quad forward and adjoint (s)", "config": {
         "workload": "C5: 64 RBF matrices n=2048, lengthscale 0.2, noise 1e-2", "nmat": nmat, "n": n},

@@ -48,33 +48,54 @@ struct BatchArgs {
   int psld;             // algo 1: leading dimension of the shared panel copy (round_up(max n, 4))
 };
 
-// The two sweeps of the solve (LLT.h:483-498) on the factored system: blocks of 32, warp 0
-// substitutes inside each diagonal block, all warps apply the off-diagonal blocks.
+// The two sweeps of the solve (LLT.h:483-498) on the factored system, in blocks of 32 rows.  Each
+// 32 x 32 diagonal block is first staged in shared memory (Dg, coalesced loads by all threads); warp 0
+// then substitutes inside it with the block's right-hand sides in registers (lane = row), one
+// warp shuffle per step and the pivots' reciprocals precomputed, so the sequential part touches
+// neither global memory nor a CTA barrier.  All warps apply the off-diagonal blocks (a GEMV
+// forward, warp-shuffle dot products backward).
+constexpr int kDgLd = 33;  // Dg[r * kDgLd + c] = L(j0 + r, j0 + c), r >= c
+
 template <typename T, int THREADS>
-__device__ void solve_sweeps(const T* M, int ld, int n, T* bv) {
+__device__ void solve_sweeps(const T* M, int ld, int n, T* bv, T* Dg) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  auto load_diag = [&](int j0, int jb) {
+    for (int idx = tid; idx < jb * jb; idx += THREADS) {
+      const int r = idx % jb, c = idx / jb;
+      if (r >= c) Dg[r * kDgLd + c] = M[(j0 + r) + (long long)(j0 + c) * ld];
+    }
+  };
+  // L y = b
   for (int j0 = 0; j0 < n; j0 += 32) {
     const int jb = min(32, n - j0);
+    load_diag(j0, jb);
+    __syncthreads();
     if (warp == 0) {
-      for (int j = j0; j < j0 + jb; ++j) {
-        const T yj = bv[j] / M[j + (long long)j * ld];
-        __syncwarp();
-        if (lane == 0) bv[j] = yj;
-        const int i = j + 1 + lane;
-        if (i < j0 + jb) bv[i] -= M[i + (long long)j * ld] * yj;
-        __syncwarp();
+      T b = lane < jb ? bv[j0 + lane] : T(0);
+      const T rinv = lane < jb ? T(1) / Dg[lane * kDgLd + lane] : T(0);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        if (j < jb) {
+          const T yj = __shfl_sync(0xffffffffu, b * rinv, j);
+          if (lane > j && lane < jb) b = fma(-Dg[lane * kDgLd + j], yj, b);
+          if (lane == j) b = yj;
+        }
       }
+      if (lane < jb) bv[j0 + lane] = b;
     }
     __syncthreads();
     for (int i = j0 + jb + tid; i < n; i += THREADS) {
       T s = T(0);
+#pragma unroll 8
       for (int p = j0; p < j0 + jb; ++p) s = fma(M[i + (long long)p * ld], bv[p], s);
       bv[i] -= s;
     }
     __syncthreads();
   }
+  // L^T x = y
   for (int j0 = ((n - 1) / 32) * 32; j0 >= 0; j0 -= 32) {
     const int jb = min(32, n - j0);
+    load_diag(j0, jb);
     for (int c = j0 + warp; c < j0 + jb; c += THREADS / 32) {
       T s = T(0);
       for (int r = j0 + jb + lane; r < n; r += 32) s = fma(M[r + (long long)c * ld], bv[r], s);
@@ -84,14 +105,17 @@ __device__ void solve_sweeps(const T* M, int ld, int n, T* bv) {
     }
     __syncthreads();
     if (warp == 0) {
-      for (int j = j0 + jb - 1; j >= j0; --j) {
-        const T xj = bv[j] / M[j + (long long)j * ld];
-        __syncwarp();
-        if (lane == 0) bv[j] = xj;
-        const int i = j0 + lane;
-        if (i < j) bv[i] -= M[j + (long long)i * ld] * xj;
-        __syncwarp();
+      T b = lane < jb ? bv[j0 + lane] : T(0);
+      const T rinv = lane < jb ? T(1) / Dg[lane * kDgLd + lane] : T(0);
+#pragma unroll
+      for (int j = 31; j >= 0; --j) {
+        if (j < jb) {
+          const T xj = __shfl_sync(0xffffffffu, b * rinv, j);
+          if (lane < j) b = fma(-Dg[j * kDgLd + lane], xj, b);
+          if (lane == j) b = xj;
+        }
       }
+      if (lane < jb) bv[j0 + lane] = b;
     }
     __syncthreads();
   }
@@ -100,7 +124,7 @@ __device__ void solve_sweeps(const T* M, int ld, int n, T* bv) {
 // Factor + solve one system held in M (leading dimension ld), right-hand side in bv (shared).
 // Returns -1 on success or the failing column.  All threads of the CTA call it.
 template <typename T, int NBP, int THREADS>
-__device__ int factor_solve(T* M, int ld, int n, T* bv, int* s_fail, T* s_inv) {
+__device__ int factor_solve(T* M, int ld, int n, T* bv, T* Dg, int* s_fail, T* s_inv) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) *s_fail = -1;
   __syncthreads();
@@ -167,7 +191,7 @@ __device__ int factor_solve(T* M, int ld, int n, T* bv, int* s_fail, T* s_inv) {
     }
     __syncthreads();
   }
-  solve_sweeps<T, THREADS>(M, ld, n, bv);
+  solve_sweeps<T, THREADS>(M, ld, n, bv, Dg);
   return -1;
 }
 
@@ -269,11 +293,15 @@ __device__ int factor_blk(T* M, int ld, int n, T* Ds, T* Dinv, T* Ps, int psld, 
       for (int t = tid; t < ntile; t += THREADS) {
         const int ti = tj + o;
         const int i0 = 4 * ti, j0 = 4 * tj;
+        // the tile of A22 is fetched before the product, so its (L2) latency overlaps the FMAs
         T acc[4][4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int v = 0; v < 4; ++v)
 #pragma unroll
-          for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+          for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u, j = j0 + v;
+            acc[u][v] = (i < m && j < m && i >= j) ? M[(r0 + i) + (long long)(r0 + j) * ld] : T(0);
+          }
         for (int p = 0; p < kb; ++p) {
           const T* pr = Ps + p * psld;
           T ar[4], ac[4];
@@ -282,14 +310,14 @@ __device__ int factor_blk(T* M, int ld, int n, T* Ds, T* Dinv, T* Ps, int psld, 
 #pragma unroll
           for (int u = 0; u < 4; ++u)
 #pragma unroll
-            for (int v = 0; v < 4; ++v) acc[u][v] = fma(ar[u], ac[v], acc[u][v]);
+            for (int v = 0; v < 4; ++v) acc[u][v] = fma(-ar[u], ac[v], acc[u][v]);
         }
 #pragma unroll
         for (int v = 0; v < 4; ++v)
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             const int i = i0 + u, j = j0 + v;
-            if (i < m && j < m && i >= j) M[(r0 + i) + (long long)(r0 + j) * ld] -= acc[u][v];
+            if (i < m && j < m && i >= j) M[(r0 + i) + (long long)(r0 + j) * ld] = acc[u][v];
           }
         o += THREADS;
         while (tj < mt && o >= mt - tj) { o -= mt - tj; ++tj; }
@@ -300,21 +328,23 @@ __device__ int factor_blk(T* M, int ld, int n, T* Ds, T* Dinv, T* Ps, int psld, 
   return -1;
 }
 
-// Shared-memory carve-up of the kernels: [bv: kMaxBatchN][Ds: NBP(NBP+1)][Dinv: NBP][Ps: NBP psld]
-// [staged matrix], the middle three only for algo 1; every part starts on a multiple of 4 elements.
+// Shared-memory carve-up of the kernels: [bv: kMaxBatchN][Dg: 32 x 33][Ds: NBP(NBP+1)][Dinv: NBP]
+// [Ps: NBP psld][staged matrix], Ds/Dinv/Ps only for algo 1; every part starts on a multiple of 4
+// elements (32 x 33 = 1056).
 template <typename T>
 __host__ __device__ constexpr size_t blk_elems(int nbp, int psld) {
   return (size_t)nbp * (nbp + 1) + (size_t)nbp + (size_t)nbp * psld;
 }
 
-template <typename T, int NBP, int THREADS, int ALGO>
-__global__ void __launch_bounds__(THREADS) batched_posv_kernel(BatchArgs<T> p) {
+template <typename T, int NBP, int THREADS, int ALGO, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) batched_posv_kernel(BatchArgs<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* bv = reinterpret_cast<T*>(smem_raw);          // kMaxBatchN values
-  T* Ds = bv + kMaxBatchN;                         // algo 1: diagonal block, its inverse pivots, panel
+  T* Dg = bv + kMaxBatchN;                         // the solve's 32 x 32 diagonal block
+  T* Ds = Dg + 32 * kDgLd;                         // algo 1: diagonal block, its inverse pivots, panel
   T* Dinv = Ds + NBP * (NBP + 1);
   T* Ps = Dinv + NBP;
-  T* sm = ALGO == 1 ? bv + kMaxBatchN + blk_elems<T>(NBP, p.psld) : bv + kMaxBatchN;  // staged matrix
+  T* sm = ALGO == 1 ? Ds + blk_elems<T>(NBP, p.psld) : Ds;  // staged matrix
   __shared__ int s_ticket, s_fail;
   __shared__ T s_inv;
   const int tid = threadIdx.x;
@@ -341,10 +371,10 @@ __global__ void __launch_bounds__(THREADS) batched_posv_kernel(BatchArgs<T> p) {
     int fail = -1;
     if (n > 0) {
       if (ALGO == 0) {
-        fail = factor_solve<T, NBP, THREADS>(M, ld, n, bv, &s_fail, &s_inv);
+        fail = factor_solve<T, NBP, THREADS>(M, ld, n, bv, Dg, &s_fail, &s_inv);
       } else {
         fail = factor_blk<T, NBP, THREADS>(M, ld, n, Ds, Dinv, Ps, p.psld, &s_fail);
-        if (fail < 0) solve_sweeps<T, THREADS>(M, ld, n, bv);
+        if (fail < 0) solve_sweeps<T, THREADS>(M, ld, n, bv, Dg);
       }
     }
     if (staged)
@@ -365,13 +395,16 @@ __global__ void __launch_bounds__(THREADS) batched_posv_kernel(BatchArgs<T> p) {
 // width x threads per CTA x the largest order staged in shared memory (-1 = as large as fits in one
 // CTA's shared memory; smaller caps leave room for more CTAs per SM, the larger systems then running
 // in place in global memory, L2-resident).
+// The last two variants ask the compiler for 8 (4) resident CTAs of 128 (256) threads, i.e. at
+// most 64 registers per thread, trading registers for warps that hide latency.
 struct Variant {
-  int algo, nbp, threads, smem_cap;
+  int algo, nbp, threads, smem_cap, min_blocks;
 };
-constexpr Variant kVariants[] = {{0, 16, 128, -1}, {0, 32, 128, -1}, {0, 16, 256, -1}, {0, 32, 256, -1},
-                                 {0, 16, 128, 96},  {0, 16, 256, 96},  {0, 16, 128, 0},  {0, 16, 256, 0},
-                                 {1, 16, 128, 0},   {1, 16, 256, 0},   {1, 32, 128, 0},  {1, 32, 256, 0},
-                                 {1, 16, 128, -1},  {1, 16, 256, 96}};
+constexpr Variant kVariants[] = {
+    {0, 16, 128, -1, 1}, {0, 32, 128, -1, 1}, {0, 16, 256, -1, 1}, {0, 32, 256, -1, 1},
+    {0, 16, 128, 96, 1}, {0, 16, 256, 96, 1}, {0, 16, 128, 0, 1},  {0, 16, 256, 0, 1},
+    {1, 16, 128, 0, 1},  {1, 16, 256, 0, 1},  {1, 32, 128, 0, 1},  {1, 32, 256, 0, 1},
+    {1, 16, 128, -1, 1}, {1, 16, 256, 96, 1}, {1, 16, 128, 0, 8},  {1, 16, 256, 0, 4}};
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 static_assert(kNumVariants == GBLLT_BATCH_VARIANTS, "gbllt.h states the number of batched kernel variants");
 
@@ -382,11 +415,14 @@ using BatchKernel = void (*)(BatchArgs<T>);
 template <typename T>
 BatchKernel<T> kernel_of(int v) {
   static const BatchKernel<T> table[] = {
-      batched_posv_kernel<T, 16, 128, 0>, batched_posv_kernel<T, 32, 128, 0>, batched_posv_kernel<T, 16, 256, 0>,
-      batched_posv_kernel<T, 32, 256, 0>, batched_posv_kernel<T, 16, 128, 0>, batched_posv_kernel<T, 16, 256, 0>,
-      batched_posv_kernel<T, 16, 128, 0>, batched_posv_kernel<T, 16, 256, 0>, batched_posv_kernel<T, 16, 128, 1>,
-      batched_posv_kernel<T, 16, 256, 1>, batched_posv_kernel<T, 32, 128, 1>, batched_posv_kernel<T, 32, 256, 1>,
-      batched_posv_kernel<T, 16, 128, 1>, batched_posv_kernel<T, 16, 256, 1>};
+      batched_posv_kernel<T, 16, 128, 0, 1>, batched_posv_kernel<T, 32, 128, 0, 1>,
+      batched_posv_kernel<T, 16, 256, 0, 1>, batched_posv_kernel<T, 32, 256, 0, 1>,
+      batched_posv_kernel<T, 16, 128, 0, 1>, batched_posv_kernel<T, 16, 256, 0, 1>,
+      batched_posv_kernel<T, 16, 128, 0, 1>, batched_posv_kernel<T, 16, 256, 0, 1>,
+      batched_posv_kernel<T, 16, 128, 1, 1>, batched_posv_kernel<T, 16, 256, 1, 1>,
+      batched_posv_kernel<T, 32, 128, 1, 1>, batched_posv_kernel<T, 32, 256, 1, 1>,
+      batched_posv_kernel<T, 16, 128, 1, 1>, batched_posv_kernel<T, 16, 256, 1, 1>,
+      batched_posv_kernel<T, 16, 128, 1, 8>, batched_posv_kernel<T, 16, 256, 1, 4>};
   static_assert(sizeof(table) / sizeof(table[0]) == kNumVariants, "one kernel per variant");
   return table[v];
 }
@@ -395,7 +431,7 @@ BatchKernel<T> kernel_of(int v) {
 template <typename T>
 size_t smem_bytes(int variant, int smem_max_n, int psld) {
   const Variant v = kVariants[variant];
-  size_t e = (size_t)kMaxBatchN + (v.algo == 1 ? blk_elems<T>(v.nbp, psld) : 0);
+  size_t e = (size_t)kMaxBatchN + 32 * kDgLd + (v.algo == 1 ? blk_elems<T>(v.nbp, psld) : 0);
   if (smem_max_n > 0) e += (size_t)(smem_max_n | 1) * smem_max_n;
   return e * sizeof(T);
 }

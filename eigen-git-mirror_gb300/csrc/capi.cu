@@ -19,6 +19,9 @@ void set_last_error(cudaError_t e, const char* what, const char* file, int line)
   char buf[512];
   snprintf(buf, sizeof buf, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
   g_last_error = buf;
+  // a non-sticky error stays reported to the next caller of cudaGetLastError (another library in
+  // the process) unless it is consumed here; it has been turned into our return code
+  cudaGetLastError();
 }
 
 void set_error_message(const char* msg) { g_last_error = msg; }

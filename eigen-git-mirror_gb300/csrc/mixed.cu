@@ -7,9 +7,10 @@
 //      and rounds the scaled lower triangle to an FP32 working matrix;
 //   2. factors it with the blocked right-looking algorithm of llt_inplace::blocked (LLT.h:338-368)
 //      in two levels: panels of width `panel` are factored in 64-column steps (diagonal blocks in
-//      FP64 arithmetic, panel TRSM and in-panel updates on FP32 cores), and the trailing SYRK of
-//      each panel -- almost all of the n^3/3 flops -- runs on tcgen05 tensor cores in TF32 or
-//      BF16 (optionally as three split-precision products) with FP32 accumulation;
+//      FP64 arithmetic, the panel TRSM on FP32 cores, its result split into tensor-core operands
+//      for the in-panel update on tcgen05), and the trailing SYRK of each panel
+//      -- almost all of the n^3/3 flops -- runs on tcgen05 tensor cores in TF32 or BF16 (optionally
+//      as split-precision products) with FP32 accumulation, one panel ahead on a second stream;
 //   3. refines in FP64: r = b - A x (FP64, reading only the stored triangle of A), solve with the
 //      FP32 factor, x += d, until ||r||_F / (||A||_F ||x||_F) <= tol (LAPACK dsposv-style
 //      refinement, with the FP64 GPU factorisation as fallback).
@@ -66,15 +67,17 @@ __global__ void diag_scale_kernel(const double* __restrict__ a, long long lda, l
   }
 }
 
-// K-major copies of the panel block Af(r0 .. r0+rows, c0 .. c0+bs) split into NP successive
-// roundings: part0 = round(v), part1 = round(v - part0), part2 = round(v - part0 - part1), stored at
-// out[r * ldk + p] for p < bs (zero beyond).  KIND 0 = bf16, 1 = tf32 (fp32 with 13 zero low bits).
+// Tensor-core operands are K-major copies of panel values split into NP successive roundings:
+// part0 = round(v), part1 = round(v - part0), part2 = round(v - part0 - part1).  KIND 0 = bf16,
+// 1 = tf32 (fp32 with 13 zero low bits, rounded to nearest, ties away).
 __device__ __forceinline__ float to_tf32(float x) {
   uint32_t r;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
   return __uint_as_float(r);
 }
 
+// K-major copies of the block Af(r0 .. r0+rows, c0 .. c0+bs) in NP parts, stored at
+// out[k][r * ldk + p] for p < bs (zero for bs <= p < ldk).
 template <int KIND>
 __global__ void __launch_bounds__(256) split_panel_kernel(const float* __restrict__ af, long long ldf, long long r0,
                                                           long long c0, long long rows, int bs, int np,
@@ -296,8 +299,13 @@ int split_parts(int prec) {
 // first) and the rest (side stream), so panel k+1's factorisation overlaps the large update.
 //   ev[0/1]: panel k's operands are split (side waits before its update)
 //   ev[2/3]: side update k finished (main waits before touching those columns / operand buffers)
-int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void* const* parts, void* const* parts2,
-                    int64_t ldk, DevStatus* st, int* d_err, cudaStream_t s, cudaStream_t side, cudaEvent_t* ev) {
+// In-panel updates (the remaining columns of the current panel by each 64-column step) also run
+// on tcgen05: the step's 64 columns are split into ipparts (K-major, 64 wide) and applied to the
+// lower part of the panel's remaining columns.  While the look-ahead update occupies the other
+// SMs, these launches are capped to the reserved SMs.
+int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int reserve_sms, void* const* parts,
+                    void* const* parts2, void* const* ipparts, int64_t ldk, DevStatus* st, int* d_err,
+                    cudaStream_t s, cudaStream_t side, cudaEvent_t* ev) {
   static const std::string ksplit = "split_panel";
   const int kind = (prec == GBLLT_PREC_BF16 || prec == GBLLT_PREC_BF16X3 || prec == GBLLT_PREC_BF16X6) ? kTcBF16
                                                                                                        : kTcTF32;
@@ -314,13 +322,27 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void
     for (int64_t j0 = k0; j0 < k0 + bs; j0 += kNB) {
       const int jb = (int)(k0 + bs - j0 < kNB ? k0 + bs - j0 : kNB);
       const int64_t below = n - j0 - jb;
+      const int64_t cols_left = k0 + bs - (j0 + jb);
       launch_potrf_diag<float, double>(af, ldf, j0, jb, st, s);
       launch_trsm_panel<float>(af, ldf, j0, jb, below, st, s);
-      const int64_t cols_left = k0 + bs - (j0 + jb);
       if (prec == GBLLT_PREC_FP32) {
         if (cols_left > 0 || rs > 0) launch_syrk_lower<float>(af, ldf, j0, jb, below, below, st, s);
       } else if (cols_left > 0) {
-        launch_syrk_lower<float>(af, ldf, j0, jb, below, cols_left, st, s);
+        {
+          ProfScope ps(ksplit.c_str(), s, 0.0, (double)below * jb * 4.0 + (double)below * kNB * (kind == kTcBF16 ? 2 : 4) * np);
+          dim3 grid((unsigned)ceil_div(below, TS), (unsigned)ceil_div(kNB, TS));
+          if (kind == kTcBF16)
+            split_panel_kernel<0><<<grid, 256, 0, s>>>(af, ldf, j0 + jb, j0, below, jb, np, ipparts[0], ipparts[1],
+                                                        ipparts[2], kNB);
+          else
+            split_panel_kernel<1><<<grid, 256, 0, s>>>(af, ldf, j0 + jb, j0, below, jb, np, ipparts[0], ipparts[1],
+                                                        ipparts[2], kNB);
+        }
+        TcOperand ip{{ipparts[0], ipparts[1], ipparts[2]}, below, kNB, kNB, 0};
+        const int cap = (lookahead && side_pending && reserve_sms > 0) ? reserve_sms : 0;
+        const int rc = tc_update(ip, ip, kind, nseg, code, af + (j0 + jb) * ldf + (j0 + jb), ldf, below, cols_left,
+                                 kTcLowerRect, d_err, s, 0, cap);
+        if (rc) return rc;
       }
     }
     if (rs > 0 && prec != GBLLT_PREC_FP32) {
@@ -340,7 +362,6 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void
       float* c0 = af + (k0 + bs) * ldf + (k0 + bs);
       int rc;
       if (!lookahead || rs <= panel) {
-        if (lookahead && side_pending) GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[2 + ((iter + 1) & 1)], 0));
         rc = tc_update(op, op, kind, nseg, code, c0, ldf, rs, rs, kTcLowerTri, d_err, s);
         if (rc) return rc;
       } else {
@@ -353,7 +374,7 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void
         GB_CUDA_TRY(cudaStreamWaitEvent(side, ev[iter & 1], 0));
         TcOperand op2{{pp[0], pp[1], pp[2]}, rs, bs, ldk, nb};
         rc = tc_update(op2, op2, kind, nseg, code, c0 + nb * ldf + nb, ldf, rs - nb, rs - nb, kTcLowerTri, d_err,
-                       side);
+                       side, reserve_sms > 0 ? reserve_sms : 0);
         if (rc) return rc;
         GB_CUDA_TRY(cudaEventRecord(ev[2 + (iter & 1)], side));
         side_pending = true;
@@ -367,6 +388,9 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, void
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
 }
+
+// SMs left to the panel factorisation while the look-ahead update of the previous panel runs.
+constexpr int kDefaultReserveSms = 24;
 
 int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o) {
   memset(o, 0, sizeof *o);
@@ -382,6 +406,7 @@ int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o) {
     if (!(o->tol > 0)) o->tol = 1e-14;
     if (o->panel <= 0) o->panel = 256;
   }
+  if (o->reserve_sms == 0) o->reserve_sms = kDefaultReserveSms;
   if (o->precision < GBLLT_PREC_FP32 || o->precision > GBLLT_PREC_BF16X6) return -1;
   if (o->panel % kNB != 0) return -1;
   return 0;
@@ -402,6 +427,7 @@ MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o, boo
                ? 2 : 4;
   L.bytes = (size_t)L.ldf * n * 4 + (size_t)n * 8 + (size_t)n * nrhs * (8 + 4) + (size_t)L.nparts * n * nrhs * 8 +
             (size_t)L.nsq * 8 + 64 + (size_t)split_parts(o.precision) * (lookahead ? 2 : 1) * n * L.ldk * L.es_k +
+            (size_t)split_parts(o.precision) * (n * kNB * L.es_k + 256) +
             sizeof(DevStatus) + 16 * 256 + potrs_ws_bytes(n, 8);
   L.fallback_bytes = (size_t)n * n * 8 + 256;
   return L;
@@ -437,6 +463,8 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   for (int i = 0; i < split_parts(o.precision); ++i) parts[i] = ar.take<char>((size_t)n * ldk * es_k);
   if (may_allocate)
     for (int i = 0; i < split_parts(o.precision); ++i) parts2[i] = ar.take<char>((size_t)n * ldk * es_k);
+  void* ipparts[3] = {nullptr, nullptr, nullptr};  // one 64-column step's operands for the in-panel update
+  for (int i = 0; i < split_parts(o.precision); ++i) ipparts[i] = ar.take<char>((size_t)n * kNB * es_k);
   DevStatus* st = ar.take<DevStatus>(1);
   int* d_err = (int*)&st->timeout;
   void* solve_ws = ar.take<char>(potrs_ws_bytes(n, 8));  // sized for the FP64 fallback solve too
@@ -504,7 +532,8 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     GB_CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     for (auto& e : lev) GB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
-  rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, parts, parts2, ldk, st, d_err, s, side, lev);
+  rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, o.reserve_sms, parts, parts2, ipparts, ldk, st, d_err, s,
+                       side, lev);
   if (side) {
     cudaStreamDestroy(side);  // work already issued on it completes; s waited on its last event
     for (auto& e : lev) cudaEventDestroy(e);

@@ -186,12 +186,9 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
 template <typename T, bool UP, bool BWD, int RCT>
 void launch_sweep_rc(int nb, const T* a, long long lda, long long n, T* b, long long ldb, int nrhs, const T* inv,
                      int* flags, int* counter, int* err, cudaStream_t s) {
-  static bool attr = false;
+  // set on every launch: cheap, and correct for every device and host thread
   const int smem = (int)sizeof(SweepSmem<T, RCT>);
-  if (!attr) {
-    cudaFuncSetAttribute(sweep_kernel<T, UP, BWD, RCT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr = true;
-  }
+  cudaFuncSetAttribute(sweep_kernel<T, UP, BWD, RCT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   dim3 grid((unsigned)nb, (unsigned)((nrhs + RCT - 1) / RCT));
   sweep_kernel<T, UP, BWD, RCT><<<grid, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, flags, counter, err);
 }

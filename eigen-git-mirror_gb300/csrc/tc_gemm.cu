@@ -26,6 +26,8 @@
 #include <cudaTypedefs.h>
 
 #include "internal.h"
+#include <mutex>
+
 #include "tc_gemm.h"
 
 namespace gbllt {
@@ -331,15 +333,64 @@ __global__ void __launch_bounds__(192, 1) tc_update_kernel(const __grid_constant
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  // initialised once, thread-safely (function-local static)
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     void* f = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
-  }
+      return (PFN_cuTensorMapEncodeTiled_v12000)f;
+    cudaGetLastError();
+    return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+  }();
   return fn;
+}
+
+// Per-device launch configuration of the update kernels, set up once per device under a lock
+// (calls may come from several host threads): SM count, the largest dynamic shared-memory request
+// (the per-block limit less the kernels' static shared memory), and the kernels' attribute raised
+// to it.
+struct TcDevCfg {
+  int sms = 0;
+  int smem_optin = 0;
+  int rc = 0;
+};
+
+const TcDevCfg& tc_cfg() {
+  constexpr int kMaxDev = 64;
+  static std::mutex mu;
+  static TcDevCfg cfg[kMaxDev];
+  static bool done[kMaxDev] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) {
+    cudaGetLastError();
+    dev = 0;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  TcDevCfg& c = cfg[dev];
+  if (!done[dev]) {
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, dev);
+    if (c.sms <= 0) c.sms = 1;
+    size_t stat = 0;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, tc_update_kernel<0>) == cudaSuccess) stat = fa.sharedSizeBytes;
+    if (cudaFuncGetAttributes(&fa, tc_update_kernel<1>) == cudaSuccess && fa.sharedSizeBytes > stat)
+      stat = fa.sharedSizeBytes;
+    cudaGetLastError();
+    c.smem_optin = optin - (int)stat - 64;
+    if (c.smem_optin < SMEM_BYTES) c.smem_optin = SMEM_BYTES;
+    if (cudaFuncSetAttribute(tc_update_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, c.smem_optin) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(tc_update_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, c.smem_optin) !=
+            cudaSuccess) {
+      set_last_error(cudaGetLastError(), "cudaFuncSetAttribute(tc_update_kernel)", __FILE__, __LINE__);
+      c.rc = GBLLT_ERR_CUDA;
+    }
+    done[dev] = true;
+  }
+  return c;
 }
 
 // 2-D map over a K-major operand: `rows` rows of `k` elements, `ld` elements apart.
@@ -360,7 +411,7 @@ int make_map(CUtensorMap* m, const void* base, int kind, int64_t rows, int64_t k
 }  // namespace
 
 int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32_t seg_code, float* c, int64_t ldc,
-              int64_t m, int64_t n, int lower, int* d_err, cudaStream_t s) {
+              int64_t m, int64_t n, int lower, int* d_err, cudaStream_t s, int reserve_sms, int max_ctas) {
   if (m <= 0 || n <= 0 || a.k <= 0) return GBLLT_SUCCESS;
   if (nseg < 1 || nseg > 8) return GBLLT_ERR_INTERNAL;
   const int es = kind == 0 ? 2 : 4;
@@ -389,15 +440,17 @@ int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32
   p.err = d_err;
   const int64_t nt = ceil_div(n, BN);
   p.tiles = lower == 1 ? (int64_t)p.mt * (p.mt + 1) / 2 : (int64_t)p.mt * nt;
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
+  const TcDevCfg& cfg = tc_cfg();
+  if (cfg.rc) return cfg.rc;
+  const int sms = cfg.sms;
+  int usable = sms;
+  size_t smem = SMEM_BYTES;
+  if (reserve_sms > 0 && reserve_sms < sms) {
+    usable = sms - reserve_sms;
+    smem = (size_t)cfg.smem_optin;  // one CTA fills its SM's shared memory: nothing else is placed beside it
   }
-  const unsigned grid = (unsigned)(p.tiles < sms ? p.tiles : sms);
-  static bool attr_set[2] = {false, false};
+  if (max_ctas > 0 && max_ctas < usable) usable = max_ctas;
+  const unsigned grid = (unsigned)(p.tiles < usable ? p.tiles : usable);
   static const std::string kname[2] = {"tc_update_bf16", "tc_update_tf32"};
   // algorithmic work: 2 k flops per updated entry and segment; operands read once, C read+written
   const double entries = lower == 1   ? (double)m * (m + 1) / 2.0
@@ -406,17 +459,9 @@ int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32
   ProfScope ps(kname[kind].c_str(), s, 2.0 * entries * a.k * nseg,
                ((double)(m + (lower == 1 ? 0 : n)) * a.k * nseg * es) + entries * 8.0);
   if (kind == 0) {
-    if (!attr_set[0]) {
-      GB_CUDA_TRY(cudaFuncSetAttribute(tc_update_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-      attr_set[0] = true;
-    }
-    tc_update_kernel<0><<<grid, 192, SMEM_BYTES, s>>>(maps, p);
+    tc_update_kernel<0><<<grid, 192, smem, s>>>(maps, p);
   } else {
-    if (!attr_set[1]) {
-      GB_CUDA_TRY(cudaFuncSetAttribute(tc_update_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-      attr_set[1] = true;
-    }
-    tc_update_kernel<1><<<grid, 192, SMEM_BYTES, s>>>(maps, p);
+    tc_update_kernel<1><<<grid, 192, smem, s>>>(maps, p);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;

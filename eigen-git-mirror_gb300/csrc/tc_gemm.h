@@ -24,9 +24,13 @@ constexpr int kTcTF32 = 1;
 // (code & 3) of A and part (code >> 2) of B, code = (seg_code >> 4s) & 15.  lower: 0 = the whole
 // rectangle; 1 = the lower triangle of a square C (SYRK); 2 = the rectangle, writing only entries
 // with row >= column.  d_err receives 1 if a bounded wait ran out.
+// reserve_sms > 0: the persistent grid leaves that many SMs out and each CTA claims the whole
+// shared memory of its SM, so kernels launched meanwhile on other streams (the panel factorisation
+// of the look-ahead schedule) run on the reserved SMs instead of sharing the update's SMs.
+// max_ctas > 0 caps the persistent grid (an update that must fit on the reserved SMs).
 constexpr int kTcFull = 0, kTcLowerTri = 1, kTcLowerRect = 2;
 int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32_t seg_code, float* c, int64_t ldc,
-              int64_t m, int64_t n, int lower, int* d_err, cudaStream_t s);
+              int64_t m, int64_t n, int lower, int* d_err, cudaStream_t s, int reserve_sms = 0, int max_ctas = 0);
 
 // Segment tables (parts: 0 = hi, 1 = mid/lo of a two-way split, 2 = lo of a three-way split),
 // ordered smallest terms first.

@@ -87,7 +87,7 @@ PREC = {"fp32": 0, "tf32": 1, "tf32x3": 2, "bf16": 3, "bf16x3": 4, "bf16x6": 5}
 
 class MixedOpts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("max_steps", ctypes.c_int), ("tol", ctypes.c_double),
-                ("fallback_fp64", ctypes.c_int), ("panel", ctypes.c_int)]
+                ("fallback_fp64", ctypes.c_int), ("panel", ctypes.c_int), ("reserve_sms", ctypes.c_int)]
 
 
 class MixedReport(ctypes.Structure):
@@ -104,8 +104,8 @@ class MixedReport(ctypes.Structure):
 
 
 def mixed_opts(precision: str = "tf32x3", max_steps: int = 10, tol: float = 1e-14, fallback: bool = True,
-               panel: int = 256) -> MixedOpts:
-    return MixedOpts(PREC[precision], max_steps, tol, 1 if fallback else 0, panel)
+               panel: int = 256, reserve_sms: int = 0) -> MixedOpts:
+    return MixedOpts(PREC[precision], max_steps, tol, 1 if fallback else 0, panel, reserve_sms)
 
 
 class GblltError(RuntimeError):
@@ -135,7 +135,7 @@ def lib() -> ctypes.CDLL:
     return _lib
 
 
-BATCH_VARIANTS = 14  # GBLLT_BATCH_VARIANTS of include/gbllt.h
+BATCH_VARIANTS = 16  # GBLLT_BATCH_VARIANTS of include/gbllt.h
 
 LAPACK_PATH = PKG_DIR / "lib" / "libgbllt_lapack.so"
 _lapack = None

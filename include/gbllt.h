@@ -115,6 +115,8 @@ typedef struct {
   double tol;        /* target normwise backward error; <= 0 -> 1e-14 */
   int fallback_fp64; /* when refinement fails, solve with the plain FP64 GPU factorisation */
   int panel;         /* outer panel width, a multiple of 64; <= 0 -> 256 */
+  int reserve_sms;   /* SMs left to the panel factorisation while the look-ahead update runs on the
+                        others: 0 -> library default, < 0 -> none (the update may use every SM) */
 } gbllt_mixed_opts;
 
 typedef struct {
@@ -174,7 +176,7 @@ GBLLT_API int gbllt_batch_plan_layout(const gbllt_batch_plan* plan, int64_t* aof
                                       int64_t* b_elems);
 /* Number of batched kernel variants: algorithm (column at a time / panel-blocked) x panel width x
  * threads per CTA x the largest order staged in shared memory. */
-#define GBLLT_BATCH_VARIANTS 14
+#define GBLLT_BATCH_VARIANTS 16
 /* Autotuner: times each kernel variant on synthetic SPD systems of the plan's sizes and keeps the
  * fastest; with cache_path, a previous choice for the same sizes is read from / a new one written
  * to that JSON file.  Returns the variant index (>= 0). */

@@ -58,10 +58,10 @@ def test_batched_host_matches_oracle(oracle, gbllt, dtype):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-@pytest.mark.parametrize("variant", list(range(14)))
+@pytest.mark.parametrize("variant", list(range(16)))
 def test_batched_every_variant_graph_replay(oracle, gbllt, variant, dtype):
     torch = pytest.importorskip("torch")
-    assert gbllt.BATCH_VARIANTS == 14
+    assert gbllt.BATCH_VARIANTS == 16
     sizes = list(oracle.batch_sizes(120, seed=22, lo=4, hi=256)) + [1, 2, 4, 5, 16, 17, 33, 170, 255, 256]
     _, a, b = _batch(oracle, sizes, dtype, seed=300)
     plan = gbllt.BatchPlan(sizes, dtype)
@@ -81,7 +81,7 @@ def test_batched_every_variant_graph_replay(oracle, gbllt, variant, dtype):
     _check(oracle, sizes, a, b, da.cpu().numpy(), db.cpu().numpy(), di.cpu().numpy(), dtype)
 
 
-@pytest.mark.parametrize("variant", [3, 7, 8, 11, 12])
+@pytest.mark.parametrize("variant", [3, 7, 8, 11, 12, 14])
 def test_batched_failing_systems(oracle, gbllt, variant):
     sizes = [10, 70, 200, 40]
     mats, _, _ = _batch(oracle, sizes, np.float64, seed=500)

@@ -159,3 +159,24 @@ def test_gpu_full_size_config2_backward_error(oracle, gbllt):
     cols = [0, 17, 63]
     be = oracle.backward_error(a, np.asfortranarray(x[:, cols]), np.asfortranarray(b[:, cols]))
     assert be <= 1e-14
+
+
+def test_gpu_diagonal_pivots_are_square_roots(gbllt):
+    """The FP64 diagonal-block kernel forms each pivot's reciprocal square root by Newton-Raphson
+    from an FP32 estimate (library sqrt outside the FP32 range).  On a diagonal matrix the factor is
+    the square root of each entry: it must match numpy's correctly rounded sqrt within 4 ulp, over
+    magnitudes 1e-300 .. 1e300 (both code paths), and the solve must divide by them."""
+    n = 192
+    e = np.linspace(-300, 300, n)
+    d = 10.0 ** e
+    d[::7] *= 1.0 + 1e-9 * np.arange(len(d[::7]))  # mantissas other than powers of ten
+    a = np.asfortranarray(np.diag(d))
+    f = np.array(a, order="F", copy=True)
+    assert gbllt.potrf(f, "L") == 0
+    want = np.sqrt(d)
+    got = np.diag(f)
+    assert np.all(np.abs(got - want) <= 4 * np.spacing(want))
+    assert np.all(np.tril(f, -1) == 0)
+    x = np.asfortranarray(np.ones((n, 1)))
+    gbllt.potrs(f, x, "L")
+    assert np.allclose(x[:, 0] * d, 1.0, rtol=1e-14, atol=0)

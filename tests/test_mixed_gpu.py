@@ -109,3 +109,43 @@ def test_mixed_not_positive_definite(oracle, gbllt):
     b = np.asfortranarray(oracle.normal(5, n).reshape(n, 1))
     rc, rep, x = _dev_solve(gbllt, a, b, gbllt.mixed_opts("tf32x3", 10, 1e-14, fallback=True))
     assert rc == gbllt.SUCCESS and rep["info"] == 124 and rep["used_fallback"]
+
+
+def test_mixed_concurrent_host_threads(oracle, gbllt):
+    """Mixed solves issued from 4 host threads on 4 streams at once (the look-ahead updates of the
+    different solves then compete for SMs) give the same solutions as the same solves run one after
+    another: the entry points are thread-safe and every kernel is deterministic."""
+    torch = pytest.importorskip("torch")
+    from concurrent.futures import ThreadPoolExecutor
+
+    n, k, nsol = 1100, 3, 8
+    mats = [np.asfortranarray(oracle.gen_householder(n, 1e4, v_seed0=60 + i)) for i in range(nsol)]
+    rhs = [np.asfortranarray(oracle.normal(80 + i, n * k).reshape(n, k, order="F")) for i in range(nsol)]
+    A = [torch.from_numpy(np.ascontiguousarray(m.T)).cuda() for m in mats]
+    B = [torch.from_numpy(np.ascontiguousarray(r.T)).cuda() for r in rhs]
+    opts = gbllt.mixed_opts("bf16x6", 10, 1e-14, False)
+
+    def solve(i, stream):
+        X = torch.zeros_like(B[i])
+        rc, rep = gbllt.posv_mixed_dev(A[i], n, n, B[i], n, X, n, k, opts, "L", stream.cuda_stream,
+                                       raise_on_error=False)
+        stream.synchronize()
+        return rc, rep, X
+
+    serial = [solve(i, torch.cuda.current_stream()) for i in range(nsol)]
+    streams = [torch.cuda.Stream() for _ in range(4)]
+
+    def chain(t):
+        torch.cuda.set_device(0)
+        return [(i, solve(i, streams[t])) for i in range(t, nsol, 4)]
+
+    with ThreadPoolExecutor(4) as pool:
+        par = dict(kv for c in pool.map(chain, range(4)) for kv in c)
+    for i in range(nsol):
+        rc_s, rep_s, x_s = serial[i]
+        rc_p, rep_p, x_p = par[i]
+        assert rc_s == 0 and rc_p == 0, (rc_s, rc_p)
+        assert rep_p["steps"] == rep_s["steps"]
+        assert torch.equal(x_p, x_s)
+        x = np.asfortranarray(x_p.cpu().numpy().T)
+        assert oracle.backward_error(mats[i], x, rhs[i]) <= 1e-14
