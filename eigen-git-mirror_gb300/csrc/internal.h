@@ -91,6 +91,11 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
 int posv_mixed_dev(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
                    double* x, int64_t ldx, const gbllt_mixed_opts* opts, gbllt_mixed_report* rep, cudaStream_t s);
 
+// Rank-1 update / downdate of the factor at l (device), L L^T + sigma v v^T; *d_info (device)
+// receives 0, the failing column + 1 of a downdate, or GBLLT_ERR_TIMEOUT.
+template <typename T>
+int rank_update_dev(bool upper, int64_t n, T* l, int64_t ldl, const T* v, T sigma, int64_t* d_info, cudaStream_t s);
+
 // Validates (uplo, n, lda) the way dpotrf_ does (lapack/cholesky.cpp:17-19); returns 0 or -argpos.
 int check_uplo(char uplo);
 

@@ -64,6 +64,10 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_sposv_batched": (_int, [_vp, _vp, _vp, _vp]),
     "gbllt_dpotrf_adjoint_dev": (_int, [_i64, _vp, _i64, _vp, _i64, _vp]),
     "gbllt_dpotrs_adjoint_dev": (_int, [_i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp]),
+    "gbllt_drank_update": (_int, [_int, _ch, _i64, _vp, _i64, _vp, ctypes.c_double, _i64p]),
+    "gbllt_srank_update": (_int, [_int, _ch, _i64, _vp, _i64, _vp, ctypes.c_float, _i64p]),
+    "gbllt_drank_update_dev": (_int, [_ch, _i64, _vp, _i64, _vp, ctypes.c_double, _vp, _vp]),
+    "gbllt_srank_update_dev": (_int, [_ch, _i64, _vp, _i64, _vp, ctypes.c_float, _vp, _vp]),
     "gbllt_dlansy_l1_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
     "gbllt_slansy_l1_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
     "gbllt_dpocon_dev": (_int, [_ch, _i64, _vp, _i64, ctypes.c_double, _dp, _vp]),
@@ -357,6 +361,25 @@ class BatchPlan:
 
 def profile_enable(on: bool = True) -> None:
     check("gbllt_profile_enable", lib().gbllt_profile_enable(1 if on else 0))
+
+
+def rank_update(l: np.ndarray, v: np.ndarray, sigma: float, uplo: str = "L") -> int:
+    """In place on a Fortran-order factor: the factor of A + sigma v v^T; returns the LAPACK-style info."""
+    dbl = l.dtype == np.float64
+    fn = lib().gbllt_drank_update if dbl else lib().gbllt_srank_update
+    n = l.shape[0]
+    vv = np.ascontiguousarray(v, dtype=l.dtype)
+    info = ctypes.c_int64(0)
+    check("gbllt_?rank_update", fn(COL_MAJOR, uplo.encode(), n, l.ctypes.data if n else None, max(n, 1),
+                                    vv.ctypes.data if n else None, sigma, ctypes.byref(info)))
+    return info.value
+
+
+def rank_update_dev(d_l, n: int, ldl: int, d_v, sigma: float, d_info, uplo: str = "L", stream=None,
+                    dtype=np.float64) -> None:
+    """Device-pointer form (torch tensors); the info is written to the device scalar d_info."""
+    fn = lib().gbllt_drank_update_dev if dtype == np.float64 else lib().gbllt_srank_update_dev
+    check("gbllt_?rank_update_dev", fn(uplo.encode(), n, _ptr(d_l), ldl, _ptr(d_v), sigma, _ptr(d_info), stream))
 
 
 def pocon(l: np.ndarray, anorm: float, uplo: str = "L") -> float:

@@ -9,8 +9,9 @@
 // What is routed to the GPU (through the C ABI of gbllt.h):
 //   - the factorisation: full specialisations of internal::llt_inplace<T, Lower|Upper> for
 //     T = double, float, whose blocked() calls gbllt_?potrf -- the same boundary and the same
-//     info mapping (0 -> -1, i > 0 -> i - 1) as LLT_LAPACKE.h:42-93.  rankUpdate stays on the CPU
-//     (llt_rank_update_lower, LLT.h:239-307), exactly as in LLT_LAPACKE.h:71-73;
+//     info mapping (0 -> -1, i > 0 -> i - 1) as LLT_LAPACKE.h:42-93.  Their rankUpdate (which
+//     LLT_LAPACKE.h:71-73 leaves to llt_rank_update_lower on the CPU) calls gbllt_?rank_update, the
+//     same algorithm (LLT.h:238-307) on the GPU;
 //   - the solve: partial specialisations of internal::Assignment<Dst, Solve<LLT<...>, Rhs>, ...>
 //     (dst = llt.solve(b), Solve.h:137-149) and internal::evaluator<Solve<LLT<...>, Rhs>>
 //     (dst += / -= / noalias, Solve.h:114-131) call gbllt_?potrs on the current host factor
@@ -19,7 +20,7 @@
 //     dynamic-size LLTs (called by LLT::rcond, LLT.h:166-171) call gbllt_?pocon, which runs
 //     Eigen's estimator (ConditionEstimator.h:56-171) with the factor resident on the device.
 // What stays on Eigen's CPU code: LLT::solveInPlace (LLT.h:514-522) calls the triangular views
-// directly and bypasses Solve<>; rankUpdate; the L1 norm that LLT::compute keeps for rcond
+// directly and bypasses Solve<>; the L1 norm that LLT::compute keeps for rcond
 // (LLT.h:443-453; gbllt_?lansy_l1_dev is its device form for callers outside Eigen).
 //
 // Errors: a failing library call (no usable GPU, CUDA error) trips eigen_assert; with assertions
@@ -53,7 +54,7 @@ inline bool gb300_check(const char* fn, int rc) {
 template <typename Scalar>
 struct gb300_llt;
 
-#define EIGEN_GB300_LLT(EIGTYPE, POTRF, POTRS)                                                          \
+#define EIGEN_GB300_LLT(EIGTYPE, POTRF, POTRS, RANKUPD)                                                 \
   template <>                                                                                          \
   struct gb300_llt<EIGTYPE> {                                                                          \
     template <typename MatrixType>                                                                     \
@@ -78,6 +79,20 @@ struct gb300_llt;
       if (!gb300_check(#POTRS, rc))                                                                    \
         for (int64_t i = 0; i < n * k; ++i) x[i] = std::numeric_limits<EIGTYPE>::quiet_NaN();          \
     }                                                                                                  \
+    /* llt_rank_update_lower (LLT.h:238-307) on the `uplo` triangle: -1 or the failing column */     \
+    template <typename MatrixType, typename VectorType>                                                \
+    static Index rank_update(MatrixType& m, const VectorType& vec, EIGTYPE sigma, char uplo) {         \
+      eigen_assert(m.rows() == m.cols() && vec.size() == m.rows());                                   \
+      const int64_t n = (int64_t)m.rows();                                                             \
+      if (n == 0) return -1;                                                                           \
+      const int layout = (MatrixType::Flags & RowMajorBit) ? GBLLT_ROW_MAJOR : GBLLT_COL_MAJOR;       \
+      const Matrix<EIGTYPE, Dynamic, 1> v = vec;                                                       \
+      int64_t info = 0;                                                                                \
+      const int rc = RANKUPD(layout, uplo, n, &m.coeffRef(0, 0), (int64_t)m.outerStride(), v.data(),   \
+                             sigma, &info);                                                            \
+      if (!gb300_check(#RANKUPD, rc)) return 0;                                                        \
+      return info == 0 ? -1 : (Index)(info - 1);                                                       \
+    }                                                                                                  \
   };                                                                                                   \
   template <>                                                                                          \
   struct llt_inplace<EIGTYPE, Lower> {                                                                 \
@@ -88,7 +103,7 @@ struct gb300_llt;
     template <typename MatrixType, typename VectorType>                                                \
     static Index rankUpdate(MatrixType& mat, const VectorType& vec,                                    \
                             const typename MatrixType::RealScalar& sigma) {                            \
-      return Eigen::internal::llt_rank_update_lower(mat, vec, sigma);                                  \
+      return gb300_llt<EIGTYPE>::rank_update(mat, vec, sigma, 'L');                                    \
     }                                                                                                  \
   };                                                                                                   \
   template <>                                                                                          \
@@ -100,13 +115,12 @@ struct gb300_llt;
     template <typename MatrixType, typename VectorType>                                                \
     static Index rankUpdate(MatrixType& mat, const VectorType& vec,                                    \
                             const typename MatrixType::RealScalar& sigma) {                            \
-      Transpose<MatrixType> matt(mat);                                                                 \
-      return llt_inplace<EIGTYPE, Lower>::rankUpdate(matt, vec.conjugate(), sigma);                    \
+      return gb300_llt<EIGTYPE>::rank_update(mat, vec, sigma, 'U');                                    \
     }                                                                                                  \
   };
 
-EIGEN_GB300_LLT(double, gbllt_dpotrf, gbllt_dpotrs)
-EIGEN_GB300_LLT(float, gbllt_spotrf, gbllt_spotrs)
+EIGEN_GB300_LLT(double, gbllt_dpotrf, gbllt_dpotrs, gbllt_drank_update)
+EIGEN_GB300_LLT(float, gbllt_spotrf, gbllt_spotrs, gbllt_srank_update)
 
 #undef EIGEN_GB300_LLT
 

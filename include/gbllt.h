@@ -210,6 +210,22 @@ GBLLT_API int gbllt_dpotrs_adjoint_dev(int64_t n, int64_t nrhs, const double* d_
                                        int64_t ldx, const double* d_xbar, int64_t ldxb, double* d_bbar, int64_t ldbb,
                                        double* d_abar, int64_t ldab, void* stream);
 
+/* ---- Rank-1 update / downdate (LLT::rankUpdate, Eigen/src/Cholesky/LLT.h:469-478) ----------
+ * Given the factor of A in the `uplo` triangle, overwrite it with the factor of A + sigma v v^T:
+ * llt_rank_update_lower (LLT.h:238-307) -- Givens rotations for sigma > 0, the beta recurrence for
+ * sigma <= 0.  info = 0, or k + 1 when a downdate leaves A + sigma v v^T not positive definite at
+ * column k (the factor's contents are then unspecified; LLT reports NumericalIssue). */
+GBLLT_API int gbllt_drank_update(int layout, char uplo, int64_t n, double* l, int64_t ldl, const double* v,
+                                 double sigma, int64_t* info);
+GBLLT_API int gbllt_srank_update(int layout, char uplo, int64_t n, float* l, int64_t ldl, const float* v,
+                                 float sigma, int64_t* info);
+/* Device pointers (column-major), stream-ordered; *d_info is device memory and may also receive
+ * GBLLT_ERR_TIMEOUT if a bounded device-side wait ran out. */
+GBLLT_API int gbllt_drank_update_dev(char uplo, int64_t n, double* d_l, int64_t ldl, const double* d_v,
+                                     double sigma, int64_t* d_info, void* stream);
+GBLLT_API int gbllt_srank_update_dev(char uplo, int64_t n, float* d_l, int64_t ldl, const float* d_v, float sigma,
+                                     int64_t* d_info, void* stream);
+
 /* ---- Condition estimate (LLT::rcond, Eigen/src/Cholesky/LLT.h:166-171) ---------------------- */
 
 /* 1-norm (max absolute column sum) of the symmetric n x n matrix stored in the `uplo` triangle of

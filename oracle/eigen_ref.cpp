@@ -52,7 +52,29 @@ static double rcond(int64_t n, const T* a, int64_t lda) {
   return (double)llt.rcond();
 }
 
+// LLT<Matrix,UpLo>::rankUpdate(v, sigma) (LLT.h:469-478) on the factor of A; the updated factor
+// is written back to a (its UpLo triangle), returns 0 on success, 1 when Eigen reports
+// NumericalIssue.
+template <typename T, int UpLo>
+static int64_t rank_update(int64_t n, T* a, int64_t lda, const T* v, T sigma) {
+  typedef Matrix<T, Dynamic, Dynamic> M;
+  typedef Matrix<T, Dynamic, 1> V;
+  Map<M, 0, OuterStride<>> A(a, n, n, OuterStride<>(lda));
+  LLT<M, UpLo> llt(A);
+  if (llt.info() != Success) return 2;
+  llt.rankUpdate(Map<const V>(v, n), sigma);
+  A.template triangularView<UpLo>() = llt.matrixLLT().template triangularView<UpLo>();
+  return llt.info() == Success ? 0 : 1;
+}
+
 extern "C" {
+
+int64_t ref_drank_update(char uplo, int64_t n, double* a, int64_t lda, const double* v, double sigma) {
+  return uplo == 'U' ? rank_update<double, Upper>(n, a, lda, v, sigma) : rank_update<double, Lower>(n, a, lda, v, sigma);
+}
+int64_t ref_srank_update(char uplo, int64_t n, float* a, int64_t lda, const float* v, float sigma) {
+  return uplo == 'U' ? rank_update<float, Upper>(n, a, lda, v, sigma) : rank_update<float, Lower>(n, a, lda, v, sigma);
+}
 
 double ref_drcond(char uplo, int64_t n, const double* a, int64_t lda) {
   return uplo == 'U' ? rcond<double, Upper>(n, a, lda) : rcond<double, Lower>(n, a, lda);

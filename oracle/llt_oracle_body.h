@@ -238,7 +238,6 @@ double P(backward_error)(char uplo, int64_t n, int64_t nrhs, const T* a, int64_t
   return sqrt(nr) / (sqrt(na) * sqrt(nx));
 }
 
-#undef EL
 
 /* 1-norm of the symmetric matrix of which only the `uplo` triangle of the column-major a is read:
  * the m_l1_norm loop of LLT::compute (Eigen/src/Cholesky/LLT.h:443-453), column by column, the
@@ -317,3 +316,83 @@ double P(rcond)(char uplo, int64_t n, const T* l, int64_t ldl, double anorm) {
   free(old_sign);
   return est == (T)0 ? 0.0 : ((double)((T)1 / est) / anorm);
 }
+
+/* Rank-1 update / downdate of a Cholesky factor, A + sigma v v^T = L' L'^T: the restatement of
+ * llt_rank_update_lower (Eigen/src/Cholesky/LLT.h:238-307) on the `uplo` triangle of the
+ * column-major l (Upper runs the same steps on the transpose, LLT.h:394-398; real scalars, so the
+ * vector's conjugate is itself).  sigma > 0: Givens rotations, with JacobiRotation::makeGivens
+ * (Eigen/src/Jacobi/Jacobi.h:231-267) and the plane rotation of Jacobi.h:327-335; sigma <= 0: the
+ * beta recurrence, which returns the column j at which x <= 0 (the factor is then partly updated).
+ * Returns -1 on success, like llt_rank_update_lower. */
+int64_t P(rank_update)(char uplo, int64_t n, T* l, int64_t ldl, const T* v, T sigma) {
+  const int up = (uplo == 'U' || uplo == 'u');
+  const int64_t rs = up ? ldl : 1, cs = up ? 1 : ldl;  /* EL(l, i, j) = L(i, j) of the lower view */
+  T* temp = (T*)malloc(sizeof(T) * (n > 0 ? n : 1));
+  int64_t ret = -1;
+  if (sigma > 0) {
+    const T ss = (T)sqrt((double)sigma);
+    for (int64_t i = 0; i < n; ++i) temp[i] = ss * v[i];
+    for (int64_t i = 0; i < n; ++i) {
+      const T p = EL(l, i, i), q = -temp[i];
+      T c, s, r;
+      if (q == 0) {
+        c = p < 0 ? (T)-1 : (T)1;
+        s = 0;
+        r = (T)fabs((double)p);
+      } else if (p == 0) {
+        c = 0;
+        s = q < 0 ? (T)1 : (T)-1;
+        r = (T)fabs((double)q);
+      } else if (fabs((double)p) > fabs((double)q)) {
+        const T t = q / p;
+        T u = (T)sqrt((double)((T)1 + t * t));
+        if (p < 0) u = -u;
+        c = (T)1 / u;
+        s = -t * c;
+        r = p * u;
+      } else {
+        const T t = p / q;
+        T u = (T)sqrt((double)((T)1 + t * t));
+        if (q < 0) u = -u;
+        s = -(T)1 / u;
+        c = -t * s;
+        r = q * u;
+      }
+      EL(l, i, i) = r;
+      for (int64_t k = i + 1; k < n; ++k) {
+        const T xk = EL(l, k, i), yk = temp[k];
+        EL(l, k, i) = c * xk + s * yk;
+        temp[k] = -s * xk + c * yk;
+      }
+    }
+  } else {
+    for (int64_t i = 0; i < n; ++i) temp[i] = v[i];
+    T beta = 1;
+    for (int64_t j = 0; j < n; ++j) {
+      const T Ljj = EL(l, j, j);
+      const T dj = Ljj * Ljj;
+      const T wj = temp[j];
+      const T swj2 = sigma * wj * wj;
+      const T gamma = dj * beta + swj2;
+      const T x = dj + swj2 / beta;
+      if (x <= 0) {
+        ret = j;
+        break;
+      }
+      const T nLjj = (T)sqrt((double)x);
+      EL(l, j, j) = nLjj;
+      beta += swj2 / dj;
+      const T f = wj / Ljj;
+      const T a = nLjj / Ljj;
+      const T b = nLjj * sigma * wj / gamma;
+      for (int64_t k = j + 1; k < n; ++k) {
+        temp[k] -= f * EL(l, k, j);
+        if (gamma != 0) EL(l, k, j) = a * EL(l, k, j) + b * temp[k];
+      }
+    }
+  }
+  free(temp);
+  return ret;
+}
+
+#undef EL

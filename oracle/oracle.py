@@ -31,6 +31,8 @@ _SIGS = {
     "oracle_dsym_l1_norm": (_dbl, [_ch, _i64, _vp, _i64]),
     "oracle_ssym_l1_norm": (ctypes.c_float, [_ch, _i64, _vp, _i64]),
     "oracle_drcond": (_dbl, [_ch, _i64, _vp, _i64, _dbl]),
+    "oracle_drank_update": (_i64, [_ch, _i64, _vp, _i64, _vp, _dbl]),
+    "oracle_srank_update": (_i64, [_ch, _i64, _vp, _i64, _vp, ctypes.c_float]),
     "oracle_srcond": (_dbl, [_ch, _i64, _vp, _i64, _dbl]),
     "oracle_philox4x32_10": (None, [_vp, _vp, _vp]),
     "oracle_normal": (_dbl, [_u64, _u64]),
@@ -106,6 +108,10 @@ def eigen_ref():
         for nm in ("ref_drcond", "ref_srcond"):
             getattr(R, nm).restype = _dbl
             getattr(R, nm).argtypes = [_ch, _i64, _vp, _i64]
+        R.ref_drank_update.restype = _i64
+        R.ref_drank_update.argtypes = [_ch, _i64, _vp, _i64, _vp, _dbl]
+        R.ref_srank_update.restype = _i64
+        R.ref_srank_update.argtypes = [_ch, _i64, _vp, _i64, _vp, ctypes.c_float]
         _ref = R
     return _ref
 
@@ -210,6 +216,15 @@ def rcond(l: np.ndarray, anorm: float, uplo: str = "L") -> float:
     n = l.shape[0]
     fn = lib().oracle_drcond if l.dtype == np.float64 else lib().oracle_srcond
     return float(fn(uplo.encode(), n, _p(l) if n else None, max(1, n), float(anorm)))
+
+
+def rank_update(l: np.ndarray, v: np.ndarray, sigma: float, uplo: str = "L") -> int:
+    """In place: the factor of A + sigma v v^T from the factor l of A (LLT.h:238-307); returns the
+    column where a downdate fails, or -1."""
+    n = l.shape[0]
+    fn = lib().oracle_drank_update if l.dtype == np.float64 else lib().oracle_srank_update
+    vv = np.ascontiguousarray(v, dtype=l.dtype)
+    return int(fn(uplo.encode(), n, _p(l) if n else None, max(1, n), _p(vv) if n else None, sigma))
 
 
 def backward_error(a: np.ndarray, x: np.ndarray, b: np.ndarray, uplo: str = "L") -> float:

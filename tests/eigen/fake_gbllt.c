@@ -13,10 +13,12 @@ int oracle_dpotrf(char uplo, int64_t n, double* a, int64_t lda, int64_t* info);
 int oracle_spotrf(char uplo, int64_t n, float* a, int64_t lda, int64_t* info);
 int oracle_dpotrs(char uplo, int64_t n, int64_t nrhs, const double* a, int64_t lda, double* b, int64_t ldb);
 int oracle_spotrs(char uplo, int64_t n, int64_t nrhs, const float* a, int64_t lda, float* b, int64_t ldb);
+int64_t oracle_drank_update(char uplo, int64_t n, double* l, int64_t ldl, const double* v, double sigma);
+int64_t oracle_srank_update(char uplo, int64_t n, float* l, int64_t ldl, const float* v, float sigma);
 double oracle_drcond(char uplo, int64_t n, const double* l, int64_t ldl, double anorm);
 double oracle_srcond(char uplo, int64_t n, const float* l, int64_t ldl, double anorm);
 
-long fake_calls[6];
+long fake_calls[8];
 
 static char eff_uplo(int layout, char uplo) {
   const int up = uplo == 'U' || uplo == 'u';
@@ -54,8 +56,26 @@ int gbllt_spocon(int layout, char uplo, int64_t n, const float* l, int64_t ldl, 
   return 0;
 }
 
+int gbllt_drank_update(int layout, char uplo, int64_t n, double* l, int64_t ldl, const double* v, double sigma,
+                       int64_t* info) {
+  ++fake_calls[6];
+  const int64_t r = oracle_drank_update(eff_uplo(layout, uplo), n, l, ldl, v, sigma);
+  *info = r < 0 ? 0 : r + 1;
+  return 0;
+}
+int gbllt_srank_update(int layout, char uplo, int64_t n, float* l, int64_t ldl, const float* v, float sigma,
+                       int64_t* info) {
+  ++fake_calls[7];
+  const int64_t r = oracle_srank_update(eff_uplo(layout, uplo), n, l, ldl, v, sigma);
+  *info = r < 0 ? 0 : r + 1;
+  return 0;
+}
+
 /* Prints the call counts at exit so that the test can check the backend was used. */
 __attribute__((destructor)) static void fake_report(void) {
-  fprintf(stderr, "fake_gbllt calls: dpotrf=%ld spotrf=%ld dpotrs=%ld spotrs=%ld dpocon=%ld spocon=%ld\n",
-          fake_calls[0], fake_calls[1], fake_calls[2], fake_calls[3], fake_calls[4], fake_calls[5]);
+  fprintf(stderr,
+          "fake_gbllt calls: dpotrf=%ld spotrf=%ld dpotrs=%ld spotrs=%ld dpocon=%ld spocon=%ld drankupd=%ld "
+          "srankupd=%ld\n",
+          fake_calls[0], fake_calls[1], fake_calls[2], fake_calls[3], fake_calls[4], fake_calls[5], fake_calls[6],
+          fake_calls[7]);
 }
