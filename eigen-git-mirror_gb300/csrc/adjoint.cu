@@ -258,7 +258,7 @@ int potrf_adjoint_dev(int64_t n, const double* L, int64_t ldl, double* M, int64_
   static const std::string kt = "adjoint_trsm_f64", kd = "adjoint_diag_f64";
   // split-K partials of the long, narrow products (stream-ordered, from the pool)
   double* part = nullptr;
-  if (cudaMallocAsync((void**)&part, (size_t)kSplitElems * sizeof(double), s) != cudaSuccess) {
+  if (dev_malloc_async((void**)&part, (size_t)kSplitElems * sizeof(double), s) != cudaSuccess) {
     cudaGetLastError();
     set_error_message("gbllt_dpotrf_adjoint_dev: cudaMallocAsync of the split-K scratch failed");
     return GBLLT_ERR_ALLOC;

@@ -9,11 +9,16 @@
 // tail.  A system whose matrix fits in shared memory is staged there (lower triangle, odd leading
 // dimension), otherwise it is worked on in place in global memory (L2-resident at these sizes).
 // Per system, the blocked right-looking algorithm of llt_inplace::blocked (LLT.h:338-368) runs
-// with NBP-wide panels: the panel is factored one column at a time by all threads (the role of
-// unblocked(), LLT.h:312-336, with the same `x <= 0` pivot test; the column is scaled by the
-// reciprocal of its pivot), then all threads apply the trailing update with 4 x 4 register tiles.  The solve is blocked the same way: warp 0 solves each diagonal
-// triangle, all warps apply the off-diagonal blocks (GEMV forward, warp-shuffle dot products
-// backward).
+// with NBP-wide panels, in one of two forms the autotuner chooses between:
+//   algo 0: the panel is factored one column at a time by all threads (the role of unblocked(),
+//           LLT.h:312-336, with the same `x <= 0` pivot test), then all threads apply the trailing
+//           update with 4 x 4 register tiles;
+//   algo 1 (factor_blk): warp 0 factors the panel's diagonal block, each thread solves whole rows
+//           below it, and the trailing update reads the panel from a shared-memory copy (lower
+//           tiles only, column-major tile order).
+// The solve is blocked by 32 rows in both: each diagonal block is staged in shared memory and
+// substituted by warp 0 with shuffles, all warps apply the off-diagonal blocks (GEMV forward,
+// warp-shuffle dot products backward).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -576,7 +581,7 @@ int batch_plan_create(int64_t count, const int64_t* n, int elem, BatchPlan** out
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return p->h_n[x] > p->h_n[y]; });
   cudaGetDevice(&p->device);
   const size_t bytes = (size_t)count * (4 + 4 + 8 + 8) + 256 * 4;
-  if (cudaMalloc(&p->dev, bytes) != cudaSuccess) {
+  if (dev_malloc((void**)&p->dev, bytes) != cudaSuccess) {
     cudaGetLastError();
     delete p;
     return GBLLT_ERR_ALLOC;
@@ -616,7 +621,7 @@ int batch_plan_tune(BatchPlan* p, cudaStream_t s) {
   const size_t es = p->elem;
   void* buf = nullptr;
   const size_t bytes = (size_t)p->a_elems * es + (size_t)p->b_elems * es + (size_t)p->count * 8 + 512;
-  if (cudaMalloc(&buf, bytes) != cudaSuccess) {
+  if (dev_malloc((void**)&buf, bytes) != cudaSuccess) {
     cudaGetLastError();
     return GBLLT_ERR_ALLOC;
   }
@@ -883,7 +888,7 @@ static int host_batched(gbllt_batch_plan* plan, void* a, void* b, int64_t* info,
   cudaStream_t s = lib_stream();
   const size_t ab = (size_t)p->a_elems * elem, bb = (size_t)p->b_elems * elem, ib = (size_t)p->count * 8;
   char* d = nullptr;
-  if (cudaMallocAsync((void**)&d, ab + bb + ib + 512, s) != cudaSuccess) {
+  if (dev_malloc_async((void**)&d, ab + bb + ib + 512, s) != cudaSuccess) {
     cudaGetLastError();
     return GBLLT_ERR_ALLOC;
   }

@@ -5,6 +5,8 @@
 #include <mutex>
 #include <string>
 
+#include <cstdlib>
+
 #include "internal.h"
 
 namespace gbllt {
@@ -25,6 +27,27 @@ void set_last_error(cudaError_t e, const char* what, const char* file, int line)
 }
 
 void set_error_message(const char* msg) { g_last_error = msg; }
+
+static bool alloc_failure_injected() {
+  const char* e = getenv("GBLLT_INJECT_ALLOC_FAILURE");
+  return e && e[0] == '1';
+}
+
+cudaError_t dev_malloc_async(void** p, size_t bytes, cudaStream_t s) {
+  if (alloc_failure_injected()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocAsync(p, bytes, s);
+}
+
+cudaError_t dev_malloc(void** p, size_t bytes) {
+  if (alloc_failure_injected()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
 
 int ensure_device() {
   int dev = 0;
@@ -74,7 +97,7 @@ struct DevBuf {
 
 int alloc(DevBuf& b, size_t bytes, cudaStream_t s) {
   b.s = s;
-  if (cudaMallocAsync(&b.p, bytes < 256 ? 256 : bytes, s) != cudaSuccess) {
+  if (dev_malloc_async(&b.p, bytes < 256 ? 256 : bytes, s) != cudaSuccess) {
     cudaGetLastError();
     g_last_error = "cudaMallocAsync failed";
     b.p = nullptr;

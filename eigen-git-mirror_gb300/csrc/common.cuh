@@ -33,6 +33,13 @@ void set_error_message(const char* msg);
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Every device allocation of the library goes through these (stream-ordered, or plain for the
+// long-lived plan buffers).  With GBLLT_INJECT_ALLOC_FAILURE=1 in the environment they fail with
+// cudaErrorMemoryAllocation without calling CUDA: host-side fault injection, so that the
+// allocation-failure paths can be tested without exhausting a shared GPU's memory.
+cudaError_t dev_malloc_async(void** p, size_t bytes, cudaStream_t s);
+cudaError_t dev_malloc(void** p, size_t bytes);
+
 // Per-thread, per-device library stream for the synchronous host-pointer entry points.
 cudaStream_t lib_stream();
 

@@ -165,7 +165,7 @@ int sym_l1_norm_into(bool upper, int64_t n, const T* a, int64_t lda, double* d_c
 }
 
 int alloc_async(void** p, size_t bytes, cudaStream_t s) {
-  if (cudaMallocAsync(p, bytes, s) != cudaSuccess) {
+  if (dev_malloc_async((void**)p, bytes, s) != cudaSuccess) {
     cudaGetLastError();
     set_error_message("cudaMallocAsync failed");
     return GBLLT_ERR_ALLOC;

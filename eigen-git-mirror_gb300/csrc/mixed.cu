@@ -587,7 +587,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   if (!ok && o.fallback_fp64) {
     // plain FP64 GPU factorisation of a copy of A (the LAPACK dsposv fallback)
     if (may_allocate) {
-      if (cudaMallocAsync(&w, (size_t)n * n * 8, s) != cudaSuccess) {
+      if (dev_malloc_async((void**)&w, (size_t)n * n * 8, s) != cudaSuccess) {
         cudaGetLastError();
         return GBLLT_ERR_ALLOC;
       }
@@ -634,8 +634,9 @@ int posv_mixed_dev(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t
   if (resolve_mixed_opts(opts, &o)) return -10;
   const MixedLayout Ly = mixed_layout(n, nrhs, o, true);
   void* raw = nullptr;
-  if (cudaMallocAsync(&raw, Ly.bytes, s) != cudaSuccess) {
+  if (dev_malloc_async((void**)&raw, Ly.bytes, s) != cudaSuccess) {
     cudaGetLastError();
+    set_error_message("gbllt_dposv_mixed: allocation of the workspace failed");
     return GBLLT_ERR_ALLOC;
   }
   const int rc = posv_mixed_core(upper, n, nrhs, a, lda, b, ldb, x, ldx, o, rep, raw, Ly.bytes, true, s);

@@ -9,7 +9,7 @@ template <typename T>
 int potrs_dev(bool upper, int64_t n, int64_t nrhs, const T* d_a, int64_t lda, T* d_b, int64_t ldb, cudaStream_t s) {
   if (n <= 0 || nrhs <= 0) return GBLLT_SUCCESS;
   void* ws = nullptr;
-  if (cudaMallocAsync(&ws, potrs_ws_bytes(n, sizeof(T)), s) != cudaSuccess) {
+  if (dev_malloc_async((void**)&ws, potrs_ws_bytes(n, sizeof(T)), s) != cudaSuccess) {
     cudaGetLastError();
     return GBLLT_ERR_ALLOC;
   }

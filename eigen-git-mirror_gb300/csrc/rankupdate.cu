@@ -200,7 +200,7 @@ int rank_update_dev(bool upper, int64_t n, T* l, int64_t ldl, const T* v, T sigm
   const int nb = (int)ceil_div(n, RB);
   const size_t cbytes = ((size_t)nb * RB * CW * sizeof(T) + 255) & ~(size_t)255;
   void* w = nullptr;
-  if (cudaMallocAsync(&w, cbytes + (size_t)(nb + 4) * sizeof(int), s) != cudaSuccess) {
+  if (dev_malloc_async((void**)&w, cbytes + (size_t)(nb + 4) * sizeof(int), s) != cudaSuccess) {
     cudaGetLastError();
     set_error_message("gbllt_?rank_update_dev: cudaMallocAsync failed");
     return GBLLT_ERR_ALLOC;
@@ -278,7 +278,7 @@ int host_rank_update(int layout, char uplo, int64_t n, T* l, int64_t ldl, const 
   cudaStream_t s = lib_stream();
   const size_t es = sizeof(T), lbytes = ((size_t)n * n * es + 255) & ~(size_t)255;
   void* w = nullptr;
-  if (cudaMallocAsync(&w, lbytes + (size_t)n * es + 256 + sizeof(int64_t), s) != cudaSuccess) {
+  if (dev_malloc_async((void**)&w, lbytes + (size_t)n * es + 256 + sizeof(int64_t), s) != cudaSuccess) {
     cudaGetLastError();
     set_error_message("gbllt_?rank_update: cudaMallocAsync failed");
     return GBLLT_ERR_ALLOC;
