@@ -22,10 +22,11 @@ void launch_potrf_diag(T* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cud
 // Rows below the block: A(k0+bs.., k0..k0+bs) <- A(...) L11^{-T}, rs rows.
 template <typename T>
 void launch_trsm_panel(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, cudaStream_t s);
-// Lower update of the first ncols columns of the rs x rs trailing matrix by the bs-wide panel.
+// Lower update of the first ncols columns of the rs x rs trailing matrix by the bs-wide panel:
+// A22 -= A21 A21^T, or A22 -= A21 B^T with B the rs x bs array at bsrc (leading dimension ldb).
 template <typename T>
 void launch_syrk_lower(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, int64_t ncols, DevStatus* st,
-                       cudaStream_t s);
+                       cudaStream_t s, const T* bsrc = nullptr, int64_t ldb = 0);
 
 // Swap the strict lower and strict upper triangles of the n x n matrix at d_a in place
 // (A <- A^T).  Used to run the lower algorithm on an upper-stored factor, the same trick as
@@ -90,6 +91,23 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
                     size_t ws_bytes, bool may_allocate, cudaStream_t s);
 int posv_mixed_dev(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
                    double* x, int64_t ldx, const gbllt_mixed_opts* opts, gbllt_mixed_report* rep, cudaStream_t s);
+
+// The LDL^T solve's two sweeps in place on b (already permuted): unit L from the factor at a, D^+
+// from its diagonal; workspace of potrs_ws_bytes(n, sizeof(T)) bytes.
+template <typename T>
+int ldlt_sweeps_ws(bool upper, int64_t n, int64_t nrhs, const T* d_a, int64_t lda, T* d_b, int64_t ldb, void* ws,
+                   cudaStream_t s);
+
+// Pivoted LDL^T (LDLT::compute) of the symmetric matrix in the `upper ? upper : lower` triangle of
+// the column-major device matrix d_a; transpositions, sign and info (0 Success, 1 NumericalIssue)
+// are written to host memory.  Synchronises s.
+template <typename T>
+int ldlt_factor_dev(bool upper, int64_t n, T* d_a, int64_t lda, int32_t* transp, int32_t* sign, int64_t* info,
+                    cudaStream_t s);
+// x = A^{-1} b from the factor and host transpositions, b column-major n x nrhs on the device.
+template <typename T>
+int ldlt_solve_dev(bool upper, int64_t n, int64_t nrhs, const T* d_a, int64_t lda, const int32_t* transp, T* d_b,
+                   int64_t ldb, cudaStream_t s);
 
 // Rank-1 update / downdate of the factor at l (device), L L^T + sigma v v^T; *d_info (device)
 // receives 0, the failing column + 1 of a downdate, or GBLLT_ERR_TIMEOUT.

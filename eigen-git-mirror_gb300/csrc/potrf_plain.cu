@@ -217,14 +217,16 @@ __global__ void __launch_bounds__(128) trsm_panel_kernel(T* __restrict__ a, long
     if (p < bs) row[(long long)p * lda] = x[p];
 }
 
-// A22 (rs x rs lower) -= A21 A21^T, A21 = rs x bs.  One CTA per 64 x 64 lower tile.  Only the
+// A22 (rs x rs lower) -= A21 B^T, A21 = rs x bs, B = A21 (Cholesky) or the rs x bs array at bsrc
+// with leading dimension ldb (LDL^T: B = A21 D).  One CTA per 64 x 64 lower tile.  Only the
 // first `ncols` columns of A22 are updated (nct = ceil(ncols / 64) column tiles): the whole lower
 // triangle when ncols = rs, or the remaining columns of the current panel when the mixed-precision
 // path factors a wide panel in 64-column steps.
 template <typename T>
 __global__ void __launch_bounds__(256) syrk_lower_kernel(T* __restrict__ a, long long lda, long long k0, int bs,
                                                          long long rs, long long ncols, int nct,
-                                                         const DevStatus* __restrict__ st) {
+                                                         const DevStatus* __restrict__ st,
+                                                         const T* __restrict__ bsrc, long long ldb) {
   if (st->fail_col >= 0) return;
   constexpr int KC = 32;
   __shared__ T As[KC][64 + 1];
@@ -242,6 +244,8 @@ __global__ void __launch_bounds__(256) syrk_lower_kernel(T* __restrict__ a, long
   const long long i0 = (long long)ti * 64, j0 = (long long)tj * 64;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const T* A = a + (long long)k0 * lda + (k0 + bs);  // A21(0, 0)
+  const T* B = bsrc ? bsrc : A;
+  if (!bsrc) ldb = lda;
   T acc[4][4];
 #pragma unroll
   for (int m = 0; m < 4; ++m)
@@ -253,7 +257,7 @@ __global__ void __launch_bounds__(256) syrk_lower_kernel(T* __restrict__ a, long
       T va = T(0), vb = T(0);
       if (p0 + p < bs) {
         if (i0 + i < rs) va = A[(long long)(p0 + p) * lda + i0 + i];
-        if (j0 + i < rs) vb = A[(long long)(p0 + p) * lda + j0 + i];
+        if (j0 + i < rs) vb = B[(long long)(p0 + p) * ldb + j0 + i];
       }
       As[p][i] = va;
       Bs[p][i] = vb;
@@ -348,7 +352,7 @@ void launch_trsm_panel(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevSta
 
 template <typename T>
 void launch_syrk_lower(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, int64_t ncols, DevStatus* st,
-                       cudaStream_t s) {
+                       cudaStream_t s, const T* bsrc, int64_t ldb) {
   if (rs <= 0 || ncols <= 0) return;
   static const std::string ks = std::string("syrk_lower_") + tname<T>();
   const int64_t mt = ceil_div(rs, 64);
@@ -359,7 +363,7 @@ void launch_syrk_lower(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, int64_
   const double w = (double)ncols;
   const double entries = ncols >= rs ? (double)rs * (rs + 1) / 2.0 : w * (double)rs - w * (w - 1) / 2.0;
   ProfScope ps(ks.c_str(), s, 2.0 * entries * bs, ((double)rs * bs + 2.0 * entries) * sizeof(T));
-  syrk_lower_kernel<T><<<(unsigned)tiles, 256, 0, s>>>(a, lda, k0, bs, rs, ncols, (int)nct, st);
+  syrk_lower_kernel<T><<<(unsigned)tiles, 256, 0, s>>>(a, lda, k0, bs, rs, ncols, (int)nct, st, bsrc, ldb);
 }
 
 template <typename T>
@@ -377,7 +381,10 @@ int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t 
 
 template void launch_potrf_diag<float, double>(float*, int64_t, int64_t, int, DevStatus*, cudaStream_t);
 template void launch_trsm_panel<float>(float*, int64_t, int64_t, int, int64_t, DevStatus*, cudaStream_t);
-template void launch_syrk_lower<float>(float*, int64_t, int64_t, int, int64_t, int64_t, DevStatus*, cudaStream_t);
+template void launch_syrk_lower<float>(float*, int64_t, int64_t, int, int64_t, int64_t, DevStatus*, cudaStream_t,
+                                       const float*, int64_t);
+template void launch_syrk_lower<double>(double*, int64_t, int64_t, int, int64_t, int64_t, DevStatus*, cudaStream_t,
+                                        const double*, int64_t);
 
 template <typename T>
 int transpose_inplace_dev(int64_t n, T* d_a, int64_t lda, cudaStream_t s) {

@@ -15,6 +15,13 @@
 // work of the last row blocks is spread over several SMs.
 //
 // The diagonal inverses come from trinv_kernel (one CTA per block, column-wise substitution).
+//
+// The same sweeps solve with the factor of LDL^T (LDLT::_solve_impl_transposed, LDLT.h:573-613):
+// L has a unit diagonal (trinv_kernel<UNIT>) and the diagonal of the stored factor holds D; the
+// backward sweep applies D's pseudo-inverse to each block's right-hand sides as it loads them
+// (DSCALE: divide where |d| > the smallest normal number, else 0, LDLT.h:587-600).
+#include <cfloat>
+
 #include "internal.h"
 
 namespace gbllt {
@@ -36,8 +43,9 @@ __device__ __forceinline__ T lget(const T* __restrict__ a, long long lda, long l
   return UP ? a[i * lda + j] : a[j * lda + i];  // L(i, j)
 }
 
-// inv[blk] (64 x 64, column-major, lower) = L_blk^{-1}; identity padding beyond n.
-template <typename T, bool UP>
+// inv[blk] (64 x 64, column-major, lower) = L_blk^{-1}; identity padding beyond n.  UNIT: the
+// diagonal of L is 1 and the stored diagonal (D of an LDL^T factor) is not read.
+template <typename T, bool UP, bool UNIT>
 __global__ void __launch_bounds__(128) trinv_kernel(const T* __restrict__ a, long long lda, long long n,
                                                     T* __restrict__ inv) {
   __shared__ T L[RB][RB + 1];  // L[i][p]
@@ -48,7 +56,7 @@ __global__ void __launch_bounds__(128) trinv_kernel(const T* __restrict__ a, lon
     if (UP) { p = idx % RB; i = idx / RB; }
     else    { i = idx % RB; p = idx / RB; }
     T v = (i == p) ? T(1) : T(0);
-    if (i < bs && p < bs && i >= p) v = lget<T, UP>(a, lda, b0 + i, b0 + p);
+    if (i < bs && p < bs && (UNIT ? i > p : i >= p)) v = lget<T, UP>(a, lda, b0 + i, b0 + p);
     L[i][p] = v;
   }
   __syncthreads();
@@ -61,7 +69,7 @@ __global__ void __launch_bounds__(128) trinv_kernel(const T* __restrict__ a, lon
       T v = (i == c) ? T(1) : T(0);
 #pragma unroll
       for (int p = 0; p < i; ++p) v = fma(-L[i][p], x[p], v);
-      x[i] = i < c ? T(0) : v / L[i][i];
+      x[i] = i < c ? T(0) : (UNIT ? v : v / L[i][i]);
     }
 #pragma unroll
     for (int i = 0; i < RB; ++i) out[(long long)c * RB + i] = x[i];
@@ -76,8 +84,16 @@ struct SweepSmem {
   T Bs[RB][RCT + 1];   // this block's right-hand sides
 };
 
-// RCT right-hand sides per pass; thread (r, cq) owns row r and RCT/4 of them.
-template <typename T, bool UP, bool BWD, int RCT>
+// The pseudo-inverse of one entry of D (LDLT.h:594-600).
+template <typename T>
+__device__ __forceinline__ T dplus(T v, T d) {
+  const T tiny = sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN;
+  return fabs(d) > tiny ? v / d : T(0);
+}
+
+// RCT right-hand sides per pass; thread (r, cq) owns row r and RCT/4 of them.  DSCALE (backward
+// sweep of the LDL^T solve): the block's right-hand sides are multiplied by D^+ as they are loaded.
+template <typename T, bool UP, bool BWD, int RCT, bool DSCALE>
 __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, long long lda, long long n,
                                                     T* __restrict__ b, long long ldb, int nrhs, const T* __restrict__ inv,
                                                     int* __restrict__ flags, int* __restrict__ counter,
@@ -111,7 +127,9 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
   }
   for (int idx = tid; idx < RB * RCT; idx += 256) {
     const int p = idx & 63, c = idx >> 6;
-    sm.Bs[p][c] = (I0 + p < n && c < nrhs) ? b[(long long)c * ldb + I0 + p] : T(0);
+    T v = (I0 + p < n && c < nrhs) ? b[(long long)c * ldb + I0 + p] : T(0);
+    if (DSCALE && I0 + p < n) v = dplus(v, a[(I0 + p) * (lda + 1)]);
+    sm.Bs[p][c] = v;
   }
   T acc[CPT];
 #pragma unroll
@@ -183,24 +201,24 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
   if (tid == 0) atomicExch(flags + I, 1);
 }
 
-template <typename T, bool UP, bool BWD, int RCT>
+template <typename T, bool UP, bool BWD, int RCT, bool DSCALE>
 void launch_sweep_rc(int nb, const T* a, long long lda, long long n, T* b, long long ldb, int nrhs, const T* inv,
                      int* flags, int* counter, int* err, cudaStream_t s) {
   // set on every launch: cheap, and correct for every device and host thread
   const int smem = (int)sizeof(SweepSmem<T, RCT>);
-  cudaFuncSetAttribute(sweep_kernel<T, UP, BWD, RCT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaFuncSetAttribute(sweep_kernel<T, UP, BWD, RCT, DSCALE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   dim3 grid((unsigned)nb, (unsigned)((nrhs + RCT - 1) / RCT));
-  sweep_kernel<T, UP, BWD, RCT><<<grid, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, flags, counter, err);
+  sweep_kernel<T, UP, BWD, RCT, DSCALE><<<grid, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, flags, counter, err);
 }
 
 // One launch per sweep: chunks of RCT right-hand sides run as parallel chains (grid.y); 4 columns
 // per chunk for a single right-hand side, 16 otherwise (more chains spread the FP64 work of the
 // last row blocks over more SMs).
-template <typename T, bool UP, bool BWD>
+template <typename T, bool UP, bool BWD, bool DSCALE = false>
 void launch_sweep(int nb, const T* a, long long lda, long long n, T* b, long long ldb, int nrhs, const T* inv,
                   int* flags, int* counter, int* err, cudaStream_t s) {
-  if (nrhs <= 4) launch_sweep_rc<T, UP, BWD, 4>(nb, a, lda, n, b, ldb, nrhs, inv, flags, counter, err, s);
-  else launch_sweep_rc<T, UP, BWD, 16>(nb, a, lda, n, b, ldb, nrhs, inv, flags, counter, err, s);
+  if (nrhs <= 4) launch_sweep_rc<T, UP, BWD, 4, DSCALE>(nb, a, lda, n, b, ldb, nrhs, inv, flags, counter, err, s);
+  else launch_sweep_rc<T, UP, BWD, 16, DSCALE>(nb, a, lda, n, b, ldb, nrhs, inv, flags, counter, err, s);
 }
 
 }  // namespace
@@ -211,9 +229,10 @@ size_t potrs_ws_bytes(int64_t n, size_t elem) {
   return (size_t)nb * RB * RB * elem + (size_t)(2 * nch * nb + 2 * nch + 8) * sizeof(int) + 512;
 }
 
+// Both sweeps; ldl: the factor is the unit L of LDL^T with D on its diagonal.
 template <typename T>
-int potrs_ws(bool upper, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b, int64_t ldb, void* ws,
-             cudaStream_t s) {
+int sweeps_ws(bool upper, bool ldl, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b, int64_t ldb, void* ws,
+              cudaStream_t s) {
   if (n <= 0 || nrhs <= 0) return GBLLT_SUCCESS;
   static const std::string ki = std::string("trinv_diag_") + tname<T>();
   static const std::string kf = std::string("sweep_") + tname<T>();
@@ -222,8 +241,13 @@ int potrs_ws(bool upper, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b,
   int* base = (int*)((char*)ws + (((size_t)nb * RB * RB * sizeof(T) + 255) & ~(size_t)255));
   {
     ProfScope ps(ki.c_str(), s, (double)nb * RB * RB * RB / 3.0, (double)n * RB * sizeof(T) * 1.5);
-    if (upper) trinv_kernel<T, true><<<nb, 128, 0, s>>>(a, lda, n, inv);
-    else trinv_kernel<T, false><<<nb, 128, 0, s>>>(a, lda, n, inv);
+    if (ldl) {
+      if (upper) trinv_kernel<T, true, true><<<nb, 128, 0, s>>>(a, lda, n, inv);
+      else trinv_kernel<T, false, true><<<nb, 128, 0, s>>>(a, lda, n, inv);
+    } else {
+      if (upper) trinv_kernel<T, true, false><<<nb, 128, 0, s>>>(a, lda, n, inv);
+      else trinv_kernel<T, false, false><<<nb, 128, 0, s>>>(a, lda, n, inv);
+    }
   }
   for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
     const int nc = (int)(nrhs - c0 < RC ? nrhs - c0 : RC);
@@ -244,15 +268,35 @@ int potrs_ws(bool upper, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b,
     }
     {
       ProfScope ps(kf.c_str(), s, fl, by);
-      if (upper) launch_sweep<T, true, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
-      else launch_sweep<T, false, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
+      if (ldl) {
+        if (upper) launch_sweep<T, true, true, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
+        else launch_sweep<T, false, true, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
+      } else {
+        if (upper) launch_sweep<T, true, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
+        else launch_sweep<T, false, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
+      }
     }
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
 }
 
+template <typename T>
+int potrs_ws(bool upper, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b, int64_t ldb, void* ws,
+             cudaStream_t s) {
+  return sweeps_ws<T>(upper, false, n, nrhs, a, lda, b, ldb, ws, s);
+}
+
+template <typename T>
+int ldlt_sweeps_ws(bool upper, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b, int64_t ldb, void* ws,
+                   cudaStream_t s) {
+  return sweeps_ws<T>(upper, true, n, nrhs, a, lda, b, ldb, ws, s);
+}
+
 template int potrs_ws<double>(bool, int64_t, int64_t, const double*, int64_t, double*, int64_t, void*, cudaStream_t);
 template int potrs_ws<float>(bool, int64_t, int64_t, const float*, int64_t, float*, int64_t, void*, cudaStream_t);
+template int ldlt_sweeps_ws<double>(bool, int64_t, int64_t, const double*, int64_t, double*, int64_t, void*,
+                                    cudaStream_t);
+template int ldlt_sweeps_ws<float>(bool, int64_t, int64_t, const float*, int64_t, float*, int64_t, void*, cudaStream_t);
 
 }  // namespace gbllt

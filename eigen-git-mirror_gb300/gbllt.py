@@ -68,6 +68,16 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_srank_update": (_int, [_int, _ch, _i64, _vp, _i64, _vp, ctypes.c_float, _i64p]),
     "gbllt_drank_update_dev": (_int, [_ch, _i64, _vp, _i64, _vp, ctypes.c_double, _vp, _vp]),
     "gbllt_srank_update_dev": (_int, [_ch, _i64, _vp, _i64, _vp, ctypes.c_float, _vp, _vp]),
+    "gbllt_dldlt": (_int, [_int, _ch, _i64, _vp, _i64, _vp, _vp, _i64p]),
+    "gbllt_sldlt": (_int, [_int, _ch, _i64, _vp, _i64, _vp, _vp, _i64p]),
+    "gbllt_dldlt_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp, _i64p, _vp]),
+    "gbllt_sldlt_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp, _i64p, _vp]),
+    "gbllt_dldlt_pivots": (_int, [_i64, _vp, _i64, _vp]),
+    "gbllt_sldlt_pivots": (_int, [_i64, _vp, _i64, _vp]),
+    "gbllt_dldlt_solve": (_int, [_int, _ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64]),
+    "gbllt_sldlt_solve": (_int, [_int, _ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64]),
+    "gbllt_dldlt_solve_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _vp]),
+    "gbllt_sldlt_solve_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _vp]),
     "gbllt_dlansy_l1_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
     "gbllt_slansy_l1_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
     "gbllt_dpocon_dev": (_int, [_ch, _i64, _vp, _i64, ctypes.c_double, _dp, _vp]),
@@ -380,6 +390,62 @@ def rank_update_dev(d_l, n: int, ldl: int, d_v, sigma: float, d_info, uplo: str 
     """Device-pointer form (torch tensors); the info is written to the device scalar d_info."""
     fn = lib().gbllt_drank_update_dev if dtype == np.float64 else lib().gbllt_srank_update_dev
     check("gbllt_?rank_update_dev", fn(uplo.encode(), n, _ptr(d_l), ldl, _ptr(d_v), sigma, _ptr(d_info), stream))
+
+
+SIGN_NAMES = ("PositiveSemiDef", "NegativeSemiDef", "ZeroSign", "Indefinite")
+
+
+def ldlt(a: np.ndarray, uplo: str = "L") -> tuple[int, np.ndarray, int]:
+    """Pivoted LDL^T in place on a Fortran-order array (LDLT::compute); returns (info, transpositions,
+    sign): info 0 = Success, 1 = NumericalIssue; sign indexes SIGN_NAMES."""
+    dbl = a.dtype == np.float64
+    fn = lib().gbllt_dldlt if dbl else lib().gbllt_sldlt
+    n = a.shape[0]
+    t = np.zeros(max(n, 1), dtype=np.int32)
+    sign = ctypes.c_int32(0)
+    info = ctypes.c_int64(0)
+    check("gbllt_?ldlt", fn(COL_MAJOR, uplo.encode(), n, a.ctypes.data if n else None, max(n, 1), t.ctypes.data,
+                            ctypes.byref(sign), ctypes.byref(info)))
+    return int(info.value), t[:n], int(sign.value)
+
+
+def ldlt_pivots(diag: np.ndarray) -> np.ndarray:
+    """The transpositions LDLT::compute chooses for this diagonal (host computation)."""
+    d = np.ascontiguousarray(diag)
+    fn = lib().gbllt_dldlt_pivots if d.dtype == np.float64 else lib().gbllt_sldlt_pivots
+    n = d.shape[0]
+    t = np.zeros(max(n, 1), dtype=np.int32)
+    check("gbllt_?ldlt_pivots", fn(n, d.ctypes.data if n else None, 1, t.ctypes.data))
+    return t[:n]
+
+
+def ldlt_solve(f: np.ndarray, transp: np.ndarray, b: np.ndarray, uplo: str = "L") -> None:
+    """In place in b (n or n x k, Fortran order): A^{-1} b from the LDL^T factor and transpositions."""
+    dbl = f.dtype == np.float64
+    fn = lib().gbllt_dldlt_solve if dbl else lib().gbllt_sldlt_solve
+    n = f.shape[0]
+    k = 1 if b.ndim == 1 else b.shape[1]
+    t = np.ascontiguousarray(transp, dtype=np.int32)
+    check("gbllt_?ldlt_solve", fn(COL_MAJOR, uplo.encode(), n, k, f.ctypes.data if n else None, max(n, 1),
+                                  t.ctypes.data if n else None, b.ctypes.data if n else None, max(n, 1)))
+
+
+def ldlt_dev(d_a, n: int, lda: int, uplo: str = "L", stream=None, dtype=np.float64) -> tuple[int, np.ndarray, int]:
+    """Device-pointer form (torch tensor, column-major); returns (info, transpositions, sign)."""
+    fn = lib().gbllt_dldlt_dev if dtype == np.float64 else lib().gbllt_sldlt_dev
+    t = np.zeros(max(n, 1), dtype=np.int32)
+    sign = ctypes.c_int32(0)
+    info = ctypes.c_int64(0)
+    check("gbllt_?ldlt_dev", fn(uplo.encode(), n, _ptr(d_a), lda, t.ctypes.data, ctypes.byref(sign),
+                                ctypes.byref(info), stream))
+    return int(info.value), t[:n], int(sign.value)
+
+
+def ldlt_solve_dev(d_a, n: int, lda: int, transp: np.ndarray, d_b, nrhs: int, ldb: int, uplo: str = "L",
+                   stream=None, dtype=np.float64) -> None:
+    fn = lib().gbllt_dldlt_solve_dev if dtype == np.float64 else lib().gbllt_sldlt_solve_dev
+    t = np.ascontiguousarray(transp, dtype=np.int32)
+    check("gbllt_?ldlt_solve_dev", fn(uplo.encode(), n, nrhs, _ptr(d_a), lda, t.ctypes.data, _ptr(d_b), ldb, stream))
 
 
 def pocon(l: np.ndarray, anorm: float, uplo: str = "L") -> float:

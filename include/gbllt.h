@@ -259,6 +259,48 @@ typedef struct {
   double bytes;
 } gbllt_kernel_stat;
 
+/* ---- Pivoted LDL^T (LDLT<MatrixXd|MatrixXf, UpLo>, Eigen/src/Cholesky/LDLT.h) -----------------
+ * Factorisation, replacing LDLT::compute (LDLT.h:497-530 -> ldlt_inplace<Lower>::unblocked,
+ * LDLT.h:297-403; Upper runs on the transpose, LDLT.h:460-466): P A P^T = L D L^T with Eigen's
+ * symmetric pivoting (largest remaining |diagonal entry|, first on ties).  On return the `uplo`
+ * triangle holds L (unit diagonal, not stored) and D on the diagonal -- LDLT::matrixLDLT() -- and
+ * the other triangle is untouched; transp[k] (n entries, host memory) is the row swapped with row k
+ * at step k -- LDLT::transpositionsP().indices(); *sign is one of the GBLLT_SIGN_* values below
+ * (Eigen's internal::SignMatrix, LDLT.h:31); *info = 0 (Success) or 1 (NumericalIssue: a zero
+ * pivot with a nonzero column below it, or a nonzero pivot after a zero one, LDLT.h:383-387).
+ * The pivot order is computed on the host from the diagonal, so the _dev entry synchronises its
+ * stream (once to read the diagonal, once for sign and info); transp, sign and info are host
+ * memory in both entries. */
+#define GBLLT_SIGN_POSITIVE_SEMIDEF 0
+#define GBLLT_SIGN_NEGATIVE_SEMIDEF 1
+#define GBLLT_SIGN_ZERO 2
+#define GBLLT_SIGN_INDEFINITE 3
+GBLLT_API int gbllt_dldlt(int layout, char uplo, int64_t n, double* a, int64_t lda, int32_t* transp, int32_t* sign,
+                          int64_t* info);
+GBLLT_API int gbllt_sldlt(int layout, char uplo, int64_t n, float* a, int64_t lda, int32_t* transp, int32_t* sign,
+                          int64_t* info);
+GBLLT_API int gbllt_dldlt_dev(char uplo, int64_t n, double* d_a, int64_t lda, int32_t* transp, int32_t* sign,
+                              int64_t* info, void* stream);
+GBLLT_API int gbllt_sldlt_dev(char uplo, int64_t n, float* d_a, int64_t lda, int32_t* transp, int32_t* sign,
+                              int64_t* info, void* stream);
+/* The transpositions that LDLT::compute chooses for a matrix whose diagonal is diag[0], diag[incd],
+ * ... (the pivot order depends on nothing else): host computation, no device needed.  The
+ * factorisation entries above compute the same order. */
+GBLLT_API int gbllt_dldlt_pivots(int64_t n, const double* diag, int64_t incd, int32_t* transp);
+GBLLT_API int gbllt_sldlt_pivots(int64_t n, const float* diag, int64_t incd, int32_t* transp);
+/* X = A^{-1} B in place in B from that factor and its transpositions (host memory), replacing
+ * LDLT::_solve_impl_transposed (LDLT.h:573-613): P, the unit-L solve, D's pseudo-inverse (entries
+ * with |d| <= the smallest normal number give 0), the L^T solve, P^T.  The _dev entry is
+ * stream-ordered. */
+GBLLT_API int gbllt_dldlt_solve(int layout, char uplo, int64_t n, int64_t nrhs, const double* a, int64_t lda,
+                                const int32_t* transp, double* b, int64_t ldb);
+GBLLT_API int gbllt_sldlt_solve(int layout, char uplo, int64_t n, int64_t nrhs, const float* a, int64_t lda,
+                                const int32_t* transp, float* b, int64_t ldb);
+GBLLT_API int gbllt_dldlt_solve_dev(char uplo, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
+                                    const int32_t* transp, double* d_b, int64_t ldb, void* stream);
+GBLLT_API int gbllt_sldlt_solve_dev(char uplo, int64_t n, int64_t nrhs, const float* d_a, int64_t lda,
+                                    const int32_t* transp, float* d_b, int64_t ldb, void* stream);
+
 /* Turn per-launch event timing on (1) or off (0); either call discards earlier records. */
 GBLLT_API int gbllt_profile_enable(int on);
 /* Wait for the recorded launches and return up to max_entries classes; *n_entries = classes seen. */

@@ -67,6 +67,33 @@ static int64_t rank_update(int64_t n, T* a, int64_t lda, const T* v, T sigma) {
   return llt.info() == Success ? 0 : 1;
 }
 
+// LDLT<Matrix,UpLo>(A) (LDLT.h:497-530): the factor (UpLo triangle of matrixLDLT()) is written back
+// to a, the transpositions to transp, Eigen's sign (0 PositiveSemiDef, 1 NegativeSemiDef, 2 ZeroSign,
+// 3 Indefinite, recovered from isPositive()/isNegative(), LDLT.h:178-190) to *sign; returns 0 for
+// Success, 1 for NumericalIssue.
+template <typename T, int UpLo>
+static int64_t ldlt(int64_t n, T* a, int64_t lda, int32_t* transp, int32_t* sign) {
+  typedef Matrix<T, Dynamic, Dynamic> M;
+  Map<M, 0, OuterStride<>> A(a, n, n, OuterStride<>(lda));
+  LDLT<M, UpLo> f(A);
+  A.template triangularView<UpLo>() = f.matrixLDLT().template triangularView<UpLo>();
+  for (int64_t k = 0; k < n; ++k) transp[k] = (int32_t)f.transpositionsP().indices()(k);
+  const bool pos = f.isPositive(), neg = f.isNegative();
+  *sign = pos && neg ? 2 : pos ? 0 : neg ? 1 : 3;
+  return f.info() == Success ? 0 : 1;
+}
+
+// x = LDLT<Matrix,UpLo>(A).solve(b) (LDLT.h:573-613), b overwritten by x.
+template <typename T, int UpLo>
+static void ldlt_solve(int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b, int64_t ldb) {
+  typedef Matrix<T, Dynamic, Dynamic> M;
+  Map<const M, 0, OuterStride<>> A(a, n, n, OuterStride<>(lda));
+  Map<M, 0, OuterStride<>> B(b, n, nrhs, OuterStride<>(ldb));
+  LDLT<M, UpLo> f(A);
+  M X = f.solve(B);
+  B = X;
+}
+
 extern "C" {
 
 int64_t ref_drank_update(char uplo, int64_t n, double* a, int64_t lda, const double* v, double sigma) {
@@ -96,6 +123,21 @@ int64_t ref_dblocked(char uplo, int64_t n, double* a, int64_t lda) {
 }
 int64_t ref_sblocked(char uplo, int64_t n, float* a, int64_t lda) {
   return uplo == 'U' ? blocked<float, Upper>(n, a, lda) : blocked<float, Lower>(n, a, lda);
+}
+
+int64_t ref_dldlt(char uplo, int64_t n, double* a, int64_t lda, int32_t* transp, int32_t* sign) {
+  return uplo == 'U' ? ldlt<double, Upper>(n, a, lda, transp, sign) : ldlt<double, Lower>(n, a, lda, transp, sign);
+}
+int64_t ref_sldlt(char uplo, int64_t n, float* a, int64_t lda, int32_t* transp, int32_t* sign) {
+  return uplo == 'U' ? ldlt<float, Upper>(n, a, lda, transp, sign) : ldlt<float, Lower>(n, a, lda, transp, sign);
+}
+void ref_dldlt_solve(char uplo, int64_t n, int64_t nrhs, const double* a, int64_t lda, double* b, int64_t ldb) {
+  if (uplo == 'U') ldlt_solve<double, Upper>(n, nrhs, a, lda, b, ldb);
+  else ldlt_solve<double, Lower>(n, nrhs, a, lda, b, ldb);
+}
+void ref_sldlt_solve(char uplo, int64_t n, int64_t nrhs, const float* a, int64_t lda, float* b, int64_t ldb) {
+  if (uplo == 'U') ldlt_solve<float, Upper>(n, nrhs, a, lda, b, ldb);
+  else ldlt_solve<float, Lower>(n, nrhs, a, lda, b, ldb);
 }
 
 }  // extern "C"

@@ -395,4 +395,102 @@ int64_t P(rank_update)(char uplo, int64_t n, T* l, int64_t ldl, const T* v, T si
   return ret;
 }
 
+
+/* LDL^T with Eigen's symmetric pivoting: the restatement of ldlt_inplace<Lower>::unblocked
+ * (Eigen/src/Cholesky/LDLT.h:297-403) on the `uplo` triangle of the column-major a (Upper runs the
+ * same steps on the transpose, LDLT.h:460-466).  On return the lower view holds L (unit diagonal
+ * not stored) and D on the diagonal; transp[k] is the row swapped with row k at step k; *sign is
+ * Eigen's SignMatrix (0 PositiveSemiDef, 1 NegativeSemiDef, 2 ZeroSign, 3 Indefinite).  Returns 1
+ * for success (Eigen's `ret`), 0 for NumericalIssue.  The column update is left-looking, as in the
+ * reference: A11 -= A10 D A10^T, A21 -= A20 D A10^T, then A21 /= A11 unless the pivot is 0. */
+int P(ldlt)(char uplo, int64_t n, T* a, int64_t lda, int* transp, int* sign) {
+  const int up = (uplo == 'U' || uplo == 'u');
+  const int64_t rs = up ? lda : 1, cs = up ? 1 : lda;
+  int ret = 1, found_zero = 0;
+  *sign = 2; /* ZeroSign */
+  if (n <= 1) {
+    for (int64_t i = 0; i < n; ++i) transp[i] = (int)i;
+    if (n == 1) {
+      const T a00 = EL(a, 0, 0);
+      *sign = a00 > 0 ? 0 : (a00 < 0 ? 1 : 2);
+    }
+    return 1;
+  }
+  T* temp = (T*)malloc(sizeof(T) * n);
+  for (int64_t k = 0; k < n; ++k) {
+    /* largest |diagonal| in the corner, first index on ties (LDLT.h:323-326) */
+    int64_t p = k;
+    T best = (T)fabs((double)EL(a, k, k));
+    for (int64_t i = k + 1; i < n; ++i) {
+      const T v = (T)fabs((double)EL(a, i, i));
+      if (v > best) { best = v; p = i; }
+    }
+    transp[k] = (int)p;
+    if (p != k) { /* the swap of LDLT.h:329-345, lower triangle only */
+      for (int64_t j = 0; j < k; ++j) { const T t = EL(a, k, j); EL(a, k, j) = EL(a, p, j); EL(a, p, j) = t; }
+      for (int64_t i = p + 1; i < n; ++i) { const T t = EL(a, i, k); EL(a, i, k) = EL(a, i, p); EL(a, i, p) = t; }
+      { const T t = EL(a, k, k); EL(a, k, k) = EL(a, p, p); EL(a, p, p) = t; }
+      for (int64_t i = k + 1; i < p; ++i) { const T t = EL(a, i, k); EL(a, i, k) = EL(a, p, i); EL(a, p, i) = t; }
+    }
+    if (k > 0) { /* LDLT.h:356-362 */
+      for (int64_t j = 0; j < k; ++j) temp[j] = EL(a, j, j) * EL(a, k, j);
+      T s = 0;
+      for (int64_t j = 0; j < k; ++j) s += EL(a, k, j) * temp[j];
+      EL(a, k, k) -= s;
+      for (int64_t i = k + 1; i < n; ++i) {
+        T t = 0;
+        for (int64_t j = 0; j < k; ++j) t += EL(a, i, j) * temp[j];
+        EL(a, i, k) -= t;
+      }
+    }
+    const T akk = EL(a, k, k);
+    const int valid = fabs((double)akk) > 0;
+    if (k == 0 && !valid) { /* LDLT.h:371-382: the diagonal is entirely zero */
+      *sign = 2;
+      for (int64_t j = 0; j < n; ++j) {
+        transp[j] = (int)j;
+        for (int64_t i = j + 1; i < n; ++i) if (EL(a, i, j) != 0) ret = 0;
+      }
+      free(temp);
+      return ret;
+    }
+    if (valid) {
+      for (int64_t i = k + 1; i < n; ++i) EL(a, i, k) /= akk;
+    } else {
+      for (int64_t i = k + 1; i < n; ++i) if (EL(a, i, k) != 0) ret = 0;
+    }
+    if (found_zero && valid) ret = 0;
+    else if (!valid) found_zero = 1;
+    if (*sign == 0) { if (akk < 0) *sign = 3; }
+    else if (*sign == 1) { if (akk > 0) *sign = 3; }
+    else if (*sign == 2) { if (akk > 0) *sign = 0; else if (akk < 0) *sign = 1; }
+  }
+  free(temp);
+  return ret;
+}
+
+/* x = A^{-1} b from the LDL^T factor (LDLT::_solve_impl_transposed, LDLT.h:573-613): P b, L^{-1},
+ * the pseudo-inverse of D (|d| > the smallest normal number, else 0), L^{-T}, P^T. */
+void P(ldlt_solve)(char uplo, int64_t n, int64_t nrhs, const T* a, int64_t lda, const int* transp, T* b, int64_t ldb) {
+  const int up = (uplo == 'U' || uplo == 'u');
+  const int64_t rs = up ? lda : 1, cs = up ? 1 : lda;
+  const T tiny = sizeof(T) == 8 ? (T)2.2250738585072014e-308 : (T)1.17549435e-38f;
+  for (int64_t c = 0; c < nrhs; ++c) {
+    T* x = b + c * ldb;
+    for (int64_t k = 0; k < n; ++k) { const int64_t p = transp[k]; const T t = x[k]; x[k] = x[p]; x[p] = t; }
+    for (int64_t j = 0; j < n; ++j)
+      for (int64_t i = j + 1; i < n; ++i) x[i] -= EL(a, i, j) * x[j];
+    for (int64_t i = 0; i < n; ++i) {
+      const T d = EL(a, i, i);
+      x[i] = fabs((double)d) > (double)tiny ? x[i] / d : (T)0;
+    }
+    for (int64_t j = n - 1; j >= 0; --j) {
+      T s = x[j];
+      for (int64_t i = j + 1; i < n; ++i) s -= EL(a, i, j) * x[i];
+      x[j] = s;
+    }
+    for (int64_t k = n - 1; k >= 0; --k) { const int64_t p = transp[k]; const T t = x[k]; x[k] = x[p]; x[p] = t; }
+  }
+}
+
 #undef EL

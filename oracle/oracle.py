@@ -34,6 +34,10 @@ _SIGS = {
     "oracle_drank_update": (_i64, [_ch, _i64, _vp, _i64, _vp, _dbl]),
     "oracle_srank_update": (_i64, [_ch, _i64, _vp, _i64, _vp, ctypes.c_float]),
     "oracle_srcond": (_dbl, [_ch, _i64, _vp, _i64, _dbl]),
+    "oracle_dldlt": (ctypes.c_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
+    "oracle_sldlt": (ctypes.c_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
+    "oracle_dldlt_solve": (None, [_ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64]),
+    "oracle_sldlt_solve": (None, [_ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64]),
     "oracle_philox4x32_10": (None, [_vp, _vp, _vp]),
     "oracle_normal": (_dbl, [_u64, _u64]),
     "oracle_uniform": (_dbl, [_u64, _u64]),
@@ -65,12 +69,14 @@ _ref = None
 
 def build(ref: bool = True) -> None:
     """Compile liboracle.so; also Eigen's own LLT when the reference headers are present.
-    Same commands as oracle/Makefile, issued directly so that `make` is not required."""
+    Same commands as oracle/Makefile, issued directly so that `make` is not required.  No FMA
+    contraction: every product and sum is rounded, as in Eigen's SSE2 build, on x86-64 and aarch64
+    alike."""
     src = ORACLE_DIR / "llt_oracle.c"
     deps = [src, ORACLE_DIR / "llt_oracle_body.h"]
     if not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < max(d.stat().st_mtime for d in deps):
-        subprocess.run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-Wall", "-o", str(LIB_PATH), str(src), "-lm"],
-                       check=True)
+        subprocess.run(["gcc", "-O3", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-Wall", "-o",
+                        str(LIB_PATH), str(src), "-lm"], check=True)
     eigen = os.environ.get("EIGEN_REF", "/root/reference")
     if ref and Path(eigen, "Eigen").is_dir():
         REF_PATH.parent.mkdir(exist_ok=True)
@@ -112,6 +118,12 @@ def eigen_ref():
         R.ref_drank_update.argtypes = [_ch, _i64, _vp, _i64, _vp, _dbl]
         R.ref_srank_update.restype = _i64
         R.ref_srank_update.argtypes = [_ch, _i64, _vp, _i64, _vp, ctypes.c_float]
+        for nm in ("ref_dldlt", "ref_sldlt"):
+            getattr(R, nm).restype = _i64
+            getattr(R, nm).argtypes = [_ch, _i64, _vp, _i64, _vp, _vp]
+        for nm in ("ref_dldlt_solve", "ref_sldlt_solve"):
+            getattr(R, nm).restype = None
+            getattr(R, nm).argtypes = [_ch, _i64, _i64, _vp, _i64, _vp, _i64]
         _ref = R
     return _ref
 
@@ -177,6 +189,57 @@ def gen_rbf(m: int, seed: int = 31, offset: int = 0, ell: float = 0.2, sigma2: f
     return a
 
 
+LDLT_KINDS = ("gram", "indef", "wide", "lagrange", "lowrank", "diag", "zerocol", "zerodiag")
+
+
+def gen_sym(kind: str, n: int, seed: int) -> np.ndarray:
+    """Symmetric inputs for the LDL^T path (Fortran order, double):
+    gram      G G^T/n + I (positive definite);
+    indef     (G + G^T)/(2n) + diag(+-(2 + u)): diagonally dominant, indefinite;
+    wide      a diag(d) a^T, a uniform[-1,1], d_k uniform[-1,1] * 10^r, r uniform[-4,4] (the
+              wide-spectrum matrices of test/cholesky.cpp:248-255, exponent range narrowed);
+    lagrange  gram with its trailing n/3 x n/3 block zeroed (test/cholesky.cpp:214-228);
+    lowrank   a a^T, a n x max(1, n/2) uniform[-1,1] (test/cholesky.cpp:230-245);
+    diag      integer diagonal in [-3, 3], zeros included (pivots and signs exact);
+    zerocol   gram with row and column n/2 zeroed (an exact zero pivot with a zero column);
+    zerodiag  (G + G^T) with a zero diagonal (NumericalIssue unless n <= 1)."""
+    if n == 0:
+        return np.zeros((0, 0), order="F")
+    g = normal(seed, n * n).reshape(n, n, order="F")
+    u = uniform(seed + 1, n)
+    if kind == "gram":
+        return gen_gram(n, seed=seed)
+    if kind == "indef":
+        d = np.where(u < 0.5, -1.0, 1.0) * (2.0 + uniform(seed + 2, n))
+        return np.asfortranarray((g + g.T) / (2.0 * n) + np.diag(d))
+    if kind == "wide":
+        a = 2.0 * uniform(seed + 3, n * n).reshape(n, n, order="F") - 1.0
+        d = (2.0 * u - 1.0) * 10.0 ** (8.0 * uniform(seed + 4, n) - 4.0)
+        return np.asfortranarray((a * d) @ a.T)
+    if kind == "lagrange":
+        a = gen_gram(n, seed=seed)
+        c = n // 3
+        if c:
+            a[n - c:, n - c:] = 0.0
+        return a
+    if kind == "lowrank":
+        r = max(1, n // 2)
+        a = 2.0 * uniform(seed + 3, n * r).reshape(n, r, order="F") - 1.0
+        return np.asfortranarray(a @ a.T)
+    if kind == "diag":
+        return np.asfortranarray(np.diag(np.floor(7.0 * u) - 3.0))
+    if kind == "zerocol":
+        a = gen_gram(n, seed=seed)
+        a[n // 2, :] = 0.0
+        a[:, n // 2] = 0.0
+        return a
+    if kind == "zerodiag":
+        a = np.asfortranarray(g + g.T)
+        np.fill_diagonal(a, 0.0)
+        return a
+    raise ValueError(kind)
+
+
 # ---- LLT restatement ---------------------------------------------------------------------------
 
 def blocked(a: np.ndarray, uplo: str = "L") -> int:
@@ -225,6 +288,29 @@ def rank_update(l: np.ndarray, v: np.ndarray, sigma: float, uplo: str = "L") -> 
     fn = lib().oracle_drank_update if l.dtype == np.float64 else lib().oracle_srank_update
     vv = np.ascontiguousarray(v, dtype=l.dtype)
     return int(fn(uplo.encode(), n, _p(l) if n else None, max(1, n), _p(vv) if n else None, sigma))
+
+
+SIGN_NAMES = ("PositiveSemiDef", "NegativeSemiDef", "ZeroSign", "Indefinite")
+
+
+def ldlt(a: np.ndarray, uplo: str = "L") -> tuple[bool, np.ndarray, int]:
+    """In place: Eigen's pivoted LDL^T of the symmetric matrix in the `uplo` triangle of a
+    (ldlt_inplace<Lower>::unblocked, LDLT.h:297-403).  Returns (success, transpositions, sign)."""
+    n = a.shape[0]
+    t = np.zeros(max(n, 1), dtype=np.int32)
+    sg = ctypes.c_int(0)
+    fn = lib().oracle_dldlt if a.dtype == np.float64 else lib().oracle_sldlt
+    ok = fn(uplo.encode(), n, _p(a) if n else None, max(1, n), _p(t), ctypes.byref(sg))
+    return bool(ok), t[:n], int(sg.value)
+
+
+def ldlt_solve(f: np.ndarray, transp: np.ndarray, b: np.ndarray, uplo: str = "L") -> None:
+    """In place: b <- A^{-1} b from an LDL^T factor (LDLT.h:573-613)."""
+    n = f.shape[0]
+    k = 1 if b.ndim == 1 else b.shape[1]
+    t = np.ascontiguousarray(transp, dtype=np.int32)
+    fn = lib().oracle_dldlt_solve if f.dtype == np.float64 else lib().oracle_sldlt_solve
+    fn(uplo.encode(), n, k, _p(f) if n else None, max(1, n), _p(t) if n else None, _p(b) if n else None, max(1, n))
 
 
 def backward_error(a: np.ndarray, x: np.ndarray, b: np.ndarray, uplo: str = "L") -> float:
