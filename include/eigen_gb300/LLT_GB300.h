@@ -19,9 +19,14 @@
 //   - the condition estimate: explicit specialisations of internal::rcond_estimate_helper for the
 //     dynamic-size LLTs (called by LLT::rcond, LLT.h:166-171) call gbllt_?pocon, which runs
 //     Eigen's estimator (ConditionEstimator.h:56-171) with the factor resident on the device.
+//   - LDLT<MatrixXd|MatrixXf> (and LDLT<Ref<...>>): the pivoted factorisation, through explicit
+//     specialisations of internal::ldlt_inplace<Lower>::unblocked (LDLT.h:297-403) that call
+//     gbllt_?ldlt; ldlt.solve(b) through Solve<LDLT<...>> specialisations calling gbllt_?ldlt_solve.
 // What stays on Eigen's CPU code: LLT::solveInPlace (LLT.h:514-522) calls the triangular views
 // directly and bypasses Solve<>; the L1 norm that LLT::compute keeps for rcond
-// (LLT.h:443-453; gbllt_?lansy_l1_dev is its device form for callers outside Eigen).
+// (LLT.h:443-453; gbllt_?lansy_l1_dev is its device form for callers outside Eigen); fixed-size
+// LDLTs; LDLT::rankUpdate (ldlt_inplace::update, LDLT.h:405-456); LDLT::rcond, whose estimator
+// (ConditionEstimator.h) runs its solves through the GPU solve above.
 //
 // Errors: a failing library call (no usable GPU, CUDA error) trips eigen_assert; with assertions
 // disabled the factorisation reports NumericalIssue and a solve leaves NaN in its result.
@@ -124,14 +129,32 @@ EIGEN_GB300_LLT(float, gbllt_spotrf, gbllt_spotrs, gbllt_srank_update)
 
 #undef EIGEN_GB300_LLT
 
-// Runs the GPU solve of `dec` against `rhs` into the column-major temporary `x`.
-template <typename DecType, typename RhsType, typename Scalar>
-void gb300_solve(const DecType& dec, const RhsType& rhs, Matrix<Scalar, Dynamic, Dynamic, ColMajor>& x) {
-  typedef typename DecType::MatrixType FactorType;
-  x = rhs;
+// The GPU solve of an LLT in place in the column-major n x k array x (leading dimension n).
+template <typename MatrixType, int UpLo, typename Scalar>
+void gb300_run_solve(const LLT<MatrixType, UpLo>& dec, int64_t n, int64_t k, Scalar* x) {
   const auto& f = dec.matrixLLT();
-  gb300_llt<Scalar>::potrs(f.data(), (int64_t)f.outerStride(), (FactorType::Flags & RowMajorBit) != 0,
-                           DecType::UpLo == Lower ? 1 : 0, (int64_t)x.rows(), (int64_t)x.cols(), x.data());
+  gb300_llt<Scalar>::potrs(f.data(), (int64_t)f.outerStride(), (MatrixType::Flags & RowMajorBit) != 0,
+                           UpLo == Lower ? 1 : 0, n, k, x);
+}
+
+template <typename Scalar>
+struct gb300_ldlt;
+template <typename MatrixType, int UpLo, typename Scalar>
+void gb300_run_solve(const LDLT<MatrixType, UpLo>& dec, int64_t n, int64_t k, Scalar* x);
+
+// dst = dec.solve(rhs).  A plain column-major destination is solved in its own storage (no
+// temporary, so `x = dec.solve(x)` allocates nothing, as Eigen's in-place solve does); any other
+// destination goes through a column-major temporary.
+template <typename DecType, typename RhsType, typename Scalar, int Rows, int Cols, int MaxRows, int MaxCols>
+void gb300_solve_assign(const DecType& dec, const RhsType& rhs, Matrix<Scalar, Rows, Cols, ColMajor, MaxRows, MaxCols>& dst) {
+  dst = rhs;  // no-op when rhs is dst itself
+  gb300_run_solve(dec, (int64_t)dst.rows(), (int64_t)dst.cols(), dst.data());
+}
+template <typename DecType, typename RhsType, typename DstType>
+void gb300_solve_assign(const DecType& dec, const RhsType& rhs, DstType& dst) {
+  Matrix<typename DstType::Scalar, Dynamic, Dynamic, ColMajor> x = rhs;
+  gb300_run_solve(dec, (int64_t)x.rows(), (int64_t)x.cols(), x.data());
+  dst = x;
 }
 
 #define EIGEN_GB300_SOLVE(EIGTYPE)                                                                     \
@@ -143,9 +166,7 @@ void gb300_solve(const DecType& dec, const RhsType& rhs, Matrix<Scalar, Dynamic,
     typedef Solve<LLT<Matrix<EIGTYPE, Dynamic, Dynamic, Options, MaxRows, MaxCols>, UpLo>, RhsType> SrcXprType; \
     static void run(DstXprType& dst, const SrcXprType& src, const assign_op<EIGTYPE, EIGTYPE>&) {      \
       if ((dst.rows() != src.rows()) || (dst.cols() != src.cols())) dst.resize(src.rows(), src.cols()); \
-      Matrix<EIGTYPE, Dynamic, Dynamic, ColMajor> x;                                                   \
-      gb300_solve(src.dec(), src.rhs(), x);                                                            \
-      dst = x;                                                                                         \
+      gb300_solve_assign(src.dec(), src.rhs(), dst);                                                   \
     }                                                                                                  \
   };                                                                                                   \
   /* llt.solve(rhs) used inside a larger expression (+=, -=, noalias): evaluated into a temporary */  \
@@ -159,8 +180,8 @@ void gb300_solve(const DecType& dec, const RhsType& rhs, Matrix<Scalar, Dynamic,
     enum { Flags = Base::Flags | EvalBeforeNestingBit };                                               \
     explicit evaluator(const SolveType& solve) : m_result(solve.rows(), solve.cols()) {                \
       ::new (static_cast<Base*>(this)) Base(m_result);                                                 \
-      Matrix<EIGTYPE, Dynamic, Dynamic, ColMajor> x;                                                   \
-      gb300_solve(solve.dec(), solve.rhs(), x);                                                        \
+      Matrix<EIGTYPE, Dynamic, Dynamic, ColMajor> x = solve.rhs();                                     \
+      gb300_run_solve(solve.dec(), (int64_t)x.rows(), (int64_t)x.cols(), x.data());                   \
       m_result = x;                                                                                    \
     }                                                                                                  \
                                                                                                        \
@@ -202,6 +223,125 @@ EIGEN_GB300_RCOND(float, gbllt_spocon, RowMajor, Lower)
 EIGEN_GB300_RCOND(float, gbllt_spocon, RowMajor, Upper)
 
 #undef EIGEN_GB300_RCOND
+
+// ---- LDLT ---------------------------------------------------------------------------------------
+// LDLT::compute (LDLT.h:497-530) calls ldlt_inplace<UpLo>::unblocked; Upper passes a Transpose<> of
+// its matrix to ldlt_inplace<Lower> (LDLT.h:460-466).  These explicit specialisations of that member
+// template for the dynamic-size double/float matrices (plain and Ref<>, either storage order, and
+// their transposes) call gbllt_?ldlt, which returns Eigen's transpositions, sign and success flag.
+#define EIGEN_GB300_LDLT_FACTOR(EIGTYPE, LDLTFN, MTYPE, LAYOUT, UPLO, BASE)                               \
+  template <>                                                                                          \
+  inline bool ldlt_inplace<Lower>::unblocked<MTYPE, Transpositions<Dynamic, Dynamic, int>,              \
+                                             Matrix<EIGTYPE, Dynamic, 1> >(                            \
+      MTYPE & mat, Transpositions<Dynamic, Dynamic, int> & transpositions, Matrix<EIGTYPE, Dynamic, 1> & temp, \
+      SignMatrix & sign) {                                                                             \
+    EIGEN_UNUSED_VARIABLE(temp);                                                                       \
+    eigen_assert(mat.rows() == mat.cols());                                                            \
+    const int64_t n = (int64_t)mat.rows();                                                             \
+    if (n == 0) {                                                                                      \
+      sign = ZeroSign;                                                                                 \
+      return true;                                                                                     \
+    }                                                                                                  \
+    int32_t sg = 2;                                                                                    \
+    int64_t info = 0;                                                                                  \
+    const int rc = LDLTFN(LAYOUT, UPLO, n, &mat.coeffRef(0, 0), (int64_t)BASE.outerStride(),           \
+                          transpositions.indices().data(), &sg, &info);                                \
+    if (!gb300_check(#LDLTFN, rc)) return false;                                                       \
+    sign = static_cast<SignMatrix>(sg);                                                                \
+    return info == 0;                                                                                  \
+  }
+
+#define EIGEN_GB300_LDLT_TYPES(EIGTYPE, LDLTFN)                                                          \
+  EIGEN_GB300_LDLT_FACTOR(EIGTYPE, LDLTFN, Matrix<EIGTYPE EIGEN_COMMA Dynamic EIGEN_COMMA Dynamic EIGEN_COMMA ColMajor>, \
+                          GBLLT_COL_MAJOR, 'L', mat)                                                   \
+  EIGEN_GB300_LDLT_FACTOR(EIGTYPE, LDLTFN, Matrix<EIGTYPE EIGEN_COMMA Dynamic EIGEN_COMMA Dynamic EIGEN_COMMA RowMajor>, \
+                          GBLLT_ROW_MAJOR, 'L', mat)                                                   \
+  EIGEN_GB300_LDLT_FACTOR(EIGTYPE, LDLTFN,                                                             \
+                          Transpose<Matrix<EIGTYPE EIGEN_COMMA Dynamic EIGEN_COMMA Dynamic EIGEN_COMMA ColMajor> >, \
+                          GBLLT_COL_MAJOR, 'U', mat.nestedExpression())                                \
+  EIGEN_GB300_LDLT_FACTOR(EIGTYPE, LDLTFN,                                                             \
+                          Transpose<Matrix<EIGTYPE EIGEN_COMMA Dynamic EIGEN_COMMA Dynamic EIGEN_COMMA RowMajor> >, \
+                          GBLLT_ROW_MAJOR, 'U', mat.nestedExpression())                                \
+  EIGEN_GB300_LDLT_FACTOR(EIGTYPE, LDLTFN,                                                             \
+                          Ref<Matrix<EIGTYPE EIGEN_COMMA Dynamic EIGEN_COMMA Dynamic EIGEN_COMMA ColMajor> >, \
+                          GBLLT_COL_MAJOR, 'L', mat)                                                   \
+  EIGEN_GB300_LDLT_FACTOR(EIGTYPE, LDLTFN,                                                             \
+                          Ref<Matrix<EIGTYPE EIGEN_COMMA Dynamic EIGEN_COMMA Dynamic EIGEN_COMMA RowMajor> >, \
+                          GBLLT_ROW_MAJOR, 'L', mat)                                                   \
+  EIGEN_GB300_LDLT_FACTOR(EIGTYPE, LDLTFN,                                                             \
+                          Transpose<Ref<Matrix<EIGTYPE EIGEN_COMMA Dynamic EIGEN_COMMA Dynamic EIGEN_COMMA ColMajor> > >, \
+                          GBLLT_COL_MAJOR, 'U', mat.nestedExpression())                                \
+  EIGEN_GB300_LDLT_FACTOR(EIGTYPE, LDLTFN,                                                             \
+                          Transpose<Ref<Matrix<EIGTYPE EIGEN_COMMA Dynamic EIGEN_COMMA Dynamic EIGEN_COMMA RowMajor> > >, \
+                          GBLLT_ROW_MAJOR, 'U', mat.nestedExpression())
+
+EIGEN_GB300_LDLT_TYPES(double, gbllt_dldlt)
+EIGEN_GB300_LDLT_TYPES(float, gbllt_sldlt)
+
+#undef EIGEN_GB300_LDLT_TYPES
+#undef EIGEN_GB300_LDLT_FACTOR
+
+#define EIGEN_GB300_LDLT_SOLVER(EIGTYPE, SOLVEFN)                                                        \
+  template <>                                                                                          \
+  struct gb300_ldlt<EIGTYPE> {                                                                         \
+    static void solve(const EIGTYPE* fac, int64_t ldf, bool rowmajor, int uplo_lower, const int* transp, \
+                      int64_t n, int64_t k, EIGTYPE* x) {                                              \
+      if (n == 0 || k == 0) return;                                                                    \
+      const char uplo = ((uplo_lower != 0) != rowmajor) ? 'L' : 'U';                                   \
+      const int rc = SOLVEFN(GBLLT_COL_MAJOR, uplo, n, k, fac, ldf, transp, x, n);                     \
+      if (!gb300_check(#SOLVEFN, rc))                                                                  \
+        for (int64_t i = 0; i < n * k; ++i) x[i] = std::numeric_limits<EIGTYPE>::quiet_NaN();          \
+    }                                                                                                  \
+  };
+EIGEN_GB300_LDLT_SOLVER(double, gbllt_dldlt_solve)
+EIGEN_GB300_LDLT_SOLVER(float, gbllt_sldlt_solve)
+#undef EIGEN_GB300_LDLT_SOLVER
+
+// The GPU solve of an LDLT in place in x (LDLT::_solve_impl_transposed, LDLT.h:573-613: P, L, D^+,
+// L^T, P^T).
+template <typename MatrixType, int UpLo, typename Scalar>
+void gb300_run_solve(const LDLT<MatrixType, UpLo>& dec, int64_t n, int64_t k, Scalar* x) {
+  const auto& f = dec.matrixLDLT();
+  gb300_ldlt<Scalar>::solve(f.data(), (int64_t)f.outerStride(), (MatrixType::Flags & RowMajorBit) != 0,
+                            UpLo == Lower ? 1 : 0, dec.transpositionsP().indices().data(), n, k, x);
+}
+
+#define EIGEN_GB300_LDLT_SOLVE(EIGTYPE)                                                                \
+  /* dst = ldlt.solve(rhs) */                                                                          \
+  template <typename DstXprType, int Options, int MaxRows, int MaxCols, int UpLo, typename RhsType>    \
+  struct Assignment<DstXprType,                                                                        \
+                    Solve<LDLT<Matrix<EIGTYPE, Dynamic, Dynamic, Options, MaxRows, MaxCols>, UpLo>, RhsType>, \
+                    assign_op<EIGTYPE, EIGTYPE>, Dense2Dense> {                                        \
+    typedef Solve<LDLT<Matrix<EIGTYPE, Dynamic, Dynamic, Options, MaxRows, MaxCols>, UpLo>, RhsType> SrcXprType; \
+    static void run(DstXprType& dst, const SrcXprType& src, const assign_op<EIGTYPE, EIGTYPE>&) {      \
+      if ((dst.rows() != src.rows()) || (dst.cols() != src.cols())) dst.resize(src.rows(), src.cols()); \
+      gb300_solve_assign(src.dec(), src.rhs(), dst);                                                   \
+    }                                                                                                  \
+  };                                                                                                   \
+  /* ldlt.solve(rhs) inside a larger expression (+=, -=, noalias): evaluated into a temporary */      \
+  template <int Options, int MaxRows, int MaxCols, int UpLo, typename RhsType>                         \
+  struct evaluator<Solve<LDLT<Matrix<EIGTYPE, Dynamic, Dynamic, Options, MaxRows, MaxCols>, UpLo>, RhsType> > \
+      : public evaluator<typename Solve<LDLT<Matrix<EIGTYPE, Dynamic, Dynamic, Options, MaxRows, MaxCols>, UpLo>, \
+                                        RhsType>::PlainObject> {                                       \
+    typedef Solve<LDLT<Matrix<EIGTYPE, Dynamic, Dynamic, Options, MaxRows, MaxCols>, UpLo>, RhsType> SolveType; \
+    typedef typename SolveType::PlainObject PlainObject;                                               \
+    typedef evaluator<PlainObject> Base;                                                               \
+    enum { Flags = Base::Flags | EvalBeforeNestingBit };                                               \
+    explicit evaluator(const SolveType& solve) : m_result(solve.rows(), solve.cols()) {                \
+      ::new (static_cast<Base*>(this)) Base(m_result);                                                 \
+      Matrix<EIGTYPE, Dynamic, Dynamic, ColMajor> x = solve.rhs();                                     \
+      gb300_run_solve(solve.dec(), (int64_t)x.rows(), (int64_t)x.cols(), x.data());                   \
+      m_result = x;                                                                                    \
+    }                                                                                                  \
+                                                                                                       \
+   protected:                                                                                          \
+    PlainObject m_result;                                                                              \
+  };
+
+EIGEN_GB300_LDLT_SOLVE(double)
+EIGEN_GB300_LDLT_SOLVE(float)
+
+#undef EIGEN_GB300_LDLT_SOLVE
 
 }  // namespace internal
 }  // namespace Eigen

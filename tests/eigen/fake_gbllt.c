@@ -17,8 +17,14 @@ int64_t oracle_drank_update(char uplo, int64_t n, double* l, int64_t ldl, const 
 int64_t oracle_srank_update(char uplo, int64_t n, float* l, int64_t ldl, const float* v, float sigma);
 double oracle_drcond(char uplo, int64_t n, const double* l, int64_t ldl, double anorm);
 double oracle_srcond(char uplo, int64_t n, const float* l, int64_t ldl, double anorm);
+int oracle_dldlt(char uplo, int64_t n, double* a, int64_t lda, int* transp, int* sign);
+int oracle_sldlt(char uplo, int64_t n, float* a, int64_t lda, int* transp, int* sign);
+void oracle_dldlt_solve(char uplo, int64_t n, int64_t nrhs, const double* a, int64_t lda, const int* transp, double* b,
+                        int64_t ldb);
+void oracle_sldlt_solve(char uplo, int64_t n, int64_t nrhs, const float* a, int64_t lda, const int* transp, float* b,
+                        int64_t ldb);
 
-long fake_calls[8];
+long fake_calls[12];
 
 static char eff_uplo(int layout, char uplo) {
   const int up = uplo == 'U' || uplo == 'u';
@@ -71,11 +77,38 @@ int gbllt_srank_update(int layout, char uplo, int64_t n, float* l, int64_t ldl, 
   return 0;
 }
 
+int gbllt_dldlt(int layout, char uplo, int64_t n, double* a, int64_t lda, int32_t* transp, int32_t* sign,
+                int64_t* info) {
+  ++fake_calls[8];
+  *info = oracle_dldlt(eff_uplo(layout, uplo), n, a, lda, transp, sign) ? 0 : 1;
+  return 0;
+}
+int gbllt_sldlt(int layout, char uplo, int64_t n, float* a, int64_t lda, int32_t* transp, int32_t* sign,
+                int64_t* info) {
+  ++fake_calls[9];
+  *info = oracle_sldlt(eff_uplo(layout, uplo), n, a, lda, transp, sign) ? 0 : 1;
+  return 0;
+}
+int gbllt_dldlt_solve(int layout, char uplo, int64_t n, int64_t nrhs, const double* a, int64_t lda,
+                      const int32_t* transp, double* b, int64_t ldb) {
+  ++fake_calls[10];
+  if (layout != GBLLT_COL_MAJOR) return -1;
+  oracle_dldlt_solve(uplo, n, nrhs, a, lda, transp, b, ldb);
+  return 0;
+}
+int gbllt_sldlt_solve(int layout, char uplo, int64_t n, int64_t nrhs, const float* a, int64_t lda,
+                      const int32_t* transp, float* b, int64_t ldb) {
+  ++fake_calls[11];
+  if (layout != GBLLT_COL_MAJOR) return -1;
+  oracle_sldlt_solve(uplo, n, nrhs, a, lda, transp, b, ldb);
+  return 0;
+}
+
 /* Prints the call counts at exit so that the test can check the backend was used. */
 __attribute__((destructor)) static void fake_report(void) {
   fprintf(stderr,
           "fake_gbllt calls: dpotrf=%ld spotrf=%ld dpotrs=%ld spotrs=%ld dpocon=%ld spocon=%ld drankupd=%ld "
-          "srankupd=%ld\n",
+          "srankupd=%ld dldlt=%ld sldlt=%ld dldlts=%ld sldlts=%ld\n",
           fake_calls[0], fake_calls[1], fake_calls[2], fake_calls[3], fake_calls[4], fake_calls[5], fake_calls[6],
-          fake_calls[7]);
+          fake_calls[7], fake_calls[8], fake_calls[9], fake_calls[10], fake_calls[11]);
 }

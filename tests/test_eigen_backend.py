@@ -48,19 +48,24 @@ def _build_and_run(objs, test_name):
     res = subprocess.run([str(exe), "r3", "s1234"], capture_output=True, text=True, timeout=600)
     assert res.returncode == 0, res.stdout[-2000:] + res.stderr[-2000:]
     m = re.search(r"fake_gbllt calls: dpotrf=(\d+) spotrf=(\d+) dpotrs=(\d+) spotrs=(\d+) dpocon=(\d+) "
-                  r"spocon=(\d+) drankupd=(\d+) srankupd=(\d+)", res.stderr)
+                  r"spocon=(\d+) drankupd=(\d+) srankupd=(\d+) dldlt=(\d+) sldlt=(\d+) dldlts=(\d+) "
+                  r"sldlts=(\d+)", res.stderr)
     assert m, res.stderr[-2000:]
     return [int(v) for v in m.groups()]
 
 
 def test_eigen_cholesky_suite_through_backend(objs):
-    dpotrf, spotrf, dpotrs, _, dpocon, _, drankupd, srankupd = _build_and_run(objs, "cholesky")
+    dpotrf, spotrf, dpotrs, _, dpocon, _, drankupd, srankupd, dldlt, _, dldlts, _ = _build_and_run(objs, "cholesky")
     # MatrixXd factorisations, solves, condition estimates and rank updates, and fixed-size float
     # factorisations and rank updates, went through the C ABI (the rcond checks of
     # test/cholesky.cpp:94-115 ran on gbllt_dpocon, the rankUpdate checks of :44-56 on gbllt_?rank_update)
     assert dpotrf > 0 and dpotrs > 0 and spotrf > 0 and dpocon > 0 and drankupd > 0 and srankupd > 0
+    # LDLT<MatrixXd> factorisations (including the definiteness and failure cases of
+    # test/cholesky.cpp:358-469) and solves went through gbllt_dldlt / gbllt_dldlt_solve
+    assert dldlt > 0 and dldlts > 0
 
 
 def test_eigen_inplace_decomposition_through_backend(objs):
-    dpotrf = _build_and_run(objs, "inplace_decomposition")[0]
-    assert dpotrf > 0
+    counts = _build_and_run(objs, "inplace_decomposition")
+    assert counts[0] > 0  # LLT<Ref<MatrixXd>>
+    assert counts[8] > 0  # LDLT<Ref<MatrixXd>> (test/inplace_decomposition.cpp runs both)
