@@ -700,7 +700,7 @@ def main():
     ap.add_argument("--config", choices=sorted(CONFIGS) + ["c3", "c4", "c5"], default="c2")
     ap.add_argument("--c3-precisions", default="bf16x6,tf32x3,bf16x3,tf32,bf16")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mixed-precision", default="tf32x3", choices=["fp32", "tf32", "tf32x3", "bf16", "bf16x3", "bf16x6"])
+    ap.add_argument("--mixed-precision", default="bf16x6", choices=["fp32", "tf32", "tf32x3", "bf16", "bf16x3", "bf16x6"])
     ap.add_argument("--n", type=int, default=0, help="override the order n (profiling a smaller case)")
     ap.add_argument("--arms", default="both", choices=["both", "fp64", "mixed"])
     args = ap.parse_args()

@@ -98,6 +98,13 @@ template <typename T>
 int ldlt_sweeps_ws(bool upper, int64_t n, int64_t nrhs, const T* d_a, int64_t lda, T* d_b, int64_t ldb, void* ws,
                    cudaStream_t s);
 
+// One triangular sweep in place on b (n x nrhs): L X = B (forward) or L^T X = B (bwd), L lower
+// column-major (upper == false) or stored as its transpose in an upper triangle (upper == true);
+// unit: L's diagonal is 1 and not read.  Workspace of potrs_ws_bytes(n, sizeof(T)) bytes.
+template <typename T>
+int trsm_sweep_ws(bool upper, bool bwd, bool unit, int64_t n, int64_t nrhs, const T* d_a, int64_t lda, T* d_b,
+                  int64_t ldb, void* ws, cudaStream_t s);
+
 // Pivoted LDL^T (LDLT::compute) of the symmetric matrix in the `upper ? upper : lower` triangle of
 // the column-major device matrix d_a; transpositions, sign and info (0 Success, 1 NumericalIssue)
 // are written to host memory.  Synchronises s.

@@ -288,6 +288,47 @@ int potrs_ws(bool upper, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b,
 }
 
 template <typename T>
+int trsm_sweep_ws(bool upper, bool bwd, bool unit, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b,
+                  int64_t ldb, void* ws, cudaStream_t s) {
+  if (n <= 0 || nrhs <= 0) return GBLLT_SUCCESS;
+  static const std::string ki = std::string("trinv_diag_") + tname<T>();
+  static const std::string kf = std::string("sweep_") + tname<T>();
+  const int nb = (int)ceil_div(n, RB);
+  T* inv = (T*)ws;
+  int* base = (int*)((char*)ws + (((size_t)nb * RB * RB * sizeof(T) + 255) & ~(size_t)255));
+  {
+    ProfScope ps(ki.c_str(), s, (double)nb * RB * RB * RB / 3.0, (double)n * RB * sizeof(T) * 1.5);
+    if (unit) {
+      if (upper) trinv_kernel<T, true, true><<<nb, 128, 0, s>>>(a, lda, n, inv);
+      else trinv_kernel<T, false, true><<<nb, 128, 0, s>>>(a, lda, n, inv);
+    } else {
+      if (upper) trinv_kernel<T, true, false><<<nb, 128, 0, s>>>(a, lda, n, inv);
+      else trinv_kernel<T, false, false><<<nb, 128, 0, s>>>(a, lda, n, inv);
+    }
+  }
+  for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
+    const int nc = (int)(nrhs - c0 < RC ? nrhs - c0 : RC);
+    const int nch = nc <= 4 ? 1 : (nc + 15) / 16;
+    int* flags = base;
+    int* ctr = base + nch * nb;
+    int* err = ctr + nch;
+    T* bc = b + c0 * ldb;
+    GB_CUDA_TRY(cudaMemsetAsync(base, 0, (size_t)(nch * nb + nch + 1) * sizeof(int), s));
+    const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
+    ProfScope ps(kf.c_str(), s, fl, by);
+    if (bwd) {
+      if (upper) launch_sweep<T, true, true>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
+      else launch_sweep<T, false, true>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
+    } else {
+      if (upper) launch_sweep<T, true, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
+      else launch_sweep<T, false, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
+    }
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+template <typename T>
 int ldlt_sweeps_ws(bool upper, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b, int64_t ldb, void* ws,
                    cudaStream_t s) {
   return sweeps_ws<T>(upper, true, n, nrhs, a, lda, b, ldb, ws, s);
@@ -298,5 +339,9 @@ template int potrs_ws<float>(bool, int64_t, int64_t, const float*, int64_t, floa
 template int ldlt_sweeps_ws<double>(bool, int64_t, int64_t, const double*, int64_t, double*, int64_t, void*,
                                     cudaStream_t);
 template int ldlt_sweeps_ws<float>(bool, int64_t, int64_t, const float*, int64_t, float*, int64_t, void*, cudaStream_t);
+template int trsm_sweep_ws<double>(bool, bool, bool, int64_t, int64_t, const double*, int64_t, double*, int64_t, void*,
+                                   cudaStream_t);
+template int trsm_sweep_ws<float>(bool, bool, bool, int64_t, int64_t, const float*, int64_t, float*, int64_t, void*,
+                                  cudaStream_t);
 
 }  // namespace gbllt

@@ -78,6 +78,14 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_sldlt_solve": (_int, [_int, _ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64]),
     "gbllt_dldlt_solve_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _vp]),
     "gbllt_sldlt_solve_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _vp]),
+    "gbllt_dsyrk": (_int, [_int, _ch, _ch, _i64, _i64, ctypes.c_double, _vp, _i64, ctypes.c_double, _vp, _i64]),
+    "gbllt_ssyrk": (_int, [_int, _ch, _ch, _i64, _i64, ctypes.c_float, _vp, _i64, ctypes.c_float, _vp, _i64]),
+    "gbllt_dsyrk_dev": (_int, [_ch, _ch, _i64, _i64, ctypes.c_double, _vp, _i64, ctypes.c_double, _vp, _i64, _vp]),
+    "gbllt_ssyrk_dev": (_int, [_ch, _ch, _i64, _i64, ctypes.c_float, _vp, _i64, ctypes.c_float, _vp, _i64, _vp]),
+    "gbllt_dtrsm": (_int, [_int, _ch, _ch, _ch, _ch, _i64, _i64, ctypes.c_double, _vp, _i64, _vp, _i64]),
+    "gbllt_strsm": (_int, [_int, _ch, _ch, _ch, _ch, _i64, _i64, ctypes.c_float, _vp, _i64, _vp, _i64]),
+    "gbllt_dtrsm_dev": (_int, [_ch, _ch, _ch, _ch, _i64, _i64, ctypes.c_double, _vp, _i64, _vp, _i64, _vp]),
+    "gbllt_strsm_dev": (_int, [_ch, _ch, _ch, _ch, _i64, _i64, ctypes.c_float, _vp, _i64, _vp, _i64, _vp]),
     "gbllt_dlansy_l1_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
     "gbllt_slansy_l1_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
     "gbllt_dpocon_dev": (_int, [_ch, _i64, _vp, _i64, ctypes.c_double, _dp, _vp]),
@@ -162,6 +170,10 @@ LAPACK_SIGNATURES = {
     "spotrf_": (ctypes.c_int, [_C, _I, _F, _I, _I]),
     "dpotrs_": (ctypes.c_int, [_C, _I, _I, _D, _I, _D, _I, _I]),
     "spotrs_": (ctypes.c_int, [_C, _I, _I, _F, _I, _F, _I, _I]),
+    "dsyrk_": (ctypes.c_int, [_C, _C, _I, _I, _D, _D, _I, _D, _D, _I]),
+    "ssyrk_": (ctypes.c_int, [_C, _C, _I, _I, _F, _F, _I, _F, _F, _I]),
+    "dtrsm_": (ctypes.c_int, [_C, _C, _C, _C, _I, _I, _D, _D, _I, _D, _I]),
+    "strsm_": (ctypes.c_int, [_C, _C, _C, _C, _I, _I, _F, _F, _I, _F, _I]),
 }
 
 
@@ -183,6 +195,40 @@ def lapack() -> ctypes.CDLL:
 
 def _cptr(a: np.ndarray, ct):
     return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def _ci(v: int):
+    return ctypes.byref(ctypes.c_int(v))
+
+
+def blas_syrk(c: np.ndarray, a: np.ndarray, uplo: str = "L", trans: str = "N", alpha: float = 1.0, beta: float = 0.0,
+              n: int | None = None, k: int | None = None, lda: int | None = None, ldc: int | None = None) -> int:
+    """dsyrk_ / ssyrk_ of libgbllt_lapack.so on Fortran-order arrays; returns the routine's int."""
+    dbl = c.dtype == np.float64
+    ct = ctypes.c_double if dbl else ctypes.c_float
+    fn = lapack().dsyrk_ if dbl else lapack().ssyrk_
+    n = c.shape[0] if n is None else n
+    k = (a.shape[1] if trans.upper() == "N" else a.shape[0]) if k is None else k
+    lda = max(1, a.shape[0]) if lda is None else lda
+    ldc = max(1, c.shape[0]) if ldc is None else ldc
+    return fn(ctypes.c_char_p(uplo.encode()), ctypes.c_char_p(trans.encode()), _ci(n), _ci(k),
+              ctypes.byref(ct(alpha)), _cptr(a, ct), _ci(lda), ctypes.byref(ct(beta)), _cptr(c, ct), _ci(ldc))
+
+
+def blas_trsm(b: np.ndarray, a: np.ndarray, side: str = "L", uplo: str = "L", trans: str = "N", diag: str = "N",
+              alpha: float = 1.0, m: int | None = None, n: int | None = None, lda: int | None = None,
+              ldb: int | None = None) -> int:
+    """dtrsm_ / strsm_ of libgbllt_lapack.so on Fortran-order arrays; returns the routine's int."""
+    dbl = b.dtype == np.float64
+    ct = ctypes.c_double if dbl else ctypes.c_float
+    fn = lapack().dtrsm_ if dbl else lapack().strsm_
+    m = b.shape[0] if m is None else m
+    n = b.shape[1] if n is None else n
+    lda = max(1, a.shape[0]) if lda is None else lda
+    ldb = max(1, b.shape[0]) if ldb is None else ldb
+    return fn(ctypes.c_char_p(side.encode()), ctypes.c_char_p(uplo.encode()), ctypes.c_char_p(trans.encode()),
+              ctypes.c_char_p(diag.encode()), _ci(m), _ci(n), ctypes.byref(ct(alpha)), _cptr(a, ct), _ci(lda),
+              _cptr(b, ct), _ci(ldb))
 
 
 def lapack_potrf(a: np.ndarray, uplo: str = "L", lda: int | None = None, n: int | None = None) -> int:
@@ -446,6 +492,29 @@ def ldlt_solve_dev(d_a, n: int, lda: int, transp: np.ndarray, d_b, nrhs: int, ld
     fn = lib().gbllt_dldlt_solve_dev if dtype == np.float64 else lib().gbllt_sldlt_solve_dev
     t = np.ascontiguousarray(transp, dtype=np.int32)
     check("gbllt_?ldlt_solve_dev", fn(uplo.encode(), n, nrhs, _ptr(d_a), lda, t.ctypes.data, _ptr(d_b), ldb, stream))
+
+
+def syrk(c: np.ndarray, a: np.ndarray, uplo: str = "L", trans: str = "N", alpha: float = 1.0,
+         beta: float = 0.0) -> None:
+    """In place on the Fortran-order c (n x n): the `uplo` triangle <- alpha op(a) op(a)^T + beta c."""
+    dbl = c.dtype == np.float64
+    fn = lib().gbllt_dsyrk if dbl else lib().gbllt_ssyrk
+    n = c.shape[0]
+    k = a.shape[1] if trans.upper() == "N" else a.shape[0]
+    lda = max(1, a.shape[0])
+    check("gbllt_?syrk", fn(COL_MAJOR, uplo.encode(), trans.encode(), n, k, alpha, a.ctypes.data if a.size else None,
+                            lda, beta, c.ctypes.data if n else None, max(1, n)))
+
+
+def trsm(b: np.ndarray, a: np.ndarray, side: str = "L", uplo: str = "L", trans: str = "N", diag: str = "N",
+         alpha: float = 1.0) -> None:
+    """In place on the Fortran-order b (m x n): alpha op(a)^{-1} b (side 'L') or alpha b op(a)^{-1}."""
+    dbl = b.dtype == np.float64
+    fn = lib().gbllt_dtrsm if dbl else lib().gbllt_strsm
+    m, n = b.shape
+    check("gbllt_?trsm", fn(COL_MAJOR, side.encode(), uplo.encode(), trans.encode(), diag.encode(), m, n, alpha,
+                            a.ctypes.data if a.size else None, max(1, a.shape[0]), b.ctypes.data if b.size else None,
+                            max(1, m)))
 
 
 def pocon(l: np.ndarray, anorm: float, uplo: str = "L") -> float:

@@ -301,6 +301,33 @@ GBLLT_API int gbllt_dldlt_solve_dev(char uplo, int64_t n, int64_t nrhs, const do
 GBLLT_API int gbllt_sldlt_solve_dev(char uplo, int64_t n, int64_t nrhs, const float* d_a, int64_t lda,
                                     const int32_t* transp, float* d_b, int64_t ldb, void* stream);
 
+/* ---- BLAS level 3 of the Cholesky path (Eigen's Fortran BLAS, blas/level3_impl.h) -------------
+ * SYRK replaces dsyrk_ / ssyrk_ (blas/level3_impl.h:355-417): C = alpha op(A) op(A)^T + beta C on
+ * the `uplo` triangle of the n x n C, op(A) = A (n x k) for trans 'N', A^T (A k x n) for 'T'/'C'.
+ * beta is applied first (0 clears the triangle without reading it), then alpha times the product;
+ * the other triangle of C is untouched.  Argument errors return -i with i the argument's position
+ * (the _dev forms have no layout argument). */
+GBLLT_API int gbllt_dsyrk(int layout, char uplo, char trans, int64_t n, int64_t k, double alpha, const double* a,
+                          int64_t lda, double beta, double* c, int64_t ldc);
+GBLLT_API int gbllt_ssyrk(int layout, char uplo, char trans, int64_t n, int64_t k, float alpha, const float* a,
+                          int64_t lda, float beta, float* c, int64_t ldc);
+GBLLT_API int gbllt_dsyrk_dev(char uplo, char trans, int64_t n, int64_t k, double alpha, const double* d_a,
+                              int64_t lda, double beta, double* d_c, int64_t ldc, void* stream);
+GBLLT_API int gbllt_ssyrk_dev(char uplo, char trans, int64_t n, int64_t k, float alpha, const float* d_a,
+                              int64_t lda, float beta, float* d_c, int64_t ldc, void* stream);
+/* TRSM replaces dtrsm_ / strsm_ (blas/level3_impl.h:78-160): B (m x n) = alpha op(A)^{-1} B for
+ * side 'L' (A m x m) or alpha B op(A)^{-1} for side 'R' (A n x n); A upper or lower triangular
+ * (`uplo`), op 'N' or 'T'/'C', diag 'U' (unit, not read) or 'N'.  As in the reference the solve
+ * comes first and alpha scales its result. */
+GBLLT_API int gbllt_dtrsm(int layout, char side, char uplo, char transa, char diag, int64_t m, int64_t n,
+                          double alpha, const double* a, int64_t lda, double* b, int64_t ldb);
+GBLLT_API int gbllt_strsm(int layout, char side, char uplo, char transa, char diag, int64_t m, int64_t n,
+                          float alpha, const float* a, int64_t lda, float* b, int64_t ldb);
+GBLLT_API int gbllt_dtrsm_dev(char side, char uplo, char transa, char diag, int64_t m, int64_t n, double alpha,
+                              const double* d_a, int64_t lda, double* d_b, int64_t ldb, void* stream);
+GBLLT_API int gbllt_strsm_dev(char side, char uplo, char transa, char diag, int64_t m, int64_t n, float alpha,
+                              const float* d_a, int64_t lda, float* d_b, int64_t ldb, void* stream);
+
 /* Turn per-launch event timing on (1) or off (0); either call discards earlier records. */
 GBLLT_API int gbllt_profile_enable(int on);
 /* Wait for the recorded launches and return up to max_entries classes; *n_entries = classes seen. */

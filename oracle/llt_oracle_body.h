@@ -493,4 +493,58 @@ void P(ldlt_solve)(char uplo, int64_t n, int64_t nrhs, const T* a, int64_t lda, 
   }
 }
 
+/* C = alpha op(A) op(A)^T + beta C on the `uplo` triangle (Eigen's BLAS syrk,
+ * blas/level3_impl.h:355-417): beta first (0 clears, 1 leaves), then the product times alpha. */
+void P(syrk)(char uplo, char op, int64_t n, int64_t k, T alpha, const T* a, int64_t lda, T beta, T* c, int64_t ldc) {
+  const int up = (uplo == 'U' || uplo == 'u');
+  const int tr = !(op == 'N' || op == 'n');
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t i = up ? 0 : j; i < (up ? j + 1 : n); ++i) {
+      T* cij = c + j * ldc + i;
+      if (beta == (T)0) *cij = 0;
+      else if (beta != (T)1) *cij *= beta;
+    }
+  if (n == 0 || k == 0) return;
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t i = up ? 0 : j; i < (up ? j + 1 : n); ++i) {
+      T s = 0;
+      for (int64_t p = 0; p < k; ++p) {
+        const T x = tr ? a[i * lda + p] : a[p * lda + i];
+        const T y = tr ? a[j * lda + p] : a[p * lda + j];
+        s += x * y;
+      }
+      c[j * ldc + i] += alpha * s;
+    }
+}
+
+/* B = alpha op(A)^{-1} B (side 'L') or alpha B op(A)^{-1} (side 'R') (Eigen's BLAS trsm,
+ * blas/level3_impl.h:78-160): substitution, then the scaling by alpha. */
+void P(trsm)(char side, char uplo, char op, char diag, int64_t m, int64_t n, T alpha, const T* a, int64_t lda, T* b,
+             int64_t ldb) {
+  const int left = (side == 'L' || side == 'l');
+  const int up = (uplo == 'U' || uplo == 'u');
+  const int tr = !(op == 'N' || op == 'n');
+  const int unit = (diag == 'U' || diag == 'u');
+  if (m == 0 || n == 0) return;
+  /* the system matrix S: op(A) (left) or op(A)^T (right, solving for rows of B) */
+  const int st = left ? tr : !tr;           /* S(r, q) = st ? A(q, r) : A(r, q) */
+  const int slower = (!up) != st;           /* S is lower triangular */
+  const int64_t ns = left ? m : n, nv = left ? n : m;
+  for (int64_t v = 0; v < nv; ++v) {
+    /* the v-th right-hand side: column v of B (left) or row v of B (right) */
+    const int64_t inc = left ? 1 : ldb;
+    T* x = left ? b + v * ldb : b + v;
+    for (int64_t t = 0; t < ns; ++t) {
+      const int64_t r = slower ? t : ns - 1 - t;
+      const int64_t q0 = slower ? 0 : r + 1, q1 = slower ? r : ns;
+      T s = x[r * inc];
+      for (int64_t q = q0; q < q1; ++q) s -= (st ? a[r * lda + q] : a[q * lda + r]) * x[q * inc];
+      x[r * inc] = unit ? s : s / a[r * lda + r];
+    }
+  }
+  if (alpha != (T)1)
+    for (int64_t j = 0; j < n; ++j)
+      for (int64_t i = 0; i < m; ++i) b[j * ldb + i] *= alpha;
+}
+
 #undef EL

@@ -20,6 +20,7 @@ import numpy as np
 ORACLE_DIR = Path(__file__).resolve().parent
 LIB_PATH = ORACLE_DIR / "liboracle.so"
 REF_PATH = ORACLE_DIR / "_ref" / "libeigen_ref.so"
+BLAS_REF_PATH = ORACLE_DIR / "_ref" / "libeigen_blas.so"  # Eigen's own Fortran BLAS (blas/*.cpp)
 
 _i64 = ctypes.c_int64
 _u64 = ctypes.c_uint64
@@ -34,6 +35,10 @@ _SIGS = {
     "oracle_drank_update": (_i64, [_ch, _i64, _vp, _i64, _vp, _dbl]),
     "oracle_srank_update": (_i64, [_ch, _i64, _vp, _i64, _vp, ctypes.c_float]),
     "oracle_srcond": (_dbl, [_ch, _i64, _vp, _i64, _dbl]),
+    "oracle_dsyrk": (None, [_ch, _ch, _i64, _i64, _dbl, _vp, _i64, _dbl, _vp, _i64]),
+    "oracle_ssyrk": (None, [_ch, _ch, _i64, _i64, ctypes.c_float, _vp, _i64, ctypes.c_float, _vp, _i64]),
+    "oracle_dtrsm": (None, [_ch, _ch, _ch, _ch, _i64, _i64, _dbl, _vp, _i64, _vp, _i64]),
+    "oracle_strsm": (None, [_ch, _ch, _ch, _ch, _i64, _i64, ctypes.c_float, _vp, _i64, _vp, _i64]),
     "oracle_dldlt": (ctypes.c_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
     "oracle_sldlt": (ctypes.c_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
     "oracle_dldlt_solve": (None, [_ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64]),
@@ -84,6 +89,10 @@ def build(ref: bool = True) -> None:
         if not REF_PATH.exists() or REF_PATH.stat().st_mtime < cpp.stat().st_mtime:
             subprocess.run(["g++", "-O3", "-DNDEBUG", "-fopenmp", "-fPIC", "-shared", f"-I{eigen}", "-o",
                             str(REF_PATH), str(cpp)], check=True)
+        if not BLAS_REF_PATH.exists():
+            subprocess.run(["g++", "-O2", "-fPIC", "-shared", f"-I{eigen}", "-o", str(BLAS_REF_PATH)] +
+                           [str(Path(eigen, "blas", f)) for f in ("double.cpp", "single.cpp", "xerbla.cpp")],
+                           check=True)
 
 
 def lib() -> ctypes.CDLL:
@@ -126,6 +135,17 @@ def eigen_ref():
             getattr(R, nm).argtypes = [_ch, _i64, _i64, _vp, _i64, _vp, _i64]
         _ref = R
     return _ref
+
+
+_blas_ref = None
+
+
+def eigen_blas_ref():
+    """Eigen's own BLAS library (dsyrk_, dtrsm_, ...), None when it was not built here."""
+    global _blas_ref
+    if _blas_ref is None and BLAS_REF_PATH.exists():
+        _blas_ref = ctypes.CDLL(str(BLAS_REF_PATH))
+    return _blas_ref
 
 
 def _p(a: np.ndarray) -> int:
@@ -288,6 +308,25 @@ def rank_update(l: np.ndarray, v: np.ndarray, sigma: float, uplo: str = "L") -> 
     fn = lib().oracle_drank_update if l.dtype == np.float64 else lib().oracle_srank_update
     vv = np.ascontiguousarray(v, dtype=l.dtype)
     return int(fn(uplo.encode(), n, _p(l) if n else None, max(1, n), _p(vv) if n else None, sigma))
+
+
+def syrk(c: np.ndarray, a: np.ndarray, uplo: str = "L", trans: str = "N", alpha: float = 1.0,
+         beta: float = 0.0) -> None:
+    """In place on the Fortran-order c: Eigen's BLAS syrk (blas/level3_impl.h:355-417)."""
+    n = c.shape[0]
+    k = a.shape[1] if trans.upper() == "N" else a.shape[0]
+    fn = lib().oracle_dsyrk if c.dtype == np.float64 else lib().oracle_ssyrk
+    fn(uplo.encode(), trans.encode(), n, k, alpha, _p(a) if a.size else None, max(1, a.shape[0]), beta,
+       _p(c) if n else None, max(1, n))
+
+
+def trsm(b: np.ndarray, a: np.ndarray, side: str = "L", uplo: str = "L", trans: str = "N", diag: str = "N",
+         alpha: float = 1.0) -> None:
+    """In place on the Fortran-order b: Eigen's BLAS trsm (blas/level3_impl.h:78-160)."""
+    m, n = b.shape
+    fn = lib().oracle_dtrsm if b.dtype == np.float64 else lib().oracle_strsm
+    fn(side.encode(), uplo.encode(), trans.encode(), diag.encode(), m, n, alpha, _p(a) if a.size else None,
+       max(1, a.shape[0]), _p(b) if b.size else None, max(1, m))
 
 
 SIGN_NAMES = ("PositiveSemiDef", "NegativeSemiDef", "ZeroSign", "Indefinite")

@@ -14,7 +14,7 @@ import pytest
 
 import gbllt as G
 
-ROUTINES = ["dpotrf_", "spotrf_", "dpotrs_", "spotrs_"]
+ROUTINES = ["dpotrf_", "spotrf_", "dpotrs_", "spotrs_", "dsyrk_", "ssyrk_", "dtrsm_", "strsm_"]
 
 
 def test_shim_exports_the_lapack_routines():
