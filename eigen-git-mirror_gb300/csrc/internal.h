@@ -116,6 +116,30 @@ template <typename T>
 int ldlt_solve_dev(bool upper, int64_t n, int64_t nrhs, const T* d_a, int64_t lda, const int32_t* transp, T* d_b,
                    int64_t ldb, cudaStream_t s);
 
+// FP64 residual R = B - A X of a symmetric A on the BF16 tensor cores (error-free slicing of A and X,
+// exact FP32 accumulation in 256-deep chunks, int64 combination; ozaki.cu).  setup() slices A once
+// (n^2 * 16 bytes of device memory, stream-ordered); residual() slices X and forms R.  A non-finite
+// input gives a NaN residual.  The object owns its device memory.
+struct OzakiResidual {
+  int64_t n = 0, nrhs = 0, lds = 0;
+  void* buf = nullptr;
+  cudaStream_t stream = nullptr;
+  void* aslices = nullptr;
+  void* xslices = nullptr;
+  unsigned long long* rmax = nullptr;
+  int* xexp = nullptr;
+  int* flags = nullptr;
+  OzakiResidual() = default;
+  OzakiResidual(const OzakiResidual&) = delete;
+  OzakiResidual& operator=(const OzakiResidual&) = delete;
+  ~OzakiResidual();
+  static size_t bytes(int64_t n, int64_t nrhs);
+  int setup(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, cudaStream_t s);
+  int residual(const double* x, int64_t ldx, const double* b, int64_t ldb, double* r, int64_t ldr, cudaStream_t s);
+  // copies the device timeout word (1 if a bounded wait of the product kernel ran out) to host memory
+  int timeout_flag_into(int* host_flag, cudaStream_t s) const;
+};
+
 // Rank-1 update / downdate of the factor at l (device), L L^T + sigma v v^T; *d_info (device)
 // receives 0, the failing column + 1 of a downdate, or GBLLT_ERR_TIMEOUT.
 template <typename T>

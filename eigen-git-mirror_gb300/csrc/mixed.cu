@@ -197,6 +197,35 @@ __global__ void residual_reduce_kernel(const double* __restrict__ part, int npar
   r[c * ldr + i] = b[c * ldb + i] - s;
 }
 
+// Split-K partition of the FP64 residual: nparts partial sums of jpc row blocks each.
+void residual_parts(int64_t n, int64_t nrhs, int* nparts_out, int* jpc_out) {
+  const int nb = (int)ceil_div(n, RB), zc = (int)ceil_div(nrhs, RCH);
+  int nparts = (int)(1216 / ((int64_t)nb * zc));
+  nparts = nparts < 1 ? 1 : (nparts > nb ? nb : nparts);
+  const int jpc = (nb + nparts - 1) / nparts;
+  *jpc_out = jpc;
+  *nparts_out = (nb + jpc - 1) / jpc;
+}
+
+// R = B - A X on the FP64 pipe; part holds nparts * n * nrhs doubles.
+void symm_residual_fp64(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, const double* x,
+                        int64_t ldx, const double* b, int64_t ldb, double* R, int64_t ldr, double* part, int nparts,
+                        int jpc, cudaStream_t s) {
+  static const std::string kr = "symm_residual_f64";
+  ProfScope ps(kr.c_str(), s, 2.0 * n * n * nrhs, (double)n * n * 8.0 + 3.0 * n * nrhs * 8.0);
+  const int nb = (int)ceil_div(n, RB), zc = (int)ceil_div(nrhs, RCH);
+  if (nrhs == 1) {
+    dim3 grid((unsigned)nb, (unsigned)nparts, 1);
+    if (upper) symm_partial_kernel<true, 1><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
+    else symm_partial_kernel<false, 1><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
+  } else {
+    dim3 grid((unsigned)nb, (unsigned)nparts, (unsigned)zc);
+    if (upper) symm_partial_kernel<true, RCH><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
+    else symm_partial_kernel<false, RCH><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
+  }
+  residual_reduce_kernel<<<(unsigned)ceil_div(n * nrhs, 256), 256, 0, s>>>(part, nparts, n, nrhs, b, ldb, R, ldr);
+}
+
 // ---- deterministic sums of squares ------------------------------------------------------------
 
 // mode 0: column-major m x k block (ld);  mode 1/2: symmetric matrix from its lower/upper triangle
@@ -408,6 +437,7 @@ int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o) {
   }
   if (o->reserve_sms == 0) o->reserve_sms = kDefaultReserveSms;
   if (o->precision < GBLLT_PREC_FP32 || o->precision > GBLLT_PREC_BF16X6) return -1;
+  if (o->residual != GBLLT_RESIDUAL_TENSOR && o->residual != GBLLT_RESIDUAL_FP64) return -1;
   if (o->panel % kNB != 0) return -1;
   return 0;
 }
@@ -418,10 +448,7 @@ MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o, boo
   L.ldk = round_up(o.panel, 64);
   L.nb = (int)ceil_div(n, RB);
   L.zc = (int)ceil_div(nrhs, RCH);
-  int nparts = (int)(1216 / ((int64_t)L.nb * L.zc));
-  nparts = nparts < 1 ? 1 : (nparts > L.nb ? L.nb : nparts);
-  L.jpc = (L.nb + nparts - 1) / nparts;
-  L.nparts = (L.nb + L.jpc - 1) / L.jpc;
+  residual_parts(n, nrhs, &L.nparts, &L.jpc);
   L.nsq = 512;
   L.es_k = (o.precision == GBLLT_PREC_BF16 || o.precision == GBLLT_PREC_BF16X3 || o.precision == GBLLT_PREC_BF16X6)
                ? 2 : 4;
@@ -441,7 +468,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   const MixedLayout Ly = mixed_layout(n, nrhs, o, may_allocate);
   if (ws_bytes < Ly.bytes) return GBLLT_ERR_ALLOC;
   const int64_t ldf = Ly.ldf, ldk = Ly.ldk;
-  const int nb = Ly.nb, zc = Ly.zc, nparts = Ly.nparts, jpc = Ly.jpc, nsq = Ly.nsq;
+  const int nparts = Ly.nparts, jpc = Ly.jpc, nsq = Ly.nsq;
   const size_t es_k = Ly.es_k;
   struct Free {
     void* p;
@@ -497,19 +524,24 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     sumsq_kernel<<<blocks, 256, 0, s>>>(p, ld, m, k, mode, sq);
     sum_parts_kernel<<<1, 256, 0, s>>>(sq, blocks, out);
   };
-  auto residual = [&]() {  // R = B - A X
-    static const std::string kr = "symm_residual_f64";
-    ProfScope ps(kr.c_str(), s, 2.0 * n * n * nrhs, (double)n * n * 8.0 + 3.0 * n * nrhs * 8.0);
-    if (nrhs == 1) {
-      dim3 grid((unsigned)nb, (unsigned)nparts, 1);
-      if (upper) symm_partial_kernel<true, 1><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
-      else symm_partial_kernel<false, 1><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
-    } else {
-      dim3 grid((unsigned)nb, (unsigned)nparts, (unsigned)zc);
-      if (upper) symm_partial_kernel<true, RCH><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
-      else symm_partial_kernel<false, RCH><<<grid, 256, 0, s>>>(a, lda, n, x, ldx, nrhs, jpc, part);
-    }
-    residual_reduce_kernel<<<grid1(n * nrhs), 256, 0, s>>>(part, nparts, n, nrhs, b, ldb, R, n);
+  // the residual on the tensor cores needs A's slices (n^2 * 16 bytes): only where allocating is allowed
+  OzakiResidual oz;
+  bool use_oz = may_allocate && o.residual == GBLLT_RESIDUAL_TENSOR;
+  auto residual = [&]() -> int {  // R = B - A X
+    if (use_oz) return oz.residual(x, ldx, b, ldb, R, n, s);
+    symm_residual_fp64(upper, n, nrhs, a, lda, x, ldx, b, ldb, R, n, part, nparts, jpc, s);
+    return GBLLT_SUCCESS;
+  };
+  // the tensor-core residual's bounded waits report through its own word
+  auto residual_timed_out = [&](bool* out) -> int {
+    *out = false;
+    if (!use_oz) return GBLLT_SUCCESS;
+    int h = 0;
+    int rc2 = oz.timeout_flag_into(&h, s);
+    if (rc2) return rc2;
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    *out = h != 0;
+    return GBLLT_SUCCESS;
   };
 
   GB_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(DevStatus), s));
@@ -548,6 +580,11 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   r.factor_ms = elapsed(0, 1);
 
   bool ok = false;
+  if (r.info == 0 && use_oz) {
+    rc = oz.setup(upper, n, nrhs, a, lda, s);
+    if (rc == GBLLT_ERR_ALLOC) use_oz = false;  // not enough device memory for the slices: FP64 residual
+    else if (rc) return rc;
+  }
   if (r.info == 0) {
     // 3. refinement: x_0 = 0, r_0 = b
     sumsq(a, lda, n, n, upper ? 2 : 1, &norms[0]);
@@ -558,12 +595,15 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
       residual_to_f32_kernel<<<grid1(n * nrhs), 256, 0, s>>>(R, n, n, nrhs, dsc, &norms[1], Rf, n);
       if ((rc = potrs_ws<float>(false, n, nrhs, af, ldf, Rf, n, solve_ws, s))) return rc;
       update_x_kernel<<<grid1(n * nrhs), 256, 0, s>>>(Rf, n, n, nrhs, dsc, &norms[1], x, ldx, step == 0);
-      residual();
+      if ((rc = residual())) return rc;
       sumsq(R, n, n, nrhs, 0, &norms[1]);
       sumsq(x, ldx, n, nrhs, 0, &norms[2]);
       double hn[3];
       GB_CUDA_TRY(cudaMemcpyAsync(hn, norms, sizeof hn, cudaMemcpyDeviceToHost, s));
       GB_CUDA_TRY(cudaStreamSynchronize(s));
+      bool tmo = false;
+      if ((rc = residual_timed_out(&tmo))) return rc;
+      if (tmo) return GBLLT_ERR_TIMEOUT;
       const double be =
           (hn[0] > 0 && hn[2] > 0) ? sqrt(hn[1]) / (sqrt(hn[0]) * sqrt(hn[2])) : (hn[1] > 0 ? INFINITY : 0.0);
       r.steps = step + 1;
@@ -610,7 +650,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
       r.info = 0;
       copy_cols_kernel<<<grid1(n * nrhs), 256, 0, s>>>(b, ldb, n, nrhs, x, ldx);
       if ((rc = potrs_ws<double>(false, n, nrhs, w, n, x, ldx, solve_ws, s))) return rc;
-      residual();
+      if ((rc = residual())) return rc;
       sumsq(R, n, n, nrhs, 0, &norms[1]);
       sumsq(x, ldx, n, nrhs, 0, &norms[2]);
       sumsq(a, lda, n, n, upper ? 2 : 1, &norms[0]);
@@ -645,3 +685,43 @@ int posv_mixed_dev(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t
 }
 
 }  // namespace gbllt
+
+extern "C" int gbllt_dsyresid_dev(char uplo, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
+                                  const double* d_x, int64_t ldx, const double* d_b, int64_t ldb, double* d_r,
+                                  int64_t ldr, int method, void* stream) {
+  using namespace gbllt;
+  if (check_uplo(uplo)) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (n > 0 && !d_a) return -4;
+  if (lda < (n > 1 ? n : 1)) return -5;
+  if (n > 0 && nrhs > 0 && !d_x) return -6;
+  if (ldx < (n > 1 ? n : 1)) return -7;
+  if (n > 0 && nrhs > 0 && !d_b) return -8;
+  if (ldb < (n > 1 ? n : 1)) return -9;
+  if (n > 0 && nrhs > 0 && !d_r) return -10;
+  if (ldr < (n > 1 ? n : 1)) return -11;
+  if (method != GBLLT_RESIDUAL_TENSOR && method != GBLLT_RESIDUAL_FP64) return -12;
+  if (n == 0 || nrhs == 0) return GBLLT_SUCCESS;
+  int rc = ensure_device();
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool upper = uplo == 'U' || uplo == 'u';
+  if (method == GBLLT_RESIDUAL_TENSOR) {
+    OzakiResidual oz;
+    if ((rc = oz.setup(upper, n, nrhs, d_a, lda, s))) return rc;
+    return oz.residual(d_x, ldx, d_b, ldb, d_r, ldr, s);
+  }
+  int nparts = 1, jpc = 1;
+  residual_parts(n, nrhs, &nparts, &jpc);
+  void* part = nullptr;
+  if (dev_malloc_async(&part, (size_t)nparts * n * nrhs * 8, s) != cudaSuccess) {
+    cudaGetLastError();
+    set_error_message("cudaMallocAsync failed");
+    return GBLLT_ERR_ALLOC;
+  }
+  symm_residual_fp64(upper, n, nrhs, d_a, lda, d_x, ldx, d_b, ldb, d_r, ldr, (double*)part, nparts, jpc, s);
+  cudaFreeAsync(part, s);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}

@@ -1,0 +1,496 @@
+// FP64 residual R = B - A X on the BF16 tensor cores, exact to FP64 level, for the refinement of
+// the mixed-precision solve (A symmetric, stored in one triangle; X, B column-major n x nrhs).
+//
+// The FP64 pipe of GB300 delivers about 1.1 TFLOP/s, so the FP64 residual of a 16384 x 16384
+// system with 64 right-hand sides (34 GFLOP) takes about 31 ms, more than the whole tensor-core
+// factorisation.  This file computes the same product with error-free splitting (the Ozaki scheme:
+// Ozaki, Ogita, Oishi, Rump, "Error-free transformations of matrix multiplication by using fast
+// routines of matrix multiplication and its applications", Numer. Algorithms 59, 2012):
+//
+//   - every row i of A is scaled by a power of two 2^-e_i so that |a| < 1, and every column j of X
+//     by 2^-f_j; the scaled values are split into S = 8 slices of BETA = 7 bits,
+//         a / 2^e_i = sum_p s_p 2^(-7p),  s_1 in [-128, 128], s_p in [-64, 64] (p > 1),
+//     each slice an integer, so each is exact in BF16 (8 significant bits);
+//   - the product is sum over slice pairs (p, q) with p + q <= S + 1 (36 pairs; the dropped terms
+//     are below 2^-63 relative to 2^(e_i + f_j)) of 2^(-7(p+q)) (S_p X_q); pairs with the same
+//     weight w = p + q accumulate in one TMEM accumulator (8 of them, 64 columns each);
+//   - the products of integer slices are integers, and a chunk of KC = 256 K-elements keeps every
+//     partial sum of every weight below 2^24 (the largest weight sums 2^14 + 6 * 2^12 per K term),
+//     so the FP32 tensor-core accumulation of a chunk is exact; after each chunk the epilogue warps
+//     convert the accumulators to integers and add them into two int64 sums per output (weights
+//     2-5 and 6-9, each a fixed-point number), which stay exact for n up to about 2^20;
+//   - at the end, R = B - 2^(e_i + f_j) (hi 2^-35 + lo 2^-63), rounded once to FP64.
+//
+// oz_gemm_kernel: one CTA per 128-row x 64-column tile of R, 576 threads: a TMA producer warp
+// (A slice tiles through a 4-stage ring, the 8 X slice tiles of a 64-wide K block double-
+// buffered), an MMA warp (tcgen05.mma M = 128, N = 64, K = 16, 144 per K block) and 16 epilogue
+// warps (four per TMEM lane quadrant, 16 columns each).  Every mbarrier wait is bounded.
+// A non-finite value in A or X makes the whole residual NaN, which the refinement reports as
+// non-convergence, as it would with an FP64 residual.
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+#include "internal.h"
+#include "tc_ptx.cuh"
+
+namespace gbllt {
+
+namespace {
+
+using namespace tcptx;
+
+constexpr int S = 8;          // slices per operand
+constexpr int BETA = 7;       // bits per slice
+constexpr int KB = 64;        // K elements per 128-byte row (BF16)
+constexpr int KC_BLOCKS = 4;  // K blocks per exact chunk (KC = 256)
+constexpr int BM = 128;
+constexpr int BN = 64;
+constexpr int A_STAGES = 4;
+constexpr int A_BYTES = BM * 128;  // 16 KB: one A slice tile
+constexpr int X_BYTES = BN * 128;  // 8 KB: one X slice tile
+constexpr int X_SET = S * X_BYTES;  // 64 KB: the 8 X slices of one K block
+constexpr int SMEM_BYTES = A_STAGES * A_BYTES + 2 * X_SET + 1024;
+constexpr int EPI_WARPS = 16;  // four per TMEM lane quadrant, 16 columns each
+constexpr int THREADS = (2 + EPI_WARPS) * 32;  // 576
+constexpr int TMEM_COLS = S * BN;  // 512: one 64-column accumulator per weight w = 2 .. 9
+
+// ---- slicing ------------------------------------------------------------------------------------
+
+// |A| maxima per row of the full symmetric matrix (bit patterns of non-negative doubles compare
+// like unsigned integers), one CTA per stored 64 x 64 tile: entry (i, j) counts for rows i and j.
+// flag: set when A holds a non-finite value.
+template <bool UP>
+__global__ void __launch_bounds__(256) oz_rowmax_kernel(const double* __restrict__ a, long long lda, long long n,
+                                                        unsigned long long* __restrict__ rmax, int* __restrict__ flag) {
+  __shared__ unsigned long long rm[64], cm[64];
+  int ti, tj;
+  lower_tile_coords(blockIdx.x, ti, tj);
+  // lower storage: tile rows ti, columns tj (ti >= tj); upper: rows tj, columns ti
+  const long long i0 = (long long)(UP ? tj : ti) * 64, j0 = (long long)(UP ? ti : tj) * 64;
+  if (threadIdx.x < 64) {
+    rm[threadIdx.x] = 0;
+    cm[threadIdx.x] = 0;
+  }
+  __syncthreads();
+  int bad = 0;
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+    const int r = idx & 63, c = idx >> 6;
+    const long long i = i0 + r, j = j0 + c;
+    if (i < n && j < n && (UP ? i <= j : i >= j)) {
+      const double v = fabs(a[j * lda + i]);
+      if (!(v <= 1.7976931348623157e308)) bad = 1;  // inf or NaN
+      const unsigned long long bits = __double_as_longlong(v);
+      atomicMax(&rm[r], bits);
+      atomicMax(&cm[c], bits);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 64) {
+    if (i0 + threadIdx.x < n) atomicMax(&rmax[i0 + threadIdx.x], rm[threadIdx.x]);
+    if (j0 + threadIdx.x < n) atomicMax(&rmax[j0 + threadIdx.x], cm[threadIdx.x]);
+  }
+  if (bad) atomicOr(flag, 1);
+}
+
+// The scale exponent of a maximum m: |v| <= m < 2^e (e = 0 for m = 0).
+__device__ __forceinline__ int scale_exp(double m) {
+  int e = 0;
+  if (m > 0.0) frexp(m, &e);
+  return e;
+}
+
+// The 8 slices of a value already scaled into (-1, 1); each is an integer of at most 8 bits.
+__device__ __forceinline__ void split8(double t, float* sl) {
+#pragma unroll
+  for (int p = 0; p < S; ++p) {
+    t *= (double)(1 << BETA);
+    const double q = rint(t);
+    t -= q;
+    sl[p] = (float)q;
+  }
+}
+
+// Slices of the full symmetric A, row-major (row i holds its n entries contiguously: the K-major
+// layout of the MMA's A operand), slice p at slices + p * sstride, leading dimension lds.  One CTA
+// per 64 x 64 tile of the full matrix; the tile is read from the stored triangle (mirrored where
+// needed) through shared memory so that reads and writes are both coalesced.
+template <bool UP>
+__global__ void __launch_bounds__(256) oz_slice_a_kernel(const double* __restrict__ a, long long lda, long long n,
+                                                         const unsigned long long* __restrict__ rmax,
+                                                         __nv_bfloat16* __restrict__ slices, long long lds,
+                                                         long long sstride) {
+  __shared__ double tile[64][65];  // tile[r][c] = A(i0 + r, j0 + c)
+  const long long i0 = (long long)blockIdx.y * 64, j0 = (long long)blockIdx.x * 64;
+  // stored orientation of this tile: (i, j) with i >= j (lower) or i <= j (upper) is read directly
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+    // direct entries: consecutive threads walk r (contiguous in a column of the storage)
+    const int r = idx & 63, c = idx >> 6;
+    const long long i = i0 + r, j = j0 + c;
+    if (i < n && j < n && (UP ? i <= j : i >= j)) tile[r][c] = a[j * lda + i];
+  }
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+    // mirrored entries: A(i, j) = A(j, i), stored at a[i * lda + j]; consecutive threads walk c
+    const int c = idx & 63, r = idx >> 6;
+    const long long i = i0 + r, j = j0 + c;
+    if (i < n && j < n && !(UP ? i <= j : i >= j)) tile[r][c] = a[i * lda + j];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
+    const int c = idx & 63, r = idx >> 6;
+    const long long i = i0 + r, j = j0 + c;
+    if (i >= n || j >= n) continue;
+    const int e = scale_exp(__longlong_as_double(rmax[i]));
+    float sl[S];
+    split8(ldexp(tile[r][c], -e), sl);
+#pragma unroll
+    for (int p = 0; p < S; ++p) slices[p * sstride + i * lds + j] = __float2bfloat16_rn(sl[p]);
+  }
+}
+
+// Slices of X: one CTA per right-hand side j (column j of X, contiguous): its maximum, the scale
+// exponent f_j (stored in xexp[j]), then slice q of column j at xs + q * xstride + j * ldxs.
+__global__ void __launch_bounds__(256) oz_slice_x_kernel(const double* __restrict__ x, long long ldx, long long n,
+                                                         __nv_bfloat16* __restrict__ xs, long long ldxs,
+                                                         long long xstride, int* __restrict__ xexp,
+                                                         int* __restrict__ flag) {
+  __shared__ double red[256];
+  const long long j = blockIdx.x;
+  const double* col = x + j * ldx;
+  double m = 0.0;
+  int bad = 0;
+  for (long long l = threadIdx.x; l < n; l += 256) {
+    const double v = fabs(col[l]);
+    if (!(v <= 1.7976931348623157e308)) bad = 1;
+    m = fmax(m, v);
+  }
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  const int f = scale_exp(red[0]);
+  if (threadIdx.x == 0) xexp[j] = f;
+  if (bad) atomicOr(flag, 1);
+  for (long long l = threadIdx.x; l < n; l += 256) {
+    float sl[S];
+    split8(ldexp(col[l], -f), sl);
+#pragma unroll
+    for (int q = 0; q < S; ++q) xs[q * xstride + j * ldxs + l] = __float2bfloat16_rn(sl[q]);
+  }
+}
+
+}  // namespace
+
+namespace {
+
+// ---- the product --------------------------------------------------------------------------------
+
+struct OzMaps {
+  CUtensorMap a[S];  // A slices: n rows of n K-elements, box 64 x 128
+  CUtensorMap x[S];  // X slices: nrhs rows of n K-elements, box 64 x 64
+};
+
+struct OzParams {
+  long long n, nrhs;
+  const unsigned long long* rmax;  // per-row |A| maxima (bit patterns)
+  const int* xexp;                 // per-column scale exponents of X
+  const int* flag;                 // [0]: A holds a non-finite value, [1]: X does
+  const double* b;
+  long long ldb;
+  double* r;
+  long long ldr;
+  int* err;                        // set to 1 when a bounded wait ran out
+};
+
+__global__ void __launch_bounds__(THREADS, 1) oz_gemm_kernel(const __grid_constant__ OzMaps maps, const OzParams p) {
+  extern __shared__ uint8_t oz_smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)oz_smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* a_ring = smem;                           // A_STAGES x 16 KB
+  uint8_t* x_buf = smem + A_STAGES * A_BYTES;       // 2 x (8 x 8 KB)
+  __shared__ __align__(8) uint64_t afull[A_STAGES], aempty[A_STAGES];
+  __shared__ __align__(8) uint64_t xfull[2], xempty[2];
+  __shared__ __align__(8) uint64_t tfull, tempty;
+  __shared__ uint32_t tmem_base_s;
+  __shared__ volatile int abort_s;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long row0 = (long long)blockIdx.x * BM, col0 = (long long)blockIdx.y * BN;
+  const int nkb = (int)((p.n + KB - 1) / KB);
+  const int nchunks = (nkb + KC_BLOCKS - 1) / KC_BLOCKS;
+
+  if (threadIdx.x == 0) {
+    abort_s = 0;
+    for (int s = 0; s < A_STAGES; ++s) {
+      mbar_init(&afull[s], 1);
+      mbar_init(&aempty[s], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&xfull[i], 1);
+      mbar_init(&xempty[i], 1);
+    }
+    mbar_init(&tfull, 1);
+    mbar_init(&tempty, EPI_WARPS);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_s;
+
+  if (warp == 0 && lane == 0) {
+    // ---- TMA producer: per K block, the 8 X slice tiles (double-buffered), then the 8 A slice
+    // tiles through the A ring
+    long long issued_a = 0;
+    int issued_x = 0;
+    for (int kb = 0; kb < nkb && !abort_s; ++kb) {
+      const int xb = kb & 1;
+      if (!mbar_wait(&xempty[xb], ((uint32_t)(kb >> 1) & 1u) ^ 1u, &abort_s)) break;
+      mbar_expect_tx(&xfull[xb], X_SET);
+      for (int q = 0; q < S; ++q)
+        tma_load_2d(x_buf + xb * X_SET + q * X_BYTES, &maps.x[q], &xfull[xb], kb * KB, (int)col0);
+      issued_x = kb + 1;
+      bool ok = true;
+      for (int sp = 0; sp < S; ++sp) {
+        const long long it = (long long)kb * S + sp;
+        const int st = (int)(it % A_STAGES);
+        if (!mbar_wait(&aempty[st], ((uint32_t)(it / A_STAGES) & 1u) ^ 1u, &abort_s)) { ok = false; break; }
+        mbar_expect_tx(&afull[st], A_BYTES);
+        tma_load_2d(a_ring + st * A_BYTES, &maps.a[sp], &afull[st], kb * KB, (int)row0);
+        issued_a = it + 1;
+      }
+      if (!ok) break;
+    }
+    if (abort_s) {
+      // let the copies this thread started land before the CTA exits (bounded)
+      volatile int dummy = 0;
+      for (long long i = issued_a - A_STAGES < 0 ? 0 : issued_a - A_STAGES; i < issued_a; ++i)
+        mbar_wait(&afull[i % A_STAGES], (uint32_t)(i / A_STAGES) & 1u, &dummy);
+      for (int k = issued_x - 2 < 0 ? 0 : issued_x - 2; k < issued_x; ++k)
+        mbar_wait(&xfull[k & 1], (uint32_t)(k >> 1) & 1u, &dummy);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer: pairs (p, q) with p + q <= S - 1 (0-based) into accumulator w = p + q
+    constexpr uint32_t idesc = instr_desc_mn(1u, BM, BN);
+    bool ok = true;
+    for (int kb = 0; kb < nkb && ok; ++kb) {
+      const int chunk = kb / KC_BLOCKS;
+      const bool first = (kb % KC_BLOCKS) == 0;
+      if (first && chunk > 0) {  // the epilogue has taken the previous chunk's sums out of TMEM
+        if (!mbar_wait(&tempty, (uint32_t)(chunk - 1) & 1u, &abort_s)) break;
+        tc_fence_after();
+      }
+      const int xb = kb & 1;
+      if (!mbar_wait(&xfull[xb], (uint32_t)(kb >> 1) & 1u, &abort_s)) break;
+      tc_fence_after();
+      const uint32_t xs0 = smem_u32(x_buf + xb * X_SET);
+      for (int sp = 0; sp < S; ++sp) {
+        const long long it = (long long)kb * S + sp;
+        const int st = (int)(it % A_STAGES);
+        if (!mbar_wait(&afull[st], (uint32_t)(it / A_STAGES) & 1u, &abort_s)) { ok = false; break; }
+        tc_fence_after();
+        const uint64_t ad = sw128_desc(smem_u32(a_ring + st * A_BYTES));
+        for (int q = 0; q + sp < S; ++q) {
+          const uint64_t bd = sw128_desc(xs0 + q * X_BYTES);
+          const uint32_t d = tmem + (uint32_t)((sp + q) * BN);
+#pragma unroll
+          for (int j = 0; j < KB / 16; ++j)  // 32 bytes along K per MMA: +2 in the (addr >> 4) field
+            mma<0>(d, ad + 2 * j, bd + 2 * j, idesc, (first && sp == 0 && j == 0) ? 0u : 1u);
+        }
+        mma_commit(&aempty[st]);
+      }
+      if (!ok) break;
+      mma_commit(&xempty[xb]);
+      if ((kb % KC_BLOCKS) == KC_BLOCKS - 1 || kb == nkb - 1) mma_commit(&tfull);
+    }
+  } else if (warp >= 2) {
+    // ---- epilogue: per chunk, the 8 weight accumulators of this thread's row and 16 columns into
+    // two int64 fixed-point sums; at the end R = B - 2^(e_i + f_j) (hi 2^-35 + lo 2^-63)
+    const int quad = warp & 3;                  // TMEM lane quadrant this warp may access
+    const int part = (warp - 2) >> 2;           // which 16 of the 64 columns
+    const int r = quad * 32 + lane;             // tile row
+    long long hi[16], lo[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      hi[c] = 0;
+      lo[c] = 0;
+    }
+    bool ok = true;
+    for (int chunk = 0; chunk < nchunks; ++chunk) {
+      if (!mbar_wait(&tfull, (uint32_t)chunk & 1u, &abort_s)) { ok = false; break; }
+      tc_fence_after();
+      const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(part * 16);
+#pragma unroll
+      for (int w = 0; w < S; ++w) {
+        float v[16];
+        tmem_ld16(base + (uint32_t)(w * BN), v);
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const long long P = (long long)__float2int_rn(v[c]);  // an exact integer below 2^24
+          if (w < 4) hi[c] += P * (1ll << (BETA * (3 - w)));
+          else lo[c] += P * (1ll << (BETA * (7 - w)));
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty);
+    }
+    if (ok) {
+      const long long i = row0 + r;
+      if (i < p.n) {
+        const int e = scale_exp(__longlong_as_double(p.rmax[i]));
+        const bool bad = (p.flag[0] | p.flag[1]) != 0;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const long long j = col0 + part * 16 + c;
+          if (j < p.nrhs) {
+            const double ax = ldexp(ldexp((double)hi[c], -35) + ldexp((double)lo[c], -63), e + p.xexp[j]);
+            p.r[j * p.ldr + i] = bad ? __longlong_as_double(0x7ff8000000000000ll) : p.b[j * p.ldb + i] - ax;
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0 && abort_s) atomicExch(p.err, 1);
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+}  // namespace
+
+// ---- host driver --------------------------------------------------------------------------------
+
+namespace {
+
+// Per-device setup of the product kernel's shared-memory size, once, under a lock.
+int oz_prepare_device() {
+  static std::mutex mu;
+  static int done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return GBLLT_ERR_NO_DEVICE;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (!done[dev]) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    done[dev] = 1;
+  }
+  return GBLLT_SUCCESS;
+}
+
+inline size_t oz_up256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+OzakiResidual::~OzakiResidual() {
+  if (buf) cudaFreeAsync(buf, stream);
+}
+
+size_t OzakiResidual::bytes(int64_t n, int64_t nrhs) {
+  const int64_t lds = (n + 7) / 8 * 8;  // 16-byte row pitch for TMA
+  return oz_up256((size_t)S * n * lds * 2) + oz_up256((size_t)S * nrhs * lds * 2) + oz_up256((size_t)n * 8) +
+         oz_up256((size_t)nrhs * 4) + 256 + 256;
+}
+
+int OzakiResidual::setup(bool upper, int64_t n_, int64_t nrhs_, const double* a, int64_t lda, cudaStream_t s) {
+  int rc = oz_prepare_device();
+  if (rc) return rc;
+  n = n_;
+  nrhs = nrhs_;
+  stream = s;
+  lds = (n + 7) / 8 * 8;
+  if (dev_malloc_async(&buf, bytes(n, nrhs), s) != cudaSuccess) {
+    cudaGetLastError();
+    buf = nullptr;
+    set_error_message("cudaMallocAsync failed (tensor-core residual slices)");
+    return GBLLT_ERR_ALLOC;
+  }
+  char* q = (char*)buf;
+  aslices = q;
+  q += oz_up256((size_t)S * n * lds * 2);
+  xslices = q;
+  q += oz_up256((size_t)S * nrhs * lds * 2);
+  rmax = (unsigned long long*)q;
+  q += oz_up256((size_t)n * 8);
+  xexp = (int*)q;
+  q += oz_up256((size_t)nrhs * 4);
+  flags = (int*)q;  // [0] A non-finite, [1] X non-finite, [2] timeout
+  GB_CUDA_TRY(cudaMemsetAsync(rmax, 0, (size_t)n * 8, s));
+  GB_CUDA_TRY(cudaMemsetAsync(flags, 0, 16, s));
+  const int64_t t = ceil_div(n, 64);
+  static const std::string ks = "residual_slices_a";
+  {
+    ProfScope ps(ks.c_str(), s, 0.0, (double)n * n * 8.0 + (double)S * n * n * 2.0);
+    if (upper) oz_rowmax_kernel<true><<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(a, lda, n, rmax, flags);
+    else oz_rowmax_kernel<false><<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(a, lda, n, rmax, flags);
+    const dim3 g((unsigned)t, (unsigned)t);
+    __nv_bfloat16* as = (__nv_bfloat16*)aslices;
+    if (upper) oz_slice_a_kernel<true><<<g, 256, 0, s>>>(a, lda, n, rmax, as, lds, (long long)n * lds);
+    else oz_slice_a_kernel<false><<<g, 256, 0, s>>>(a, lda, n, rmax, as, lds, (long long)n * lds);
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+int OzakiResidual::residual(const double* x, int64_t ldx, const double* b, int64_t ldb, double* r, int64_t ldr,
+                            cudaStream_t s) {
+  if (!buf) return GBLLT_ERR_INTERNAL;
+  OzMaps maps;
+  const __nv_bfloat16* as = (const __nv_bfloat16*)aslices;
+  __nv_bfloat16* xs = (__nv_bfloat16*)xslices;
+  for (int i = 0; i < S; ++i) {
+    if (!make_map_2d(&maps.a[i], as + (size_t)i * n * lds, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, n, n, lds, KB, BM) ||
+        !make_map_2d(&maps.x[i], xs + (size_t)i * nrhs * lds, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nrhs, n, lds, KB,
+                     BN)) {
+      set_error_message("cuTensorMapEncodeTiled failed (tensor-core residual)");
+      return GBLLT_ERR_INTERNAL;
+    }
+  }
+  GB_CUDA_TRY(cudaMemsetAsync(flags + 1, 0, 8, s));
+  static const std::string kx = "residual_slices_x";
+  static const std::string kg = "residual_tc";
+  {
+    ProfScope ps(kx.c_str(), s, 0.0, (double)n * nrhs * (8.0 + S * 2.0));
+    oz_slice_x_kernel<<<(unsigned)nrhs, 256, 0, s>>>(x, ldx, n, xs, lds, (long long)nrhs * lds, xexp, flags);
+  }
+  OzParams p;
+  p.n = n;
+  p.nrhs = nrhs;
+  p.rmax = rmax;
+  p.xexp = xexp;
+  p.flag = flags;
+  p.b = b;
+  p.ldb = ldb;
+  p.r = r;
+  p.ldr = ldr;
+  p.err = flags + 2;
+  const dim3 grid((unsigned)ceil_div(n, BM), (unsigned)ceil_div(nrhs, BN));
+  {
+    // algorithmic work: the FP64 product 2 n^2 nrhs; bytes: the 8 A slices read once per column tile,
+    // X slices, B read and R written
+    ProfScope ps(kg.c_str(), s, 2.0 * n * n * nrhs,
+                 (double)S * n * n * 2.0 * grid.y + (double)S * n * nrhs * 2.0 + 2.0 * n * nrhs * 8.0);
+    oz_gemm_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(maps, p);
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+int OzakiResidual::timeout_flag_into(int* host_flag, cudaStream_t s) const {
+  GB_CUDA_TRY(cudaMemcpyAsync(host_flag, flags + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+  return GBLLT_SUCCESS;
+}
+
+}  // namespace gbllt

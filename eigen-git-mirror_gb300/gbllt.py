@@ -86,6 +86,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_strsm": (_int, [_int, _ch, _ch, _ch, _ch, _i64, _i64, ctypes.c_float, _vp, _i64, _vp, _i64]),
     "gbllt_dtrsm_dev": (_int, [_ch, _ch, _ch, _ch, _i64, _i64, ctypes.c_double, _vp, _i64, _vp, _i64, _vp]),
     "gbllt_strsm_dev": (_int, [_ch, _ch, _ch, _ch, _i64, _i64, ctypes.c_float, _vp, _i64, _vp, _i64, _vp]),
+    "gbllt_dsyresid_dev": (_int, [_ch, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _int, _vp]),
     "gbllt_dlansy_l1_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
     "gbllt_slansy_l1_dev": (_int, [_ch, _i64, _vp, _i64, _vp, _vp]),
     "gbllt_dpocon_dev": (_int, [_ch, _i64, _vp, _i64, ctypes.c_double, _dp, _vp]),
@@ -109,7 +110,8 @@ PREC = {"fp32": 0, "tf32": 1, "tf32x3": 2, "bf16": 3, "bf16x3": 4, "bf16x6": 5}
 
 class MixedOpts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("max_steps", ctypes.c_int), ("tol", ctypes.c_double),
-                ("fallback_fp64", ctypes.c_int), ("panel", ctypes.c_int), ("reserve_sms", ctypes.c_int)]
+                ("fallback_fp64", ctypes.c_int), ("panel", ctypes.c_int), ("reserve_sms", ctypes.c_int),
+                ("residual", ctypes.c_int)]
 
 
 class MixedReport(ctypes.Structure):
@@ -125,9 +127,13 @@ class MixedReport(ctypes.Structure):
                 "history": [float(self.history[i]) for i in range(min(int(self.steps), 16))]}
 
 
+RESIDUAL = {"tensor": 0, "fp64": 1}
+
+
 def mixed_opts(precision: str = "tf32x3", max_steps: int = 10, tol: float = 1e-14, fallback: bool = True,
-               panel: int = 256, reserve_sms: int = 0) -> MixedOpts:
-    return MixedOpts(PREC[precision], max_steps, tol, 1 if fallback else 0, panel, reserve_sms)
+               panel: int = 256, reserve_sms: int = 0, residual: str = "tensor") -> MixedOpts:
+    return MixedOpts(PREC[precision], max_steps, tol, 1 if fallback else 0, panel, reserve_sms,
+                     RESIDUAL[residual])
 
 
 class GblltError(RuntimeError):

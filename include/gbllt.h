@@ -117,7 +117,25 @@ typedef struct {
   int panel;         /* outer panel width, a multiple of 64; <= 0 -> 256 */
   int reserve_sms;   /* SMs left to the panel factorisation while the look-ahead update runs on the
                         others: 0 -> library default, < 0 -> none (the update may use every SM) */
+  int residual;      /* how R = B - A X is formed: GBLLT_RESIDUAL_TENSOR (0, default) or
+                        GBLLT_RESIDUAL_FP64 */
 } gbllt_mixed_opts;
+
+/* Residual methods.  TENSOR: A and X are split exactly into eight 7-bit BF16 slices (per-row and
+ * per-column power-of-two scales) and the slice products run on the tensor cores with exact FP32
+ * accumulation in 256-deep chunks and exact int64 combination; the result differs from the exact
+ * B - A X by less than 2^-56 of the scaled magnitudes, i.e. at the FP64 rounding level.  It needs
+ * n^2 * 16 bytes of device memory for A's slices (the no-allocation entry uses FP64).  FP64: the
+ * product on the FP64 pipe. */
+#define GBLLT_RESIDUAL_TENSOR 0
+#define GBLLT_RESIDUAL_FP64 1
+
+/* R = B - A X for the symmetric A stored in the `uplo` triangle of d_a (column-major n x n), X, B
+ * and R n x nrhs column-major, with one of the residual methods above; the residual that LAPACK's
+ * dsposv forms with dsymm.  Stream-ordered; R may not overlap A, X or B. */
+GBLLT_API int gbllt_dsyresid_dev(char uplo, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
+                                 const double* d_x, int64_t ldx, const double* d_b, int64_t ldb, double* d_r,
+                                 int64_t ldr, int method, void* stream);
 
 typedef struct {
   int64_t info;          /* LAPACK info of the factorisation that produced X (0 = ok) */

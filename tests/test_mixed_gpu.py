@@ -65,12 +65,13 @@ def test_mixed_refines_to_fp64(oracle, gbllt, spectra, kappa, prec):
 
 
 @pytest.mark.parametrize("n", [1, 7, 64, 200, 257, 300, 700])
-@pytest.mark.parametrize("nrhs", [1, 3, 17])
-def test_mixed_sizes(oracle, gbllt, n, nrhs):
+@pytest.mark.parametrize("nrhs", [1, 3, 17, 70])
+@pytest.mark.parametrize("residual", ["tensor", "fp64"])
+def test_mixed_sizes(oracle, gbllt, n, nrhs, residual):
     pytest.importorskip("torch")
     a = oracle.gen_gram(n, seed=60 + n)
     b = np.asfortranarray(oracle.normal(61, n * nrhs).reshape(n, nrhs, order="F"))
-    rc, rep, x = _dev_solve(gbllt, a, b, gbllt.mixed_opts("tf32x3", 10, 1e-14, fallback=False))
+    rc, rep, x = _dev_solve(gbllt, a, b, gbllt.mixed_opts("tf32x3", 10, 1e-14, fallback=False, residual=residual))
     assert rc == gbllt.SUCCESS and rep["converged"], rep
     assert oracle.backward_error(a, x, b) <= 1e-14
 
