@@ -528,6 +528,11 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   OzakiResidual oz;
   bool use_oz = may_allocate && o.residual == GBLLT_RESIDUAL_TENSOR;
   auto residual = [&]() -> int {  // R = B - A X
+    if (use_oz && !oz.buf) {  // A's slices, made once, at the first residual
+      const int rc2 = oz.setup(upper, n, nrhs, a, lda, s);
+      if (rc2 == GBLLT_ERR_ALLOC) use_oz = false;  // not enough device memory: the FP64 residual
+      else if (rc2) return rc2;
+    }
     if (use_oz) return oz.residual(x, ldx, b, ldb, R, n, s);
     symm_residual_fp64(upper, n, nrhs, a, lda, x, ldx, b, ldb, R, n, part, nparts, jpc, s);
     return GBLLT_SUCCESS;
@@ -580,11 +585,6 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   r.factor_ms = elapsed(0, 1);
 
   bool ok = false;
-  if (r.info == 0 && use_oz) {
-    rc = oz.setup(upper, n, nrhs, a, lda, s);
-    if (rc == GBLLT_ERR_ALLOC) use_oz = false;  // not enough device memory for the slices: FP64 residual
-    else if (rc) return rc;
-  }
   if (r.info == 0) {
     // 3. refinement: x_0 = 0, r_0 = b
     sumsq(a, lda, n, n, upper ? 2 : 1, &norms[0]);
