@@ -127,6 +127,7 @@ struct OzakiResidual {
   void* aslices = nullptr;
   void* xslices = nullptr;
   unsigned long long* rmax = nullptr;
+  int* rexp = nullptr;
   int* xexp = nullptr;
   int* flags = nullptr;
   OzakiResidual() = default;

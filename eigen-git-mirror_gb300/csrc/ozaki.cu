@@ -100,15 +100,43 @@ __device__ __forceinline__ int scale_exp(double m) {
   return e;
 }
 
-// The 8 slices of a value already scaled into (-1, 1); each is an integer of at most 8 bits.
-__device__ __forceinline__ void split8(double t, float* sl) {
+// The 8 slices of v / 2^e (|v| < 2^e) in integer arithmetic on v's bit pattern (the FP64 pipe of
+// GB300 is too slow to spend on this): N = round(v 2^(56 - e)) as an int64, then balanced base-128
+// digits from the top, s_1 = round(N / 2^49), s_2 = round((N - s_1 2^49) / 2^42), ..., each digit
+// rounded to nearest so that |s_1| <= 128 and |s_p| <= 64 (p > 1).  What falls below 2^-56 is
+// rounded away.
+__device__ __forceinline__ void split8(double v, int e, float* sl) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int E = (int)((bits >> 52) & 0x7FF);
+  unsigned long long M = bits & 0xFFFFFFFFFFFFFull;
+  int ex;
+  if (E == 0) {
+    ex = -1074;  // subnormal
+  } else {
+    M |= 1ull << 52;
+    ex = E - 1075;
+  }
+  // |v| = M 2^ex, and N = M 2^(ex + 56 - e), |N| < 2^56
+  const int sh = ex + 56 - e;
+  long long N;
+  if (E == 0x7FF) N = 0;  // non-finite: reported through the flag, not the slices
+  else if (sh >= 0) N = (long long)(M << (sh > 3 ? 3 : sh));
+  else if (sh > -64) N = (long long)((M + (1ull << (-sh - 1))) >> (-sh));
+  else N = 0;
+  if (bits >> 63) N = -N;
 #pragma unroll
   for (int p = 0; p < S; ++p) {
-    t *= (double)(1 << BETA);
-    const double q = rint(t);
-    t -= q;
-    sl[p] = (float)q;
+    const int k = BETA * (S - 1 - p);  // 49, 42, ..., 0
+    const long long d = k ? ((N + (1ll << (k - 1))) >> k) : N;  // nearest (ties up), arithmetic shift
+    N -= d * (1ll << k);
+    sl[p] = (float)d;
   }
+}
+
+// Scale exponent of every row from its maximum (one thread per row).
+__global__ void oz_rowexp_kernel(const unsigned long long* __restrict__ rmax, long long n, int* __restrict__ rexp) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) rexp[i] = scale_exp(__longlong_as_double(rmax[i]));
 }
 
 // Slices of the full symmetric A, row-major (row i holds its n entries contiguously: the K-major
@@ -117,7 +145,7 @@ __device__ __forceinline__ void split8(double t, float* sl) {
 // needed) through shared memory so that reads and writes are both coalesced.
 template <bool UP>
 __global__ void __launch_bounds__(256) oz_slice_a_kernel(const double* __restrict__ a, long long lda, long long n,
-                                                         const unsigned long long* __restrict__ rmax,
+                                                         const int* __restrict__ rexp,
                                                          __nv_bfloat16* __restrict__ slices, long long lds,
                                                          long long sstride) {
   __shared__ double tile[64][65];  // tile[r][c] = A(i0 + r, j0 + c)
@@ -140,9 +168,8 @@ __global__ void __launch_bounds__(256) oz_slice_a_kernel(const double* __restric
     const int c = idx & 63, r = idx >> 6;
     const long long i = i0 + r, j = j0 + c;
     if (i >= n || j >= n) continue;
-    const int e = scale_exp(__longlong_as_double(rmax[i]));
     float sl[S];
-    split8(ldexp(tile[r][c], -e), sl);
+    split8(tile[r][c], rexp[i], sl);
 #pragma unroll
     for (int p = 0; p < S; ++p) slices[p * sstride + i * lds + j] = __float2bfloat16_rn(sl[p]);
   }
@@ -175,7 +202,7 @@ __global__ void __launch_bounds__(256) oz_slice_x_kernel(const double* __restric
   if (bad) atomicOr(flag, 1);
   for (long long l = threadIdx.x; l < n; l += 256) {
     float sl[S];
-    split8(ldexp(col[l], -f), sl);
+    split8(col[l], f, sl);
 #pragma unroll
     for (int q = 0; q < S; ++q) xs[q * xstride + j * ldxs + l] = __float2bfloat16_rn(sl[q]);
   }
@@ -194,7 +221,7 @@ struct OzMaps {
 
 struct OzParams {
   long long n, nrhs;
-  const unsigned long long* rmax;  // per-row |A| maxima (bit patterns)
+  const int* rexp;                 // per-row scale exponents of A
   const int* xexp;                 // per-column scale exponents of X
   const int* flag;                 // [0]: A holds a non-finite value, [1]: X does
   const double* b;
@@ -345,7 +372,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_gemm_kernel(const __grid_consta
     if (ok) {
       const long long i = row0 + r;
       if (i < p.n) {
-        const int e = scale_exp(__longlong_as_double(p.rmax[i]));
+        const int e = p.rexp[i];
         const bool bad = (p.flag[0] | p.flag[1]) != 0;
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
@@ -401,7 +428,7 @@ OzakiResidual::~OzakiResidual() {
 size_t OzakiResidual::bytes(int64_t n, int64_t nrhs) {
   const int64_t lds = (n + 7) / 8 * 8;  // 16-byte row pitch for TMA
   return oz_up256((size_t)S * n * lds * 2) + oz_up256((size_t)S * nrhs * lds * 2) + oz_up256((size_t)n * 8) +
-         oz_up256((size_t)nrhs * 4) + 256 + 256;
+         oz_up256((size_t)n * 4) + oz_up256((size_t)nrhs * 4) + 256 + 256;
 }
 
 int OzakiResidual::setup(bool upper, int64_t n_, int64_t nrhs_, const double* a, int64_t lda, cudaStream_t s) {
@@ -424,6 +451,8 @@ int OzakiResidual::setup(bool upper, int64_t n_, int64_t nrhs_, const double* a,
   q += oz_up256((size_t)S * nrhs * lds * 2);
   rmax = (unsigned long long*)q;
   q += oz_up256((size_t)n * 8);
+  rexp = (int*)q;
+  q += oz_up256((size_t)n * 4);
   xexp = (int*)q;
   q += oz_up256((size_t)nrhs * 4);
   flags = (int*)q;  // [0] A non-finite, [1] X non-finite, [2] timeout
@@ -435,10 +464,11 @@ int OzakiResidual::setup(bool upper, int64_t n_, int64_t nrhs_, const double* a,
     ProfScope ps(ks.c_str(), s, 0.0, (double)n * n * 8.0 + (double)S * n * n * 2.0);
     if (upper) oz_rowmax_kernel<true><<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(a, lda, n, rmax, flags);
     else oz_rowmax_kernel<false><<<(unsigned)(t * (t + 1) / 2), 256, 0, s>>>(a, lda, n, rmax, flags);
+    oz_rowexp_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(rmax, n, rexp);
     const dim3 g((unsigned)t, (unsigned)t);
     __nv_bfloat16* as = (__nv_bfloat16*)aslices;
-    if (upper) oz_slice_a_kernel<true><<<g, 256, 0, s>>>(a, lda, n, rmax, as, lds, (long long)n * lds);
-    else oz_slice_a_kernel<false><<<g, 256, 0, s>>>(a, lda, n, rmax, as, lds, (long long)n * lds);
+    if (upper) oz_slice_a_kernel<true><<<g, 256, 0, s>>>(a, lda, n, rexp, as, lds, (long long)n * lds);
+    else oz_slice_a_kernel<false><<<g, 256, 0, s>>>(a, lda, n, rexp, as, lds, (long long)n * lds);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
@@ -468,7 +498,7 @@ int OzakiResidual::residual(const double* x, int64_t ldx, const double* b, int64
   OzParams p;
   p.n = n;
   p.nrhs = nrhs;
-  p.rmax = rmax;
+  p.rexp = rexp;
   p.xexp = xexp;
   p.flag = flags;
   p.b = b;
