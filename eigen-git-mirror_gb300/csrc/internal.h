@@ -19,6 +19,8 @@ int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t 
 // Diagonal 64 x 64 block at (k0, k0): storage T, arithmetic TC.
 template <typename T, typename TC>
 void launch_potrf_diag(T* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s);
+// FP32 diagonal block in FP32 arithmetic, one warp (the mixed-precision factorisation).
+void launch_potrf_diag_f32w(float* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s);
 // Rows below the block: A(k0+bs.., k0..k0+bs) <- A(...) L11^{-T}, rs rows.
 template <typename T>
 void launch_trsm_panel(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, cudaStream_t s);

@@ -6,14 +6,15 @@
 //   1. scales A symmetrically to unit diagonal (D A D, D = diag(a_ii)^-1/2, Higham & Pranesh 2021)
 //      and rounds the scaled lower triangle to an FP32 working matrix;
 //   2. factors it with the blocked right-looking algorithm of llt_inplace::blocked (LLT.h:338-368)
-//      in two levels: panels of width `panel` are factored in 64-column steps (diagonal blocks in
-//      FP64 arithmetic, the panel TRSM on FP32 cores, its result split into tensor-core operands
-//      for the in-panel update on tcgen05), and the trailing SYRK of each panel
+//      in two levels: panels of width `panel` are factored in 64-column steps (diagonal blocks by
+//      one warp in FP32 registers, the panel TRSM on FP32 cores, its result split into tensor-core
+//      operands for the in-panel update on tcgen05), and the trailing SYRK of each panel
 //      -- almost all of the n^3/3 flops -- runs on tcgen05 tensor cores in TF32 or BF16 (optionally
 //      as split-precision products) with FP32 accumulation, one panel ahead on a second stream;
-//   3. refines in FP64: r = b - A x (FP64, reading only the stored triangle of A), solve with the
-//      FP32 factor, x += d, until ||r||_F / (||A||_F ||x||_F) <= tol (LAPACK dsposv-style
-//      refinement, with the FP64 GPU factorisation as fallback).
+//   3. refines in FP64: r = b - A x (reading only the stored triangle of A; on the FP64 pipe, or for
+//      four or more right-hand sides on the tensor cores with FP64-exact error-free slicing,
+//      ozaki.cu), solve with the FP32 factor, x += d, until ||r||_F / (||A||_F ||x||_F) <= tol
+//      (LAPACK dsposv-style refinement, with the FP64 GPU factorisation as fallback).
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -352,7 +353,7 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
       const int jb = (int)(k0 + bs - j0 < kNB ? k0 + bs - j0 : kNB);
       const int64_t below = n - j0 - jb;
       const int64_t cols_left = k0 + bs - (j0 + jb);
-      launch_potrf_diag<float, double>(af, ldf, j0, jb, st, s);
+      launch_potrf_diag_f32w(af, ldf, j0, jb, st, s);
       launch_trsm_panel<float>(af, ldf, j0, jb, below, st, s);
       if (prec == GBLLT_PREC_FP32) {
         if (cols_left > 0 || rs > 0) launch_syrk_lower<float>(af, ldf, j0, jb, below, below, st, s);
@@ -437,7 +438,9 @@ int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o) {
   }
   if (o->reserve_sms == 0) o->reserve_sms = kDefaultReserveSms;
   if (o->precision < GBLLT_PREC_FP32 || o->precision > GBLLT_PREC_BF16X6) return -1;
-  if (o->residual != GBLLT_RESIDUAL_TENSOR && o->residual != GBLLT_RESIDUAL_FP64) return -1;
+  if (o->residual != GBLLT_RESIDUAL_AUTO && o->residual != GBLLT_RESIDUAL_TENSOR &&
+      o->residual != GBLLT_RESIDUAL_FP64)
+    return -1;
   if (o->panel % kNB != 0) return -1;
   return 0;
 }
@@ -526,7 +529,8 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   };
   // the residual on the tensor cores needs A's slices (n^2 * 16 bytes): only where allocating is allowed
   OzakiResidual oz;
-  bool use_oz = may_allocate && o.residual == GBLLT_RESIDUAL_TENSOR;
+  bool use_oz = may_allocate && (o.residual == GBLLT_RESIDUAL_TENSOR ||
+                                 (o.residual == GBLLT_RESIDUAL_AUTO && nrhs >= GBLLT_RESIDUAL_TENSOR_MIN_RHS));
   auto residual = [&]() -> int {  // R = B - A X
     if (use_oz && !oz.buf) {  // A's slices, made once, at the first residual
       const int rc2 = oz.setup(upper, n, nrhs, a, lda, s);
@@ -701,13 +705,14 @@ extern "C" int gbllt_dsyresid_dev(char uplo, int64_t n, int64_t nrhs, const doub
   if (ldb < (n > 1 ? n : 1)) return -9;
   if (n > 0 && nrhs > 0 && !d_r) return -10;
   if (ldr < (n > 1 ? n : 1)) return -11;
-  if (method != GBLLT_RESIDUAL_TENSOR && method != GBLLT_RESIDUAL_FP64) return -12;
+  if (method != GBLLT_RESIDUAL_AUTO && method != GBLLT_RESIDUAL_TENSOR && method != GBLLT_RESIDUAL_FP64) return -12;
   if (n == 0 || nrhs == 0) return GBLLT_SUCCESS;
   int rc = ensure_device();
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   const bool upper = uplo == 'U' || uplo == 'u';
-  if (method == GBLLT_RESIDUAL_TENSOR) {
+  if (method == GBLLT_RESIDUAL_TENSOR ||
+      (method == GBLLT_RESIDUAL_AUTO && nrhs >= GBLLT_RESIDUAL_TENSOR_MIN_RHS)) {
     OzakiResidual oz;
     if ((rc = oz.setup(upper, n, nrhs, d_a, lda, s))) return rc;
     return oz.residual(d_x, ldx, d_b, ldb, d_r, ldr, s);

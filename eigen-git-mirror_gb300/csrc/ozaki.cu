@@ -164,14 +164,37 @@ __global__ void __launch_bounds__(256) oz_slice_a_kernel(const double* __restric
     if (i < n && j < n && !(UP ? i <= j : i >= j)) tile[r][c] = a[i * lda + j];
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < 64 * 64; idx += 256) {
-    const int c = idx & 63, r = idx >> 6;
-    const long long i = i0 + r, j = j0 + c;
+  // each thread: 8 consecutive columns of one row, written as one 16-byte vector per slice
+  for (int idx = threadIdx.x; idx < 64 * 8; idx += 256) {
+    const int c8 = (idx & 7) * 8, r = idx >> 3;
+    const long long i = i0 + r, j = j0 + c8;
     if (i >= n || j >= n) continue;
-    float sl[S];
-    split8(tile[r][c], rexp[i], sl);
+    const int e = rexp[i];
+    if (j + 8 <= n) {
+      uint32_t packed[S][4];
 #pragma unroll
-    for (int p = 0; p < S; ++p) slices[p * sstride + i * lds + j] = __float2bfloat16_rn(sl[p]);
+      for (int h = 0; h < 4; ++h) {
+        float lo[S], hi[S];
+        split8(tile[r][c8 + 2 * h], e, lo);
+        split8(tile[r][c8 + 2 * h + 1], e, hi);
+#pragma unroll
+        for (int p = 0; p < S; ++p) {
+          const __nv_bfloat162 v2 = __floats2bfloat162_rn(lo[p], hi[p]);
+          packed[p][h] = *reinterpret_cast<const uint32_t*>(&v2);
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < S; ++p)
+        *reinterpret_cast<uint4*>(slices + p * sstride + i * lds + j) =
+            make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
+    } else {
+      for (int cc = 0; cc < 8 && j + cc < n; ++cc) {
+        float sl[S];
+        split8(tile[r][c8 + cc], e, sl);
+#pragma unroll
+        for (int p = 0; p < S; ++p) slices[p * sstride + i * lds + j + cc] = __float2bfloat16_rn(sl[p]);
+      }
+    }
   }
 }
 

@@ -28,6 +28,56 @@ namespace {
 
 constexpr int NB = kNB;
 
+// FP32 diagonal block of the mixed-precision factorisation in one warp, without block barriers: lane
+// l holds rows l and l + 32 of the block in registers (the loops are unrolled, so every index is a
+// compile-time constant); the pivot and each column of L are broadcast with shuffles.  Column j:
+// d = A(j, j) (the pivot test of LLT.h:329, `x <= 0` fails), L(i, j) = A(i, j) / sqrt(d) through
+// one IEEE reciprocal, then the rank-1 update of the later columns.  Entries above the diagonal are
+// updated too (it costs nothing to leave them) but are never read as L and never written back.
+__global__ void __launch_bounds__(32) potrf_diag_f32w_kernel(float* __restrict__ a, long long lda, long long k0,
+                                                             int bs, DevStatus* __restrict__ st) {
+  if (st->fail_col >= 0) return;
+  const int l = threadIdx.x;
+  float* blk = a + k0 * lda + k0;
+  float r0[NB], r1[NB];  // rows l and l + 32
+#pragma unroll
+  for (int c = 0; c < NB; ++c) {
+    r0[c] = (c <= l && l < bs) ? blk[(long long)c * lda + l] : 0.f;
+    r1[c] = (c <= l + 32 && l + 32 < bs && c < bs) ? blk[(long long)c * lda + l + 32] : 0.f;
+  }
+  int fail = -1;
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    if (j < bs && fail < 0) {
+      const float d = __shfl_sync(0xffffffffu, j < 32 ? r0[j] : r1[j], j & 31);
+      if (!(d > 0.f)) {
+        fail = j;
+      } else {
+        const float r = __fsqrt_rn(d);
+        const float inv = __frcp_rn(r);
+        if (j < 32) {
+          r0[j] = (l == j) ? r : r0[j] * inv;
+          r1[j] *= inv;
+        } else {
+          r1[j] = (l + 32 == j) ? r : r1[j] * inv;
+        }
+#pragma unroll
+        for (int k = j + 1; k < NB; ++k) {
+          const float lk = __shfl_sync(0xffffffffu, k < 32 ? r0[j] : r1[j], k & 31);  // L(k, j)
+          if (k < 32) r0[k] = fmaf(-r0[j], lk, r0[k]);
+          r1[k] = fmaf(-r1[j], lk, r1[k]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < NB; ++c) {
+    if (c <= l && l < bs) blk[(long long)c * lda + l] = r0[c];
+    if (c <= l + 32 && l + 32 < bs && c < bs) blk[(long long)c * lda + l + 32] = r1[c];
+  }
+  if (l == 0 && fail >= 0) st->fail_col = k0 + fail;
+}
+
 // T = storage type, TC = arithmetic type (the mixed-precision path stores float and factors the
 // diagonal block in double).
 template <typename T, typename TC>
@@ -340,6 +390,12 @@ void launch_potrf_diag(T* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cud
   ProfScope ps(kd.c_str(), s, (double)bs * bs * bs / 3.0, (double)bs * (bs + 1) * sizeof(T));
   if (sizeof(TC) == 8) potrf_diag_f64_kernel<T><<<1, 512, 0, s>>>(a, lda, k0, bs, st);
   else potrf_diag_kernel<T, TC><<<1, 256, 0, s>>>(a, lda, k0, bs, st);
+}
+
+void launch_potrf_diag_f32w(float* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s) {
+  static const std::string kd = "potrf_diag_f32";
+  ProfScope ps(kd.c_str(), s, (double)bs * bs * bs / 3.0, (double)bs * (bs + 1) * sizeof(float));
+  potrf_diag_f32w_kernel<<<1, 32, 0, s>>>(a, lda, k0, bs, st);
 }
 
 template <typename T>

@@ -127,11 +127,11 @@ class MixedReport(ctypes.Structure):
                 "history": [float(self.history[i]) for i in range(min(int(self.steps), 16))]}
 
 
-RESIDUAL = {"tensor": 0, "fp64": 1}
+RESIDUAL = {"auto": 0, "fp64": 1, "tensor": 2}
 
 
 def mixed_opts(precision: str = "tf32x3", max_steps: int = 10, tol: float = 1e-14, fallback: bool = True,
-               panel: int = 256, reserve_sms: int = 0, residual: str = "tensor") -> MixedOpts:
+               panel: int = 256, reserve_sms: int = 0, residual: str = "auto") -> MixedOpts:
     return MixedOpts(PREC[precision], max_steps, tol, 1 if fallback else 0, panel, reserve_sms,
                      RESIDUAL[residual])
 

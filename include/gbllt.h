@@ -117,8 +117,8 @@ typedef struct {
   int panel;         /* outer panel width, a multiple of 64; <= 0 -> 256 */
   int reserve_sms;   /* SMs left to the panel factorisation while the look-ahead update runs on the
                         others: 0 -> library default, < 0 -> none (the update may use every SM) */
-  int residual;      /* how R = B - A X is formed: GBLLT_RESIDUAL_TENSOR (0, default) or
-                        GBLLT_RESIDUAL_FP64 */
+  int residual;      /* how R = B - A X is formed: GBLLT_RESIDUAL_AUTO (0, default), _FP64 or
+                        _TENSOR */
 } gbllt_mixed_opts;
 
 /* Residual methods.  TENSOR: A and X are split exactly into eight 7-bit BF16 slices (per-row and
@@ -126,9 +126,12 @@ typedef struct {
  * accumulation in 256-deep chunks and exact int64 combination; the result differs from the exact
  * B - A X by less than 2^-56 of the scaled magnitudes, i.e. at the FP64 rounding level.  It needs
  * n^2 * 16 bytes of device memory for A's slices (the no-allocation entry uses FP64).  FP64: the
- * product on the FP64 pipe. */
-#define GBLLT_RESIDUAL_TENSOR 0
+ * product on the FP64 pipe, which is memory-bound for a few right-hand sides.  AUTO: TENSOR for
+ * nrhs >= GBLLT_RESIDUAL_TENSOR_MIN_RHS, FP64 below. */
+#define GBLLT_RESIDUAL_AUTO 0
 #define GBLLT_RESIDUAL_FP64 1
+#define GBLLT_RESIDUAL_TENSOR 2
+#define GBLLT_RESIDUAL_TENSOR_MIN_RHS 4
 
 /* R = B - A X for the symmetric A stored in the `uplo` triangle of d_a (column-major n x n), X, B
  * and R n x nrhs column-major, with one of the residual methods above; the residual that LAPACK's

@@ -66,7 +66,7 @@ def test_mixed_refines_to_fp64(oracle, gbllt, spectra, kappa, prec):
 
 @pytest.mark.parametrize("n", [1, 7, 64, 200, 257, 300, 700])
 @pytest.mark.parametrize("nrhs", [1, 3, 17, 70])
-@pytest.mark.parametrize("residual", ["tensor", "fp64"])
+@pytest.mark.parametrize("residual", ["auto", "tensor", "fp64"])
 def test_mixed_sizes(oracle, gbllt, n, nrhs, residual):
     pytest.importorskip("torch")
     a = oracle.gen_gram(n, seed=60 + n)

@@ -17,7 +17,7 @@ import pytest
 
 import gbllt as G
 
-TENSOR, FP64 = 0, 1
+AUTO, FP64, TENSOR = 0, 1, 2
 
 
 def _sym_full(a):
@@ -55,7 +55,8 @@ def test_residual_argument_errors():
     assert L.gbllt_dsyresid_dev(b"L", 4, 1, 1, 3, 1, 4, 1, 4, 1, 4, 0, None) == -5
     assert L.gbllt_dsyresid_dev(b"L", 4, 1, 1, 4, 1, 4, 1, 4, 1, 2, 0, None) == -11
     assert L.gbllt_dsyresid_dev(b"L", 4, 1, 1, 4, 1, 4, 1, 4, 1, 4, 5, None) == -12
-    assert L.gbllt_dsyresid_dev(b"L", 0, 1, None, 1, None, 1, None, 1, None, 1, 0, None) == 0
+    assert L.gbllt_dsyresid_dev(b"L", 4, 1, 1, 4, 1, 4, 1, 4, 1, 4, -1, None) == -12
+    assert L.gbllt_dsyresid_dev(b"L", 0, 1, None, 1, None, 1, None, 1, None, 1, AUTO, None) == 0
 
 
 @pytest.mark.gpu
