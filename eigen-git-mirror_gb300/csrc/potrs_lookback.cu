@@ -134,15 +134,10 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
   T acc[CPT];
 #pragma unroll
   for (int q = 0; q < CPT; ++q) acc[q] = T(0);
-  // Off-diagonal blocks in the order they become ready.  The last one, the block just before I in
-  // the chain, is taken apart: with W = Dinv (B_I - sum of the others) and M = Dinv L(I, last), both
-  // formed while that block is still being solved, X_I = W - M X_last leaves one 64 x 64 x RCT
-  // product on the chain's critical path instead of two.
+  // off-diagonal blocks in the order they become ready
   const int jfirst = BWD ? nb - 1 : 0;
   const int jstep = BWD ? -1 : 1;
-  const int jlast = I - jstep;
-  const bool has_last = BWD ? (I < nb - 1) : (I > 0);
-  auto load_tile = [&](int J) {  // Ls[p][rr] = coefficient of block J's row p in row rr of block I
+  for (int J = jfirst; J != I; J += jstep) {
     const long long J0 = (long long)J * RB;
     constexpr bool r_fast = (!BWD && !UP) || (BWD && UP);
     for (int idx = tid; idx < RB * RB; idx += 256) {
@@ -154,8 +149,6 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
         v = BWD ? lget<T, UP>(a, lda, J0 + p, I0 + rr) : lget<T, UP>(a, lda, I0 + rr, J0 + p);
       sm.Ls[p][rr] = v;
     }
-  };
-  auto wait_flag = [&](int J) -> bool {  // bounded; ends with a block barrier
     if (tid == 0) {
       const volatile int* f = flags + J;
       const unsigned long long t0 = gtimer();
@@ -169,32 +162,21 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
       __threadfence();
     }
     __syncthreads();
-    return !s_abort;
-  };
-  auto load_y = [&](int J) {  // the solved block J, through L2
-    const long long J0 = (long long)J * RB;
+    if (s_abort) return;
     for (int idx = tid; idx < RB * RCT; idx += 256) {
       const int p = idx & 63, c = idx >> 6;
       sm.Ys[p][c] = (J0 + p < n && c < nrhs) ? __ldcg(b + (long long)c * ldb + J0 + p) : T(0);
     }
-  };
-  if (has_last) {
-    for (int J = jfirst; J != jlast; J += jstep) {
-      load_tile(J);
-      if (!wait_flag(J)) return;
-      load_y(J);
-      __syncthreads();
+    __syncthreads();
 #pragma unroll 4
-      for (int p = 0; p < RB; ++p) {
-        const T l = sm.Ls[p][r];
+    for (int p = 0; p < RB; ++p) {
+      const T l = sm.Ls[p][r];
 #pragma unroll
-        for (int q = 0; q < CPT; ++q) acc[q] = fma(l, sm.Ys[p][cq * CPT + q], acc[q]);
-      }
-      __syncthreads();
+      for (int q = 0; q < CPT; ++q) acc[q] = fma(l, sm.Ys[p][cq * CPT + q], acc[q]);
     }
-    load_tile(jlast);  // needs no flag
+    __syncthreads();
   }
-  // V = B_I - acc, then W = Linv V (forward) or Linv^T V (backward).  The barrier orders the Ds/Bs
+  // V = B_I - acc, then X_I = Linv V (forward) or Linv^T V (backward).  The barrier orders the Ds/Bs
   // preload (written under another thread mapping) before these reads when the J loop ran no pass.
   __syncthreads();
 #pragma unroll
@@ -208,31 +190,6 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
     const T d = BWD ? sm.Ds[p][r] : sm.Ds[r][p];
 #pragma unroll
     for (int q = 0; q < CPT; ++q) x[q] = fma(d, sm.Ys[p][cq * CPT + q], x[q]);
-  }
-  if (has_last) {
-    // M(r, p) = sum_t Dinv(r, t) C(t, p): this thread forms 16 entries of row r
-    const int g = cq * 16;
-    T m[16];
-#pragma unroll
-    for (int pp = 0; pp < 16; ++pp) m[pp] = T(0);
-#pragma unroll 4
-    for (int t = 0; t < RB; ++t) {
-      const T d = BWD ? sm.Ds[t][r] : sm.Ds[r][t];
-#pragma unroll
-      for (int pp = 0; pp < 16; ++pp) m[pp] = fma(d, sm.Ls[g + pp][t], m[pp]);
-    }
-    __syncthreads();  // every read of the tile and of V is done
-#pragma unroll
-    for (int pp = 0; pp < 16; ++pp) sm.Ls[g + pp][r] = m[pp];
-    if (!wait_flag(jlast)) return;  // its barrier also publishes M
-    load_y(jlast);
-    __syncthreads();
-#pragma unroll 4
-    for (int p = 0; p < RB; ++p) {
-      const T mv = sm.Ls[p][r];
-#pragma unroll
-      for (int q = 0; q < CPT; ++q) x[q] = fma(-mv, sm.Ys[p][cq * CPT + q], x[q]);
-    }
   }
 #pragma unroll
   for (int q = 0; q < CPT; ++q) {
