@@ -29,71 +29,51 @@ namespace {
 constexpr int NB = kNB;
 
 // FP32 diagonal block of the mixed-precision factorisation in one warp, without block barriers: lane
-// l holds rows l and l + 32 of the block in registers and the pivot and each column of L are
-// broadcast with shuffles.  Column j: d = A(j, j) (the pivot test of LLT.h:329, `x <= 0` fails),
-// L(i, j) = A(i, j) / sqrt(d) through one IEEE reciprocal, then the rank-1 update of the later
-// columns.  The columns are taken 8 at a time by a loop whose body is unrolled (register indices
-// must be compile-time constants): after each group the finished columns are stored and the
-// register rows shift left by 8, so the same body serves every group and stays in the instruction
-// cache (a fully unrolled 64-column body did not, and stalled on instruction fetch).  Entries above
-// the diagonal are updated too (it costs nothing to leave them) but are never read as L or stored.
+// l holds rows l and l + 32 of the block in registers (the loops are unrolled, so every index is a
+// compile-time constant); the pivot and each column of L are broadcast with shuffles.  Column j:
+// d = A(j, j) (the pivot test of LLT.h:329, `x <= 0` fails), L(i, j) = A(i, j) / sqrt(d) through
+// one IEEE reciprocal, then the rank-1 update of the later columns.  Entries above the diagonal are
+// updated too (it costs nothing to leave them) but are never read as L and never written back.
 __global__ void __launch_bounds__(32) potrf_diag_f32w_kernel(float* __restrict__ a, long long lda, long long k0,
                                                              int bs, DevStatus* __restrict__ st) {
   if (st->fail_col >= 0) return;
-  constexpr int G = 8;
   const int l = threadIdx.x;
   float* blk = a + k0 * lda + k0;
-  float r0[NB], r1[NB];  // rows l and l + 32; index c holds column jb + c
+  float r0[NB], r1[NB];  // rows l and l + 32
 #pragma unroll
   for (int c = 0; c < NB; ++c) {
     r0[c] = (c <= l && l < bs) ? blk[(long long)c * lda + l] : 0.f;
     r1[c] = (c <= l + 32 && l + 32 < bs && c < bs) ? blk[(long long)c * lda + l + 32] : 0.f;
   }
   int fail = -1;
-  for (int jb = 0; jb < bs && fail < 0; jb += G) {
 #pragma unroll
-    for (int jj = 0; jj < G; ++jj) {
-      const int j = jb + jj;
-      if (j < bs && fail < 0) {
-        const float d = __shfl_sync(0xffffffffu, j < 32 ? r0[jj] : r1[jj], j & 31);
-        if (!(d > 0.f)) {
-          fail = j;
+  for (int j = 0; j < NB; ++j) {
+    if (j < bs && fail < 0) {
+      const float d = __shfl_sync(0xffffffffu, j < 32 ? r0[j] : r1[j], j & 31);
+      if (!(d > 0.f)) {
+        fail = j;
+      } else {
+        const float r = __fsqrt_rn(d);
+        const float inv = __frcp_rn(r);
+        if (j < 32) {
+          r0[j] = (l == j) ? r : r0[j] * inv;
+          r1[j] *= inv;
         } else {
-          const float r = __fsqrt_rn(d);
-          const float inv = __frcp_rn(r);
-          r0[jj] = (l == j) ? r : r0[jj] * inv;
-          r1[jj] = (l + 32 == j) ? r : r1[jj] * inv;
+          r1[j] = (l + 32 == j) ? r : r1[j] * inv;
+        }
 #pragma unroll
-          for (int k = jj + 1; k < NB; ++k) {
-            const int kk = jb + k;  // absolute column
-            if (kk < bs) {
-              const float lk = __shfl_sync(0xffffffffu, kk < 32 ? r0[jj] : r1[jj], kk & 31);  // L(kk, j)
-              r0[k] = fmaf(-r0[jj], lk, r0[k]);
-              r1[k] = fmaf(-r1[jj], lk, r1[k]);
-            }
-          }
+        for (int k = j + 1; k < NB; ++k) {
+          const float lk = __shfl_sync(0xffffffffu, k < 32 ? r0[j] : r1[j], k & 31);  // L(k, j)
+          if (k < 32) r0[k] = fmaf(-r0[j], lk, r0[k]);
+          r1[k] = fmaf(-r1[j], lk, r1[k]);
         }
       }
     }
-    // the group's columns are final: store them, then shift the rows left by one group
+  }
 #pragma unroll
-    for (int jj = 0; jj < G; ++jj) {
-      const int j = jb + jj;
-      if (j < bs) {
-        if (j <= l && l < bs) blk[(long long)j * lda + l] = r0[jj];
-        if (j <= l + 32 && l + 32 < bs) blk[(long long)j * lda + l + 32] = r1[jj];
-      }
-    }
-#pragma unroll
-    for (int c = 0; c < NB - G; ++c) {
-      r0[c] = r0[c + G];
-      r1[c] = r1[c + G];
-    }
-#pragma unroll
-    for (int c = NB - G; c < NB; ++c) {
-      r0[c] = 0.f;
-      r1[c] = 0.f;
-    }
+  for (int c = 0; c < NB; ++c) {
+    if (c <= l && l < bs) blk[(long long)c * lda + l] = r0[c];
+    if (c <= l + 32 && l + 32 < bs && c < bs) blk[(long long)c * lda + l + 32] = r1[c];
   }
   if (l == 0 && fail >= 0) st->fail_col = k0 + fail;
 }
