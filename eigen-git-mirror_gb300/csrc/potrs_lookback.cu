@@ -9,8 +9,7 @@
 //   - waits for block J's flag (bounded: 2 s, then an error word is set and the CTA stops), reads
 //     Y_J through L2 (ld.global.cg) and accumulates the tile product;
 //   - applies the pre-inverted diagonal triangle (a 64 x 64 product instead of a 64-step
-//     substitution on the critical path), stores Y_I, and after a block barrier one thread raises its
-//     flag with a GPU-scope release store (the waiting thread polls with acquire loads).
+//     substitution on the critical path), stores Y_I, fences, and raises its flag.
 // The backward sweep runs the same scheme on L^T from the last block up.  Right-hand sides are
 // split into chunks of 16 that run as independent chains in the same launch (grid.y), so the FP64
 // work of the last row blocks is spread over several SMs.
@@ -37,16 +36,6 @@ __device__ __forceinline__ unsigned long long gtimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
-}
-
-__device__ __forceinline__ int ld_acquire(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ void st_release(int* p, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 template <typename T, bool UP>
@@ -161,14 +150,16 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
       sm.Ls[p][rr] = v;
     }
     if (tid == 0) {
+      const volatile int* f = flags + J;
       const unsigned long long t0 = gtimer();
-      while (ld_acquire(flags + J) == 0) {  // acquire: block J's stores are visible after it
+      while (*f == 0) {
         if (gtimer() - t0 > WAIT_NS) {
           s_abort = 1;
           atomicExch(err, 1);
           break;
         }
       }
+      __threadfence();
     }
     __syncthreads();
     if (s_abort) return;
@@ -205,9 +196,9 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
     const int c = cq * CPT + q;
     if (I0 + r < n && c < nrhs) b[(long long)c * ldb + I0 + r] = x[q];
   }
-  // publish: the barrier orders every thread's stores before thread 0's release of the flag
+  __threadfence();
   __syncthreads();
-  if (tid == 0) st_release(flags + I, 1);
+  if (tid == 0) atomicExch(flags + I, 1);
 }
 
 template <typename T, bool UP, bool BWD, int RCT, bool DSCALE>
