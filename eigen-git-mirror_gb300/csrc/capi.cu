@@ -192,6 +192,7 @@ int host_posv(bool do_factor, bool do_solve, int layout, char uplo, int64_t n, i
     GB_CUDA_TRY(cudaMemcpy2DAsync(a, lda * es, d_a, n * es, n * es, n, cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaMemcpyAsync(&h_info, dinfo, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h_info == GBLLT_ERR_TIMEOUT) return GBLLT_ERR_TIMEOUT;
     if (info) *info = h_info;
   }
   if (do_solve && nrhs > 0 && h_info == 0) {

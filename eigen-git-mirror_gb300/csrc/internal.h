@@ -12,8 +12,11 @@ constexpr int kNB = 64;
 
 // Stream-ordered factorisation of the lower triangle of the column-major n x n matrix at
 // d_a (device).  `st` is a device status word, initialised by the caller to fail_col = -1.
+// For T = double and n of at least kTensorSyrkMinN, the trailing updates run on the tensor cores
+// (OzakiSyrk) when may_allocate allows its workspace; otherwise, and for float, on the FP64/FP32 pipe.
+constexpr int64_t kTensorSyrkMinN = 1024;
 template <typename T>
-int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t s);
+int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t s, bool may_allocate = true);
 
 // Kernel launchers of the blocked factorisation, shared with the mixed-precision path.
 // Diagonal 64 x 64 block at (k0, k0): storage T, arithmetic TC.
@@ -141,6 +144,27 @@ struct OzakiResidual {
   int residual(const double* x, int64_t ldx, const double* b, int64_t ldb, double* r, int64_t ldr, cudaStream_t s);
   // copies the device timeout word (1 if a bounded wait of the product kernel ran out) to host memory
   int timeout_flag_into(int* host_flag, cudaStream_t s) const;
+};
+
+// The trailing update A22 -= L21 L21^T of the FP64 factorisation on the BF16 tensor cores, FP64-exact
+// (ozaki.cu): init() allocates the panel slices for panels of up to nmax rows (nmax * 1 KB, stream-
+// ordered) and encodes their tensor maps; update() slices the panel below the diagonal block at
+// (k0, k0) and updates the rs x rs trailing lower triangle.  A bounded wait that runs out sets
+// st->timeout.
+struct OzakiSyrk {
+  int64_t nmax = 0;
+  void* buf = nullptr;
+  void* slices = nullptr;
+  int* pexp = nullptr;
+  void* maps = nullptr;
+  cudaStream_t stream = nullptr;
+  OzakiSyrk() = default;
+  OzakiSyrk(const OzakiSyrk&) = delete;
+  OzakiSyrk& operator=(const OzakiSyrk&) = delete;
+  ~OzakiSyrk();
+  int init(int64_t nmax, cudaStream_t s);
+  int update(double* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, cudaStream_t s);
+  void release_maps();
 };
 
 // Rank-1 update / downdate of the factor at l (device), L L^T + sigma v v^T; *d_info (device)

@@ -644,9 +644,10 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     GB_CUDA_TRY(cudaMemcpy2DAsync(w, n * 8, a, lda * 8, n * 8, n, cudaMemcpyDeviceToDevice, s));
     GB_CUDA_TRY(cudaMemsetAsync(&st->fail_col, 0xFF, sizeof(long long), s));
     if (upper && (rc = transpose_inplace_dev<double>(n, w, n, s))) return rc;
-    if ((rc = potrf_lower_dev<double>(n, w, n, st, s))) return rc;
+    if ((rc = potrf_lower_dev<double>(n, w, n, st, s, may_allocate))) return rc;
     GB_CUDA_TRY(cudaMemcpyAsync(&hst, st, sizeof hst, cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hst.timeout) return GBLLT_ERR_TIMEOUT;
     r.used_fallback = 1;
     if (hst.fail_col >= 0) {
       r.info = hst.fail_col + 1;

@@ -547,3 +547,249 @@ int OzakiResidual::timeout_flag_into(int* host_flag, cudaStream_t s) const {
 }
 
 }  // namespace gbllt
+
+// ---- the trailing update of the FP64 factorisation on the tensor cores ------------------------
+//
+// A22 -= L21 L21^T (lower tiles), L21 the rs x 64 panel below the diagonal block: the same
+// error-free slicing, with one exponent per row of L21 (its maximum), so the product of rows i and j
+// carries 2^(e_i + e_j).  The depth is one panel (64), so a single exact FP32 chunk holds every
+// weight (at most 64 * 2.5 * 2^14 < 2^22) and the epilogue rounds once into FP64.
+
+namespace gbllt {
+
+namespace {
+
+constexpr int PK = 64;                         // panel width = K
+constexpr int SY_A = BM * 128;                 // 16 KB per A slice tile (128 rows)
+constexpr int SY_B = BN * 128;                 // 8 KB per B slice tile (64 rows)
+constexpr int SY_SMEM = S * SY_A + S * SY_B + 1024;
+
+// Slices of the panel L21 (rs x 64, column-major at l21 with leading dimension lda), K-major:
+// row i of slice q at slices + q * sstride + i * 64; pexp[i] = the scale exponent of row i.
+__global__ void __launch_bounds__(128) oz_panel_slice_kernel(const double* __restrict__ l21, long long lda,
+                                                             long long rs, int bs, __nv_bfloat16* __restrict__ slices,
+                                                             long long sstride, int* __restrict__ pexp) {
+  const long long i = (long long)blockIdx.x * 128 + threadIdx.x;
+  if (i >= rs) return;
+  double m = 0.0;
+  for (int p = 0; p < bs; ++p) m = fmax(m, fabs(l21[(long long)p * lda + i]));
+  const int e = scale_exp(m);
+  pexp[i] = e;
+#pragma unroll 1
+  for (int p0 = 0; p0 < PK; p0 += 8) {
+    uint32_t packed[S][4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const int pa = p0 + 2 * h, pb = pa + 1;
+      float lo[S], hi[S];
+      split8(pa < bs ? l21[(long long)pa * lda + i] : 0.0, e, lo);
+      split8(pb < bs ? l21[(long long)pb * lda + i] : 0.0, e, hi);
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        const __nv_bfloat162 v2 = __floats2bfloat162_rn(lo[q], hi[q]);
+        packed[q][h] = *reinterpret_cast<const uint32_t*>(&v2);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < S; ++q)
+      *reinterpret_cast<uint4*>(slices + q * sstride + i * PK + p0) =
+          make_uint4(packed[q][0], packed[q][1], packed[q][2], packed[q][3]);
+  }
+}
+
+struct OzSyrkMaps {
+  CUtensorMap a[S];  // panel slices, box 64 x 128 rows
+  CUtensorMap b[S];  // panel slices, box 64 x 64 rows
+};
+
+struct OzSyrkParams {
+  double* c;         // A22(0, 0)
+  long long ldc;
+  long long rs;
+  const int* pexp;
+  const DevStatus* st;
+  int* err;
+};
+
+// One CTA per 128 x 64 tile of A22 with at least one entry on or below the diagonal.
+__global__ void __launch_bounds__(THREADS, 1) oz_syrk_kernel(const __grid_constant__ OzSyrkMaps maps,
+                                                             const OzSyrkParams p) {
+  const long long i0 = (long long)blockIdx.y * BM, j0 = (long long)blockIdx.x * BN;
+  if (j0 > i0 + BM - 1 || i0 >= p.rs || j0 >= p.rs) return;  // strictly above the diagonal
+  if (p.st->fail_col >= 0) return;                            // an earlier pivot failed
+  extern __shared__ uint8_t sy_smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)sy_smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* sa = smem;                 // 8 x 16 KB
+  uint8_t* sb = smem + S * SY_A;      // 8 x 8 KB
+  __shared__ __align__(8) uint64_t full, tfull;
+  __shared__ uint32_t tmem_base_s;
+  __shared__ volatile int abort_s;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    abort_s = 0;
+    mbar_init(&full, 1);
+    mbar_init(&tfull, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_s;
+  if (warp == 0 && lane == 0) {
+    mbar_expect_tx(&full, S * (SY_A + SY_B));
+    for (int q = 0; q < S; ++q) {
+      tma_load_2d(sa + q * SY_A, &maps.a[q], &full, 0, (int)i0);
+      tma_load_2d(sb + q * SY_B, &maps.b[q], &full, 0, (int)j0);
+    }
+    // the copies land before the CTA exits: the MMA warp (or, after an abort, the final wait) sees them
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = instr_desc_mn(1u, BM, BN);
+    if (mbar_wait(&full, 0u, &abort_s)) {
+      tc_fence_after();
+      for (int sp = 0; sp < S; ++sp) {
+        const uint64_t ad = sw128_desc(smem_u32(sa + sp * SY_A));
+        for (int q = 0; q + sp < S; ++q) {
+          const uint64_t bd = sw128_desc(smem_u32(sb + q * SY_B));
+          const uint32_t d = tmem + (uint32_t)((sp + q) * BN);
+#pragma unroll
+          for (int j = 0; j < PK / 16; ++j) mma<0>(d, ad + 2 * j, bd + 2 * j, idesc, (sp == 0 && j == 0) ? 0u : 1u);
+        }
+      }
+      mma_commit(&tfull);
+    }
+  } else if (warp >= 2) {
+    const int quad = warp & 3, part = (warp - 2) >> 2, r = quad * 32 + lane;
+    if (mbar_wait(&tfull, 0u, &abort_s)) {
+      tc_fence_after();
+      long long hi[16], lo[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        hi[c] = 0;
+        lo[c] = 0;
+      }
+      const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(part * 16);
+#pragma unroll
+      for (int w = 0; w < S; ++w) {
+        float v[16];
+        tmem_ld16(base + (uint32_t)(w * BN), v);
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const long long P = (long long)__float2int_rn(v[c]);
+          if (w < 4) hi[c] += P * (1ll << (BETA * (3 - w)));
+          else lo[c] += P * (1ll << (BETA * (7 - w)));
+        }
+      }
+      const long long i = i0 + r;
+      if (i < p.rs) {
+        const int ei = p.pexp[i];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const long long j = j0 + part * 16 + c;
+          if (j <= i) {
+            const double prod = ldexp(ldexp((double)hi[c], -35) + ldexp((double)lo[c], -63), ei + p.pexp[j]);
+            p.c[j * p.ldc + i] -= prod;
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0 && abort_s) {
+    atomicExch(p.err, 1);
+    volatile int dummy = 0;
+    mbar_wait(&full, 0u, &dummy);  // bounded: the copies issued above land before the CTA exits
+  }
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+std::mutex g_syrk_mu;
+int g_syrk_done[64] = {};
+
+}  // namespace
+
+OzakiSyrk::~OzakiSyrk() {
+  release_maps();
+  if (buf) cudaFreeAsync(buf, stream);
+}
+
+int OzakiSyrk::init(int64_t nmax_, cudaStream_t s) {
+  {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+      cudaGetLastError();
+      return GBLLT_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> lk(g_syrk_mu);
+    if (!g_syrk_done[dev]) {
+      GB_CUDA_TRY(cudaFuncSetAttribute(oz_syrk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SY_SMEM));
+      g_syrk_done[dev] = 1;
+    }
+  }
+  nmax = nmax_;
+  stream = s;
+  const size_t sb = oz_up256((size_t)S * nmax * PK * 2);
+  if (dev_malloc_async(&buf, sb + oz_up256((size_t)nmax * 4), s) != cudaSuccess) {
+    cudaGetLastError();
+    buf = nullptr;
+    return GBLLT_ERR_ALLOC;
+  }
+  slices = buf;
+  pexp = (int*)((char*)buf + sb);
+  maps = new OzSyrkMaps;
+  const __nv_bfloat16* sl = (const __nv_bfloat16*)slices;
+  OzSyrkMaps& m = *(OzSyrkMaps*)maps;
+  for (int q = 0; q < S; ++q) {
+    if (!make_map_2d(&m.a[q], sl + (size_t)q * nmax * PK, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BM) ||
+        !make_map_2d(&m.b[q], sl + (size_t)q * nmax * PK, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BN)) {
+      set_error_message("cuTensorMapEncodeTiled failed (tensor-core trailing update)");
+      return GBLLT_ERR_INTERNAL;
+    }
+  }
+  return GBLLT_SUCCESS;
+}
+
+void OzakiSyrk::release_maps() {
+  delete (OzSyrkMaps*)maps;
+  maps = nullptr;
+}
+
+int OzakiSyrk::update(double* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, cudaStream_t s) {
+  if (rs <= 0) return GBLLT_SUCCESS;
+  if (!buf || !maps || rs > nmax) return GBLLT_ERR_INTERNAL;
+  static const std::string kp = "panel_slices_f64";
+  static const std::string ks = "syrk_tc_f64";
+  const double* l21 = a + k0 * lda + k0 + bs;
+  {
+    ProfScope ps(kp.c_str(), s, 0.0, (double)rs * bs * 8.0 + (double)S * rs * PK * 2.0);
+    oz_panel_slice_kernel<<<(unsigned)ceil_div(rs, 128), 128, 0, s>>>(l21, lda, rs, bs, (__nv_bfloat16*)slices,
+                                                                     (long long)nmax * PK, pexp);
+  }
+  OzSyrkParams p;
+  p.c = a + (k0 + bs) * lda + k0 + bs;
+  p.ldc = lda;
+  p.rs = rs;
+  p.pexp = pexp;
+  p.st = st;
+  p.err = &st->timeout;
+  const dim3 grid((unsigned)ceil_div(rs, BN), (unsigned)ceil_div(rs, BM));
+  {
+    // algorithmic work: the FP64 update of the lower triangle, 2 bs flops per entry
+    const double entries = (double)rs * (rs + 1) / 2.0;
+    ProfScope ps(ks.c_str(), s, 2.0 * entries * bs, 2.0 * entries * 8.0 + (double)S * rs * PK * 2.0);
+    oz_syrk_kernel<<<grid, THREADS, SY_SMEM, s>>>(*(const OzSyrkMaps*)maps, p);
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+}  // namespace gbllt

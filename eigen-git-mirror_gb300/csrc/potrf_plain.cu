@@ -379,7 +379,8 @@ __global__ void __launch_bounds__(256) transpose_kernel(long long rows, long lon
 }
 
 __global__ void finalize_info_kernel(const DevStatus* __restrict__ st, int64_t* __restrict__ info) {
-  info[0] = st->fail_col >= 0 ? (int64_t)(st->fail_col + 1) : 0;
+  // a bounded device-side wait that ran out leaves the factor incomplete: reported instead of info
+  info[0] = st->timeout ? (int64_t)GBLLT_ERR_TIMEOUT : st->fail_col >= 0 ? (int64_t)(st->fail_col + 1) : 0;
 }
 
 }  // namespace
@@ -423,12 +424,30 @@ void launch_syrk_lower(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, int64_
 }
 
 template <typename T>
-int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t s) {
+int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t s, bool may_allocate) {
+  // FP64: trailing updates on the tensor cores, FP64-exact (error-free slicing; ozaki.cu), unless the
+  // matrix is small or the workspace (n KB) cannot be allocated
+  OzakiSyrk oz;
+  bool tc = false;
+  if constexpr (sizeof(T) == 8) {
+    if (may_allocate && n >= kTensorSyrkMinN) {
+      const int rc = oz.init(n, s);
+      if (rc == GBLLT_SUCCESS) tc = true;
+      else if (rc != GBLLT_ERR_ALLOC) return rc;
+    }
+  }
   for (int64_t k0 = 0; k0 < n; k0 += NB) {
     const int bs = (int)(n - k0 < NB ? n - k0 : NB);
     const int64_t rs = n - k0 - bs;
     launch_potrf_diag<T, T>(d_a, lda, k0, bs, st, s);
     launch_trsm_panel<T>(d_a, lda, k0, bs, rs, st, s);
+    if constexpr (sizeof(T) == 8) {
+      if (tc && rs >= 128) {
+        const int rc = oz.update(d_a, lda, k0, bs, rs, st, s);
+        if (rc) return rc;
+        continue;
+      }
+    }
     launch_syrk_lower<T>(d_a, lda, k0, bs, rs, rs, st, s);
   }
   GB_CUDA_TRY(cudaGetLastError());
@@ -466,8 +485,8 @@ int finalize_info_dev(const DevStatus* st, int64_t* d_info, cudaStream_t s) {
   return GBLLT_SUCCESS;
 }
 
-template int potrf_lower_dev<double>(int64_t, double*, int64_t, DevStatus*, cudaStream_t);
-template int potrf_lower_dev<float>(int64_t, float*, int64_t, DevStatus*, cudaStream_t);
+template int potrf_lower_dev<double>(int64_t, double*, int64_t, DevStatus*, cudaStream_t, bool);
+template int potrf_lower_dev<float>(int64_t, float*, int64_t, DevStatus*, cudaStream_t, bool);
 template int transpose_inplace_dev<double>(int64_t, double*, int64_t, cudaStream_t);
 template int transpose_inplace_dev<float>(int64_t, float*, int64_t, cudaStream_t);
 template int transpose_dev<double>(int64_t, int64_t, const double*, int64_t, double*, int64_t, cudaStream_t);
