@@ -153,6 +153,7 @@ struct OzakiResidual {
 // st->timeout.
 struct OzakiSyrk {
   int64_t nmax = 0;
+  int sms = 0;
   void* buf = nullptr;
   void* slices = nullptr;
   int* pexp = nullptr;

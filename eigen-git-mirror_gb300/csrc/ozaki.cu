@@ -21,14 +21,17 @@
 //     2-5 and 6-9, each a fixed-point number), which stay exact for n up to about 2^20;
 //   - at the end, R = B - 2^(e_i + f_j) (hi 2^-35 + lo 2^-63), rounded once to FP64.
 //
-// oz_gemm_kernel: one CTA per 128-row x 64-column tile of R, 576 threads: a TMA producer warp
-// (A slice tiles through a 4-stage ring, the 8 X slice tiles of a 64-wide K block double-
-// buffered), an MMA warp (tcgen05.mma M = 128, N = 64, K = 16, 144 per K block) and 16 epilogue
-// warps (four per TMEM lane quadrant, 16 columns each).  Every mbarrier wait is bounded.
+// oz_kernel: persistent CTAs walking a list of 128-row x 64-column output tiles, 576 threads: a TMA
+// producer warp (A slice tiles through a 4-stage ring, the 8 X slice tiles of a 64-wide K block
+// double-buffered, running ahead across tiles), an MMA warp (tcgen05.mma M = 128, N = 64, K = 16,
+// 144 per K block) and 16 epilogue warps (four per TMEM lane quadrant, 16 columns each).  The same
+// kernel forms the residual (K = n, chunks of 256) and the trailing update of the FP64 factorisation
+// (K = one 64-wide panel, one chunk, C -= product on the lower tiles).  Every mbarrier wait is bounded.
 // A non-finite value in A or X makes the whole residual NaN, which the refinement reports as
 // non-convergence, as it would with an FP64 residual.
 #include <cuda_bf16.h>
 
+#include <cstring>
 #include <mutex>
 
 #include "internal.h"
@@ -238,11 +241,16 @@ namespace {
 // ---- the product --------------------------------------------------------------------------------
 
 struct OzMaps {
-  CUtensorMap a[S];  // A slices: n rows of n K-elements, box 64 x 128
-  CUtensorMap x[S];  // X slices: nrhs rows of n K-elements, box 64 x 64
+  CUtensorMap a[S];  // slices of the M operand (rows of A, or of the panel), box 64 x 128 rows
+  CUtensorMap x[S];  // slices of the N operand (columns of X, or rows of the panel), box 64 x 64 rows
 };
 
 struct OzParams {
+  long long kdim;                  // K: n for the residual, the panel width for the trailing update
+  long long tiles;                 // entries of the tile list
+  int nrt, nct;                    // row tiles (128) and column tiles (64)
+  int* err;                        // set to 1 when a bounded wait ran out
+  // residual R = B - A X
   long long n, nrhs;
   const int* rexp;                 // per-row scale exponents of A
   const int* xexp;                 // per-column scale exponents of X
@@ -251,10 +259,38 @@ struct OzParams {
   long long ldb;
   double* r;
   long long ldr;
-  int* err;                        // set to 1 when a bounded wait ran out
+  // trailing update C -= L21 L21^T (lower)
+  double* c;
+  long long ldc;
+  long long rs;
+  const int* pexp;                 // per-row scale exponents of L21
+  const DevStatus* st;
 };
 
-__global__ void __launch_bounds__(THREADS, 1) oz_gemm_kernel(const __grid_constant__ OzMaps maps, const OzParams p) {
+// Tile t of the list: the residual walks row tiles fastest; the trailing update walks the lower
+// triangle row tile by row tile, row tile ti holding column tiles 0 .. 2 ti + 1 (128-row by 64-column
+// tiles), of which those past the last column tile are skipped.
+template <bool SYRK>
+__device__ __forceinline__ bool oz_tile(const OzParams& p, long long t, long long& row0, long long& col0) {
+  if (!SYRK) {
+    row0 = (t % p.nrt) * BM;
+    col0 = (t / p.nrt) * BN;
+    return true;
+  }
+  long long ti = (long long)((sqrt(4.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while ((ti + 1) * (ti + 2) <= t) ++ti;
+  while (ti * (ti + 1) > t) --ti;
+  const long long tj = t - ti * (ti + 1);
+  row0 = ti * BM;
+  col0 = tj * BN;
+  return tj < p.nct && col0 < p.rs;
+}
+
+// Persistent: each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The producer runs up to
+// two K blocks (of any tile) ahead of the MMA warp, so the next tile's loads overlap this tile's
+// products and epilogue; the TMEM accumulators (all 512 columns) are released chunk by chunk.
+template <bool SYRK>
+__global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ OzMaps maps, const OzParams p) {
   extern __shared__ uint8_t oz_smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)oz_smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* a_ring = smem;                           // A_STAGES x 16 KB
@@ -265,9 +301,9 @@ __global__ void __launch_bounds__(THREADS, 1) oz_gemm_kernel(const __grid_consta
   __shared__ uint32_t tmem_base_s;
   __shared__ volatile int abort_s;
 
+  if (SYRK && p.st->fail_col >= 0) return;  // an earlier pivot failed: nothing to update
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long row0 = (long long)blockIdx.x * BM, col0 = (long long)blockIdx.y * BN;
-  const int nkb = (int)((p.n + KB - 1) / KB);
+  const int nkb = (int)((p.kdim + KB - 1) / KB);
   const int nchunks = (nkb + KC_BLOCKS - 1) / KC_BLOCKS;
 
   if (threadIdx.x == 0) {
@@ -296,105 +332,127 @@ __global__ void __launch_bounds__(THREADS, 1) oz_gemm_kernel(const __grid_consta
   const uint32_t tmem = tmem_base_s;
 
   if (warp == 0 && lane == 0) {
-    // ---- TMA producer: per K block, the 8 X slice tiles (double-buffered), then the 8 A slice
-    // tiles through the A ring
-    long long issued_a = 0;
-    int issued_x = 0;
-    for (int kb = 0; kb < nkb && !abort_s; ++kb) {
-      const int xb = kb & 1;
-      if (!mbar_wait(&xempty[xb], ((uint32_t)(kb >> 1) & 1u) ^ 1u, &abort_s)) break;
-      mbar_expect_tx(&xfull[xb], X_SET);
-      for (int q = 0; q < S; ++q)
-        tma_load_2d(x_buf + xb * X_SET + q * X_BYTES, &maps.x[q], &xfull[xb], kb * KB, (int)col0);
-      issued_x = kb + 1;
-      bool ok = true;
-      for (int sp = 0; sp < S; ++sp) {
-        const long long it = (long long)kb * S + sp;
-        const int st = (int)(it % A_STAGES);
-        if (!mbar_wait(&aempty[st], ((uint32_t)(it / A_STAGES) & 1u) ^ 1u, &abort_s)) { ok = false; break; }
-        mbar_expect_tx(&afull[st], A_BYTES);
-        tma_load_2d(a_ring + st * A_BYTES, &maps.a[sp], &afull[st], kb * KB, (int)row0);
-        issued_a = it + 1;
+    // ---- TMA producer
+    long long kbg = 0, it = 0, issued_a = 0, issued_x = 0;
+    bool ok = true;
+    for (long long t = blockIdx.x; t < p.tiles && ok && !abort_s; t += gridDim.x) {
+      long long row0, col0;
+      if (!oz_tile<SYRK>(p, t, row0, col0)) continue;
+      for (int kb = 0; kb < nkb && ok; ++kb, ++kbg) {
+        const int xb = (int)(kbg & 1);
+        if (!mbar_wait(&xempty[xb], ((uint32_t)(kbg >> 1) & 1u) ^ 1u, &abort_s)) { ok = false; break; }
+        mbar_expect_tx(&xfull[xb], X_SET);
+        for (int q = 0; q < S; ++q)
+          tma_load_2d(x_buf + xb * X_SET + q * X_BYTES, &maps.x[q], &xfull[xb], kb * KB, (int)col0);
+        issued_x = kbg + 1;
+        for (int sp = 0; sp < S; ++sp, ++it) {
+          const int st = (int)(it % A_STAGES);
+          if (!mbar_wait(&aempty[st], ((uint32_t)(it / A_STAGES) & 1u) ^ 1u, &abort_s)) { ok = false; break; }
+          mbar_expect_tx(&afull[st], A_BYTES);
+          tma_load_2d(a_ring + st * A_BYTES, &maps.a[sp], &afull[st], kb * KB, (int)row0);
+          issued_a = it + 1;
+        }
       }
-      if (!ok) break;
     }
     if (abort_s) {
       // let the copies this thread started land before the CTA exits (bounded)
       volatile int dummy = 0;
       for (long long i = issued_a - A_STAGES < 0 ? 0 : issued_a - A_STAGES; i < issued_a; ++i)
         mbar_wait(&afull[i % A_STAGES], (uint32_t)(i / A_STAGES) & 1u, &dummy);
-      for (int k = issued_x - 2 < 0 ? 0 : issued_x - 2; k < issued_x; ++k)
+      for (long long k = issued_x - 2 < 0 ? 0 : issued_x - 2; k < issued_x; ++k)
         mbar_wait(&xfull[k & 1], (uint32_t)(k >> 1) & 1u, &dummy);
     }
   } else if (warp == 1 && lane == 0) {
     // ---- MMA issuer: pairs (p, q) with p + q <= S - 1 (0-based) into accumulator w = p + q
     constexpr uint32_t idesc = instr_desc_mn(1u, BM, BN);
+    long long kbg = 0, it = 0, chunkg = 0;
     bool ok = true;
-    for (int kb = 0; kb < nkb && ok; ++kb) {
-      const int chunk = kb / KC_BLOCKS;
-      const bool first = (kb % KC_BLOCKS) == 0;
-      if (first && chunk > 0) {  // the epilogue has taken the previous chunk's sums out of TMEM
-        if (!mbar_wait(&tempty, (uint32_t)(chunk - 1) & 1u, &abort_s)) break;
-        tc_fence_after();
-      }
-      const int xb = kb & 1;
-      if (!mbar_wait(&xfull[xb], (uint32_t)(kb >> 1) & 1u, &abort_s)) break;
-      tc_fence_after();
-      const uint32_t xs0 = smem_u32(x_buf + xb * X_SET);
-      for (int sp = 0; sp < S; ++sp) {
-        const long long it = (long long)kb * S + sp;
-        const int st = (int)(it % A_STAGES);
-        if (!mbar_wait(&afull[st], (uint32_t)(it / A_STAGES) & 1u, &abort_s)) { ok = false; break; }
-        tc_fence_after();
-        const uint64_t ad = sw128_desc(smem_u32(a_ring + st * A_BYTES));
-        for (int q = 0; q + sp < S; ++q) {
-          const uint64_t bd = sw128_desc(xs0 + q * X_BYTES);
-          const uint32_t d = tmem + (uint32_t)((sp + q) * BN);
-#pragma unroll
-          for (int j = 0; j < KB / 16; ++j)  // 32 bytes along K per MMA: +2 in the (addr >> 4) field
-            mma<0>(d, ad + 2 * j, bd + 2 * j, idesc, (first && sp == 0 && j == 0) ? 0u : 1u);
+    for (long long t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
+      long long row0, col0;
+      if (!oz_tile<SYRK>(p, t, row0, col0)) continue;
+      for (int kb = 0; kb < nkb && ok; ++kb, ++kbg) {
+        const bool first = (kb % KC_BLOCKS) == 0;
+        if (first && chunkg > 0) {  // the epilogue has taken the previous chunk's sums out of TMEM
+          if (!mbar_wait(&tempty, (uint32_t)(chunkg - 1) & 1u, &abort_s)) { ok = false; break; }
+          tc_fence_after();
         }
-        mma_commit(&aempty[st]);
+        const int xb = (int)(kbg & 1);
+        if (!mbar_wait(&xfull[xb], (uint32_t)(kbg >> 1) & 1u, &abort_s)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t xs0 = smem_u32(x_buf + xb * X_SET);
+        for (int sp = 0; sp < S; ++sp, ++it) {
+          const int st = (int)(it % A_STAGES);
+          if (!mbar_wait(&afull[st], (uint32_t)(it / A_STAGES) & 1u, &abort_s)) { ok = false; break; }
+          tc_fence_after();
+          const uint64_t ad = sw128_desc(smem_u32(a_ring + st * A_BYTES));
+          for (int q = 0; q + sp < S; ++q) {
+            const uint64_t bd = sw128_desc(xs0 + q * X_BYTES);
+            const uint32_t d = tmem + (uint32_t)((sp + q) * BN);
+#pragma unroll
+            for (int j = 0; j < KB / 16; ++j)  // 32 bytes along K per MMA: +2 in the (addr >> 4) field
+              mma<0>(d, ad + 2 * j, bd + 2 * j, idesc, (first && sp == 0 && j == 0) ? 0u : 1u);
+          }
+          mma_commit(&aempty[st]);
+        }
+        if (!ok) break;
+        mma_commit(&xempty[xb]);
+        if ((kb % KC_BLOCKS) == KC_BLOCKS - 1 || kb == nkb - 1) {
+          mma_commit(&tfull);
+          ++chunkg;
+        }
       }
-      if (!ok) break;
-      mma_commit(&xempty[xb]);
-      if ((kb % KC_BLOCKS) == KC_BLOCKS - 1 || kb == nkb - 1) mma_commit(&tfull);
     }
   } else if (warp >= 2) {
     // ---- epilogue: per chunk, the 8 weight accumulators of this thread's row and 16 columns into
-    // two int64 fixed-point sums; at the end R = B - 2^(e_i + f_j) (hi 2^-35 + lo 2^-63)
+    // two int64 fixed-point sums; per tile, the FP64 result 2^(e_i + f_j) (hi 2^-35 + lo 2^-63)
     const int quad = warp & 3;                  // TMEM lane quadrant this warp may access
     const int part = (warp - 2) >> 2;           // which 16 of the 64 columns
     const int r = quad * 32 + lane;             // tile row
-    long long hi[16], lo[16];
-#pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      hi[c] = 0;
-      lo[c] = 0;
-    }
+    long long chunkg = 0;
     bool ok = true;
-    for (int chunk = 0; chunk < nchunks; ++chunk) {
-      if (!mbar_wait(&tfull, (uint32_t)chunk & 1u, &abort_s)) { ok = false; break; }
-      tc_fence_after();
-      const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(part * 16);
+    for (long long t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
+      long long row0, col0;
+      if (!oz_tile<SYRK>(p, t, row0, col0)) continue;
+      long long hi[16], lo[16];
 #pragma unroll
-      for (int w = 0; w < S; ++w) {
-        float v[16];
-        tmem_ld16(base + (uint32_t)(w * BN), v);
-#pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          const long long P = (long long)__float2int_rn(v[c]);  // an exact integer below 2^24
-          if (w < 4) hi[c] += P * (1ll << (BETA * (3 - w)));
-          else lo[c] += P * (1ll << (BETA * (7 - w)));
-        }
+      for (int c = 0; c < 16; ++c) {
+        hi[c] = 0;
+        lo[c] = 0;
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&tempty);
-    }
-    if (ok) {
+      for (int ch = 0; ch < nchunks; ++ch, ++chunkg) {
+        if (!mbar_wait(&tfull, (uint32_t)chunkg & 1u, &abort_s)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(part * 16);
+#pragma unroll
+        for (int w = 0; w < S; ++w) {
+          float v[16];
+          tmem_ld16(base + (uint32_t)(w * BN), v);
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const long long P = (long long)__float2int_rn(v[c]);  // an exact integer below 2^24
+            if (w < 4) hi[c] += P * (1ll << (BETA * (3 - w)));
+            else lo[c] += P * (1ll << (BETA * (7 - w)));
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tempty);
+      }
+      if (!ok) break;
       const long long i = row0 + r;
-      if (i < p.n) {
+      if (SYRK) {
+        if (i < p.rs) {
+          const int ei = p.pexp[i];
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const long long j = col0 + part * 16 + c;
+            if (j <= i) {
+              const double prod = ldexp(ldexp((double)hi[c], -35) + ldexp((double)lo[c], -63), ei + p.pexp[j]);
+              p.c[j * p.ldc + i] -= prod;
+            }
+          }
+        }
+      } else if (i < p.n) {
         const int e = p.rexp[i];
         const bool bad = (p.flag[0] | p.flag[1]) != 0;
 #pragma unroll
@@ -423,20 +481,25 @@ __global__ void __launch_bounds__(THREADS, 1) oz_gemm_kernel(const __grid_consta
 
 namespace {
 
-// Per-device setup of the product kernel's shared-memory size, once, under a lock.
-int oz_prepare_device() {
+// Per-device setup, once, under a lock: the product kernels' shared-memory size and the SM count
+// (the persistent grid).
+int oz_prepare_device(int* sms) {
   static std::mutex mu;
-  static int done[64] = {};
+  static int nsm[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
     cudaGetLastError();
     return GBLLT_ERR_NO_DEVICE;
   }
   std::lock_guard<std::mutex> lk(mu);
-  if (!done[dev]) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    done[dev] = 1;
+  if (!nsm[dev]) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(oz_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    GB_CUDA_TRY(cudaFuncSetAttribute(oz_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    int v = 0;
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    nsm[dev] = v > 0 ? v : 1;
   }
+  *sms = nsm[dev];
   return GBLLT_SUCCESS;
 }
 
@@ -455,7 +518,8 @@ size_t OzakiResidual::bytes(int64_t n, int64_t nrhs) {
 }
 
 int OzakiResidual::setup(bool upper, int64_t n_, int64_t nrhs_, const double* a, int64_t lda, cudaStream_t s) {
-  int rc = oz_prepare_device();
+  int sms = 0;
+  int rc = oz_prepare_device(&sms);
   if (rc) return rc;
   n = n_;
   nrhs = nrhs_;
@@ -518,7 +582,15 @@ int OzakiResidual::residual(const double* x, int64_t ldx, const double* b, int64
     ProfScope ps(kx.c_str(), s, 0.0, (double)n * nrhs * (8.0 + S * 2.0));
     oz_slice_x_kernel<<<(unsigned)nrhs, 256, 0, s>>>(x, ldx, n, xs, lds, (long long)nrhs * lds, xexp, flags);
   }
+  int sms = 0;
+  int rc = oz_prepare_device(&sms);
+  if (rc) return rc;
   OzParams p;
+  memset(&p, 0, sizeof p);
+  p.kdim = n;
+  p.nrt = (int)ceil_div(n, BM);
+  p.nct = (int)ceil_div(nrhs, BN);
+  p.tiles = (long long)p.nrt * p.nct;
   p.n = n;
   p.nrhs = nrhs;
   p.rexp = rexp;
@@ -529,13 +601,13 @@ int OzakiResidual::residual(const double* x, int64_t ldx, const double* b, int64
   p.r = r;
   p.ldr = ldr;
   p.err = flags + 2;
-  const dim3 grid((unsigned)ceil_div(n, BM), (unsigned)ceil_div(nrhs, BN));
+  const unsigned grid = (unsigned)(p.tiles < sms ? p.tiles : sms);
   {
     // algorithmic work: the FP64 product 2 n^2 nrhs; bytes: the 8 A slices read once per column tile,
     // X slices, B read and R written
     ProfScope ps(kg.c_str(), s, 2.0 * n * n * nrhs,
-                 (double)S * n * n * 2.0 * grid.y + (double)S * n * nrhs * 2.0 + 2.0 * n * nrhs * 8.0);
-    oz_gemm_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(maps, p);
+                 (double)S * n * n * 2.0 * p.nct + (double)S * n * nrhs * 2.0 + 2.0 * n * nrhs * 8.0);
+    oz_kernel<false><<<grid, THREADS, SMEM_BYTES, s>>>(maps, p);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
@@ -559,10 +631,7 @@ namespace gbllt {
 
 namespace {
 
-constexpr int PK = 64;                         // panel width = K
-constexpr int SY_A = BM * 128;                 // 16 KB per A slice tile (128 rows)
-constexpr int SY_B = BN * 128;                 // 8 KB per B slice tile (64 rows)
-constexpr int SY_SMEM = S * SY_A + S * SY_B + 1024;
+constexpr int PK = 64;  // panel width = K
 
 // Slices of the panel L21 (rs x 64, column-major at l21 with leading dimension lda), K-major:
 // row i of slice q at slices + q * sstride + i * 64; pexp[i] = the scale exponent of row i.
@@ -597,124 +666,6 @@ __global__ void __launch_bounds__(128) oz_panel_slice_kernel(const double* __res
   }
 }
 
-struct OzSyrkMaps {
-  CUtensorMap a[S];  // panel slices, box 64 x 128 rows
-  CUtensorMap b[S];  // panel slices, box 64 x 64 rows
-};
-
-struct OzSyrkParams {
-  double* c;         // A22(0, 0)
-  long long ldc;
-  long long rs;
-  const int* pexp;
-  const DevStatus* st;
-  int* err;
-};
-
-// One CTA per 128 x 64 tile of A22 with at least one entry on or below the diagonal.
-__global__ void __launch_bounds__(THREADS, 1) oz_syrk_kernel(const __grid_constant__ OzSyrkMaps maps,
-                                                             const OzSyrkParams p) {
-  const long long i0 = (long long)blockIdx.y * BM, j0 = (long long)blockIdx.x * BN;
-  if (j0 > i0 + BM - 1 || i0 >= p.rs || j0 >= p.rs) return;  // strictly above the diagonal
-  if (p.st->fail_col >= 0) return;                            // an earlier pivot failed
-  extern __shared__ uint8_t sy_smem_raw[];
-  uint8_t* smem = (uint8_t*)(((uintptr_t)sy_smem_raw + 1023) & ~(uintptr_t)1023);
-  uint8_t* sa = smem;                 // 8 x 16 KB
-  uint8_t* sb = smem + S * SY_A;      // 8 x 8 KB
-  __shared__ __align__(8) uint64_t full, tfull;
-  __shared__ uint32_t tmem_base_s;
-  __shared__ volatile int abort_s;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) {
-    abort_s = 0;
-    mbar_init(&full, 1);
-    mbar_init(&tfull, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
-                 "r"(TMEM_COLS));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = tmem_base_s;
-  if (warp == 0 && lane == 0) {
-    mbar_expect_tx(&full, S * (SY_A + SY_B));
-    for (int q = 0; q < S; ++q) {
-      tma_load_2d(sa + q * SY_A, &maps.a[q], &full, 0, (int)i0);
-      tma_load_2d(sb + q * SY_B, &maps.b[q], &full, 0, (int)j0);
-    }
-    // the copies land before the CTA exits: the MMA warp (or, after an abort, the final wait) sees them
-  } else if (warp == 1 && lane == 0) {
-    constexpr uint32_t idesc = instr_desc_mn(1u, BM, BN);
-    if (mbar_wait(&full, 0u, &abort_s)) {
-      tc_fence_after();
-      for (int sp = 0; sp < S; ++sp) {
-        const uint64_t ad = sw128_desc(smem_u32(sa + sp * SY_A));
-        for (int q = 0; q + sp < S; ++q) {
-          const uint64_t bd = sw128_desc(smem_u32(sb + q * SY_B));
-          const uint32_t d = tmem + (uint32_t)((sp + q) * BN);
-#pragma unroll
-          for (int j = 0; j < PK / 16; ++j) mma<0>(d, ad + 2 * j, bd + 2 * j, idesc, (sp == 0 && j == 0) ? 0u : 1u);
-        }
-      }
-      mma_commit(&tfull);
-    }
-  } else if (warp >= 2) {
-    const int quad = warp & 3, part = (warp - 2) >> 2, r = quad * 32 + lane;
-    if (mbar_wait(&tfull, 0u, &abort_s)) {
-      tc_fence_after();
-      long long hi[16], lo[16];
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        hi[c] = 0;
-        lo[c] = 0;
-      }
-      const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(part * 16);
-#pragma unroll
-      for (int w = 0; w < S; ++w) {
-        float v[16];
-        tmem_ld16(base + (uint32_t)(w * BN), v);
-#pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          const long long P = (long long)__float2int_rn(v[c]);
-          if (w < 4) hi[c] += P * (1ll << (BETA * (3 - w)));
-          else lo[c] += P * (1ll << (BETA * (7 - w)));
-        }
-      }
-      const long long i = i0 + r;
-      if (i < p.rs) {
-        const int ei = p.pexp[i];
-#pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          const long long j = j0 + part * 16 + c;
-          if (j <= i) {
-            const double prod = ldexp(ldexp((double)hi[c], -35) + ldexp((double)lo[c], -63), ei + p.pexp[j]);
-            p.c[j * p.ldc + i] -= prod;
-          }
-        }
-      }
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  if (threadIdx.x == 0 && abort_s) {
-    atomicExch(p.err, 1);
-    volatile int dummy = 0;
-    mbar_wait(&full, 0u, &dummy);  // bounded: the copies issued above land before the CTA exits
-  }
-  if (warp == 1) {
-    tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
-  }
-}
-
-std::mutex g_syrk_mu;
-int g_syrk_done[64] = {};
-
 }  // namespace
 
 OzakiSyrk::~OzakiSyrk() {
@@ -723,18 +674,8 @@ OzakiSyrk::~OzakiSyrk() {
 }
 
 int OzakiSyrk::init(int64_t nmax_, cudaStream_t s) {
-  {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
-      cudaGetLastError();
-      return GBLLT_ERR_NO_DEVICE;
-    }
-    std::lock_guard<std::mutex> lk(g_syrk_mu);
-    if (!g_syrk_done[dev]) {
-      GB_CUDA_TRY(cudaFuncSetAttribute(oz_syrk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SY_SMEM));
-      g_syrk_done[dev] = 1;
-    }
-  }
+  int rc = oz_prepare_device(&sms);
+  if (rc) return rc;
   nmax = nmax_;
   stream = s;
   const size_t sb = oz_up256((size_t)S * nmax * PK * 2);
@@ -745,12 +686,12 @@ int OzakiSyrk::init(int64_t nmax_, cudaStream_t s) {
   }
   slices = buf;
   pexp = (int*)((char*)buf + sb);
-  maps = new OzSyrkMaps;
+  maps = new OzMaps;
   const __nv_bfloat16* sl = (const __nv_bfloat16*)slices;
-  OzSyrkMaps& m = *(OzSyrkMaps*)maps;
+  OzMaps& m = *(OzMaps*)maps;
   for (int q = 0; q < S; ++q) {
     if (!make_map_2d(&m.a[q], sl + (size_t)q * nmax * PK, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BM) ||
-        !make_map_2d(&m.b[q], sl + (size_t)q * nmax * PK, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BN)) {
+        !make_map_2d(&m.x[q], sl + (size_t)q * nmax * PK, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BN)) {
       set_error_message("cuTensorMapEncodeTiled failed (tensor-core trailing update)");
       return GBLLT_ERR_INTERNAL;
     }
@@ -759,7 +700,7 @@ int OzakiSyrk::init(int64_t nmax_, cudaStream_t s) {
 }
 
 void OzakiSyrk::release_maps() {
-  delete (OzSyrkMaps*)maps;
+  delete (OzMaps*)maps;
   maps = nullptr;
 }
 
@@ -774,19 +715,24 @@ int OzakiSyrk::update(double* a, int64_t lda, int64_t k0, int bs, int64_t rs, De
     oz_panel_slice_kernel<<<(unsigned)ceil_div(rs, 128), 128, 0, s>>>(l21, lda, rs, bs, (__nv_bfloat16*)slices,
                                                                      (long long)nmax * PK, pexp);
   }
-  OzSyrkParams p;
+  OzParams p;
+  memset(&p, 0, sizeof p);
+  p.kdim = PK;
+  p.nrt = (int)ceil_div(rs, BM);
+  p.nct = (int)ceil_div(rs, BN);
+  p.tiles = (long long)p.nrt * (p.nrt + 1);  // row tile ti: column tiles 0 .. 2 ti + 1
   p.c = a + (k0 + bs) * lda + k0 + bs;
   p.ldc = lda;
   p.rs = rs;
   p.pexp = pexp;
   p.st = st;
   p.err = &st->timeout;
-  const dim3 grid((unsigned)ceil_div(rs, BN), (unsigned)ceil_div(rs, BM));
+  const unsigned grid = (unsigned)(p.tiles < sms ? p.tiles : sms);
   {
     // algorithmic work: the FP64 update of the lower triangle, 2 bs flops per entry
     const double entries = (double)rs * (rs + 1) / 2.0;
     ProfScope ps(ks.c_str(), s, 2.0 * entries * bs, 2.0 * entries * 8.0 + (double)S * rs * PK * 2.0);
-    oz_syrk_kernel<<<grid, THREADS, SY_SMEM, s>>>(*(const OzSyrkMaps*)maps, p);
+    oz_kernel<true><<<grid, THREADS, SMEM_BYTES, s>>>(*(const OzMaps*)maps, p);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
