@@ -19,7 +19,8 @@
 //     so the FP32 tensor-core accumulation of a chunk is exact; after each chunk the epilogue warps
 //     convert the accumulators to integers and add them into two int64 sums per output (weights
 //     2-5 and 6-9, each a fixed-point number), which stay exact for n up to about 2^20;
-//   - at the end, R = B - 2^(e_i + f_j) (hi 2^-35 + lo 2^-63), rounded once to FP64.
+//   - at the end, R = B - 2^(e_i + f_j) (hi 2^-35 + lo 2^-63), rounded once to FP64 (in integer
+//     arithmetic: the FP64 pipe is kept for the final subtraction).
 //
 // oz_kernel: persistent CTAs walking a list of 128-row x 64-column output tiles, 576 threads: a TMA
 // producer warp (A slice tiles through a 4-stage ring, the 8 X slice tiles of a 64-wide K block
@@ -267,6 +268,41 @@ struct OzParams {
   const DevStatus* st;
 };
 
+// round((hi 2^28 + lo) 2^(e - 63)) to FP64, to nearest even, in integer arithmetic (the FP64 pipe
+// of GB300 retires two operations per SM clock, too few for a per-element conversion); the value is
+// rounded once, as ldexp(hi, -35) + ldexp(lo, -63) would round it.  Subnormal and overflowing results
+// (far outside any residual or update) take the library's ldexp.
+__device__ __forceinline__ double fixed_to_double(long long hi, long long lo, int e) {
+  const __int128 v = ((__int128)hi << 28) + (__int128)lo;
+  if (v == 0) return 0.0;
+  const bool neg = v < 0;
+  const unsigned __int128 m = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  const unsigned long long mh = (unsigned long long)(m >> 64), ml = (unsigned long long)m;
+  const int bl = mh ? 128 - __clzll((long long)mh) : 64 - __clzll((long long)ml);  // bit length
+  int sh = bl - 53;
+  unsigned long long mant;
+  if (sh <= 0) {
+    mant = (unsigned long long)(m << (-sh));
+  } else {
+    unsigned __int128 q = m >> sh;
+    const unsigned __int128 rem = m - (q << sh), half = (unsigned __int128)1 << (sh - 1);
+    if (rem > half || (rem == half && (q & 1))) q += 1;
+    if (q >> 53) {
+      q >>= 1;
+      sh += 1;
+    }
+    mant = (unsigned long long)q;
+  }
+  const int biased = sh + e - 63 + 52 + 1023;  // exponent field of mant * 2^(sh + e - 63)
+  if (biased <= 0 || biased >= 2047) {
+    const double d = ldexp((double)(long long)mant, sh + e - 63);
+    return neg ? -d : d;
+  }
+  const unsigned long long bits = ((unsigned long long)neg << 63) | ((unsigned long long)biased << 52) |
+                                  (mant & ((1ull << 52) - 1));
+  return __longlong_as_double((long long)bits);
+}
+
 // Tile t of the list: the residual walks row tiles fastest; the trailing update walks the lower
 // triangle row tile by row tile, row tile ti holding column tiles 0 .. 2 ti + 1 (128-row by 64-column
 // tiles), of which those past the last column tile are skipped.
@@ -277,7 +313,7 @@ __device__ __forceinline__ bool oz_tile(const OzParams& p, long long t, long lon
     col0 = (t / p.nrt) * BN;
     return true;
   }
-  long long ti = (long long)((sqrt(4.0 * (double)t + 1.0) - 1.0) * 0.5);
+  long long ti = (long long)((sqrtf(4.0f * (float)t + 1.0f) - 1.0f) * 0.5f);  // corrected below
   while ((ti + 1) * (ti + 2) <= t) ++ti;
   while (ti * (ti + 1) > t) --ti;
   const long long tj = t - ti * (ti + 1);
@@ -447,8 +483,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
           for (int c = 0; c < 16; ++c) {
             const long long j = col0 + part * 16 + c;
             if (j <= i) {
-              const double prod = ldexp(ldexp((double)hi[c], -35) + ldexp((double)lo[c], -63), ei + p.pexp[j]);
-              p.c[j * p.ldc + i] -= prod;
+              p.c[j * p.ldc + i] -= fixed_to_double(hi[c], lo[c], ei + p.pexp[j]);
             }
           }
         }
@@ -459,7 +494,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
         for (int c = 0; c < 16; ++c) {
           const long long j = col0 + part * 16 + c;
           if (j < p.nrhs) {
-            const double ax = ldexp(ldexp((double)hi[c], -35) + ldexp((double)lo[c], -63), e + p.xexp[j]);
+            const double ax = fixed_to_double(hi[c], lo[c], e + p.xexp[j]);
             p.r[j * p.ldr + i] = bad ? __longlong_as_double(0x7ff8000000000000ll) : p.b[j * p.ldb + i] - ax;
           }
         }
