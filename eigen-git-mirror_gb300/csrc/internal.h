@@ -146,17 +146,21 @@ struct OzakiResidual {
   int timeout_flag_into(int* host_flag, cudaStream_t s) const;
 };
 
-// The trailing update A22 -= L21 L21^T of the FP64 factorisation on the BF16 tensor cores, FP64-exact
-// (ozaki.cu): init() allocates the panel slices for panels of up to nmax rows (nmax * 1 KB, stream-
-// ordered) and encodes their tensor maps; update() slices the panel below the diagonal block at
-// (k0, k0) and updates the rs x rs trailing lower triangle.  A bounded wait that runs out sets
+// The trailing updates of the FP64 factorisation on the BF16 tensor cores, FP64-exact (ozaki.cu):
+// init() allocates panel slices for panels of up to nmax rows (about 5 nmax KB, stream-ordered) and
+// encodes their tensor maps; update() slices the rs x pw panel below the diagonal block at (k0, k0)
+// (pw <= 64, or up to kWide columns at once: one exact 256-deep chunk) and applies C -= L21 L21^T to
+// the lower part of the rs x ncols block at (k0 + pw, k0 + pw).  A bounded wait that runs out sets
 // st->timeout.
+constexpr int kWide = 256;
 struct OzakiSyrk {
   int64_t nmax = 0;
   int sms = 0;
   void* buf = nullptr;
-  void* slices = nullptr;
+  void* slices = nullptr;    // 64-wide sub-panel slices
   int* pexp = nullptr;
+  void* slices_w = nullptr;  // kWide-wide panel slices
+  int* pexp_w = nullptr;
   void* maps = nullptr;
   cudaStream_t stream = nullptr;
   OzakiSyrk() = default;
@@ -164,7 +168,7 @@ struct OzakiSyrk {
   OzakiSyrk& operator=(const OzakiSyrk&) = delete;
   ~OzakiSyrk();
   int init(int64_t nmax, cudaStream_t s);
-  int update(double* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, cudaStream_t s);
+  int update(double* a, int64_t lda, int64_t k0, int pw, int64_t rs, int64_t ncols, DevStatus* st, cudaStream_t s);
   void release_maps();
 };
 

@@ -263,7 +263,8 @@ struct OzParams {
   // trailing update C -= L21 L21^T (lower)
   double* c;
   long long ldc;
-  long long rs;
+  long long rs;                    // rows of the updated block
+  long long ncols;                 // its columns (ncols = rs: the whole trailing lower triangle)
   const int* pexp;                 // per-row scale exponents of L21
   const DevStatus* st;
 };
@@ -303,23 +304,14 @@ __device__ __forceinline__ double fixed_to_double(long long hi, long long lo, in
   return __longlong_as_double((long long)bits);
 }
 
-// Tile t of the list: the residual walks row tiles fastest; the trailing update walks the lower
-// triangle row tile by row tile, row tile ti holding column tiles 0 .. 2 ti + 1 (128-row by 64-column
-// tiles), of which those past the last column tile are skipped.
+// Tile t of the list: the residual walks row tiles fastest; the trailing update walks the same
+// 128 x 64 grid over its rs x ncols block and skips the tiles strictly above the diagonal.
 template <bool SYRK>
 __device__ __forceinline__ bool oz_tile(const OzParams& p, long long t, long long& row0, long long& col0) {
-  if (!SYRK) {
-    row0 = (t % p.nrt) * BM;
-    col0 = (t / p.nrt) * BN;
-    return true;
-  }
-  long long ti = (long long)((sqrtf(4.0f * (float)t + 1.0f) - 1.0f) * 0.5f);  // corrected below
-  while ((ti + 1) * (ti + 2) <= t) ++ti;
-  while (ti * (ti + 1) > t) --ti;
-  const long long tj = t - ti * (ti + 1);
-  row0 = ti * BM;
-  col0 = tj * BN;
-  return tj < p.nct && col0 < p.rs;
+  row0 = (t % p.nrt) * BM;
+  col0 = (t / p.nrt) * BN;
+  if (!SYRK) return true;
+  return col0 < p.ncols && col0 <= row0 + BM - 1;
 }
 
 // Persistent: each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The producer runs up to
@@ -666,13 +658,15 @@ namespace gbllt {
 
 namespace {
 
-constexpr int PK = 64;  // panel width = K
+constexpr int PK = 64;  // sub-panel width (the diagonal-block size)
 
-// Slices of the panel L21 (rs x 64, column-major at l21 with leading dimension lda), K-major:
-// row i of slice q at slices + q * sstride + i * 64; pexp[i] = the scale exponent of row i.
+// Slices of the panel L21 (rs x bs, column-major at l21 with leading dimension lda) as K-major rows of
+// w >= bs elements (zero past bs): row i of slice q at slices + q * sstride + i * w; pexp[i] = the
+// scale exponent of row i (its maximum over the panel).
 __global__ void __launch_bounds__(128) oz_panel_slice_kernel(const double* __restrict__ l21, long long lda,
-                                                             long long rs, int bs, __nv_bfloat16* __restrict__ slices,
-                                                             long long sstride, int* __restrict__ pexp) {
+                                                             long long rs, int bs, int w,
+                                                             __nv_bfloat16* __restrict__ slices, long long sstride,
+                                                             int* __restrict__ pexp) {
   const long long i = (long long)blockIdx.x * 128 + threadIdx.x;
   if (i >= rs) return;
   double m = 0.0;
@@ -680,7 +674,7 @@ __global__ void __launch_bounds__(128) oz_panel_slice_kernel(const double* __res
   const int e = scale_exp(m);
   pexp[i] = e;
 #pragma unroll 1
-  for (int p0 = 0; p0 < PK; p0 += 8) {
+  for (int p0 = 0; p0 < w; p0 += 8) {
     uint32_t packed[S][4];
 #pragma unroll
     for (int h = 0; h < 4; ++h) {
@@ -696,7 +690,7 @@ __global__ void __launch_bounds__(128) oz_panel_slice_kernel(const double* __res
     }
 #pragma unroll
     for (int q = 0; q < S; ++q)
-      *reinterpret_cast<uint4*>(slices + q * sstride + i * PK + p0) =
+      *reinterpret_cast<uint4*>(slices + q * sstride + i * w + p0) =
           make_uint4(packed[q][0], packed[q][1], packed[q][2], packed[q][3]);
   }
 }
@@ -713,20 +707,29 @@ int OzakiSyrk::init(int64_t nmax_, cudaStream_t s) {
   if (rc) return rc;
   nmax = nmax_;
   stream = s;
-  const size_t sb = oz_up256((size_t)S * nmax * PK * 2);
-  if (dev_malloc_async(&buf, sb + oz_up256((size_t)nmax * 4), s) != cudaSuccess) {
+  // [slices of a 64-wide sub-panel | their exponents | slices of a 256-wide panel | their exponents]
+  const size_t s64 = oz_up256((size_t)S * nmax * PK * 2), s256 = oz_up256((size_t)S * nmax * kWide * 2),
+               e = oz_up256((size_t)nmax * 4);
+  if (dev_malloc_async(&buf, s64 + e + s256 + e, s) != cudaSuccess) {
     cudaGetLastError();
     buf = nullptr;
     return GBLLT_ERR_ALLOC;
   }
   slices = buf;
-  pexp = (int*)((char*)buf + sb);
-  maps = new OzMaps;
+  pexp = (int*)((char*)buf + s64);
+  slices_w = (char*)buf + s64 + e;
+  pexp_w = (int*)((char*)buf + s64 + e + s256);
+  maps = new OzMaps[2];
+  OzMaps* m = (OzMaps*)maps;
   const __nv_bfloat16* sl = (const __nv_bfloat16*)slices;
-  OzMaps& m = *(OzMaps*)maps;
+  const __nv_bfloat16* sw = (const __nv_bfloat16*)slices_w;
   for (int q = 0; q < S; ++q) {
-    if (!make_map_2d(&m.a[q], sl + (size_t)q * nmax * PK, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BM) ||
-        !make_map_2d(&m.x[q], sl + (size_t)q * nmax * PK, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BN)) {
+    const __nv_bfloat16* b64 = sl + (size_t)q * nmax * PK;
+    const __nv_bfloat16* b256 = sw + (size_t)q * nmax * kWide;
+    if (!make_map_2d(&m[0].a[q], b64, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BM) ||
+        !make_map_2d(&m[0].x[q], b64, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BN) ||
+        !make_map_2d(&m[1].a[q], b256, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, kWide, kWide, KB, BM) ||
+        !make_map_2d(&m[1].x[q], b256, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, kWide, kWide, KB, BN)) {
       set_error_message("cuTensorMapEncodeTiled failed (tensor-core trailing update)");
       return GBLLT_ERR_INTERNAL;
     }
@@ -735,39 +738,48 @@ int OzakiSyrk::init(int64_t nmax_, cudaStream_t s) {
 }
 
 void OzakiSyrk::release_maps() {
-  delete (OzMaps*)maps;
+  delete[](OzMaps*) maps;
   maps = nullptr;
 }
 
-int OzakiSyrk::update(double* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, cudaStream_t s) {
-  if (rs <= 0) return GBLLT_SUCCESS;
-  if (!buf || !maps || rs > nmax) return GBLLT_ERR_INTERNAL;
+// C -= L21 L21^T on the rs x ncols block at (k0 + pw, k0 + pw), L21 = the rs x pw panel below the
+// panel's diagonal block at (k0, k0); pw <= 64 uses the 64-wide slices, pw <= 256 the wide ones.
+int OzakiSyrk::update(double* a, int64_t lda, int64_t k0, int pw, int64_t rs, int64_t ncols, DevStatus* st,
+                      cudaStream_t s) {
+  if (rs <= 0 || ncols <= 0) return GBLLT_SUCCESS;
+  if (!buf || !maps || rs > nmax || pw > kWide) return GBLLT_ERR_INTERNAL;
+  const bool wide = pw > PK;
+  const int w = wide ? kWide : PK;
   static const std::string kp = "panel_slices_f64";
   static const std::string ks = "syrk_tc_f64";
-  const double* l21 = a + k0 * lda + k0 + bs;
+  const double* l21 = a + k0 * lda + k0 + pw;
+  __nv_bfloat16* sl = (__nv_bfloat16*)(wide ? slices_w : slices);
+  int* ex = wide ? pexp_w : pexp;
   {
-    ProfScope ps(kp.c_str(), s, 0.0, (double)rs * bs * 8.0 + (double)S * rs * PK * 2.0);
-    oz_panel_slice_kernel<<<(unsigned)ceil_div(rs, 128), 128, 0, s>>>(l21, lda, rs, bs, (__nv_bfloat16*)slices,
-                                                                     (long long)nmax * PK, pexp);
+    ProfScope ps(kp.c_str(), s, 0.0, (double)rs * pw * 8.0 + (double)S * rs * w * 2.0);
+    oz_panel_slice_kernel<<<(unsigned)ceil_div(rs, 128), 128, 0, s>>>(l21, lda, rs, pw, w, sl, (long long)nmax * w,
+                                                                     ex);
   }
   OzParams p;
   memset(&p, 0, sizeof p);
-  p.kdim = PK;
+  p.kdim = w;
   p.nrt = (int)ceil_div(rs, BM);
-  p.nct = (int)ceil_div(rs, BN);
-  p.tiles = (long long)p.nrt * (p.nrt + 1);  // row tile ti: column tiles 0 .. 2 ti + 1
-  p.c = a + (k0 + bs) * lda + k0 + bs;
+  p.nct = (int)ceil_div(ncols, BN);
+  p.tiles = (long long)p.nrt * p.nct;
+  p.c = a + (k0 + pw) * lda + k0 + pw;
   p.ldc = lda;
   p.rs = rs;
-  p.pexp = pexp;
+  p.ncols = ncols;
+  p.pexp = ex;
   p.st = st;
   p.err = &st->timeout;
   const unsigned grid = (unsigned)(p.tiles < sms ? p.tiles : sms);
   {
-    // algorithmic work: the FP64 update of the lower triangle, 2 bs flops per entry
-    const double entries = (double)rs * (rs + 1) / 2.0;
-    ProfScope ps(ks.c_str(), s, 2.0 * entries * bs, 2.0 * entries * 8.0 + (double)S * rs * PK * 2.0);
-    oz_kernel<true><<<grid, THREADS, SMEM_BYTES, s>>>(*(const OzMaps*)maps, p);
+    // algorithmic work: the FP64 update of the block's lower part, 2 pw flops per entry
+    const double c = (double)(ncols < rs ? ncols : rs);
+    const double entries = c * (double)rs - c * (c - 1) / 2.0;
+    ProfScope ps(ks.c_str(), s, 2.0 * entries * pw, 2.0 * entries * 8.0 + (double)S * rs * w * 2.0);
+    oz_kernel<true><<<grid, THREADS, SMEM_BYTES, s>>>(((const OzMaps*)maps)[wide ? 1 : 0], p);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;

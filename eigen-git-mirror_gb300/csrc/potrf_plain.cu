@@ -423,17 +423,45 @@ void launch_syrk_lower(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, int64_
   syrk_lower_kernel<T><<<(unsigned)tiles, 256, 0, s>>>(a, lda, k0, bs, rs, ncols, (int)nct, st, bsrc, ldb);
 }
 
+// FP64 with the trailing updates on the tensor cores (OzakiSyrk): panels of kWide = 256 columns,
+// each factored in 64-column steps (diagonal block, TRSM of the rows below, then the update of the
+// panel's remaining columns by that 64-wide sub-panel), then one 256-deep update of the trailing
+// matrix.  A 256-deep chunk is still exact in the tensor cores' FP32 accumulator, and a deeper
+// update means four times fewer passes over the trailing matrix than 64-wide steps would make.
+static int potrf_lower_tc(int64_t n, double* a, int64_t lda, DevStatus* st, cudaStream_t s, OzakiSyrk& oz) {
+  for (int64_t K0 = 0; K0 < n; K0 += kWide) {
+    const int pw = (int)(n - K0 < kWide ? n - K0 : kWide);
+    for (int64_t k0 = K0; k0 < K0 + pw; k0 += NB) {
+      const int bs = (int)(K0 + pw - k0 < NB ? K0 + pw - k0 : NB);
+      const int64_t rs = n - k0 - bs;
+      launch_potrf_diag<double, double>(a, lda, k0, bs, st, s);
+      launch_trsm_panel<double>(a, lda, k0, bs, rs, st, s);
+      const int64_t cols_left = K0 + pw - (k0 + bs);
+      if (cols_left > 0 && rs > 0) {
+        const int rc = oz.update(a, lda, k0, bs, rs, cols_left, st, s);
+        if (rc) return rc;
+      }
+    }
+    const int64_t rs2 = n - K0 - pw;
+    if (rs2 > 0) {
+      const int rc = oz.update(a, lda, K0, pw, rs2, rs2, st, s);
+      if (rc) return rc;
+    }
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
 template <typename T>
 int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t s, bool may_allocate) {
   // FP64: trailing updates on the tensor cores, FP64-exact (error-free slicing; ozaki.cu), unless the
-  // matrix is small or the workspace (n KB) cannot be allocated
-  OzakiSyrk oz;
-  bool tc = false;
+  // matrix is small or the workspace (about 5 n KB) cannot be allocated
   if constexpr (sizeof(T) == 8) {
     if (may_allocate && n >= kTensorSyrkMinN) {
+      OzakiSyrk oz;
       const int rc = oz.init(n, s);
-      if (rc == GBLLT_SUCCESS) tc = true;
-      else if (rc != GBLLT_ERR_ALLOC) return rc;
+      if (rc == GBLLT_SUCCESS) return potrf_lower_tc(n, d_a, lda, st, s, oz);
+      if (rc != GBLLT_ERR_ALLOC) return rc;
     }
   }
   for (int64_t k0 = 0; k0 < n; k0 += NB) {
@@ -441,13 +469,6 @@ int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t 
     const int64_t rs = n - k0 - bs;
     launch_potrf_diag<T, T>(d_a, lda, k0, bs, st, s);
     launch_trsm_panel<T>(d_a, lda, k0, bs, rs, st, s);
-    if constexpr (sizeof(T) == 8) {
-      if (tc && rs >= 128) {
-        const int rc = oz.update(d_a, lda, k0, bs, rs, st, s);
-        if (rc) return rc;
-        continue;
-      }
-    }
     launch_syrk_lower<T>(d_a, lda, k0, bs, rs, rs, st, s);
   }
   GB_CUDA_TRY(cudaGetLastError());

@@ -88,7 +88,7 @@ GBLLT_API int gbllt_sposv(int layout, char uplo, int64_t n, int64_t nrhs, float*
  * device memory that receives the LAPACK info (or GBLLT_ERR_TIMEOUT if a bounded device-side wait
  * of the tensor-core trailing update ran out); it is written before the call's work on `stream`
  * completes.  FP64 factorisations of order >= 1024 run their trailing updates on the tensor cores
- * with FP64-exact error-free slicing (about n KB of extra device memory; without it, or below that
+ * with FP64-exact error-free slicing (about 5 n KB of extra device memory; without it, or below that
  * order, on the FP64 pipe). */
 GBLLT_API int gbllt_dpotrf_dev(char uplo, int64_t n, double* d_a, int64_t lda, int64_t* d_info, void* stream);
 GBLLT_API int gbllt_spotrf_dev(char uplo, int64_t n, float* d_a, int64_t lda, int64_t* d_info, void* stream);
