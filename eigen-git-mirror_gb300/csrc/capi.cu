@@ -63,6 +63,18 @@ int ensure_device() {
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     g_dev_ok[dev] = (major == 10 && minor == 3) ? 1 : -1;
+    if (g_dev_ok[dev] > 0) {
+      // the library's workspaces come from the device's default stream-ordered pool; by default it
+      // returns freed memory to the system at every synchronisation, and the next call maps it
+      // again (gigabytes for a large solve).  Keep it cached in this process instead;
+      // gbllt_release_cached_memory() gives it back.
+      cudaMemPool_t pool;
+      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+      }
+      cudaGetLastError();
+    }
     if (g_dev_ok[dev] < 0) {
       char buf[128];
       snprintf(buf, sizeof buf, "device %d is sm_%d%d; this library is built for sm_103a only", dev, major, minor);
@@ -340,6 +352,19 @@ extern "C" {
 int gbllt_version(void) { return 100; }
 
 const char* gbllt_last_error(void) { return g_last_error.c_str(); }
+
+int gbllt_release_cached_memory(void) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return GBLLT_ERR_NO_DEVICE;
+  }
+  cudaMemPool_t pool;
+  GB_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, dev));
+  GB_CUDA_TRY(cudaDeviceSynchronize());
+  GB_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
+  return GBLLT_SUCCESS;
+}
 
 int gbllt_dpotrf(int layout, char uplo, int64_t n, double* a, int64_t lda, int64_t* info) {
   return host_potrf<double>(layout, uplo, n, a, lda, info);

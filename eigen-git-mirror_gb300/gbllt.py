@@ -39,6 +39,7 @@ _i64p = ctypes.POINTER(ctypes.c_int64)
 SIGNATURES: dict[str, tuple] = {
     "gbllt_version": (_int, []),
     "gbllt_last_error": (ctypes.c_char_p, []),
+    "gbllt_release_cached_memory": (_int, []),
     "gbllt_dpotrf": (_int, [_int, _ch, _i64, _vp, _i64, _i64p]),
     "gbllt_spotrf": (_int, [_int, _ch, _i64, _vp, _i64, _i64p]),
     "gbllt_dpotrs": (_int, [_int, _ch, _i64, _i64, _vp, _i64, _vp, _i64]),

@@ -61,6 +61,12 @@ GBLLT_API int gbllt_version(void);
 /* Message of the last GBLLT_ERR_CUDA seen by the calling thread ("" if none). */
 GBLLT_API const char* gbllt_last_error(void);
 
+/* Workspaces come from the current device's default stream-ordered memory pool (cudaMallocAsync),
+ * which the library sets, on first use of a device, to keep freed memory cached in the process
+ * instead of returning it at every synchronisation (a large solve would otherwise map gigabytes
+ * again on each call).  This returns the cached memory of the current device to the system. */
+GBLLT_API int gbllt_release_cached_memory(void);
+
 /* Factor A = L L^T ('L') or A = U^T U ('U') in place.
  * Replaces LAPACKE_dpotrf(matrix_layout, uplo, n, a, lda) as used by
  * Eigen/src/Cholesky/LLT_LAPACKE.h:59 and dpotrf_ (lapack/cholesky.cpp:14-36). */
