@@ -105,10 +105,11 @@ __device__ __forceinline__ int scale_exp(double m) {
 }
 
 // The 8 slices of v / 2^e (|v| < 2^e) in integer arithmetic on v's bit pattern (the FP64 pipe of
-// GB300 is too slow to spend on this): N = round(v 2^(56 - e)) as an int64, then balanced base-128
-// digits from the top, s_1 = round(N / 2^49), s_2 = round((N - s_1 2^49) / 2^42), ..., each digit
-// rounded to nearest so that |s_1| <= 128 and |s_p| <= 64 (p > 1).  What falls below 2^-56 is
-// rounded away.
+// GB300 is too slow to spend on this): N = round(v 2^(56 - e)), |N| < 2^56, as a 64-bit integer, then
+// balanced base-128 digits taken from the bottom in 32-bit arithmetic on its two 28-bit halves,
+// d = ((x + 64) mod 128) - 64 and x = (x - d) / 128, with the carry of the low half passed to the
+// high half.  The seven low digits lie in [-64, 63] and the top one in [-128, 128]; sum_p d_p
+// 2^(7(8-p)) = N exactly.  What falls below 2^-56 is rounded away.
 __device__ __forceinline__ void split8(double v, int e, float* sl) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
   const int E = (int)((bits >> 52) & 0x7FF);
@@ -120,21 +121,31 @@ __device__ __forceinline__ void split8(double v, int e, float* sl) {
     M |= 1ull << 52;
     ex = E - 1075;
   }
-  // |v| = M 2^ex, and N = M 2^(ex + 56 - e), |N| < 2^56
-  const int sh = ex + 56 - e;
-  long long N;
-  if (E == 0x7FF) N = 0;  // non-finite: reported through the flag, not the slices
-  else if (sh >= 0) N = (long long)(M << (sh > 3 ? 3 : sh));
-  else if (sh > -64) N = (long long)((M + (1ull << (-sh - 1))) >> (-sh));
-  else N = 0;
-  if (bits >> 63) N = -N;
+  const int sh = ex + 56 - e;  // |v| = M 2^ex, N = M 2^sh
+  unsigned long long U;
+  if (E == 0x7FF) U = 0;  // non-finite: reported through the flag, not the slices
+  else if (sh >= 0) U = M << (sh > 3 ? 3 : sh);
+  else if (sh > -64) U = (M + (1ull << (-sh - 1))) >> (-sh);
+  else U = 0;
+  const bool neg = (bits >> 63) != 0;
+  // two's-complement halves of +-U: N = hi 2^28 + lo, lo in [0, 2^28)
+  const long long N = neg ? -(long long)U : (long long)U;
+  int lo = (int)(N & 0xFFFFFFF);
+  int hi = (int)(N >> 28);
 #pragma unroll
-  for (int p = 0; p < S; ++p) {
-    const int k = BETA * (S - 1 - p);  // 49, 42, ..., 0
-    const long long d = k ? ((N + (1ll << (k - 1))) >> k) : N;  // nearest (ties up), arithmetic shift
-    N -= d * (1ll << k);
+  for (int p = S - 1; p >= 4; --p) {  // low half: digits 8, 7, 6, 5
+    const int d = ((lo + 64) & 127) - 64;
     sl[p] = (float)d;
+    lo = (lo - d) >> 7;
   }
+  hi += lo;  // the carry out of the low half (0 or 1)
+#pragma unroll
+  for (int p = 3; p >= 1; --p) {
+    const int d = ((hi + 64) & 127) - 64;
+    sl[p] = (float)d;
+    hi = (hi - d) >> 7;
+  }
+  sl[0] = (float)hi;
 }
 
 // Scale exponent of every row from its maximum (one thread per row).
@@ -669,9 +680,14 @@ __global__ void __launch_bounds__(128) oz_panel_slice_kernel(const double* __res
                                                              int* __restrict__ pexp) {
   const long long i = (long long)blockIdx.x * 128 + threadIdx.x;
   if (i >= rs) return;
-  double m = 0.0;
-  for (int p = 0; p < bs; ++p) m = fmax(m, fabs(l21[(long long)p * lda + i]));
-  const int e = scale_exp(m);
+  // the maximum of |v| on bit patterns (integer pipe): non-negative doubles order like integers
+  unsigned long long mb = 0;
+#pragma unroll 8
+  for (int p = 0; p < bs; ++p) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(l21[(long long)p * lda + i]) & ~(1ull << 63);
+    mb = b > mb ? b : mb;
+  }
+  const int e = scale_exp(__longlong_as_double((long long)mb));
   pexp[i] = e;
 #pragma unroll 1
   for (int p0 = 0; p0 < w; p0 += 8) {
