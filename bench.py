@@ -275,14 +275,20 @@ def measured_peaks() -> dict:
 # law that scales them to this run's launch (profiles/ holds the summaries with the commands):
 #   symm_residual_f64 (NR = 16 kernel): 1.628 GB at n = 8192, 64 RHS; A's stored tiles are read
 #     once per 16-column chunk of right-hand sides, so traffic grows as n^2 * ceil(k / 16).
-NCU_TRAFFIC = {"symm_residual_f64": (8192, 64, 1.628e9)}
+#   sweep_f32 (16-column chains): 141.4 MB at n = 8192, 64 RHS (mean of the forward and backward
+#     launch); the triangle of L is read once whatever k is, so traffic grows as n^2.
+NCU_TRAFFIC = {"symm_residual_f64": (8192, 64, 1.628e9, "n2_kchunks"),
+               "sweep_f32": (8192, 64, 1.414e8, "n2")}
 
 
 def ncu_traffic(name: str, n: int, k: int):
     if name not in NCU_TRAFFIC or k < 16:
         return None
-    n0, k0, by = NCU_TRAFFIC[name]
-    return by * (n / n0) ** 2 * (-(-k // 16)) / (-(-k0 // 16))
+    n0, k0, by, law = NCU_TRAFFIC[name]
+    scale = (n / n0) ** 2
+    if law == "n2_kchunks":
+        scale *= (-(-k // 16)) / (-(-k0 // 16))
+    return by * scale
 
 
 def roofline_for(name: str, st: dict, peaks: dict, n: int = 0, k: int = 0) -> dict:
@@ -304,7 +310,8 @@ def roofline_for(name: str, st: dict, peaks: dict, n: int = 0, k: int = 0) -> di
     traffic = ncu_traffic(name, n, k)
     return {"kernel": name, "bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
             "traffic": traffic, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at n=8192, "
-            "64 RHS, scaled by n^2 ceil(k/16)" if traffic else None, "launches": st["launches"],
+            f"64 RHS, scaled by {'n^2 ceil(k/16)' if NCU_TRAFFIC[name][3] == 'n2_kchunks' else 'n^2'}"
+            if traffic else None, "launches": st["launches"],
             "per_launch_flops": st["flops"] / st["launches"], "per_launch_bytes": st["bytes"] / st["launches"],
             "peak_source": src}
 
@@ -513,6 +520,7 @@ def run_c3(args):
             for prec in args.c3_precisions.split(","):
                 G.posv_mixed_dev(A0, n, n, B0, n, X, n, k, G.mixed_opts(prec, 10, 1e-14, False), "L", s,
                                  raise_on_error=False)  # warm-up
+                X.zero_()  # a failed low-precision factorisation leaves X untouched
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
                 rc, rep = G.posv_mixed_dev(A0, n, n, B0, n, X, n, k, G.mixed_opts(prec, 10, 1e-14, False), "L", s,
@@ -522,7 +530,8 @@ def run_c3(args):
                 R = A0 @ X.T - B0.T
                 be = float(torch.linalg.norm(R) / (torch.linalg.norm(A0) * torch.linalg.norm(X)))
                 out["results"].append({"path": "mixed", "precision": prec, "nrhs": k, "kappa": kappa, "seconds": dt,
-                                       "reached_1e-14": bool(rc == 0 and be <= 1e-14), "steps": rep["steps"],
+                                       "reached_1e-14": bool(rc == 0 and rep["info"] == 0 and rep["converged"]
+                                                             and be <= 1e-14), "steps": rep["steps"],
                                        "info": rep["info"], "backward_error": be, "factor_ms": rep["factor_ms"],
                                        "refine_ms": rep["refine_ms"]})
                 print(json.dumps(out["results"][-1]), file=sys.stderr, flush=True)
