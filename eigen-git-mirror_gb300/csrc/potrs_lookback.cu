@@ -12,7 +12,8 @@
 //     substitution on the critical path), stores Y_I, fences, and raises its flag.
 // The backward sweep runs the same scheme on L^T from the last block up.  Right-hand sides are
 // split into chunks of 16 that run as independent chains in the same launch (grid.y), so the FP64
-// work of the last row blocks is spread over several SMs.
+// work of the last row blocks is spread over several SMs.  That is the FP64 sweep (sweep_kernel);
+// the FP32 sweep (sweep_ll_kernel, below) shortens each link of the chain further.
 //
 // The diagonal inverses come from trinv_kernel (one CTA per block, column-wise substitution).
 //
@@ -21,6 +22,8 @@
 // backward sweep applies D's pseudo-inverse to each block's right-hand sides as it loads them
 // (DSCALE: divide where |d| > the smallest normal number, else 0, LDLT.h:587-600).
 #include <cfloat>
+#include <cstdint>
+#include <type_traits>
 
 #include "internal.h"
 
@@ -221,12 +224,390 @@ void launch_sweep(int nb, const T* a, long long lda, long long n, T* b, long lon
   else launch_sweep_rc<T, UP, BWD, 16, DSCALE>(nb, a, lda, n, b, ldb, nrhs, inv, flags, counter, err, s);
 }
 
+// ---------------------------------------------------------------------------------------------
+// FP32 sweeps that publish each solved value as its own ready signal.
+//
+// Each solved value is published once more in a word buffer that is filled with the all-ones
+// pattern (a NaN) before every sweep; a word is ready when it differs from that pattern, and a
+// solved value with exactly that bit pattern is published as the canonical NaN instead.  A
+// consumer polls the values themselves, so a chain link costs one store and one load round trip:
+// no fence, no separate flag, no re-read of the block.
+//
+// Per row block I the CTA forms, off the chain's critical path:
+//   M_I = D_I G_{I-1}            (D_I = the inverted diagonal triangle, G_{I-1} = the tile of the
+//                                 block the chain delivers last),
+//   z_I = D_I (B_I - sum_J G_J Y_J) over the blocks before that one,
+// and on the critical path only x_I = z_I - M_I Y_{I-1}: one 64 x 64 x RCT product per link.
+// Off-diagonal tiles stream into shared memory with cp.async one tile ahead, and the next block's
+// words are requested before the current product, so a CTA that starts behind the chain catches up
+// at the rate of its tile loads.  Tickets interleave the right-hand-side chains (ticket t: chain
+// t % nch, t / nch-th block of the sweep), so the CTAs resident at any time work on the same part
+// of every chain.
+// ---------------------------------------------------------------------------------------------
+
+constexpr int LL_RC = 64;     // right-hand sides per launch: up to 4 chains of 16
+constexpr int PF_PITCH = 68;  // row pitch (floats) of a tile stored with p contiguous
+
+struct LLSmem {
+  float Lb[2][RB * PF_PITCH];  // off-diagonal tiles (double-buffered)
+  float Ds[RB * (RB + 1)];     // Ds[i * 65 + r] = D(r, i)
+  float Ms[RB * RB];           // Ms[p * 64 + r] = M(r, p)
+  float Ys[RB * 16];           // staged 64 x RCT block; flat index = word index
+};
+
+__device__ __forceinline__ uint32_t sptr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(sptr(dst)), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src, int bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(sptr(dst)), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Tile G(rr, p) of the sweep for row block I0 and column block J0.  RFAST: element (rr, p) at
+// a[(J0 + p) lda + I0 + rr], kept as lb[p * 64 + rr]; otherwise at a[(I0 + rr) lda + J0 + p], kept as
+// lb[rr * 68 + p].  Entries beyond n are zero-filled.  VEC: 16-byte copies (a 16-byte aligned,
+// lda a multiple of 4).
+template <bool RFAST, bool VEC>
+__device__ __forceinline__ void load_tile(float* lb, const float* __restrict__ a, long long lda, long long n,
+                                          long long I0, long long J0, int tid) {
+  if (VEC) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int idx = tid + k * 256;
+      const int f = (idx & 15) * 4, s = idx >> 4;  // f: contiguous index (4 per chunk), s: strided
+      const long long fg = (RFAST ? I0 : J0) + f, sg = (RFAST ? J0 : I0) + s;
+      const int bytes = (fg < n && sg < n) ? (int)(n - fg < 4 ? n - fg : 4) * 4 : 0;
+      const float* src = bytes ? a + sg * lda + fg : a;
+      cp_async16(RFAST ? lb + s * 64 + f : lb + s * PF_PITCH + f, src, bytes);
+    }
+  } else {
+#pragma unroll 4
+    for (int k = 0; k < 16; ++k) {
+      const int idx = tid + k * 256;
+      const int f = idx & 63, s = idx >> 6;
+      const long long fg = (RFAST ? I0 : J0) + f, sg = (RFAST ? J0 : I0) + s;
+      const int bytes = (fg < n && sg < n) ? 4 : 0;
+      const float* src = bytes ? a + sg * lda + fg : a;
+      cp_async4(RFAST ? lb + s * 64 + f : lb + s * PF_PITCH + f, src, bytes);
+    }
+  }
+}
+
+constexpr unsigned NOT_READY = 0xFFFFFFFFu;  // the fill pattern of the word buffer
+constexpr unsigned CANON_NAN = 0x7FC00000u;
+
+template <int CPT>
+__device__ __forceinline__ void ll_load(const unsigned* src, unsigned* w) {
+  if (CPT == 4) {
+    asm volatile("ld.volatile.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3])
+                 : "l"(src)
+                 : "memory");
+  } else {
+    asm volatile("ld.volatile.global.u32 %0, [%1];" : "=r"(w[0]) : "l"(src) : "memory");
+  }
+}
+
+template <int CPT>
+__device__ __forceinline__ bool ll_valid(const unsigned* w) {
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) ok = ok && w[k] != NOT_READY;
+  return ok;
+}
+
+template <int CPT>
+__device__ __forceinline__ void ll_store(unsigned* dst, const float* x) {
+  unsigned w[CPT];
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const unsigned u = __float_as_uint(x[k]);
+    w[k] = u == NOT_READY ? CANON_NAN : u;
+  }
+  if (CPT == 4) {
+    asm volatile("st.volatile.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "r"(w[0]), "r"(w[1]), "r"(w[2]),
+                 "r"(w[3])
+                 : "memory");
+  } else {
+    asm volatile("st.volatile.global.u32 [%0], %1;" ::"l"(dst), "r"(w[0]) : "memory");
+  }
+}
+
+template <bool RFAST, int CPT>
+__device__ __forceinline__ void tile_product(const float* lb, const float* ys, int r, int cq, float* acc) {
+  constexpr int RCT = 4 * CPT;
+  if (RFAST) {
+#pragma unroll 8
+    for (int p = 0; p < RB; ++p) {
+      const float l = lb[p * 64 + r];
+      if (CPT == 4) {
+        const float4 y = *reinterpret_cast<const float4*>(ys + p * RCT + cq * 4);
+        acc[0] = fmaf(l, y.x, acc[0]);
+        acc[1] = fmaf(l, y.y, acc[1]);
+        acc[2] = fmaf(l, y.z, acc[2]);
+        acc[3] = fmaf(l, y.w, acc[3]);
+      } else {
+        acc[0] = fmaf(l, ys[p * RCT + cq], acc[0]);
+      }
+    }
+  } else {
+#pragma unroll 2
+    for (int p = 0; p < RB; p += 4) {
+      const float4 l4 = *reinterpret_cast<const float4*>(lb + r * PF_PITCH + p);
+      const float lv[4] = {l4.x, l4.y, l4.z, l4.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (CPT == 4) {
+          const float4 y = *reinterpret_cast<const float4*>(ys + (p + u) * RCT + cq * 4);
+          acc[0] = fmaf(lv[u], y.x, acc[0]);
+          acc[1] = fmaf(lv[u], y.y, acc[1]);
+          acc[2] = fmaf(lv[u], y.z, acc[2]);
+          acc[3] = fmaf(lv[u], y.w, acc[3]);
+        } else {
+          acc[0] = fmaf(lv[u], ys[(p + u) * RCT + cq], acc[0]);
+        }
+      }
+    }
+  }
+}
+
+// out[q] (+)= sum_p S[p * pitch + r] * ys[p][cq * CPT + q]: the product of a shared 64 x 64 matrix
+// stored column by column (consecutive r) with the staged block.
+template <int CPT>
+__device__ __forceinline__ void colmajor_product(const float* S, int pitch, const float* ys, int r, int cq,
+                                                 float* out) {
+  constexpr int RCT = 4 * CPT;
+#pragma unroll 8
+  for (int p = 0; p < RB; ++p) {
+    const float s = S[p * pitch + r];
+    if (CPT == 4) {
+      const float4 y = *reinterpret_cast<const float4*>(ys + p * RCT + cq * 4);
+      out[0] = fmaf(s, y.x, out[0]);
+      out[1] = fmaf(s, y.y, out[1]);
+      out[2] = fmaf(s, y.z, out[2]);
+      out[3] = fmaf(s, y.w, out[3]);
+    } else {
+      out[0] = fmaf(s, ys[p * RCT + cq], out[0]);
+    }
+  }
+}
+
+// Sleep between polls of a block `dist` links before this CTA's own: the block has dist - 1 links
+// of slack before it is on the critical path.
+__device__ __forceinline__ unsigned poll_sleep_ns(int dist) { return dist <= 1 ? 0u : (dist > 6 ? 2000u : 400u * (dist - 1)); }
+
+template <int CPT>
+__device__ __forceinline__ bool ll_wait_block(const unsigned* src, unsigned* w, int dist, int* err) {
+  if (ll_valid<CPT>(w)) return true;
+  const unsigned ns = poll_sleep_ns(dist);
+  const unsigned long long t0 = gtimer();
+  for (int it = 1;; ++it) {
+    if (ns) __nanosleep(ns);
+    ll_load<CPT>(src, w);
+    if (ll_valid<CPT>(w)) return true;
+    if ((it & 63) == 0) {
+      if (*(volatile int*)err) return false;
+      if (gtimer() - t0 > WAIT_NS) {
+        atomicExch(err, 1);
+        return false;
+      }
+    }
+  }
+}
+
+// One CTA per (row block, right-hand-side chain); 256 threads, thread (r, cq) owns row r and
+// right-hand sides cq * CPT .. cq * CPT + CPT - 1 of its chain (RCT = 4 CPT columns per chain).
+template <bool UP, bool BWD, int CPT, bool DSCALE, bool VEC>
+__global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__ a, long long lda, long long n,
+                                                       float* __restrict__ b, long long ldb, int nrhs,
+                                                       const float* __restrict__ inv, unsigned* __restrict__ ll,
+                                                       int nch, int* __restrict__ counter, int* __restrict__ err) {
+  constexpr int RCT = 4 * CPT;
+  constexpr bool RFAST = (!BWD && !UP) || (BWD && UP);
+  extern __shared__ __align__(16) unsigned char ll_raw[];
+  LLSmem& sm = *reinterpret_cast<LLSmem*>(ll_raw);
+  __shared__ int s_ticket;
+  const int tid = threadIdx.x, r = tid & 63, cq = tid >> 6;
+  const int nb = (int)((n + RB - 1) / RB);
+  if (tid == 0) s_ticket = atomicAdd(counter, 1);
+  __syncthreads();
+  const int ch = s_ticket % nch, rank = s_ticket / nch;
+  const int I = BWD ? nb - 1 - rank : rank;
+  const long long I0 = (long long)I * RB;
+  b += (long long)ch * RCT * ldb;
+  nrhs -= ch * RCT;
+  unsigned* llc = ll + (size_t)ch * nb * RB * RCT;  // block J's words at J * 64 * RCT
+  const int step = BWD ? -1 : 1;
+  const bool has_prev = BWD ? I < nb - 1 : I > 0;
+  const int Jlast = I - step;  // the block the chain delivers last to this one
+  const int Jfirst = BWD ? nb - 1 : 0;
+  const int nloop = has_prev ? (BWD ? nb - 2 - I : I - 1) : 0;  // blocks before Jlast
+
+  // 1. inputs that depend on no other block: the last-delivered tile (group 0), the first loop
+  //    tile (group 1), the diagonal inverse and this block's right-hand sides
+  if (has_prev) load_tile<RFAST, VEC>(sm.Lb[0], a, lda, n, I0, (long long)Jlast * RB, tid);
+  cp_commit();
+  if (nloop > 0) load_tile<RFAST, VEC>(sm.Lb[1], a, lda, n, I0, (long long)Jfirst * RB, tid);
+  cp_commit();
+  const float* Dinv = inv + (long long)I * RB * RB;  // column-major Linv of block I
+  for (int idx = tid; idx < RB * RB; idx += 256) {
+    const int lo = idx & 63, hi = idx >> 6;
+    if (!BWD) sm.Ds[hi * 65 + lo] = Dinv[idx];  // D(lo, hi) = Linv(lo, hi)
+    else sm.Ds[lo * 65 + hi] = Dinv[idx];       // D(hi, lo) = Linv(lo, hi)
+  }
+  float bv[CPT];
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    const int c = cq * CPT + q;
+    float v = 0.f;
+    if (I0 + r < n && c < nrhs) {
+      v = b[(long long)c * ldb + I0 + r];
+      if (DSCALE) v = dplus(v, a[(I0 + r) * (lda + 1)]);
+    }
+    bv[q] = v;
+  }
+  unsigned w[CPT];
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) w[q] = NOT_READY;
+  if (has_prev) ll_load<CPT>(llc + (size_t)(nloop > 0 ? Jfirst : Jlast) * RB * RCT + tid * CPT, w);
+
+  // 2. M = D G_last, kept column by column (Ms[p * 64 + r] = M(r, p)); thread (r, cq) forms
+  //    columns cq * 16 .. cq * 16 + 15
+  cp_wait1();
+  __syncthreads();
+  if (has_prev) {
+    float m[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) m[j] = 0.f;
+#pragma unroll 4
+    for (int i = 0; i < RB; ++i) {
+      const float d = sm.Ds[i * 65 + r];
+      if (RFAST) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) m[j] = fmaf(d, sm.Lb[0][(cq * 16 + j) * 64 + i], m[j]);
+      } else {
+#pragma unroll
+        for (int k4 = 0; k4 < 4; ++k4) {
+          const float4 g = *reinterpret_cast<const float4*>(sm.Lb[0] + i * PF_PITCH + cq * 16 + 4 * k4);
+          m[4 * k4 + 0] = fmaf(d, g.x, m[4 * k4 + 0]);
+          m[4 * k4 + 1] = fmaf(d, g.y, m[4 * k4 + 1]);
+          m[4 * k4 + 2] = fmaf(d, g.z, m[4 * k4 + 2]);
+          m[4 * k4 + 3] = fmaf(d, g.w, m[4 * k4 + 3]);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 16; ++j) sm.Ms[(cq * 16 + j) * 64 + r] = m[j];
+  }
+  __syncthreads();  // Lb[0] is free for the first prefetch
+
+  // 3. the blocks before Jlast, in the order the chain delivers them; tile k sits in Lb[(k+1) & 1]
+  float acc[CPT];
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) acc[q] = 0.f;
+  for (int k = 0; k < nloop; ++k) {
+    const int J = Jfirst + k * step;
+    if (k + 1 < nloop) load_tile<RFAST, VEC>(sm.Lb[k & 1], a, lda, n, I0, (long long)(J + step) * RB, tid);
+    cp_commit();
+    const bool ok =
+        ll_wait_block<CPT>(llc + (size_t)J * RB * RCT + tid * CPT, w, BWD ? J - I : I - J, err);
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) sm.Ys[tid * CPT + q] = __uint_as_float(w[q]);
+    cp_wait1();
+    if (__syncthreads_or(!ok)) {
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      return;
+    }
+    // request the next awaited block's words before this product
+    ll_load<CPT>(llc + (size_t)(k + 1 < nloop ? J + step : Jlast) * RB * RCT + tid * CPT, w);
+    tile_product<RFAST, CPT>(sm.Lb[(k + 1) & 1], sm.Ys, r, cq, acc);
+    __syncthreads();
+  }
+
+  // 4. z = D (B - acc), then x = z - M Y_last
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) sm.Ys[r * RCT + cq * CPT + q] = bv[q] - acc[q];
+  __syncthreads();
+  float x[CPT];
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) x[q] = 0.f;
+  colmajor_product<CPT>(sm.Ds, RB + 1, sm.Ys, r, cq, x);
+  if (has_prev) {
+    float* yl = sm.Lb[0];  // both tile buffers are idle now
+    const bool ok = ll_wait_block<CPT>(llc + (size_t)Jlast * RB * RCT + tid * CPT, w, 1, err);
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) yl[tid * CPT + q] = __uint_as_float(w[q]);
+    if (__syncthreads_or(!ok)) return;
+    float mv[CPT];
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) mv[q] = 0.f;
+    colmajor_product<CPT>(sm.Ms, RB, yl, r, cq, mv);
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) x[q] -= mv[q];
+  }
+  ll_store<CPT>(llc + (size_t)I * RB * RCT + r * RCT + cq * CPT, x);
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    const int c = cq * CPT + q;
+    if (I0 + r < n && c < nrhs) b[(long long)c * ldb + I0 + r] = x[q];
+  }
+}
+
+template <bool UP, bool BWD, int CPT, bool DSCALE>
+void launch_sweep_ll_cpt(int nb, int nch, const float* a, long long lda, long long n, float* b, long long ldb,
+                         int nrhs, const float* inv, unsigned* ll, int* counter, int* err,
+                         cudaStream_t s) {
+  const int smem = (int)sizeof(LLSmem);
+  const bool vec = ((uintptr_t)a % 16 == 0) && (lda % 4 == 0);
+  if (vec) {
+    cudaFuncSetAttribute(sweep_ll_kernel<UP, BWD, CPT, DSCALE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         smem);
+    sweep_ll_kernel<UP, BWD, CPT, DSCALE, true>
+        <<<nb * nch, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, ll, nch, counter, err);
+  } else {
+    cudaFuncSetAttribute(sweep_ll_kernel<UP, BWD, CPT, DSCALE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         smem);
+    sweep_ll_kernel<UP, BWD, CPT, DSCALE, false>
+        <<<nb * nch, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, ll, nch, counter, err);
+  }
+}
+
+// Chains of 4 right-hand sides for nrhs <= 4, else of 16 (nrhs <= LL_RC per launch).
+inline int ll_chain_cols(int nrhs) { return nrhs <= 4 ? 4 : 16; }
+
+template <bool UP, bool BWD, bool DSCALE = false>
+void launch_sweep_ll(int nb, const float* a, long long lda, long long n, float* b, long long ldb, int nrhs,
+                     const float* inv, unsigned* ll, int* counter, int* err, cudaStream_t s) {
+  const int rct = ll_chain_cols(nrhs), nch = (nrhs + rct - 1) / rct;
+  if (rct == 4)
+    launch_sweep_ll_cpt<UP, BWD, 1, DSCALE>(nb, nch, a, lda, n, b, ldb, nrhs, inv, ll, counter, err, s);
+  else
+    launch_sweep_ll_cpt<UP, BWD, 4, DSCALE>(nb, nch, a, lda, n, b, ldb, nrhs, inv, ll, counter, err, s);
+}
+
+// Workspace layouts.  FP64: diagonal inverses | flags, tickets, error word (chains of one launch).
+// FP32: diagonal inverses | tickets, error word | published words (LL_RC per row).
+size_t ws_flags_offset(int64_t nb, size_t elem) { return ((size_t)nb * RB * RB * elem + 255) & ~(size_t)255; }
+size_t ws_words_offset(int64_t nb) { return ws_flags_offset(nb, sizeof(float)) + 256; }
+size_t ws_bytes_f64(int64_t nb) {
+  const int64_t nch = RC / 16;  // chains of one launch, at most
+  return ws_flags_offset(nb, sizeof(double)) + (size_t)(2 * nch * nb + 2 * nch + 8) * sizeof(int) + 256;
+}
+size_t ws_bytes_f32(int64_t nb) { return ws_words_offset(nb) + (size_t)nb * RB * LL_RC * sizeof(unsigned) + 256; }
+
 }  // namespace
 
+// A workspace sized for FP64 also serves the FP32 solve of the same order (the mixed-precision
+// driver runs both on one workspace).
 size_t potrs_ws_bytes(int64_t n, size_t elem) {
   const int64_t nb = (n + RB - 1) / RB;
-  const int64_t nch = RC / 16;  // chains of one launch, at most
-  return (size_t)nb * RB * RB * elem + (size_t)(2 * nch * nb + 2 * nch + 8) * sizeof(int) + 512;
+  const size_t f32 = ws_bytes_f32(nb);
+  if (elem == sizeof(float)) return f32;
+  const size_t f64 = ws_bytes_f64(nb);
+  return f64 > f32 ? f64 : f32;
 }
 
 // Both sweeps; ldl: the factor is the unit L of LDL^T with D on its diagonal.
@@ -249,31 +630,63 @@ int sweeps_ws(bool upper, bool ldl, int64_t n, int64_t nrhs, const T* a, int64_t
       else trinv_kernel<T, false, false><<<nb, 128, 0, s>>>(a, lda, n, inv);
     }
   }
-  for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
-    const int nc = (int)(nrhs - c0 < RC ? nrhs - c0 : RC);
-    const int nch = nc <= 4 ? 1 : (nc + 15) / 16;  // chains in this launch
-    int* fflags = base;                 // forward: nch x nb
-    int* bflags = base + nch * nb;      // backward: nch x nb
-    int* fctr = base + 2 * nch * nb;    // nch forward tickets, nch backward tickets, error word
-    int* bctr = fctr + nch;
-    int* err = bctr + nch;
-    T* bc = b + c0 * ldb;
-    GB_CUDA_TRY(cudaMemsetAsync(base, 0, (size_t)(2 * nch * nb + 2 * nch + 1) * sizeof(int), s));
-    // algorithmic work per sweep: the lower triangle of L read once, 2 flops per entry and RHS
-    const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
-    {
-      ProfScope ps(kf.c_str(), s, fl, by);
-      if (upper) launch_sweep<T, true, false>(nb, a, lda, n, bc, ldb, nc, inv, fflags, fctr, err, s);
-      else launch_sweep<T, false, false>(nb, a, lda, n, bc, ldb, nc, inv, fflags, fctr, err, s);
+  if constexpr (std::is_same<T, float>::value) {
+    unsigned* words = (unsigned*)((char*)ws + ws_words_offset(nb));
+    int* fctr = base;
+    int* bctr = base + 1;
+    int* err = base + 2;
+    for (int64_t c0 = 0; c0 < nrhs; c0 += LL_RC) {
+      const int nc = (int)(nrhs - c0 < LL_RC ? nrhs - c0 : LL_RC);
+      const int rct = ll_chain_cols(nc), nch = (nc + rct - 1) / rct;
+      const size_t wbytes = (size_t)nch * nb * RB * rct * sizeof(unsigned);
+      float* bc = b + c0 * ldb;
+      GB_CUDA_TRY(cudaMemsetAsync(base, 0, 3 * sizeof(int), s));
+      GB_CUDA_TRY(cudaMemsetAsync(words, 0xFF, wbytes, s));
+      const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
+      {
+        ProfScope ps(kf.c_str(), s, fl, by);
+        if (upper) launch_sweep_ll<true, false>(nb, a, lda, n, bc, ldb, nc, inv, words, fctr, err, s);
+        else launch_sweep_ll<false, false>(nb, a, lda, n, bc, ldb, nc, inv, words, fctr, err, s);
+      }
+      GB_CUDA_TRY(cudaMemsetAsync(words, 0xFF, wbytes, s));
+      {
+        ProfScope ps(kf.c_str(), s, fl, by);
+        if (ldl) {
+          if (upper) launch_sweep_ll<true, true, true>(nb, a, lda, n, bc, ldb, nc, inv, words, bctr, err, s);
+          else launch_sweep_ll<false, true, true>(nb, a, lda, n, bc, ldb, nc, inv, words, bctr, err, s);
+        } else {
+          if (upper) launch_sweep_ll<true, true>(nb, a, lda, n, bc, ldb, nc, inv, words, bctr, err, s);
+          else launch_sweep_ll<false, true>(nb, a, lda, n, bc, ldb, nc, inv, words, bctr, err, s);
+        }
+      }
     }
-    {
-      ProfScope ps(kf.c_str(), s, fl, by);
-      if (ldl) {
-        if (upper) launch_sweep<T, true, true, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
-        else launch_sweep<T, false, true, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
-      } else {
-        if (upper) launch_sweep<T, true, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
-        else launch_sweep<T, false, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
+  } else {
+    for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
+      const int nc = (int)(nrhs - c0 < RC ? nrhs - c0 : RC);
+      const int nch = nc <= 4 ? 1 : (nc + 15) / 16;  // chains in this launch
+      int* fflags = base;                 // forward: nch x nb
+      int* bflags = base + nch * nb;      // backward: nch x nb
+      int* fctr = base + 2 * nch * nb;    // nch forward tickets, nch backward tickets, error word
+      int* bctr = fctr + nch;
+      int* err = bctr + nch;
+      T* bc = b + c0 * ldb;
+      GB_CUDA_TRY(cudaMemsetAsync(base, 0, (size_t)(2 * nch * nb + 2 * nch + 1) * sizeof(int), s));
+      // algorithmic work per sweep: the lower triangle of L read once, 2 flops per entry and RHS
+      const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
+      {
+        ProfScope ps(kf.c_str(), s, fl, by);
+        if (upper) launch_sweep<T, true, false>(nb, a, lda, n, bc, ldb, nc, inv, fflags, fctr, err, s);
+        else launch_sweep<T, false, false>(nb, a, lda, n, bc, ldb, nc, inv, fflags, fctr, err, s);
+      }
+      {
+        ProfScope ps(kf.c_str(), s, fl, by);
+        if (ldl) {
+          if (upper) launch_sweep<T, true, true, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
+          else launch_sweep<T, false, true, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
+        } else {
+          if (upper) launch_sweep<T, true, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
+          else launch_sweep<T, false, true>(nb, a, lda, n, bc, ldb, nc, inv, bflags, bctr, err, s);
+        }
       }
     }
   }
@@ -306,22 +719,44 @@ int trsm_sweep_ws(bool upper, bool bwd, bool unit, int64_t n, int64_t nrhs, cons
       else trinv_kernel<T, false, false><<<nb, 128, 0, s>>>(a, lda, n, inv);
     }
   }
-  for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
-    const int nc = (int)(nrhs - c0 < RC ? nrhs - c0 : RC);
-    const int nch = nc <= 4 ? 1 : (nc + 15) / 16;
-    int* flags = base;
-    int* ctr = base + nch * nb;
-    int* err = ctr + nch;
-    T* bc = b + c0 * ldb;
-    GB_CUDA_TRY(cudaMemsetAsync(base, 0, (size_t)(nch * nb + nch + 1) * sizeof(int), s));
-    const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
-    ProfScope ps(kf.c_str(), s, fl, by);
-    if (bwd) {
-      if (upper) launch_sweep<T, true, true>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
-      else launch_sweep<T, false, true>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
-    } else {
-      if (upper) launch_sweep<T, true, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
-      else launch_sweep<T, false, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
+  if constexpr (std::is_same<T, float>::value) {
+    unsigned* words = (unsigned*)((char*)ws + ws_words_offset(nb));
+    int* ctr = base;
+    int* err = base + 1;
+    for (int64_t c0 = 0; c0 < nrhs; c0 += LL_RC) {
+      const int nc = (int)(nrhs - c0 < LL_RC ? nrhs - c0 : LL_RC);
+      const int rct = ll_chain_cols(nc), nch = (nc + rct - 1) / rct;
+      float* bc = b + c0 * ldb;
+      GB_CUDA_TRY(cudaMemsetAsync(base, 0, 2 * sizeof(int), s));
+      GB_CUDA_TRY(cudaMemsetAsync(words, 0xFF, (size_t)nch * nb * RB * rct * sizeof(unsigned), s));
+      const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
+      ProfScope ps(kf.c_str(), s, fl, by);
+      if (bwd) {
+        if (upper) launch_sweep_ll<true, true>(nb, a, lda, n, bc, ldb, nc, inv, words, ctr, err, s);
+        else launch_sweep_ll<false, true>(nb, a, lda, n, bc, ldb, nc, inv, words, ctr, err, s);
+      } else {
+        if (upper) launch_sweep_ll<true, false>(nb, a, lda, n, bc, ldb, nc, inv, words, ctr, err, s);
+        else launch_sweep_ll<false, false>(nb, a, lda, n, bc, ldb, nc, inv, words, ctr, err, s);
+      }
+    }
+  } else {
+    for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
+      const int nc = (int)(nrhs - c0 < RC ? nrhs - c0 : RC);
+      const int nch = nc <= 4 ? 1 : (nc + 15) / 16;
+      int* flags = base;
+      int* ctr = base + nch * nb;
+      int* err = ctr + nch;
+      T* bc = b + c0 * ldb;
+      GB_CUDA_TRY(cudaMemsetAsync(base, 0, (size_t)(nch * nb + nch + 1) * sizeof(int), s));
+      const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
+      ProfScope ps(kf.c_str(), s, fl, by);
+      if (bwd) {
+        if (upper) launch_sweep<T, true, true>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
+        else launch_sweep<T, false, true>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
+      } else {
+        if (upper) launch_sweep<T, true, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
+        else launch_sweep<T, false, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
+      }
     }
   }
   GB_CUDA_TRY(cudaGetLastError());
