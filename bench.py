@@ -313,7 +313,8 @@ def roofline_for(name: str, st: dict, peaks: dict, n: int = 0, k: int = 0) -> di
             f"64 RHS, scaled by {'n^2 ceil(k/16)' if NCU_TRAFFIC[name][3] == 'n2_kchunks' else 'n^2'}"
             if traffic else None, "launches": st["launches"],
             "per_launch_flops": st["flops"] / st["launches"], "per_launch_bytes": st["bytes"] / st["launches"],
-            "peak_source": src}
+            "peak_source": src,
+            "timing": "CUDA events around each launch of the kernel, on its stream, in a repeat of the K timed steps"}
 
 
 def run_ours(args, ws, rank, local):
@@ -364,7 +365,6 @@ def run_ours(args, ws, rank, local):
         barrier(ws)
         torch.cuda.synchronize()
         clocks.start()
-        G.profile_enable(True)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         if flush is None:  # inputs larger than L2: one timed region over all steps
@@ -387,6 +387,16 @@ def run_ours(args, ws, rank, local):
         torch.cuda.synchronize()
         barrier(ws)
         ck = clocks.stop()
+        # per-kernel device times (roofline, shares) from a repeat of the same K steps with CUDA
+        # events around every launch; the events cost a few percent, so they stay out of the timed
+        # region above
+        G.profile_enable(True)
+        for _ in range(args.steps):
+            if flush is not None:
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+            step_fn()
+        torch.cuda.synchronize()
         prof = G.profile_read()
         G.profile_enable(False)
         return max_over_ranks(ws, total_ms), prof, ck

@@ -302,7 +302,7 @@ int potrs_adjoint_dev(int64_t n, int64_t nrhs, const double* L, int64_t ldl, con
                       const double* Xb, int64_t ldxb, double* Bb, int64_t ldbb, double* Ab, int64_t ldab,
                       cudaStream_t s) {
   // Bbar = A^{-1} Xbar (the same two sweeps as the forward solve)
-  GB_CUDA_TRY(cudaMemcpy2DAsync(Bb, ldbb * 8, Xb, ldxb * 8, n * 8, nrhs, cudaMemcpyDeviceToDevice, s));
+  GB_CUDA_TRY(copy2d_async(Bb, ldbb * 8, Xb, ldxb * 8, n * 8, nrhs, cudaMemcpyDeviceToDevice, s));
   int rc = potrs_dev<double>(false, n, nrhs, L, ldl, Bb, ldbb, s);
   if (rc) return rc;
   if (Ab) {

@@ -221,12 +221,12 @@ int host_syrk(int layout, char uplo, char trans, int64_t n, int64_t k, T alpha, 
   T* d_a = (T*)buf.p;
   T* d_c = (T*)((char*)buf.p + ab);
   if (ar > 0 && ac > 0)
-    GB_CUDA_TRY(cudaMemcpy2DAsync(d_a, ar * es, a, lda * es, ar * es, ac, cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(copy2d_async(d_a, ar * es, a, lda * es, ar * es, ac, cudaMemcpyHostToDevice, s));
   // all of C goes up and comes back, so that the triangle the kernel does not touch is returned as
   // it was (with beta = 0 the kernel does not read the updated triangle)
-  GB_CUDA_TRY(cudaMemcpy2DAsync(d_c, n * es, c, ldc * es, n * es, n, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(copy2d_async(d_c, n * es, c, ldc * es, n * es, n, cudaMemcpyHostToDevice, s));
   if ((rc = syrk_dev<T>(upper, tr, n, k, alpha, d_a, max1(ar), beta, d_c, n, s))) return rc;
-  GB_CUDA_TRY(cudaMemcpy2DAsync(c, ldc * es, d_c, n * es, n * es, n, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(copy2d_async(c, ldc * es, d_c, n * es, n * es, n, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   return GBLLT_SUCCESS;
 }
@@ -270,12 +270,12 @@ int host_trsm(int layout, char side, char uplo, char transa, char diag, int64_t 
   if ((rc = buf.get(ab + (size_t)mm * nn * es, s))) return rc;
   T* d_a = (T*)buf.p;
   T* d_b = (T*)((char*)buf.p + ab);
-  GB_CUDA_TRY(cudaMemcpy2DAsync(d_a, na * es, a, lda * es, na * es, na, cudaMemcpyHostToDevice, s));
-  GB_CUDA_TRY(cudaMemcpy2DAsync(d_b, mm * es, b, ldb * es, mm * es, nn, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(copy2d_async(d_a, na * es, a, lda * es, na * es, na, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(copy2d_async(d_b, mm * es, b, ldb * es, mm * es, nn, cudaMemcpyHostToDevice, s));
   if ((rc = trsm_dev<T>(left, upper, is_trans(transa), diag == 'U' || diag == 'u', mm, nn, alpha, d_a, na, d_b, mm,
                         s)))
     return rc;
-  GB_CUDA_TRY(cudaMemcpy2DAsync(b, ldb * es, d_b, mm * es, mm * es, nn, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(copy2d_async(b, ldb * es, d_b, mm * es, mm * es, nn, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   return GBLLT_SUCCESS;
 }

@@ -189,19 +189,19 @@ int host_posv(bool do_factor, bool do_solve, int layout, char uplo, int64_t n, i
   DevStatus* st = (DevStatus*)((char*)d_bt + ((bbytes + 255) / 256) * 256);
   int64_t* dinfo = (int64_t*)((char*)st + 256);  // the allocation reserves 2 x 256 B past d_bt
 
-  GB_CUDA_TRY(cudaMemcpy2DAsync(d_a, n * es, a, lda * es, n * es, n, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(copy2d_async(d_a, n * es, a, lda * es, n * es, n, cudaMemcpyHostToDevice, s));
   if (do_solve && nrhs > 0) {
     if (!rowmajor) {
-      GB_CUDA_TRY(cudaMemcpy2DAsync(d_b, n * es, b, ldb * es, n * es, nrhs, cudaMemcpyHostToDevice, s));
+      GB_CUDA_TRY(copy2d_async(d_b, n * es, b, ldb * es, n * es, nrhs, cudaMemcpyHostToDevice, s));
     } else {  // row-major B (n x nrhs, ldb >= nrhs) seen column-major is B^T (nrhs x n)
-      GB_CUDA_TRY(cudaMemcpy2DAsync(d_bt, nrhs * es, b, ldb * es, nrhs * es, n, cudaMemcpyHostToDevice, s));
+      GB_CUDA_TRY(copy2d_async(d_bt, nrhs * es, b, ldb * es, nrhs * es, n, cudaMemcpyHostToDevice, s));
       if ((rc = transpose_dev<T>(nrhs, n, d_bt, nrhs, d_b, n, s))) return rc;
     }
   }
   int64_t h_info = 0;
   if (do_factor) {
     if ((rc = factor_dev<T>(upper, n, d_a, n, st, dinfo, s))) return rc;
-    GB_CUDA_TRY(cudaMemcpy2DAsync(a, lda * es, d_a, n * es, n * es, n, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(copy2d_async(a, lda * es, d_a, n * es, n * es, n, cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaMemcpyAsync(&h_info, dinfo, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     if (h_info == GBLLT_ERR_TIMEOUT) return GBLLT_ERR_TIMEOUT;
@@ -210,10 +210,10 @@ int host_posv(bool do_factor, bool do_solve, int layout, char uplo, int64_t n, i
   if (do_solve && nrhs > 0 && h_info == 0) {
     if ((rc = potrs_dev<T>(upper, n, nrhs, d_a, n, d_b, n, s))) return rc;
     if (!rowmajor) {
-      GB_CUDA_TRY(cudaMemcpy2DAsync(b, ldb * es, d_b, n * es, n * es, nrhs, cudaMemcpyDeviceToHost, s));
+      GB_CUDA_TRY(copy2d_async(b, ldb * es, d_b, n * es, n * es, nrhs, cudaMemcpyDeviceToHost, s));
     } else {
       if ((rc = transpose_dev<T>(n, nrhs, d_b, n, d_bt, nrhs, s))) return rc;
-      GB_CUDA_TRY(cudaMemcpy2DAsync(b, ldb * es, d_bt, nrhs * es, nrhs * es, n, cudaMemcpyDeviceToHost, s));
+      GB_CUDA_TRY(copy2d_async(b, ldb * es, d_bt, nrhs * es, nrhs * es, n, cudaMemcpyDeviceToHost, s));
     }
     GB_CUDA_TRY(cudaStreamSynchronize(s));
   }
@@ -326,22 +326,22 @@ extern "C" int gbllt_dposv_mixed(int layout, char uplo, int64_t n, int64_t nrhs,
   double* d_b = (double*)((char*)work.p + abytes);
   double* d_x = (double*)((char*)d_b + bbytes);
   double* d_t = (double*)((char*)d_x + bbytes);
-  GB_CUDA_TRY(cudaMemcpy2DAsync(d_a, n * es, a, lda * es, n * es, n, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(copy2d_async(d_a, n * es, a, lda * es, n * es, n, cudaMemcpyHostToDevice, s));
   if (!rowmajor) {
-    GB_CUDA_TRY(cudaMemcpy2DAsync(d_b, n * es, b, ldb * es, n * es, nrhs, cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(copy2d_async(d_b, n * es, b, ldb * es, n * es, nrhs, cudaMemcpyHostToDevice, s));
   } else {
-    GB_CUDA_TRY(cudaMemcpy2DAsync(d_t, nrhs * es, b, ldb * es, nrhs * es, n, cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(copy2d_async(d_t, nrhs * es, b, ldb * es, nrhs * es, n, cudaMemcpyHostToDevice, s));
     if ((rc = transpose_dev<double>(nrhs, n, d_t, nrhs, d_b, n, s))) return rc;
   }
   gbllt_mixed_report local;
   rc = posv_mixed_dev(upper, n, nrhs, d_a, n, d_b, n, d_x, n, opts, report ? report : &local, s);
   if (rc && rc != GBLLT_ERR_NOT_CONVERGED) return rc;
   if (!rowmajor) {
-    GB_CUDA_TRY(cudaMemcpy2DAsync(x, ldx * es, d_x, n * es, n * es, nrhs, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(copy2d_async(x, ldx * es, d_x, n * es, n * es, nrhs, cudaMemcpyDeviceToHost, s));
   } else {
     int rc2 = transpose_dev<double>(n, nrhs, d_x, n, d_t, nrhs, s);
     if (rc2) return rc2;
-    GB_CUDA_TRY(cudaMemcpy2DAsync(x, ldx * es, d_t, nrhs * es, nrhs * es, n, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(copy2d_async(x, ldx * es, d_t, nrhs * es, nrhs * es, n, cudaMemcpyDeviceToHost, s));
   }
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   return rc;

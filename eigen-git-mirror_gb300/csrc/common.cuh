@@ -52,4 +52,12 @@ __device__ __forceinline__ void lower_tile_coords(long long t, int& ti, int& tj)
   tj = (int)(t - i * (i + 1) / 2);
 }
 
+// FP32 rounded to TF32 (13 zero low bits), to nearest with ties away: one part of the split
+// operands of the tensor-core updates.
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
 }  // namespace gbllt

@@ -362,7 +362,7 @@ int host_pocon(int layout, char uplo, int64_t n, const T* l, int64_t ldl, T anor
   T* d = nullptr;
   if ((rc = alloc_async((void**)&d, (size_t)n * n * sizeof(T), s))) return rc;
   double r = 0.0;
-  if (cudaMemcpy2DAsync(d, n * sizeof(T), l, ldl * sizeof(T), n * sizeof(T), n, cudaMemcpyHostToDevice, s) !=
+  if (copy2d_async(d, n * sizeof(T), l, ldl * sizeof(T), n * sizeof(T), n, cudaMemcpyHostToDevice, s) !=
       cudaSuccess) {
     cudaGetLastError();
     set_error_message("gbllt_?pocon: host-to-device copy of the factor failed");

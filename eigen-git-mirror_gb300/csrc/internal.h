@@ -6,6 +6,14 @@
 
 namespace gbllt {
 
+// A 2-D copy (cudaMemcpy2DAsync's arguments) issued as one linear copy when both pitches equal the
+// row width, so a contiguous host matrix moves as one transfer.
+inline cudaError_t copy2d_async(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width,
+                                size_t height, cudaMemcpyKind kind, cudaStream_t s) {
+  if (dpitch == width && spitch == width) return cudaMemcpyAsync(dst, src, width * height, kind, s);
+  return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, s);
+}
+
 // Plain-path panel width: the diagonal block factored by one CTA and the depth of each
 // trailing update.
 constexpr int kNB = 64;
@@ -22,11 +30,19 @@ int potrf_lower_dev(int64_t n, T* d_a, int64_t lda, DevStatus* st, cudaStream_t 
 // Diagonal 64 x 64 block at (k0, k0): storage T, arithmetic TC.
 template <typename T, typename TC>
 void launch_potrf_diag(T* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s);
-// FP32 diagonal block in FP32 arithmetic, one warp (the mixed-precision factorisation).
-void launch_potrf_diag_f32w(float* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s);
+// FP32 diagonal block in FP32 arithmetic, 512 threads, one barrier per column (the mixed-precision
+// factorisation).
+// pk > 0: the block first receives A11 -= P P^T with P the pk columns from column pk0 in the block's
+// rows (one panel step whose trailing update left the block out).
+void launch_potrf_diag_f32s(float* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s,
+                            int64_t pk0 = 0, int pk = 0);
 // Rows below the block: A(k0+bs.., k0..k0+bs) <- A(...) L11^{-T}, rs rows.
 template <typename T>
 void launch_trsm_panel(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, cudaStream_t s);
+// The same FP32 solve, also writing the solved rows as np split parts (BF16, or TF32 when tf32 is
+// set), K-major with 64 columns per row: the operand of the mixed-precision in-panel update.
+void launch_trsm_panel_split(float* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, int tf32, int np,
+                             void* const* parts, cudaStream_t s);
 // Lower update of the first ncols columns of the rs x rs trailing matrix by the bs-wide panel:
 // A22 -= A21 A21^T, or A22 -= A21 B^T with B the rs x bs array at bsrc (leading dimension ldb).
 template <typename T>

@@ -367,7 +367,7 @@ int ldlt_factor_dev(bool upper, int64_t n, T* d_a, int64_t lda, int32_t* transp,
   const size_t es = sizeof(T);
   // 1. the pivot order from the diagonal
   std::vector<T> diag(n);
-  GB_CUDA_TRY(cudaMemcpy2DAsync(diag.data(), es, d_a, (size_t)(lda + 1) * es, es, (size_t)n, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(copy2d_async(diag.data(), es, d_a, (size_t)(lda + 1) * es, es, (size_t)n, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   std::vector<double> absd(n);
   for (int64_t i = 0; i < n; ++i) absd[i] = std::fabs((double)diag[i]);
@@ -498,9 +498,9 @@ int host_ldlt(int layout, char uplo, int64_t n, T* a, int64_t lda, int32_t* tran
   Scratch buf;
   if ((rc = buf.get((size_t)n * n * es, s))) return rc;
   T* d_a = (T*)buf.p;
-  GB_CUDA_TRY(cudaMemcpy2DAsync(d_a, n * es, a, lda * es, n * es, n, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(copy2d_async(d_a, n * es, a, lda * es, n * es, n, cudaMemcpyHostToDevice, s));
   if ((rc = ldlt_factor_dev<T>(upper, n, d_a, n, transp, sign, info, s))) return rc;
-  GB_CUDA_TRY(cudaMemcpy2DAsync(a, lda * es, d_a, n * es, n * es, n, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(copy2d_async(a, lda * es, d_a, n * es, n * es, n, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   return GBLLT_SUCCESS;
 }
@@ -556,19 +556,19 @@ int host_ldlt_solve(int layout, char uplo, int64_t n, int64_t nrhs, const T* a, 
   T* d_a = (T*)buf.p;
   T* d_b = (T*)((char*)buf.p + ab);
   T* d_t = (T*)((char*)buf.p + ab + bb);
-  GB_CUDA_TRY(cudaMemcpy2DAsync(d_a, n * es, a, lda * es, n * es, n, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(copy2d_async(d_a, n * es, a, lda * es, n * es, n, cudaMemcpyHostToDevice, s));
   if (!rowmajor) {
-    GB_CUDA_TRY(cudaMemcpy2DAsync(d_b, n * es, b, ldb * es, n * es, nrhs, cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(copy2d_async(d_b, n * es, b, ldb * es, n * es, nrhs, cudaMemcpyHostToDevice, s));
   } else {  // row-major B (n x nrhs) seen column-major is B^T
-    GB_CUDA_TRY(cudaMemcpy2DAsync(d_t, nrhs * es, b, ldb * es, nrhs * es, n, cudaMemcpyHostToDevice, s));
+    GB_CUDA_TRY(copy2d_async(d_t, nrhs * es, b, ldb * es, nrhs * es, n, cudaMemcpyHostToDevice, s));
     if ((rc = transpose_dev<T>(nrhs, n, d_t, nrhs, d_b, n, s))) return rc;
   }
   if ((rc = ldlt_solve_dev<T>(upper, n, nrhs, d_a, n, transp, d_b, n, s))) return rc;
   if (!rowmajor) {
-    GB_CUDA_TRY(cudaMemcpy2DAsync(b, ldb * es, d_b, n * es, n * es, nrhs, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(copy2d_async(b, ldb * es, d_b, n * es, n * es, nrhs, cudaMemcpyDeviceToHost, s));
   } else {
     if ((rc = transpose_dev<T>(n, nrhs, d_b, n, d_t, nrhs, s))) return rc;
-    GB_CUDA_TRY(cudaMemcpy2DAsync(b, ldb * es, d_t, nrhs * es, nrhs * es, n, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(copy2d_async(b, ldb * es, d_t, nrhs * es, nrhs * es, n, cudaMemcpyDeviceToHost, s));
   }
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   return GBLLT_SUCCESS;

@@ -70,12 +70,7 @@ __global__ void diag_scale_kernel(const double* __restrict__ a, long long lda, l
 
 // Tensor-core operands are K-major copies of panel values split into NP successive roundings:
 // part0 = round(v), part1 = round(v - part0), part2 = round(v - part0 - part1).  KIND 0 = bf16,
-// 1 = tf32 (fp32 with 13 zero low bits, rounded to nearest, ties away).
-__device__ __forceinline__ float to_tf32(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
+// 1 = tf32 (to_tf32).
 
 // K-major copies of the block Af(r0 .. r0+rows, c0 .. c0+bs) in NP parts, stored at
 // out[k][r * ldk + p] for p < bs (zero for bs <= p < ldk).
@@ -333,9 +328,14 @@ int split_parts(int prec) {
 // on tcgen05: the step's 64 columns are split into ipparts (K-major, 64 wide) and applied to the
 // lower part of the panel's remaining columns.  While the look-ahead update occupies the other
 // SMs, these launches are capped to the reserved SMs.
+// With an aux stream, the next step's diagonal block is left out of the in-panel update and is
+// factored on aux right after the panel solve, with this step's contribution applied by the
+// diagonal kernel itself, so it overlaps the in-panel update:
+//   ev[4]: the step's panel solve finished (aux waits)
+//   ev[5]: the next diagonal block is factored (main waits before the next panel solve)
 int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int reserve_sms, void* const* parts,
                     void* const* parts2, void* const* ipparts, int64_t ldk, DevStatus* st, int* d_err,
-                    cudaStream_t s, cudaStream_t side, cudaEvent_t* ev) {
+                    cudaStream_t s, cudaStream_t side, cudaEvent_t* ev, cudaStream_t aux) {
   static const std::string ksplit = "split_panel";
   const int kind = (prec == GBLLT_PREC_BF16 || prec == GBLLT_PREC_BF16X3 || prec == GBLLT_PREC_BF16X6) ? kTcBF16
                                                                                                        : kTcTF32;
@@ -345,6 +345,7 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
   const uint32_t code = np == 1 ? kSegX1 : np == 2 ? kSegX3 : kSegX6;
   int iter = 0;
   bool side_pending = false;
+  bool diag_ready = false;  // the current step's diagonal block was factored on aux
   for (int64_t k0 = 0; k0 < n; k0 += panel, ++iter) {
     const int bs = (int)(n - k0 < panel ? n - k0 : panel);
     const int64_t rs = n - k0 - bs;
@@ -353,26 +354,37 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
       const int jb = (int)(k0 + bs - j0 < kNB ? k0 + bs - j0 : kNB);
       const int64_t below = n - j0 - jb;
       const int64_t cols_left = k0 + bs - (j0 + jb);
-      launch_potrf_diag_f32w(af, ldf, j0, jb, st, s);
-      launch_trsm_panel<float>(af, ldf, j0, jb, below, st, s);
+      if (diag_ready) {
+        GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[5], 0));
+        diag_ready = false;
+      } else {
+        launch_potrf_diag_f32s(af, ldf, j0, jb, st, s);
+      }
       if (prec == GBLLT_PREC_FP32) {
+        launch_trsm_panel<float>(af, ldf, j0, jb, below, st, s);
         if (cols_left > 0 || rs > 0) launch_syrk_lower<float>(af, ldf, j0, jb, below, below, st, s);
       } else if (cols_left > 0) {
-        {
-          ProfScope ps(ksplit.c_str(), s, 0.0, (double)below * jb * 4.0 + (double)below * kNB * (kind == kTcBF16 ? 2 : 4) * np);
-          dim3 grid((unsigned)ceil_div(below, TS), (unsigned)ceil_div(kNB, TS));
-          if (kind == kTcBF16)
-            split_panel_kernel<0><<<grid, 256, 0, s>>>(af, ldf, j0 + jb, j0, below, jb, np, ipparts[0], ipparts[1],
-                                                        ipparts[2], kNB);
-          else
-            split_panel_kernel<1><<<grid, 256, 0, s>>>(af, ldf, j0 + jb, j0, below, jb, np, ipparts[0], ipparts[1],
-                                                        ipparts[2], kNB);
+        // the solve writes the step's split operand too (K-major, 64 wide)
+        launch_trsm_panel_split(af, ldf, j0, jb, below, st, kind == kTcBF16 ? 0 : 1, np, ipparts, s);
+        int64_t skip = 0;  // rows of the next diagonal block, factored on aux
+        if (aux) {
+          skip = cols_left < kNB ? cols_left : kNB;
+          GB_CUDA_TRY(cudaEventRecord(ev[4], s));
+          GB_CUDA_TRY(cudaStreamWaitEvent(aux, ev[4], 0));
+          launch_potrf_diag_f32s(af, ldf, j0 + jb, (int)skip, st, aux, j0, jb);
+          GB_CUDA_TRY(cudaEventRecord(ev[5], aux));
+          diag_ready = true;
         }
-        TcOperand ip{{ipparts[0], ipparts[1], ipparts[2]}, below, kNB, kNB, 0};
-        const int cap = (lookahead && side_pending && reserve_sms > 0) ? reserve_sms : 0;
-        const int rc = tc_update(ip, ip, kind, nseg, code, af + (j0 + jb) * ldf + (j0 + jb), ldf, below, cols_left,
-                                 kTcLowerRect, d_err, s, 0, cap);
+        TcOperand ipa{{ipparts[0], ipparts[1], ipparts[2]}, below, kNB, kNB, skip};
+        TcOperand ipb{{ipparts[0], ipparts[1], ipparts[2]}, below, kNB, kNB, 0};
+        // capped to the reserved SMs, one left to the diagonal block on aux
+        int cap = (lookahead && side_pending && reserve_sms > 0) ? reserve_sms : 0;
+        if (cap > 1 && aux) --cap;
+        const int rc = tc_update(ipa, ipb, kind, nseg, code, af + (j0 + jb) * ldf + (j0 + jb + skip), ldf,
+                                 below - skip, cols_left, kTcLowerRect, d_err, s, 0, cap, (int)skip);
         if (rc) return rc;
+      } else {
+        launch_trsm_panel<float>(af, ldf, j0, jb, below, st, s);
       }
     }
     if (rs > 0 && prec != GBLLT_PREC_FP32) {
@@ -567,16 +579,18 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   }
   // 2. low-precision factorisation
   // lookahead needs a second stream and four events: only where creating them is allowed
-  cudaStream_t side = nullptr;
-  cudaEvent_t lev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t side = nullptr, aux = nullptr;
+  cudaEvent_t lev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   if (may_allocate) {
     GB_CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    GB_CUDA_TRY(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
     for (auto& e : lev) GB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, o.reserve_sms, parts, parts2, ipparts, ldk, st, d_err, s,
-                       side, lev);
+                       side, lev, aux);
   if (side) {
     cudaStreamDestroy(side);  // work already issued on it completes; s waited on its last event
+    cudaStreamDestroy(aux);
     for (auto& e : lev) cudaEventDestroy(e);
   }
   if (rc) return rc;
@@ -641,7 +655,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     }
   }
   if (w) {
-    GB_CUDA_TRY(cudaMemcpy2DAsync(w, n * 8, a, lda * 8, n * 8, n, cudaMemcpyDeviceToDevice, s));
+    GB_CUDA_TRY(copy2d_async(w, n * 8, a, lda * 8, n * 8, n, cudaMemcpyDeviceToDevice, s));
     GB_CUDA_TRY(cudaMemsetAsync(&st->fail_col, 0xFF, sizeof(long long), s));
     if (upper && (rc = transpose_inplace_dev<double>(n, w, n, s))) return rc;
     if ((rc = potrf_lower_dev<double>(n, w, n, st, s, may_allocate))) return rc;

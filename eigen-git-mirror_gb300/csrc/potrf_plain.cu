@@ -10,8 +10,8 @@
 //                       pivot, the kernel multiplies by its reciprocal (one division per column).
 //                       FP64 arithmetic uses potrf_diag_f64_kernel, laid out for GB300's narrow
 //                       FP64 pipe (balanced lanes, pivots off the critical path);
-//   trsm_panel_kernel   A21 <- A21 L11^{-T}: one thread per row of A21, the row held in
-//                       registers, L11 broadcast from shared memory (the OnTheRight solve that
+//   trsm_panel_kernel   A21 <- A21 L11^{-T}: four threads per row of A21, the row held in
+//                       registers, L11 from shared memory (the OnTheRight solve that
 //                       LLT.h:364 issues, TriangularSolverMatrix.h:188-329);
 //   syrk_lower_kernel   A22 -= A21 A21^T on 64 x 64 tiles of the lower triangle only (the rank
 //                       update of LLT.h:365 -> GeneralMatrixMatrixTriangular.h:57-194), each
@@ -20,6 +20,8 @@
 // On GB300 the FP64 pipe (DFMA and DMMA alike) delivers about 1 TFLOP/s for the whole chip,
 // i.e. under two FP64 FMAs per clock per SM, so every FP64 kernel here is bound by that pipe
 // and not by memory: a 64 x 64 x 64 tile update needs 64 KB of operands for 262144 FMAs.
+#include <cuda_bf16.h>
+
 #include "internal.h"
 
 namespace gbllt {
@@ -28,54 +30,164 @@ namespace {
 
 constexpr int NB = kNB;
 
-// FP32 diagonal block of the mixed-precision factorisation in one warp, without block barriers: lane
-// l holds rows l and l + 32 of the block in registers (the loops are unrolled, so every index is a
-// compile-time constant); the pivot and each column of L are broadcast with shuffles.  Column j:
-// d = A(j, j) (the pivot test of LLT.h:329, `x <= 0` fails), L(i, j) = A(i, j) / sqrt(d) through
-// one IEEE reciprocal, then the rank-1 update of the later columns.  Entries above the diagonal are
-// updated too (it costs nothing to leave them) but are never read as L and never written back.
-__global__ void __launch_bounds__(32) potrf_diag_f32w_kernel(float* __restrict__ a, long long lda, long long k0,
-                                                             int bs, DevStatus* __restrict__ st) {
+// FP32 diagonal block of the mixed-precision factorisation, in blocks of four columns (the pivot
+// test of LLT.h:329, `x <= 0` fails; L(i, j) = A(i, j) * rsqrt(d), L(j, j) = d * rsqrt(d)).  For each block one warp factors the four columns of the rows below
+// with shuffles (lane l holds rows j+l and j+l+32), the finished columns go to shared memory, and
+// all 512 threads apply the rank-4 update to the trailing triangle, thread (i = tid % 64,
+// g = tid / 64) in row i at columns j+4+g, j+12+g, ...  Two barriers per four columns; the loops are
+// not unrolled over the blocks, so the code stays in the instruction cache.
+// PRE: the block first receives the update of one more panel step, A11 -= P P^T, where P holds the
+// pk columns pk0 .. pk0+pk-1 of the block's rows (the step's panel); the caller leaves the block out
+// of that step's own trailing update, so this factorisation does not wait for it.
+constexpr int DIAG_THREADS = 512;
+template <bool PRE>
+__global__ void __launch_bounds__(DIAG_THREADS) potrf_diag_f32s_kernel(float* __restrict__ a, long long lda,
+                                                                       long long k0, int bs,
+                                                                       DevStatus* __restrict__ st, long long pk0,
+                                                                       int pk) {
   if (st->fail_col >= 0) return;
-  const int l = threadIdx.x;
+  constexpr int G = DIAG_THREADS / NB;  // column groups
+  __shared__ float s[NB][NB + 1];         // s[c][r] = A(r, c), lower part; L once column c is done
+  __shared__ __align__(16) float Lr[NB][4];  // the current block's four columns of L, by row
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, i = tid & 63, g = tid >> 6;
   float* blk = a + k0 * lda + k0;
-  float r0[NB], r1[NB];  // rows l and l + 32
+  {
+    float v[NB * NB / DIAG_THREADS];  // all loads in flight before the first shared store
 #pragma unroll
-  for (int c = 0; c < NB; ++c) {
-    r0[c] = (c <= l && l < bs) ? blk[(long long)c * lda + l] : 0.f;
-    r1[c] = (c <= l + 32 && l + 32 < bs && c < bs) ? blk[(long long)c * lda + l + 32] : 0.f;
+    for (int u = 0; u < NB * NB / DIAG_THREADS; ++u) {
+      const int c = (tid >> 6) + u * G, r = tid & 63;
+      v[u] = (r < bs && c < bs && r >= c) ? blk[(long long)c * lda + r] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < NB * NB / DIAG_THREADS; ++u) s[(tid >> 6) + u * G][tid & 63] = v[u];
   }
-  int fail = -1;
+  if constexpr (PRE) {
+    constexpr int PP = NB + 4;                // row pitch: rows stay 16-byte aligned
+    __shared__ __align__(16) float pr[NB * PP];  // pr[r * PP + q] = P(r, q), zero beyond pk
+    const float* pan = a + pk0 * lda + k0;
+    {
+      float v[NB * NB / DIAG_THREADS];
 #pragma unroll
-  for (int j = 0; j < NB; ++j) {
-    if (j < bs && fail < 0) {
-      const float d = __shfl_sync(0xffffffffu, j < 32 ? r0[j] : r1[j], j & 31);
-      if (!(d > 0.f)) {
-        fail = j;
-      } else {
-        const float r = __fsqrt_rn(d);
-        const float inv = __frcp_rn(r);
-        if (j < 32) {
-          r0[j] = (l == j) ? r : r0[j] * inv;
-          r1[j] *= inv;
-        } else {
-          r1[j] = (l + 32 == j) ? r : r1[j] * inv;
-        }
+      for (int u = 0; u < NB * NB / DIAG_THREADS; ++u) {
+        const int q = (tid >> 6) + u * G, r = tid & 63;
+        v[u] = (r < bs && q < pk) ? pan[(long long)q * lda + r] : 0.f;
+      }
 #pragma unroll
-        for (int k = j + 1; k < NB; ++k) {
-          const float lk = __shfl_sync(0xffffffffu, k < 32 ? r0[j] : r1[j], k & 31);  // L(k, j)
-          if (k < 32) r0[k] = fmaf(-r0[j], lk, r0[k]);
-          r1[k] = fmaf(-r1[j], lk, r1[k]);
+      for (int u = 0; u < NB * NB / DIAG_THREADS; ++u) pr[(tid & 63) * PP + (tid >> 6) + u * G] = v[u];
+    }
+    __syncthreads();
+    // thread (i, g): entries (i, k) for k = g, g + 8, ... <= i, each a dot product over the pk
+    // columns, four at a time (row k's reads are the same for the whole warp)
+    float acc[NB / G];
+#pragma unroll
+    for (int m = 0; m < NB / G; ++m) acc[m] = 0.f;
+    for (int q = 0; q < NB; q += 4) {
+      const float4 pi = *reinterpret_cast<const float4*>(pr + i * PP + q);
+#pragma unroll
+      for (int m = 0; m < NB / G; ++m) {
+        if (g + G * m <= i) {
+          const float4 pk4 = *reinterpret_cast<const float4*>(pr + (g + G * m) * PP + q);
+          acc[m] = fmaf(pi.x, pk4.x, acc[m]);
+          acc[m] = fmaf(pi.y, pk4.y, acc[m]);
+          acc[m] = fmaf(pi.z, pk4.z, acc[m]);
+          acc[m] = fmaf(pi.w, pk4.w, acc[m]);
         }
       }
     }
-  }
 #pragma unroll
-  for (int c = 0; c < NB; ++c) {
-    if (c <= l && l < bs) blk[(long long)c * lda + l] = r0[c];
-    if (c <= l + 32 && l + 32 < bs && c < bs) blk[(long long)c * lda + l + 32] = r1[c];
+    for (int m = 0; m < NB / G; ++m)
+      if (g + G * m <= i) s[g + G * m][i] -= acc[m];
   }
-  if (l == 0 && fail >= 0) st->fail_col = k0 + fail;
+  if (tid == 0) s_fail = -1;
+  __syncthreads();
+  int done = bs;  // finished columns
+  for (int j = 0; j < bs; j += 4) {
+    const int w = bs - j < 4 ? bs - j : 4;  // columns of this block
+    // (a) one warp factors columns j .. j+w-1 of rows j .. bs-1: lane l holds rows j+l and j+l+32;
+    //     the pivot and L(j+c2, j+c) come from the lane that holds row j+c (j+c2) by shuffle
+    if (tid < 32) {
+      const int l = tid, r0 = j + l, r1 = j + l + 32;
+      float v0[4], v1[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        v0[c] = (c < w && r0 < bs && r0 >= j + c) ? s[j + c][r0] : 0.f;
+        v1[c] = (c < w && r1 < bs) ? s[j + c][r1] : 0.f;
+      }
+      int f = 4;  // first column of the block whose pivot fails the test (4: none)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (c < w && f == 4) {  // uniform over the warp
+          const float d = __shfl_sync(0xffffffffu, v0[c], c);
+          if (!(d > 0.f)) {
+            f = c;
+          } else {
+            // one MUFU reciprocal square root on the serial path; the refinement that uses this
+            // factor absorbs its last-bit differences from the correctly rounded sqrt and division
+            const float inv = rsqrtf(d);
+            v0[c] = l == c ? d * inv : v0[c] * inv;
+            v1[c] *= inv;
+#pragma unroll
+            for (int c2 = c + 1; c2 < 4; ++c2) {
+              const float lc = __shfl_sync(0xffffffffu, v0[c], c2);  // L(j + c2, j + c)
+              v0[c2] = fmaf(-v0[c], lc, v0[c2]);
+              v1[c2] = fmaf(-v1[c], lc, v1[c2]);
+            }
+          }
+        }
+      }
+      const int fin = f < w ? f : w;  // finished columns of the block
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (c < fin && r0 < bs && r0 >= j + c) s[j + c][r0] = v0[c];
+        if (c < fin && r1 < bs) s[j + c][r1] = v1[c];
+      }
+      if (r0 >= j + 4 && r0 < bs)
+        *reinterpret_cast<float4*>(Lr[r0]) = make_float4(0 < fin ? v0[0] : 0.f, 1 < fin ? v0[1] : 0.f,
+                                                         2 < fin ? v0[2] : 0.f, 3 < fin ? v0[3] : 0.f);
+      if (r1 < bs)
+        *reinterpret_cast<float4*>(Lr[r1]) = make_float4(0 < fin ? v1[0] : 0.f, 1 < fin ? v1[1] : 0.f,
+                                                         2 < fin ? v1[2] : 0.f, 3 < fin ? v1[3] : 0.f);
+      if (l == 0 && f < w) s_fail = j + f;
+    }
+    __syncthreads();
+    if (s_fail >= 0) {  // block-uniform
+      done = s_fail;
+      break;
+    }
+    // (b) rank-4 update of the trailing triangle, rows and columns from j + 4
+    const int jn = j + 4;
+    if (i >= jn && i < bs) {
+      const float4 li = *reinterpret_cast<const float4*>(Lr[i]);
+      int k = jn + g;
+      for (; k + G <= i; k += 2 * G) {
+        const float4 l0 = *reinterpret_cast<const float4*>(Lr[k]);
+        const float4 l1 = *reinterpret_cast<const float4*>(Lr[k + G]);
+        float a0 = s[k][i], a1 = s[k + G][i];
+        a0 = fmaf(-li.x, l0.x, a0); a1 = fmaf(-li.x, l1.x, a1);
+        a0 = fmaf(-li.y, l0.y, a0); a1 = fmaf(-li.y, l1.y, a1);
+        a0 = fmaf(-li.z, l0.z, a0); a1 = fmaf(-li.z, l1.z, a1);
+        a0 = fmaf(-li.w, l0.w, a0); a1 = fmaf(-li.w, l1.w, a1);
+        s[k][i] = a0;
+        s[k + G][i] = a1;
+      }
+      if (k <= i) {
+        const float4 l0 = *reinterpret_cast<const float4*>(Lr[k]);
+        float a0 = s[k][i];
+        a0 = fmaf(-li.x, l0.x, a0);
+        a0 = fmaf(-li.y, l0.y, a0);
+        a0 = fmaf(-li.z, l0.z, a0);
+        a0 = fmaf(-li.w, l0.w, a0);
+        s[k][i] = a0;
+      }
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < NB * NB; idx += DIAG_THREADS) {
+    const int c = idx >> 6, r = idx & 63;
+    if (c < done && r < bs && r >= c) blk[(long long)c * lda + r] = s[c][r];
+  }
+  if (tid == 0 && done < bs) st->fail_col = k0 + done;
 }
 
 // T = storage type, TC = arithmetic type (the mixed-precision path stores float and factors the
@@ -234,37 +346,113 @@ __global__ void __launch_bounds__(512) potrf_diag_f64_kernel(T* __restrict__ a, 
 
 // A21 (rs x bs, rows k0+bs.., columns k0..) <- A21 * L11^{-T}.  One thread per row.
 template <typename T>
+__device__ __forceinline__ void ld4(const T* p, T* v) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  } else {
+    const double2 q0 = *reinterpret_cast<const double2*>(p);
+    const double2 q1 = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+  }
+}
+
+// A21 <- A21 L11^{-T}, four threads per row of A21: sub-lane s of a quad holds the row's columns
+// p = 4m + s (m < 16) in registers.  The substitution runs right-looking: for column j the owner
+// (s = j % 4) scales x_j by 1 / L11(j, j), one shuffle hands it to the quad, and each thread
+// updates its later columns x_p -= x_j L11(p, j), which are independent of each other.  L11 is kept
+// per sub-lane (Lq[s][j][m] = L11(4m + s, j)), so a thread's reads are 16-byte vectors; the
+// sub-lane blocks are 16 bytes apart in bank order.  Compared with one thread per row, the code is
+// a third as long and four times as many warps share it.
+// SPLIT (FP32 only): the solved row is also written as the K-major tensor-core operand of the
+// in-panel update, np successive roundings (SPLIT 1: BF16, 2: TF32) at parts[k][r * 64 + p].
+constexpr int TRSM_ROWS = 32;  // rows per CTA of 128 threads
+template <typename T, int SPLIT>
 __global__ void __launch_bounds__(128) trsm_panel_kernel(T* __restrict__ a, long long lda, long long k0, int bs,
-                                                         long long rs, const DevStatus* __restrict__ st) {
+                                                         long long rs, const DevStatus* __restrict__ st, int np,
+                                                         void* __restrict__ p0, void* __restrict__ p1,
+                                                         void* __restrict__ p2) {
   if (st->fail_col >= 0) return;
-  __shared__ T L[NB][NB + 1];  // L[j][p] = L11(j, p); identity outside the bs x bs block
-  __shared__ T rdiag[NB];      // 1 / L11(j, j): the substitution multiplies instead of dividing
+  constexpr int QS = NB * 16 + 16 / (int)sizeof(T);  // sub-lane block stride
+  __shared__ __align__(16) T Lq[4 * QS];
+  __shared__ T rdiag[NB];  // 1 / L11(j, j); 1 outside the bs x bs block
   const T* l11 = a + (long long)k0 * lda + k0;
   for (int idx = threadIdx.x; idx < NB * NB; idx += 128) {
-    const int j = idx % NB, p = idx / NB;
-    T v = (j == p) ? T(1) : T(0);
-    if (j < bs && p < bs && j >= p) v = l11[(long long)p * lda + j];
-    L[j][p] = v;
+    const int p = idx % NB, j = idx / NB;  // consecutive threads read consecutive rows of column j
+    T v = T(0);
+    if (p > j && p < bs && j < bs) v = l11[(long long)j * lda + p];
+    Lq[(p & 3) * QS + j * 16 + (p >> 2)] = v;
   }
+  if (threadIdx.x < NB) rdiag[threadIdx.x] = threadIdx.x < bs ? T(1) / l11[(long long)threadIdx.x * (lda + 1)] : T(1);
   __syncthreads();
-  if (threadIdx.x < NB) rdiag[threadIdx.x] = T(1) / L[threadIdx.x][threadIdx.x];
-  __syncthreads();
-  const long long r = (long long)blockIdx.x * 128 + threadIdx.x;
-  if (r >= rs) return;
-  T* row = a + (long long)k0 * lda + (k0 + bs) + r;  // element (r, p) at row[p * lda]
-  T x[NB];
+  const int lane = threadIdx.x & 31, sl = threadIdx.x & 3, rl = threadIdx.x >> 2;
+  const long long r = (long long)blockIdx.x * TRSM_ROWS + rl;
+  const bool live = r < rs;  // every lane stays for the quad shuffles
+  T* row = a + (long long)k0 * lda + (k0 + bs) + (live ? r : 0);  // element (r, p) at row[p * lda]
+  T x[16];
 #pragma unroll
-  for (int p = 0; p < NB; ++p) x[p] = p < bs ? row[(long long)p * lda] : T(0);
+  for (int m = 0; m < 16; ++m) x[m] = (live && 4 * m + sl < bs) ? row[(long long)(4 * m + sl) * lda] : T(0);
+  const T* lq = Lq + sl * QS;
 #pragma unroll
-  for (int jj = 0; jj < NB; ++jj) {
-    T v = x[jj];
+  for (int j = 0; j < NB; ++j) {
+    const int owner = j & 3, mj = j >> 2;
+    if (sl == owner) x[mj] *= rdiag[j];
+    const T xj = __shfl_sync(0xffffffffu, x[mj], (lane & ~3) | owner);
+    if (sl > owner) x[mj] = fma(-xj, lq[j * 16 + mj], x[mj]);
 #pragma unroll
-    for (int p = 0; p < jj; ++p) v = fma(-x[p], L[jj][p], v);
-    x[jj] = v * rdiag[jj];
+    for (int c = (mj + 1) >> 2; c < 4; ++c) {  // later chunks of four m
+      T l[4];
+      ld4<T>(lq + j * 16 + 4 * c, l);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (4 * c + u > mj) x[4 * c + u] = fma(-xj, l[u], x[4 * c + u]);
+    }
   }
+  if (live) {
 #pragma unroll
-  for (int p = 0; p < NB; ++p)
-    if (p < bs) row[(long long)p * lda] = x[p];
+    for (int m = 0; m < 16; ++m)
+      if (4 * m + sl < bs) row[(long long)(4 * m + sl) * lda] = x[m];
+  }
+  if constexpr (SPLIT != 0) {
+    static_assert(sizeof(T) == 4, "split operands are made from FP32 panels");
+    __shared__ float xs[TRSM_ROWS][NB + 1];  // the quad's row, gathered to 16 consecutive columns each
+#pragma unroll
+    for (int m = 0; m < 16; ++m) xs[rl][4 * m + sl] = (float)x[m];
+    __syncwarp();
+    if (live) {
+#pragma unroll
+      for (int q = 0; q < 16; q += 8) {  // 8 columns: one 16-byte store of BF16, two of TF32
+        const int p = 16 * sl + q;
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = xs[rl][p + u];
+        for (int k = 0; k < np; ++k) {
+          void* part = k == 0 ? p0 : (k == 1 ? p1 : p2);
+          if (SPLIT == 1) {
+            uint32_t w[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const __nv_bfloat16 lo = __float2bfloat16_rn(v[2 * u]), hi = __float2bfloat16_rn(v[2 * u + 1]);
+              v[2 * u] -= __bfloat162float(lo);
+              v[2 * u + 1] -= __bfloat162float(hi);
+              w[u] = (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+            }
+            *reinterpret_cast<uint4*>((__nv_bfloat16*)part + r * NB + p) = make_uint4(w[0], w[1], w[2], w[3]);
+          } else {
+            float h[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              h[u] = to_tf32(v[u]);
+              v[u] -= h[u];
+            }
+            float4* dst = reinterpret_cast<float4*>((float*)part + r * NB + p);
+            dst[0] = make_float4(h[0], h[1], h[2], h[3]);
+            dst[1] = make_float4(h[4], h[5], h[6], h[7]);
+          }
+        }
+      }
+    }
+  }
 }
 
 // A22 (rs x rs lower) -= A21 B^T, A21 = rs x bs, B = A21 (Cholesky) or the rs x bs array at bsrc
@@ -393,10 +581,13 @@ void launch_potrf_diag(T* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cud
   else potrf_diag_kernel<T, TC><<<1, 256, 0, s>>>(a, lda, k0, bs, st);
 }
 
-void launch_potrf_diag_f32w(float* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s) {
+void launch_potrf_diag_f32s(float* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s, int64_t pk0,
+                            int pk) {
   static const std::string kd = "potrf_diag_f32";
-  ProfScope ps(kd.c_str(), s, (double)bs * bs * bs / 3.0, (double)bs * (bs + 1) * sizeof(float));
-  potrf_diag_f32w_kernel<<<1, 32, 0, s>>>(a, lda, k0, bs, st);
+  ProfScope ps(kd.c_str(), s, (double)bs * bs * bs / 3.0 + (double)bs * bs * pk,
+               (double)bs * (bs + 1) * sizeof(float) + (double)bs * pk * sizeof(float));
+  if (pk > 0) potrf_diag_f32s_kernel<true><<<1, DIAG_THREADS, 0, s>>>(a, lda, k0, bs, st, pk0, pk);
+  else potrf_diag_f32s_kernel<false><<<1, DIAG_THREADS, 0, s>>>(a, lda, k0, bs, st, 0, 0);
 }
 
 template <typename T>
@@ -404,7 +595,19 @@ void launch_trsm_panel(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevSta
   if (rs <= 0) return;
   static const std::string kt = std::string("trsm_panel_") + tname<T>();
   ProfScope ps(kt.c_str(), s, (double)rs * bs * bs, (2.0 * rs * bs + 0.5 * bs * bs) * sizeof(T));
-  trsm_panel_kernel<T><<<(unsigned)ceil_div(rs, 128), 128, 0, s>>>(a, lda, k0, bs, rs, st);
+  trsm_panel_kernel<T, 0><<<(unsigned)ceil_div(rs, TRSM_ROWS), 128, 0, s>>>(a, lda, k0, bs, rs, st, 0, nullptr,
+                                                                            nullptr, nullptr);
+}
+
+void launch_trsm_panel_split(float* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, int tf32, int np,
+                             void* const* parts, cudaStream_t s) {
+  if (rs <= 0) return;
+  static const std::string kt = "trsm_panel_f32";
+  ProfScope ps(kt.c_str(), s, (double)rs * bs * bs,
+               (2.0 * rs * bs + 0.5 * bs * bs) * sizeof(float) + (double)rs * NB * np * (tf32 ? 4.0 : 2.0));
+  const unsigned g = (unsigned)ceil_div(rs, TRSM_ROWS);
+  if (tf32) trsm_panel_kernel<float, 2><<<g, 128, 0, s>>>(a, lda, k0, bs, rs, st, np, parts[0], parts[1], parts[2]);
+  else trsm_panel_kernel<float, 1><<<g, 128, 0, s>>>(a, lda, k0, bs, rs, st, np, parts[0], parts[1], parts[2]);
 }
 
 template <typename T>

@@ -395,9 +395,10 @@ __device__ __forceinline__ void colmajor_product(const float* S, int pitch, cons
   }
 }
 
-// Sleep between polls of a block `dist` links before this CTA's own: the block has dist - 1 links
-// of slack before it is on the critical path.
-__device__ __forceinline__ unsigned poll_sleep_ns(int dist) { return dist <= 1 ? 0u : (dist > 6 ? 2000u : 400u * (dist - 1)); }
+// Sleep between polls of a block `dist` links before this CTA's own.  The blocks one and two links
+// back are polled without sleeping: the product with the block two back and the diagonal solve
+// that follows it must finish before the block one back arrives.
+__device__ __forceinline__ unsigned poll_sleep_ns(int dist) { return dist <= 2 ? 0u : (dist > 6 ? 2000u : 400u * (dist - 2)); }
 
 template <int CPT>
 __device__ __forceinline__ bool ll_wait_block(const unsigned* src, unsigned* w, int dist, int* err) {

@@ -288,14 +288,14 @@ int host_rank_update(int layout, char uplo, int64_t n, T* l, int64_t ldl, const 
   int64_t* d_info = (int64_t*)((char*)d_v + (((size_t)n * es + 255) & ~(size_t)255));
   int64_t h_info = 0;
   do {
-    if (cudaMemcpy2DAsync(d_l, n * es, l, ldl * es, n * es, n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+    if (copy2d_async(d_l, n * es, l, ldl * es, n * es, n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(d_v, v, n * es, cudaMemcpyHostToDevice, s) != cudaSuccess) {
       set_last_error(cudaGetLastError(), "gbllt_?rank_update: copy to the device", __FILE__, __LINE__);
       rc = GBLLT_ERR_CUDA;
       break;
     }
     if ((rc = rank_update_dev<T>(upper, n, d_l, n, d_v, sigma, d_info, s))) break;
-    if (cudaMemcpy2DAsync(l, ldl * es, d_l, n * es, n * es, n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+    if (copy2d_async(l, ldl * es, d_l, n * es, n * es, n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaMemcpyAsync(&h_info, d_info, sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) {
       set_last_error(cudaGetLastError(), "gbllt_?rank_update: copy to the host", __FILE__, __LINE__);

@@ -56,8 +56,9 @@ struct TcParams {
   int nseg;            // 1..8
   uint32_t seg_code;   // 4 bits per segment s: bits [4s, 4s+2) = part of A, [4s+2, 4s+4) = part of B
   int lower;           // 0: every tile of the m x n rectangle; 1: lower-triangle tiles of a square (SYRK);
-                       // 2: every tile of the rectangle; with 1 and 2 only entries with row >= column
-                       // are written
+                       // 2: every tile of the rectangle; with 1 and 2 only entries with
+                       // row + diag >= column are written
+  int diag;            // 0 except for an offset lower rectangle (lower == 2)
   int mt;              // tiles along m
   long long tiles;     // tiles in the launch
   int* err;            // device error word (set to 1 on a timeout)
@@ -201,7 +202,7 @@ __global__ void __launch_bounds__(192, 1) tc_update_kernel(const __grid_constant
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const long long gj = (long long)col0 + c0 + j;
-          cv[j] = (row_ok && j < jmax && (!p.lower || gi >= gj)) ? crow[(long long)(c0 + j) * p.ldc] : 0.f;
+          cv[j] = (row_ok && j < jmax && (!p.lower || gi + p.diag >= gj)) ? crow[(long long)(c0 + j) * p.ldc] : 0.f;
         }
         float v[32];
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + c0), v);
@@ -209,7 +210,7 @@ __global__ void __launch_bounds__(192, 1) tc_update_kernel(const __grid_constant
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const long long gj = (long long)col0 + c0 + j;
-            if (j < jmax && (!p.lower || gi >= gj)) crow[(long long)(c0 + j) * p.ldc] = cv[j] - v[j];
+            if (j < jmax && (!p.lower || gi + p.diag >= gj)) crow[(long long)(c0 + j) * p.ldc] = cv[j] - v[j];
           }
         }
       }
@@ -286,7 +287,8 @@ int make_map(CUtensorMap* m, const void* base, int kind, int64_t rows, int64_t k
 }  // namespace
 
 int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32_t seg_code, float* c, int64_t ldc,
-              int64_t m, int64_t n, int lower, int* d_err, cudaStream_t s, int reserve_sms, int max_ctas) {
+              int64_t m, int64_t n, int lower, int* d_err, cudaStream_t s, int reserve_sms, int max_ctas,
+              int diag) {
   if (m <= 0 || n <= 0 || a.k <= 0) return GBLLT_SUCCESS;
   if (nseg < 1 || nseg > 8) return GBLLT_ERR_INTERNAL;
   const int es = kind == 0 ? 2 : 4;
@@ -311,6 +313,7 @@ int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32
   p.nseg = nseg;
   p.seg_code = seg_code;
   p.lower = lower;
+  p.diag = lower == 1 ? 0 : diag;
   p.mt = (int)ceil_div(m, BM);
   p.err = d_err;
   const int64_t nt = ceil_div(n, BN);
@@ -328,8 +331,9 @@ int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32
   const unsigned grid = (unsigned)(p.tiles < usable ? p.tiles : usable);
   static const std::string kname[2] = {"tc_update_bf16", "tc_update_tf32"};
   // algorithmic work: 2 k flops per updated entry and segment; operands read once, C read+written
+  const double nt_tri = (double)(n - diag > 0 ? n - diag : 0);  // columns that meet the masked corner
   const double entries = lower == 1   ? (double)m * (m + 1) / 2.0
-                         : lower == 2 ? (double)m * n - (double)n * (n - 1) / 2.0
+                         : lower == 2 ? (double)m * n - nt_tri * (nt_tri - 1) / 2.0
                                       : (double)m * n;
   ProfScope ps(kname[kind].c_str(), s, 2.0 * entries * a.k * nseg,
                ((double)(m + (lower == 1 ? 0 : n)) * a.k * nseg * es) + entries * 8.0);

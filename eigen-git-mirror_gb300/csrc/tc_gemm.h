@@ -28,9 +28,12 @@ constexpr int kTcTF32 = 1;
 // shared memory of its SM, so kernels launched meanwhile on other streams (the panel factorisation
 // of the look-ahead schedule) run on the reserved SMs instead of sharing the update's SMs.
 // max_ctas > 0 caps the persistent grid (an update that must fit on the reserved SMs).
+// diag (kTcLowerRect only): C's origin sits diag rows below the diagonal of the full matrix, so the
+// entries written are those with row + diag >= column.
 constexpr int kTcFull = 0, kTcLowerTri = 1, kTcLowerRect = 2;
 int tc_update(const TcOperand& a, const TcOperand& b, int kind, int nseg, uint32_t seg_code, float* c, int64_t ldc,
-              int64_t m, int64_t n, int lower, int* d_err, cudaStream_t s, int reserve_sms = 0, int max_ctas = 0);
+              int64_t m, int64_t n, int lower, int* d_err, cudaStream_t s, int reserve_sms = 0, int max_ctas = 0,
+              int diag = 0);
 
 // Segment tables (parts: 0 = hi, 1 = mid/lo of a two-way split, 2 = lo of a three-way split),
 // ordered smallest terms first.
