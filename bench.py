@@ -275,10 +275,14 @@ def measured_peaks() -> dict:
 # law that scales them to this run's launch (profiles/ holds the summaries with the commands):
 #   symm_residual_f64 (NR = 16 kernel): 1.628 GB at n = 8192, 64 RHS; A's stored tiles are read
 #     once per 16-column chunk of right-hand sides, so traffic grows as n^2 * ceil(k / 16).
-#   sweep_f32 (16-column chains): 141.4 MB at n = 8192, 64 RHS (mean of the forward and backward
+#   sweep_f32 (16-column chains): 143.9 MB at n = 8192, 64 RHS (mean of the forward and backward
 #     launch); the triangle of L is read once whatever k is, so traffic grows as n^2.
+#   tc_update_bf16: 15.3 MB per launch at n = 8192, the mean over the 158 launches of one BF16x6
+#     factorisation (in-panel, strip and look-ahead updates); the C traffic of a factorisation
+#     grows as n^3 and its launches as n, so the mean per launch grows as n^2.
 NCU_TRAFFIC = {"symm_residual_f64": (8192, 64, 1.628e9, "n2_kchunks"),
-               "sweep_f32": (8192, 64, 1.414e8, "n2")}
+               "sweep_f32": (8192, 64, 1.439e8, "n2"),
+               "tc_update_bf16": (8192, 64, 1.530e7, "n2")}
 
 
 def ncu_traffic(name: str, n: int, k: int):
