@@ -329,10 +329,10 @@ int split_parts(int prec) {
 // lower part of the panel's remaining columns.  While the look-ahead update occupies the other
 // SMs, these launches are capped to the reserved SMs.
 // With an aux stream, the next step's diagonal block is left out of the in-panel update and is
-// factored on aux right after the panel solve, with this step's contribution applied by the
-// diagonal kernel itself, so it overlaps the in-panel update:
-//   ev[4]: the step's panel solve finished (aux waits)
-//   ev[5]: the next diagonal block is factored (main waits before the next panel solve)
+// factored right after the panel solve on the same stream, with this step's contribution applied by
+// the diagonal kernel itself, while the rest of the in-panel update runs on aux:
+//   ev[4]: the step's panel solve finished (aux waits before the in-panel update)
+//   ev[5]: the in-panel update finished (main waits before the next panel solve)
 int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int reserve_sms, void* const* parts,
                     void* const* parts2, void* const* ipparts, int64_t ldk, DevStatus* st, int* d_err,
                     cudaStream_t s, cudaStream_t side, cudaEvent_t* ev, cudaStream_t aux) {
@@ -345,7 +345,8 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
   const uint32_t code = np == 1 ? kSegX1 : np == 2 ? kSegX3 : kSegX6;
   int iter = 0;
   bool side_pending = false;
-  bool diag_ready = false;  // the current step's diagonal block was factored on aux
+  bool diag_ready = false;  // the current step's diagonal block is already factored (previous step)
+  bool u_pending = false;   // the previous step's in-panel update runs on aux
   for (int64_t k0 = 0; k0 < n; k0 += panel, ++iter) {
     const int bs = (int)(n - k0 < panel ? n - k0 : panel);
     const int64_t rs = n - k0 - bs;
@@ -354,38 +355,51 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
       const int jb = (int)(k0 + bs - j0 < kNB ? k0 + bs - j0 : kNB);
       const int64_t below = n - j0 - jb;
       const int64_t cols_left = k0 + bs - (j0 + jb);
-      if (diag_ready) {
-        GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[5], 0));
-        diag_ready = false;
-      } else {
-        launch_potrf_diag_f32s(af, ldf, j0, jb, st, s);
-      }
+      if (diag_ready) diag_ready = false;
+      else launch_potrf_diag_f32s(af, ldf, j0, jb, st, s);
       if (prec == GBLLT_PREC_FP32) {
         launch_trsm_panel<float>(af, ldf, j0, jb, below, st, s);
         if (cols_left > 0 || rs > 0) launch_syrk_lower<float>(af, ldf, j0, jb, below, below, st, s);
-      } else if (cols_left > 0) {
-        // the solve writes the step's split operand too (K-major, 64 wide)
-        launch_trsm_panel_split(af, ldf, j0, jb, below, st, kind == kTcBF16 ? 0 : 1, np, ipparts, s);
-        int64_t skip = 0;  // rows of the next diagonal block, factored on aux
-        if (aux) {
-          skip = cols_left < kNB ? cols_left : kNB;
-          GB_CUDA_TRY(cudaEventRecord(ev[4], s));
-          GB_CUDA_TRY(cudaStreamWaitEvent(aux, ev[4], 0));
-          launch_potrf_diag_f32s(af, ldf, j0 + jb, (int)skip, st, aux, j0, jb);
-          GB_CUDA_TRY(cudaEventRecord(ev[5], aux));
-          diag_ready = true;
-        }
-        TcOperand ipa{{ipparts[0], ipparts[1], ipparts[2]}, below, kNB, kNB, skip};
-        TcOperand ipb{{ipparts[0], ipparts[1], ipparts[2]}, below, kNB, kNB, 0};
-        // capped to the reserved SMs, one left to the diagonal block on aux
-        int cap = (lookahead && side_pending && reserve_sms > 0) ? reserve_sms : 0;
-        if (cap > 1 && aux) --cap;
-        const int rc = tc_update(ipa, ipb, kind, nseg, code, af + (j0 + jb) * ldf + (j0 + jb + skip), ldf,
-                                 below - skip, cols_left, kTcLowerRect, d_err, s, 0, cap, (int)skip);
-        if (rc) return rc;
-      } else {
-        launch_trsm_panel<float>(af, ldf, j0, jb, below, st, s);
+        continue;
       }
+      if (u_pending) {  // this step's panel rows below the block come from the previous in-panel update
+        GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[5], 0));
+        u_pending = false;
+      }
+      if (cols_left == 0) {
+        launch_trsm_panel<float>(af, ldf, j0, jb, below, st, s);
+        continue;
+      }
+      // the solve writes the step's split operand too (K-major, 64 wide)
+      launch_trsm_panel_split(af, ldf, j0, jb, below, st, kind == kTcBF16 ? 0 : 1, np, ipparts, s);
+      int64_t skip = 0;  // rows of the next diagonal block, left out of the in-panel update
+      cudaStream_t us = s;
+      if (aux) {
+        // the next diagonal block follows the solve on this stream (applying this step's contribution
+        // itself) while the rest of the in-panel update runs on aux
+        skip = cols_left < kNB ? cols_left : kNB;
+        GB_CUDA_TRY(cudaEventRecord(ev[4], s));
+        launch_potrf_diag_f32s(af, ldf, j0 + jb, (int)skip, st, s, j0, jb);
+        diag_ready = true;
+        GB_CUDA_TRY(cudaStreamWaitEvent(aux, ev[4], 0));
+        us = aux;
+      }
+      TcOperand ipa{{ipparts[0], ipparts[1], ipparts[2]}, below, kNB, kNB, skip};
+      TcOperand ipb{{ipparts[0], ipparts[1], ipparts[2]}, below, kNB, kNB, 0};
+      // capped to the reserved SMs, one left to the diagonal block
+      int cap = (lookahead && side_pending && reserve_sms > 0) ? reserve_sms : 0;
+      if (cap > 1 && aux) --cap;
+      const int rc = tc_update(ipa, ipb, kind, nseg, code, af + (j0 + jb) * ldf + (j0 + jb + skip), ldf,
+                               below - skip, cols_left, kTcLowerRect, d_err, us, 0, cap, (int)skip);
+      if (rc) return rc;
+      if (aux) {
+        GB_CUDA_TRY(cudaEventRecord(ev[5], aux));
+        u_pending = true;
+      }
+    }
+    if (u_pending) {
+      GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[5], 0));
+      u_pending = false;
     }
     if (rs > 0 && prec != GBLLT_PREC_FP32) {
       void* const* pp = (lookahead && (iter & 1)) ? parts2 : parts;
@@ -533,11 +547,14 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     return ms;
   };
 
-  auto sumsq = [&](const double* p, int64_t ld, int64_t m, int64_t k, int mode, double* out) {
+  auto sumsq_on = [&](const double* p, int64_t ld, int64_t m, int64_t k, int mode, double* out, cudaStream_t st_) {
     int blocks = (int)((m * k + 255) / 256);
     blocks = blocks < 1 ? 1 : (blocks > nsq ? nsq : blocks);
-    sumsq_kernel<<<blocks, 256, 0, s>>>(p, ld, m, k, mode, sq);
-    sum_parts_kernel<<<1, 256, 0, s>>>(sq, blocks, out);
+    sumsq_kernel<<<blocks, 256, 0, st_>>>(p, ld, m, k, mode, sq);
+    sum_parts_kernel<<<1, 256, 0, st_>>>(sq, blocks, out);
+  };
+  auto sumsq = [&](const double* p, int64_t ld, int64_t m, int64_t k, int mode, double* out) {
+    sumsq_on(p, ld, m, k, mode, out, s);
   };
   // the residual on the tensor cores needs A's slices (n^2 * 16 bytes): only where allocating is allowed
   OzakiResidual oz;
@@ -577,24 +594,60 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     if (upper) convert_scaled_kernel<true><<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(a, lda, n, dsc, af, ldf);
     else convert_scaled_kernel<false><<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(a, lda, n, dsc, af, ldf);
   }
-  // 2. low-precision factorisation
-  // lookahead needs a second stream and four events: only where creating them is allowed
-  cudaStream_t side = nullptr, aux = nullptr;
-  cudaEvent_t lev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // 2. low-precision factorisation.  Where creating streams is allowed it runs on three internal
+  // streams of the highest priority (chain, look-ahead update, next diagonal block), fenced to the
+  // caller's stream by events, while a stream of the lowest priority forms what the refinement needs
+  // from A alone (||A||_F and the tensor-core residual's slices of A): its blocks take only the slots
+  // the factorisation leaves free.
+  struct Streams {
+    cudaStream_t fs = nullptr, side = nullptr, aux = nullptr, low = nullptr;
+    cudaEvent_t lev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t in = nullptr, out = nullptr, pre = nullptr;
+    ~Streams() {  // work already issued completes; the caller's stream waited on what it needs
+      for (cudaStream_t q : {fs, side, aux, low})
+        if (q) cudaStreamDestroy(q);
+      for (auto& e : lev)
+        if (e) cudaEventDestroy(e);
+      for (cudaEvent_t e : {in, out, pre})
+        if (e) cudaEventDestroy(e);
+    }
+  } xs;
+  bool pre_ready = false;  // ||A||^2 (and A's slices) are being formed on the low-priority stream
   if (may_allocate) {
-    GB_CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-    GB_CUDA_TRY(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
-    for (auto& e : lev) GB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    int least = 0, greatest = 0;
+    GB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    GB_CUDA_TRY(cudaStreamCreateWithPriority(&xs.fs, cudaStreamNonBlocking, greatest));
+    GB_CUDA_TRY(cudaStreamCreateWithPriority(&xs.side, cudaStreamNonBlocking, greatest));
+    GB_CUDA_TRY(cudaStreamCreateWithPriority(&xs.aux, cudaStreamNonBlocking, greatest));
+    GB_CUDA_TRY(cudaStreamCreateWithPriority(&xs.low, cudaStreamNonBlocking, least));
+    for (auto& e : xs.lev) GB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (cudaEvent_t* e : {&xs.in, &xs.out, &xs.pre}) GB_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    GB_CUDA_TRY(cudaEventRecord(xs.in, s));
+    GB_CUDA_TRY(cudaStreamWaitEvent(xs.fs, xs.in, 0));
+    GB_CUDA_TRY(cudaStreamWaitEvent(xs.low, xs.in, 0));
+    sumsq_on(a, lda, n, n, upper ? 2 : 1, &norms[0], xs.low);
+    if (use_oz) {
+      const int rc2 = oz.setup(upper, n, nrhs, a, lda, xs.low);
+      if (rc2 == GBLLT_ERR_ALLOC) use_oz = false;  // not enough device memory: the FP64 residual
+      else if (rc2) return rc2;
+    }
+    GB_CUDA_TRY(cudaEventRecord(xs.pre, xs.low));
+    pre_ready = true;
+    rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, o.reserve_sms, parts, parts2, ipparts, ldk, st, d_err,
+                         xs.fs, xs.side, xs.lev, xs.aux);
+    if (rc) return rc;
+    GB_CUDA_TRY(cudaEventRecord(xs.out, xs.fs));
+    GB_CUDA_TRY(cudaStreamWaitEvent(s, xs.out, 0));
+  } else {
+    rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, o.reserve_sms, parts, parts2, ipparts, ldk, st, d_err, s,
+                         nullptr, xs.lev, nullptr);
+    if (rc) return rc;
   }
-  rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, o.reserve_sms, parts, parts2, ipparts, ldk, st, d_err, s,
-                       side, lev, aux);
-  if (side) {
-    cudaStreamDestroy(side);  // work already issued on it completes; s waited on its last event
-    cudaStreamDestroy(aux);
-    for (auto& e : lev) cudaEventDestroy(e);
-  }
-  if (rc) return rc;
   if ((rc = stamp(1))) return rc;
+  if (pre_ready) {  // everything after this point (norms, residuals, fallback) may use the low stream's results
+    GB_CUDA_TRY(cudaStreamWaitEvent(s, xs.pre, 0));
+    if (oz.buf) oz.stream = s;  // freed in the caller's stream order, after the last residual
+  }
   DevStatus hst;
   GB_CUDA_TRY(cudaMemcpyAsync(&hst, st, sizeof hst, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -605,7 +658,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   bool ok = false;
   if (r.info == 0) {
     // 3. refinement: x_0 = 0, r_0 = b
-    sumsq(a, lda, n, n, upper ? 2 : 1, &norms[0]);
+    if (!pre_ready) sumsq(a, lda, n, n, upper ? 2 : 1, &norms[0]);
     copy_cols_kernel<<<grid1(n * nrhs), 256, 0, s>>>(b, ldb, n, nrhs, R, n);
     sumsq(R, n, n, nrhs, 0, &norms[1]);
     double best = INFINITY;
