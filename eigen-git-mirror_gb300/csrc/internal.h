@@ -177,14 +177,19 @@ struct OzakiSyrk {
   int* pexp = nullptr;
   void* slices_w = nullptr;  // kWide-wide panel slices
   int* pexp_w = nullptr;
+  void* slices_b = nullptr;  // 64-wide slices of a second operand (two_sided)
+  int* pexp_b = nullptr;
   void* maps = nullptr;
   cudaStream_t stream = nullptr;
   OzakiSyrk() = default;
   OzakiSyrk(const OzakiSyrk&) = delete;
   OzakiSyrk& operator=(const OzakiSyrk&) = delete;
   ~OzakiSyrk();
-  int init(int64_t nmax, cudaStream_t s);
+  int init(int64_t nmax, cudaStream_t s, bool two_sided = false);
   int update(double* a, int64_t lda, int64_t k0, int pw, int64_t rs, int64_t ncols, DevStatus* st, cudaStream_t s);
+  // C -= P Q^T (lower) with Q given separately (the LDL^T update, Q = L21 D); needs two_sided, pw <= 64.
+  int update_pq(double* a, int64_t lda, int64_t k0, int pw, int64_t rs, const double* q, int64_t ldq, DevStatus* st,
+                cudaStream_t s);
   void release_maps();
 };
 

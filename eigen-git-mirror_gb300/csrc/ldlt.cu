@@ -400,7 +400,17 @@ int ldlt_factor_dev(bool upper, int64_t n, T* d_a, int64_t lda, int32_t* transp,
     if (upper) ldlt_gather_kernel<T, true><<<tiles, 256, 0, s>>>(d_a, lda, n, d_perm, W, ldw);
     else ldlt_gather_kernel<T, false><<<tiles, 256, 0, s>>>(d_a, lda, n, d_perm, W, ldw);
   }
-  // 3. blocked LDL^T without pivoting
+  // 3. blocked LDL^T without pivoting.  FP64 from kTensorSyrkMinN on: the trailing update
+  //    W22 -= L21 (L21 D)^T on the tensor cores, FP64-exact (both operands sliced, ozaki.cu)
+  OzakiSyrk oz;
+  bool use_oz = false;
+  if constexpr (sizeof(T) == 8) {
+    if (n >= kTensorSyrkMinN) {
+      const int rc2 = oz.init(n, s, true);
+      if (rc2 == GBLLT_SUCCESS) use_oz = true;
+      else if (rc2 != GBLLT_ERR_ALLOC) return rc2;
+    }
+  }
   for (int64_t k0 = 0; k0 < n; k0 += NB) {
     const int bs = (int)(n - k0 < NB ? n - k0 : NB);
     const int64_t rs = n - k0 - bs;
@@ -416,6 +426,12 @@ int ldlt_factor_dev(bool upper, int64_t n, T* d_a, int64_t lda, int32_t* transp,
         ldlt_panel_kernel<T><<<(unsigned)ceil_div(rs, PANEL_ROWS), PANEL_ROWS, smem, s>>>(W, ldw, k0, bs, rs, Tb,
                                                                                          ldt, flags);
       }
+      if constexpr (sizeof(T) == 8) {
+        if (use_oz) {
+          if ((rc = oz.update_pq(W, ldw, k0, bs, rs, Tb, ldt, st, s))) return rc;
+          continue;
+        }
+      }
       launch_syrk_lower<T>(W, ldw, k0, bs, rs, rs, st, s, Tb, ldt);
     }
   }
@@ -428,8 +444,11 @@ int ldlt_factor_dev(bool upper, int64_t n, T* d_a, int64_t lda, int32_t* transp,
   }
   GB_CUDA_TRY(cudaGetLastError());
   int out[2] = {0, 0};
+  DevStatus hst;
   GB_CUDA_TRY(cudaMemcpyAsync(out, flags + 1, sizeof out, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(&hst, st, sizeof hst, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hst.timeout) return GBLLT_ERR_TIMEOUT;  // a bounded wait of the tensor-core update ran out
   *sign = out[0];
   *info = out[1];
   return GBLLT_SUCCESS;

@@ -271,12 +271,13 @@ struct OzParams {
   long long ldb;
   double* r;
   long long ldr;
-  // trailing update C -= L21 L21^T (lower)
+  // trailing update C -= P Q^T (lower; P = Q = L21 for a Cholesky update, Q = L21 D for LDL^T)
   double* c;
   long long ldc;
   long long rs;                    // rows of the updated block
   long long ncols;                 // its columns (ncols = rs: the whole trailing lower triangle)
-  const int* pexp;                 // per-row scale exponents of L21
+  const int* pexp;                 // per-row scale exponents of P (the M operand)
+  const int* pexp_b;               // per-row scale exponents of Q (the N operand)
   const DevStatus* st;
 };
 
@@ -486,7 +487,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
           for (int c = 0; c < 16; ++c) {
             const long long j = col0 + part * 16 + c;
             if (j <= i) {
-              p.c[j * p.ldc + i] -= fixed_to_double(hi[c], lo[c], ei + p.pexp[j]);
+              p.c[j * p.ldc + i] -= fixed_to_double(hi[c], lo[c], ei + p.pexp_b[j]);
             }
           }
         }
@@ -718,15 +719,16 @@ OzakiSyrk::~OzakiSyrk() {
   if (buf) cudaFreeAsync(buf, stream);
 }
 
-int OzakiSyrk::init(int64_t nmax_, cudaStream_t s) {
+int OzakiSyrk::init(int64_t nmax_, cudaStream_t s, bool two_sided) {
   int rc = oz_prepare_device(&sms);
   if (rc) return rc;
   nmax = nmax_;
   stream = s;
-  // [slices of a 64-wide sub-panel | their exponents | slices of a 256-wide panel | their exponents]
+  // [slices of a 64-wide sub-panel | their exponents | slices of a 256-wide panel | their exponents
+  //  | (two_sided) slices of a second 64-wide operand | their exponents]
   const size_t s64 = oz_up256((size_t)S * nmax * PK * 2), s256 = oz_up256((size_t)S * nmax * kWide * 2),
                e = oz_up256((size_t)nmax * 4);
-  if (dev_malloc_async(&buf, s64 + e + s256 + e, s) != cudaSuccess) {
+  if (dev_malloc_async(&buf, s64 + e + s256 + e + (two_sided ? s64 + e : 0), s) != cudaSuccess) {
     cudaGetLastError();
     buf = nullptr;
     return GBLLT_ERR_ALLOC;
@@ -735,17 +737,25 @@ int OzakiSyrk::init(int64_t nmax_, cudaStream_t s) {
   pexp = (int*)((char*)buf + s64);
   slices_w = (char*)buf + s64 + e;
   pexp_w = (int*)((char*)buf + s64 + e + s256);
-  maps = new OzMaps[2];
+  if (two_sided) {
+    slices_b = (char*)buf + s64 + e + s256 + e;
+    pexp_b = (int*)((char*)buf + s64 + e + s256 + e + s64);
+  }
+  maps = new OzMaps[3];
   OzMaps* m = (OzMaps*)maps;
   const __nv_bfloat16* sl = (const __nv_bfloat16*)slices;
   const __nv_bfloat16* sw = (const __nv_bfloat16*)slices_w;
+  const __nv_bfloat16* sb = (const __nv_bfloat16*)slices_b;
   for (int q = 0; q < S; ++q) {
     const __nv_bfloat16* b64 = sl + (size_t)q * nmax * PK;
     const __nv_bfloat16* b256 = sw + (size_t)q * nmax * kWide;
     if (!make_map_2d(&m[0].a[q], b64, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BM) ||
         !make_map_2d(&m[0].x[q], b64, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BN) ||
         !make_map_2d(&m[1].a[q], b256, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, kWide, kWide, KB, BM) ||
-        !make_map_2d(&m[1].x[q], b256, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, kWide, kWide, KB, BN)) {
+        !make_map_2d(&m[1].x[q], b256, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, kWide, kWide, KB, BN) ||
+        (two_sided && (!make_map_2d(&m[2].a[q], b64, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, nmax, PK, PK, KB, BM) ||
+                       !make_map_2d(&m[2].x[q], sb + (size_t)q * nmax * PK, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                                    nmax, PK, PK, KB, BN)))) {
       set_error_message("cuTensorMapEncodeTiled failed (tensor-core trailing update)");
       return GBLLT_ERR_INTERNAL;
     }
@@ -787,6 +797,7 @@ int OzakiSyrk::update(double* a, int64_t lda, int64_t k0, int pw, int64_t rs, in
   p.rs = rs;
   p.ncols = ncols;
   p.pexp = ex;
+  p.pexp_b = ex;
   p.st = st;
   p.err = &st->timeout;
   const unsigned grid = (unsigned)(p.tiles < sms ? p.tiles : sms);
@@ -796,6 +807,47 @@ int OzakiSyrk::update(double* a, int64_t lda, int64_t k0, int pw, int64_t rs, in
     const double entries = c * (double)rs - c * (c - 1) / 2.0;
     ProfScope ps(ks.c_str(), s, 2.0 * entries * pw, 2.0 * entries * 8.0 + (double)S * rs * w * 2.0);
     oz_kernel<true><<<grid, THREADS, SMEM_BYTES, s>>>(((const OzMaps*)maps)[wide ? 1 : 0], p);
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+// C -= P Q^T on the lower part of the rs x rs block at (k0 + pw, k0 + pw): P = the rs x pw panel below
+// the diagonal block at (k0, k0) of a, Q = the rs x pw array at q (leading dimension ldq); pw <= 64.
+// The LDL^T update, Q = L21 D: both operands are sliced, each with its own row exponents.
+int OzakiSyrk::update_pq(double* a, int64_t lda, int64_t k0, int pw, int64_t rs, const double* q, int64_t ldq,
+                         DevStatus* st, cudaStream_t s) {
+  if (rs <= 0) return GBLLT_SUCCESS;
+  if (!buf || !maps || !slices_b || rs > nmax || pw > PK) return GBLLT_ERR_INTERNAL;
+  static const std::string kp = "panel_slices_f64";
+  static const std::string ks = "syrk_tc_f64";
+  const double* l21 = a + k0 * lda + k0 + pw;
+  {
+    ProfScope ps(kp.c_str(), s, 0.0, 2.0 * ((double)rs * pw * 8.0 + (double)S * rs * PK * 2.0));
+    oz_panel_slice_kernel<<<(unsigned)ceil_div(rs, 128), 128, 0, s>>>(l21, lda, rs, pw, PK, (__nv_bfloat16*)slices,
+                                                                     (long long)nmax * PK, pexp);
+    oz_panel_slice_kernel<<<(unsigned)ceil_div(rs, 128), 128, 0, s>>>(q, ldq, rs, pw, PK, (__nv_bfloat16*)slices_b,
+                                                                     (long long)nmax * PK, pexp_b);
+  }
+  OzParams p;
+  memset(&p, 0, sizeof p);
+  p.kdim = PK;
+  p.nrt = (int)ceil_div(rs, BM);
+  p.nct = (int)ceil_div(rs, BN);
+  p.tiles = (long long)p.nrt * p.nct;
+  p.c = a + (k0 + pw) * lda + k0 + pw;
+  p.ldc = lda;
+  p.rs = rs;
+  p.ncols = rs;
+  p.pexp = pexp;
+  p.pexp_b = pexp_b;
+  p.st = st;
+  p.err = &st->timeout;
+  const unsigned grid = (unsigned)(p.tiles < sms ? p.tiles : sms);
+  {
+    const double entries = (double)rs * (rs + 1) / 2.0;
+    ProfScope ps(ks.c_str(), s, 2.0 * entries * pw, 2.0 * entries * 8.0 + 2.0 * S * rs * PK * 2.0);
+    oz_kernel<true><<<grid, THREADS, SMEM_BYTES, s>>>(((const OzMaps*)maps)[2], p);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
