@@ -295,10 +295,21 @@ def ncu_traffic(name: str, n: int, k: int):
     return by * scale
 
 
+# The FP64-exact products on the tensor cores (ozaki.cu) run 36 BF16 products per FP64 product
+# (8 slices per operand, the slice pairs p + q <= 9); their roofline is that BF16 work against the
+# BF16 peak, not their FP64-equivalent rate against the FP64 pipe.
+OZAKI_KERNELS = ("syrk_tc_f64", "residual_tc")
+OZAKI_PRODUCTS = 36
+
+
 def roofline_for(name: str, st: dict, peaks: dict, n: int = 0, k: int = 0) -> dict:
     """Achieved = algorithmic work of the kernel's launches / their summed device time."""
     ms = max(st["ms"], 1e-9)
-    if name.startswith("tc_update_tf32"):
+    if name in OZAKI_KERNELS:
+        bound, unit, peak, src = "tensor", "TFLOP/s", peaks["bf16_tflops"], peaks["source"]["bf16_tflops"] + \
+            f" (BF16 work: {OZAKI_PRODUCTS} products per FP64-exact product)"
+        ach = OZAKI_PRODUCTS * st["flops"] / ms / 1e9
+    elif name.startswith("tc_update_tf32"):
         bound, unit, peak, src = "tensor", "TFLOP/s", peaks["tf32_tflops"], peaks["source"]["tf32_tflops"]
         ach = st["flops"] / ms / 1e9
     elif name.startswith("tc_update_bf16"):
