@@ -600,10 +600,24 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   // from A alone (||A||_F and the tensor-core residual's slices of A): its blocks take only the slots
   // the factorisation leaves free.
   struct Streams {
+    cudaStream_t caller = nullptr;
     cudaStream_t fs = nullptr, side = nullptr, aux = nullptr, low = nullptr;
     cudaEvent_t lev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t in = nullptr, out = nullptr, pre = nullptr;
-    ~Streams() {  // work already issued completes; the caller's stream waited on what it needs
+    ~Streams() {
+      // The caller's stream waits for everything issued on these streams before anything it orders
+      // later (the release of the workspace they use): on an early error return the factorisation's
+      // or the low-priority stream's kernels may still be running.  Work already issued completes.
+      for (cudaStream_t q : {fs, side, aux, low}) {
+        if (!q || !caller) continue;
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) {
+          if (cudaEventRecord(e, q) == cudaSuccess) cudaStreamWaitEvent(caller, e, 0);
+          cudaEventDestroy(e);
+        } else {
+          cudaStreamSynchronize(q);  // no event: wait on the host instead
+        }
+      }
       for (cudaStream_t q : {fs, side, aux, low})
         if (q) cudaStreamDestroy(q);
       for (auto& e : lev)
@@ -614,6 +628,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   } xs;
   bool pre_ready = false;  // ||A||^2 (and A's slices) are being formed on the low-priority stream
   if (may_allocate) {
+    xs.caller = s;
     int least = 0, greatest = 0;
     GB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     GB_CUDA_TRY(cudaStreamCreateWithPriority(&xs.fs, cudaStreamNonBlocking, greatest));
