@@ -1,12 +1,15 @@
 """Benchmark of the GB300 dense Cholesky (LLT) path.
 
-Default workload: n = 16384, 64 right-hand sides, A = Q diag(lambda) Q^T with Q a product of 8
-Householder reflectors and lambda log-spaced over [1e-6, 1] (kappa = 1e6), B ~ N(0,1); FP64
-factor + solve (the large plain-FP64 LLT configuration).  One step = one factor + solve of that
-system.  Inputs are synthetic and seeded; the 2.1 GB matrix is larger than the 129 MB L2, so
-no flush is needed between steps.
+Default workload (the configuration the metric is quoted on): n = 32768, 64 right-hand sides,
+A = Q diag(lambda) Q^T with Q a product of 8 Householder reflectors and lambda log-spaced over
+[1e-6, 1] and randomly permuted (kappa = 1e6), B ~ N(0,1).  One step = one solve of that system
+to normwise backward error <= 1e-14, by two arms on the same device-resident inputs: the plain
+FP64 factor + solve, and the mixed-precision factorisation + FP64 iterative refinement.  The
+8.6 GB matrix is larger than the 129 MB L2, so no flush is needed between steps.  The same line
+carries the other configurations as extra keys: the kappa / right-hand-side sweep at n = 32768,
+n = 1024 with 16 RHS, the batch of 20000 uneven small systems and the 64 GP-likelihood matrices.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config ...]
 
 --impl reference times the CPU restatement of Eigen's LLT (the oracle; Eigen's own headers do
 not exist on the GPU host) on the host cores, on a bounded sample of the same workload.
@@ -33,11 +36,18 @@ sys.path.insert(0, str(ROOT / "eigen-git-mirror_gb300"))
 METRIC = "LLT solve s & TFLOP/s: FP64 vs mixed+refinement at backward err ≤1e-14"
 
 CONFIGS = {
-    "c2": dict(workload="LLT factor+solve FP64, n=16384, 64 RHS, Householder spectrum kappa=1e6",
+    "c3": dict(workload="LLT solve to backward error <= 1e-14, n=32768, 64 RHS, Householder spectrum "
+                        "kappa=1e6: plain FP64 factor+solve vs mixed-precision factor + FP64 refinement",
+               n=32768, nrhs=64, kappa=1e6),
+    "c2": dict(workload="LLT solve to backward error <= 1e-14, n=16384, 64 RHS, Householder spectrum kappa=1e6",
                n=16384, nrhs=64, kappa=1e6),
-    "c1": dict(workload="LLT factor+solve FP64, n=1024, 16 RHS, A=G G^T/n+I", n=1024, nrhs=16, kappa=None),
+    "c1": dict(workload="LLT solve to backward error <= 1e-14, n=1024, 16 RHS, A=G G^T/n+I", n=1024, nrhs=16,
+               kappa=None),
 }
+DEFAULT_CONFIG = "c3"
 CPU_SAMPLE_N = 8192
+# split products per algorithmic product of each mixed precision (tc_update's profiled flops count them all)
+SPLIT_PRODUCTS = {"fp32": 1, "tf32": 1, "bf16": 1, "tf32x3": 3, "bf16x3": 3, "bf16x6": 6}
 
 
 def llt_flops(n: int, k: int) -> float:
@@ -223,10 +233,13 @@ def run_reference(args, ws, rank):
     value = llt_flops(n, k) * len(ts) / total / 1e12
     sample = (f"n={n}, {k} RHS, same construction as the workload, FP64 factor+solve per step "
               f"(CPU restatement of Eigen's blocked LLT; OpenMP over SYRK/TRSM rows)")
+    # config.n is the order actually timed; the workload it samples is named beside it
     out = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": total / len(ts) * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": cfg["workload"], "n": cfg["n"], "nrhs": k, "kappa": cfg["kappa"]},
+           "config": {"workload": f"LLT factor+solve FP64 on the CPU, n={n}, {k} RHS: a bounded sample of "
+                                  f"the n={cfg['n']} workload", "n": n, "nrhs": k, "kappa": cfg["kappa"],
+                      "sample_of": {"workload": cfg["workload"], "n": cfg["n"]}},
            "impl": "reference",
            "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": O.num_threads(), "kind": "port",
                             "sample": sample},
@@ -296,25 +309,28 @@ def ncu_traffic(name: str, n: int, k: int):
 
 
 # The FP64-exact products on the tensor cores (ozaki.cu) run 36 BF16 products per FP64 product
-# (8 slices per operand, the slice pairs p + q <= 9); their roofline is that BF16 work against the
-# BF16 peak, not their FP64-equivalent rate against the FP64 pipe.
+# (8 slices per operand, the slice pairs p + q <= 9); the split-precision trailing updates run 3 or 6.
+# `achieved` counts the algorithmic work only (one product); the products the tensor cores actually
+# execute are reported under `split_products`.
 OZAKI_KERNELS = ("syrk_tc_f64", "residual_tc")
 OZAKI_PRODUCTS = 36
 
 
-def roofline_for(name: str, st: dict, peaks: dict, n: int = 0, k: int = 0) -> dict:
-    """Achieved = algorithmic work of the kernel's launches / their summed device time."""
+def roofline_for(name: str, st: dict, peaks: dict, n: int = 0, k: int = 0, nseg: int = 1) -> dict:
+    """Achieved = algorithmic work of the kernel's launches / their summed device time, against the
+    peak of the unit the kernel runs on.  st["flops"] is the profiled work: for tc_update_* it counts
+    every split product (nseg per algorithmic product); for the ozaki kernels it is the FP64 product."""
     ms = max(st["ms"], 1e-9)
+    products = 1
     if name in OZAKI_KERNELS:
-        bound, unit, peak, src = "tensor", "TFLOP/s", peaks["bf16_tflops"], peaks["source"]["bf16_tflops"] + \
-            f" (BF16 work: {OZAKI_PRODUCTS} products per FP64-exact product)"
-        ach = OZAKI_PRODUCTS * st["flops"] / ms / 1e9
-    elif name.startswith("tc_update_tf32"):
-        bound, unit, peak, src = "tensor", "TFLOP/s", peaks["tf32_tflops"], peaks["source"]["tf32_tflops"]
-        ach = st["flops"] / ms / 1e9
-    elif name.startswith("tc_update_bf16"):
         bound, unit, peak, src = "tensor", "TFLOP/s", peaks["bf16_tflops"], peaks["source"]["bf16_tflops"]
         ach = st["flops"] / ms / 1e9
+        products = OZAKI_PRODUCTS
+    elif name.startswith("tc_update_tf32") or name.startswith("tc_update_bf16"):
+        key = "tf32_tflops" if name.startswith("tc_update_tf32") else "bf16_tflops"
+        bound, unit, peak, src = "tensor", "TFLOP/s", peaks[key], peaks["source"][key]
+        products = max(int(nseg), 1)
+        ach = st["flops"] / products / ms / 1e9
     elif name.endswith("_f64") and st["flops"] > 0 and not name.startswith(("trsv", "split", "transpose")):
         bound, unit, peak, src = "tensor", "TFLOP/s", peaks["fp64_tflops"], peaks["source"]["fp64_tflops"] + \
             " (FP64 pipe: DFMA and DMMA run at the same rate on GB300)"
@@ -323,25 +339,33 @@ def roofline_for(name: str, st: dict, peaks: dict, n: int = 0, k: int = 0) -> di
         bound, unit, peak, src = "hbm", "GB/s", peaks["hbm_gbs"], peaks["source"]["hbm_gbs"]
         ach = st["bytes"] / ms / 1e6
     traffic = ncu_traffic(name, n, k)
-    return {"kernel": name, "bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
-            "traffic": traffic, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at n=8192, "
-            f"64 RHS, scaled by {'n^2 ceil(k/16)' if NCU_TRAFFIC[name][3] == 'n2_kchunks' else 'n^2'}"
-            if traffic else None, "launches": st["launches"],
-            "per_launch_flops": st["flops"] / st["launches"], "per_launch_bytes": st["bytes"] / st["launches"],
-            "peak_source": src,
-            "timing": "CUDA events around each launch of the kernel, on its stream, in a repeat of the K timed steps"}
+    per_launch = st["flops"] / st["launches"] / (products if name not in OZAKI_KERNELS else 1)
+    out = {"kernel": name, "bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
+           "work": "algorithmic flops (one product per output and depth step)" if unit == "TFLOP/s"
+           else "algorithmic bytes",
+           "traffic": traffic, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at n=8192, "
+           f"64 RHS, scaled by {'n^2 ceil(k/16)' if NCU_TRAFFIC[name][3] == 'n2_kchunks' else 'n^2'}"
+           if traffic else None, "launches": st["launches"],
+           "per_launch_flops": per_launch, "per_launch_bytes": st["bytes"] / st["launches"],
+           "peak_source": src,
+           "timing": "CUDA events around each launch of the kernel, on its stream, in a repeat of the timed steps"}
+    if products > 1:
+        out["split_products"] = {"products_per_algorithmic_product": products, "tensor_achieved": ach * products,
+                                 "tensor_frac": ach * products / peak,
+                                 "note": "the tensor cores' executed work, all split products counted"}
+    return out
 
 
-def run_ours(args, ws, rank, local):
+def measure_config(args, cfg, ws, rank, local, peaks, steps, warmup, profile_steps, e2e_calls,
+                   clocks_on=True) -> dict:
+    """Both arms of one configuration on the same device-resident inputs: the plain FP64 factor +
+    solve and the mixed-precision solve with FP64 refinement.  Returns the arms, the headline (the
+    faster arm whose solution an independent torch FP64 residual puts at backward error <= 1e-14)
+    and the end-to-end figure through the host-pointer C ABI."""
     import ctypes
     import torch
     import gbllt as G
 
-    torch.cuda.set_device(local)
-    cfg = dict(CONFIGS[args.config])
-    if args.n:
-        cfg["n"] = args.n
-        cfg["workload"] += f" (n overridden to {args.n})"
     n, k = cfg["n"], cfg["nrhs"]
     flops = llt_flops(n, k)
     A0, B0 = make_inputs_gpu(cfg, seed=1 + rank)
@@ -352,6 +376,7 @@ def run_ours(args, ws, rank, local):
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     opts = G.mixed_opts(args.mixed_precision, 10, 1e-14, fallback=False)
+    nseg = SPLIT_PRODUCTS[args.mixed_precision]
     reports = []
 
     def step_fp64():
@@ -372,26 +397,27 @@ def run_ours(args, ws, rank, local):
     l2_note = (f"inputs larger than L2 (matrix {n * n * 8 / 1e9:.1f} GB vs 129 MB L2)" if flush is None else
                f"L2 flushed before each timed step (512 MB write; matrix {n * n * 8 / 1e6:.0f} MB)")
 
-    def timed(step_fn):
-        for _ in range(max(args.warmup, 0)):
+    def timed(step_fn, nprof):
+        for _ in range(max(warmup, 0)):
             step_fn()
         stream.synchronize()
-        clocks = ClockSampler(local)
+        clocks = ClockSampler(local) if clocks_on else None
         barrier(ws)
         torch.cuda.synchronize()
-        clocks.start()
+        if clocks:
+            clocks.start()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         if flush is None:  # inputs larger than L2: one timed region over all steps
             e0.record(stream)
-            for _ in range(args.steps):
+            for _ in range(steps):
                 step_fn()
             e1.record(stream)
             e1.synchronize()
             total_ms = e0.elapsed_time(e1)
         else:  # small inputs: L2 flushed (a write larger than L2) before each step, outside its timing
             total_ms = 0.0
-            for _ in range(args.steps):
+            for _ in range(steps):
                 with torch.cuda.stream(stream):
                     flush.zero_()
                 e0.record(stream)
@@ -401,171 +427,215 @@ def run_ours(args, ws, rank, local):
                 total_ms += e0.elapsed_time(e1)
         torch.cuda.synchronize()
         barrier(ws)
-        ck = clocks.stop()
-        # per-kernel device times (roofline, shares) from a repeat of the same K steps with CUDA
-        # events around every launch; the events cost a few percent, so they stay out of the timed
-        # region above
-        G.profile_enable(True)
-        for _ in range(args.steps):
-            if flush is not None:
-                with torch.cuda.stream(stream):
-                    flush.zero_()
-            step_fn()
-        torch.cuda.synchronize()
-        prof = G.profile_read()
-        G.profile_enable(False)
+        ck = clocks.stop() if clocks else None
+        # per-kernel device times (roofline, shares) from a repeat of nprof steps with CUDA events
+        # around every launch; the events cost a few percent, so they stay out of the timed region
+        prof = {}
+        if nprof > 0:
+            G.profile_enable(True)
+            for _ in range(nprof):
+                if flush is not None:
+                    with torch.cuda.stream(stream):
+                        flush.zero_()
+                step_fn()
+            torch.cuda.synchronize()
+            prof = G.profile_read()
+            G.profile_enable(False)
         return max_over_ranks(ws, total_ms), prof, ck
 
     def backward_error(Xs):  # torch FP64 GEMM as an independent check of the returned solution
         R = A0 @ Xs.T - B0.T
         return float(torch.linalg.norm(R) / (torch.linalg.norm(A0) * torch.linalg.norm(Xs)))
 
-    peaks = measured_peaks()
-    run64 = args.arms in ("both", "fp64")
-    runmx = args.arms in ("both", "mixed")
-    if run64:
-        ms64, prof64, ck64 = timed(step_fp64)
-        assert int(info.item()) == 0, f"factorisation failed, info={int(info.item())}"
-        be64 = backward_error(B)
-    if runmx:
-        reports.clear()
-        msmx, profmx, ckmx = timed(step_mixed)
-        rcs = {rc for rc, _ in reports}
-        rep = reports[-1][1]
-        bemx = backward_error(X)
-        mixed_ok = rcs == {G.SUCCESS} and rep["converged"] and bemx <= 1e-14
-    else:
-        mixed_ok = False
+    ms64, prof64, ck64 = timed(step_fp64, profile_steps[0])
+    assert int(info.item()) == 0, f"factorisation failed, info={int(info.item())}"
+    be64 = backward_error(B)
+    reports.clear()
+    msmx, profmx, ckmx = timed(step_mixed, profile_steps[1])
+    rcs = {rc for rc, _ in reports}
+    rep = reports[-1][1]
+    bemx = backward_error(X)
+    mixed_ok = rcs == {G.SUCCESS} and rep["converged"] and bemx <= 1e-14
 
-    def arm(ms, prof, be, extra):
-        top = max(prof.items(), key=lambda kv: kv[1]["ms"])
-        total = sum(v["ms"] for v in prof.values())
-        d = {"seconds_per_solve": ms / args.steps / 1e3, "tflops": ws * flops * args.steps / (ms * 1e-3) / 1e12,
-             "backward_error": be, "gpu_launches": sum(v["launches"] for v in prof.values()),
-             "roofline": dict(roofline_for(top[0], top[1], peaks, cfg["n"], cfg["nrhs"]),
-                              kernel_share_of_device_time=top[1]["ms"] / total),
-             "kernels": {kn: {"launches": v["launches"], "ms": v["ms"]} for kn, v in prof.items()}}
+    def arm(ms, prof, be, nprof, extra, seg=1):
+        d = {"seconds_per_solve": ms / steps / 1e3, "tflops": ws * flops * steps / (ms * 1e-3) / 1e12,
+             "backward_error": be, "reached_1e-14": be <= 1e-14}
+        if prof:
+            top = max(prof.items(), key=lambda kv: kv[1]["ms"])
+            total = sum(v["ms"] for v in prof.values())
+            d["gpu_launches"] = int(round(sum(v["launches"] for v in prof.values()) * steps / nprof))
+            d["roofline"] = dict(roofline_for(top[0], top[1], peaks, n, k,
+                                              seg if top[0].startswith("tc_update") else 1),
+                                 kernel_share_of_device_time=top[1]["ms"] / total)
+            d["kernels"] = {kn: {"launches": v["launches"], "ms": v["ms"]} for kn, v in prof.items()}
+            d["kernels_note"] = f"launches and device ms summed over {nprof} profiled steps"
         d.update(extra)
         return d
 
-    fp64 = arm(ms64, prof64, be64, {"path": "plain FP64: gbllt_dpotrf_dev + gbllt_dpotrs_dev"}) if run64 else None
-    mixed = arm(msmx, profmx, bemx, {"path": f"gbllt_dposv_mixed_dev precision={args.mixed_precision}, FP64 "
-                                             f"residuals, tol 1e-14, no fallback",
-                                     "reached_1e-14": mixed_ok, "steps": rep["steps"], "history": rep["history"],
-                                     "factor_ms": rep["factor_ms"], "refine_ms": rep["refine_ms"]}) if runmx else None
-    # headline: the faster path that reached backward error <= 1e-14 (the mixed arm alone when only it ran)
-    use_mixed = runmx and (not run64 or (mixed_ok and mixed["seconds_per_solve"] < fp64["seconds_per_solve"]))
+    fp64 = arm(ms64, prof64, be64, profile_steps[0], {"path": "plain FP64: gbllt_dpotrf_dev + gbllt_dpotrs_dev"})
+    mixed = arm(msmx, profmx, bemx, profile_steps[1],
+                {"path": f"gbllt_dposv_mixed_dev precision={args.mixed_precision}, FP64 residuals, tol 1e-14, "
+                         f"no fallback", "precision": args.mixed_precision, "reached_1e-14": mixed_ok,
+                 "steps": rep["steps"], "history": rep["history"], "factor_ms": rep["factor_ms"],
+                 "refine_ms": rep["refine_ms"]}, nseg)
+    use_mixed = mixed_ok and mixed["seconds_per_solve"] < fp64["seconds_per_solve"]
     head = mixed if use_mixed else fp64
-    ms_head, ck = (msmx, ckmx) if use_mixed else (ms64, ck64)
+    del A, B
+    torch.cuda.empty_cache()
 
-    # end to end through the host-pointer C ABI (pinned host buffers; copies inside the timed call)
-    hA0 = A0.cpu().pin_memory()
-    hB0 = B0.cpu().pin_memory()
-    hA = torch.empty(hA0.shape, dtype=hA0.dtype).pin_memory()
-    hB = torch.empty(hB0.shape, dtype=hB0.dtype).pin_memory()
-    hX = torch.zeros(hB0.shape, dtype=hB0.dtype).pin_memory()
-    a_np, b_np, x_np = hA.numpy(), hB.numpy(), hX.numpy()
-    tt = []
-    for i in range(1 + max(1, min(args.steps, 3))):
-        hA.copy_(hA0)
-        hB.copy_(hB0)
-        inf = ctypes.c_int64(0)
-        t0 = time.perf_counter()
-        if use_mixed:
-            r = G.MixedReport()
-            rc = G.lib().gbllt_dposv_mixed(G.COL_MAJOR, b"L", n, k, a_np.ctypes.data, n, b_np.ctypes.data, n,
-                                           x_np.ctypes.data, n, ctypes.byref(opts), ctypes.byref(r))
-        else:
-            rc = G.lib().gbllt_dposv(G.COL_MAJOR, b"L", n, k, a_np.ctypes.data, n, b_np.ctypes.data, n,
-                                     ctypes.byref(inf))
-        dt = time.perf_counter() - t0
-        G.check("e2e", rc)
-        if i > 0:
-            tt.append(dt)
-    e2e_s = max_over_ranks(ws, sum(tt) / len(tt))
-    bytes_io = int(n * n * 8 + n * k * 8)
-    e2e = {"value": ws * flops / e2e_s / 1e12, "unit": "TFLOP/s", "seconds_per_step": e2e_s,
-           "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": int(n * k * 8) if use_mixed else bytes_io,
-           "path": ("gbllt_dposv_mixed" if use_mixed else "gbllt_dposv") + " (host pointers, pinned), wall clock"}
+    # end to end through the host-pointer C ABI (pinned host buffers; the copies are inside the call)
+    e2e = None
+    if e2e_calls > 0:
+        hA = torch.empty(A0.shape, dtype=A0.dtype, pin_memory=True)
+        hA.copy_(A0)
+        hB0 = B0.cpu().pin_memory()
+        hB = torch.empty(hB0.shape, dtype=hB0.dtype).pin_memory()
+        hX = torch.zeros(hB0.shape, dtype=hB0.dtype).pin_memory()
+        hA0 = None
+        if not use_mixed:  # the FP64 entry overwrites A with its factor: keep a pristine copy
+            hA0 = torch.empty(A0.shape, dtype=A0.dtype, pin_memory=True)
+            hA0.copy_(A0)
+        a_np, b_np, x_np = hA.numpy(), hB.numpy(), hX.numpy()
+        tt = []
+        for i in range(1 + e2e_calls):
+            if hA0 is not None:
+                hA.copy_(hA0)
+            hB.copy_(hB0)
+            inf = ctypes.c_int64(0)
+            t0 = time.perf_counter()
+            if use_mixed:
+                r = G.MixedReport()
+                rc = G.lib().gbllt_dposv_mixed(G.COL_MAJOR, b"L", n, k, a_np.ctypes.data, n, b_np.ctypes.data, n,
+                                               x_np.ctypes.data, n, ctypes.byref(opts), ctypes.byref(r))
+            else:
+                rc = G.lib().gbllt_dposv(G.COL_MAJOR, b"L", n, k, a_np.ctypes.data, n, b_np.ctypes.data, n,
+                                         ctypes.byref(inf))
+            dt = time.perf_counter() - t0
+            G.check("e2e", rc)
+            if i > 0:  # the first call warms up
+                tt.append(dt)
+        e2e_s = max_over_ranks(ws, sum(tt) / len(tt))
+        bytes_io = int(n * n * 8 + n * k * 8)
+        e2e = {"value": ws * flops / e2e_s / 1e12, "unit": "TFLOP/s", "seconds_per_step": e2e_s,
+               "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": int(n * k * 8) if use_mixed else bytes_io,
+               "calls_timed": len(tt),
+               "path": ("gbllt_dposv_mixed" if use_mixed else "gbllt_dposv") + " (host pointers, pinned), wall clock"}
+        del hA, hA0, hB, hB0, hX
+    res = {"n": n, "nrhs": k, "kappa": cfg["kappa"], "fp64": fp64, "mixed": mixed, "use_mixed": use_mixed,
+           "head": head, "ms_head": msmx if use_mixed else ms64, "clocks": ckmx if use_mixed else ck64,
+           "clocks_fp64_arm": ck64, "e2e": e2e, "l2": l2_note, "flops": flops,
+           "mixed_over_fp64_speedup": fp64["seconds_per_solve"] / mixed["seconds_per_solve"] if mixed_ok else None}
+    del A0, B0, X
+    torch.cuda.empty_cache()
+    return res
 
+
+def c3_sweep(args, n: int, fp64_k64_s: float | None) -> dict:
+    """The rest of the n = 32768 configuration: kappa in {1e2, 1e4, 1e6} and 1 or 64 right-hand
+    sides, the mixed solve (the headline precision) after one warm-up call, and the plain FP64
+    factor + solve with 1 right-hand side, each checked by an independent torch FP64 residual."""
+    import torch
+    import gbllt as G
+    s = torch.cuda.current_stream().cuda_stream
+    opts = G.mixed_opts(args.mixed_precision, 10, 1e-14, False)
+    rows = []
+    fp64_s = {64: fp64_k64_s}
+    for kappa in (1e2, 1e4, 1e6):
+        A0, B64 = make_inputs_gpu({"n": n, "nrhs": 64, "kappa": kappa}, seed=3)
+        for k in (1, 64):
+            B0 = B64[:k].contiguous()
+            if k == 1 and kappa == 1e6:  # the FP64 time does not depend on kappa
+                A = A0.clone()
+                B = B0.clone()
+                info = torch.zeros(1, dtype=torch.int64, device="cuda")
+                for it in range(2):  # the first pass warms up
+                    A.copy_(A0)
+                    B.copy_(B0)
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    G.potrf_dev(A, n, n, info, "L", s)
+                    G.potrs_dev(A, n, n, B, k, n, "L", s)
+                    torch.cuda.synchronize()
+                    fp64_s[1] = time.perf_counter() - t0
+                R = A0 @ B.T - B0.T
+                be = float(torch.linalg.norm(R) / (torch.linalg.norm(A0) * torch.linalg.norm(B)))
+                rows.append({"path": "fp64", "nrhs": k, "kappa": kappa, "seconds": fp64_s[1], "backward_error": be})
+                del A, B
+            X = torch.zeros_like(B0)
+            G.posv_mixed_dev(A0, n, n, B0, n, X, n, k, opts, "L", s, raise_on_error=False)  # warm-up
+            X.zero_()  # a failed low-precision factorisation leaves X untouched
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rc, rep = G.posv_mixed_dev(A0, n, n, B0, n, X, n, k, opts, "L", s, raise_on_error=False)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            R = A0 @ X.T - B0.T
+            be = float(torch.linalg.norm(R) / (torch.linalg.norm(A0) * torch.linalg.norm(X)))
+            rows.append({"path": "mixed", "precision": args.mixed_precision, "nrhs": k, "kappa": kappa,
+                         "seconds": dt, "reached_1e-14": bool(rc == 0 and rep["info"] == 0 and rep["converged"]
+                                                              and be <= 1e-14),
+                         "steps": rep["steps"], "backward_error": be, "factor_ms": rep["factor_ms"],
+                         "refine_ms": rep["refine_ms"]})
+        del A0, B64
+        torch.cuda.empty_cache()
+    for r in rows:
+        if r["path"] == "mixed" and fp64_s.get(r["nrhs"]):
+            r["speedup_vs_fp64"] = fp64_s[r["nrhs"]] / r["seconds"]
+    return {"n": n, "timing": "wall clock around one call after one warm-up call (64-RHS FP64 time: the "
+                              "headline arm's device-timed mean)", "rows": rows}
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    cfg = dict(CONFIGS[args.config])
+    if args.n:
+        cfg["n"] = args.n
+        cfg["workload"] += f" (n overridden to {args.n})"
+    peaks = measured_peaks()
+    K, W = args.steps, args.warmup
+    # the FP64 arm's per-kernel profile repeats a few steps (its steps take a second at n = 32768)
+    main = measure_config(args, cfg, ws, rank, local, peaks, K, W, (min(K, 5), K), max(3, min(K, 10)))
+    head = main["head"]
+    extras = {}
+    if args.config == DEFAULT_CONFIG and not args.no_extras:
+        extras["c3_sweep"] = c3_sweep(args, cfg["n"], main["fp64"]["seconds_per_solve"])
+        c1 = measure_config(args, CONFIGS["c1"], ws, rank, local, peaks, max(K, 10), max(W, 3), (0, 0), 5,
+                            clocks_on=False)
+        extras["c1"] = {"workload": CONFIGS["c1"]["workload"], "l2": c1["l2"], "e2e": c1["e2e"],
+                        "headline": "mixed+refinement" if c1["use_mixed"] else "plain FP64",
+                        "fp64": c1["fp64"], "mixed": c1["mixed"]}
+        extras["c4"] = run_c4(args, ws, rank, steps=max(3, min(K, 10)))
+        extras["c5"] = run_c5(args, passes=2)
     if rank != 0:
         return
     cpu = None if args.no_cpu_baseline or ws > 1 else cpu_sample()
+    n, k = main["n"], main["nrhs"]
+    use_mixed = main["use_mixed"]
     out = {
-        "metric": METRIC, "value": ws * flops * args.steps / (ms_head * 1e-3) / 1e12, "unit": "TFLOP/s",
-        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_head / args.steps,
+        "metric": METRIC, "value": ws * main["flops"] * K / (main["ms_head"] * 1e-3) / 1e12, "unit": "TFLOP/s",
+        "n_gpus": ws, "steps": K, "warmup": W, "ms_per_step": main["ms_head"] / K,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": f"{args.mixed_precision}+f64" if use_mixed else "f64", "data": "synthetic",
         "config": {"workload": cfg["workload"], "n": n, "nrhs": k, "kappa": cfg["kappa"],
                    "headline": "mixed+refinement" if use_mixed else "plain FP64",
-                   "work_per_step_flops": flops, "accuracy": "normwise backward error <= 1e-14 (checked with a "
-                   "torch FP64 residual of the returned X)",
-                   "l2": l2_note},
+                   "work_per_step_flops": main["flops"], "work": "n^3/3 + 2 n^2 k FP64-equivalent flop per solve",
+                   "accuracy": "normwise backward error <= 1e-14 (checked with a torch FP64 residual of the "
+                               "returned X)", "l2": main["l2"]},
         "seconds_per_solve": head["seconds_per_solve"], "backward_error": head["backward_error"],
+        "mixed_over_fp64_speedup": main["mixed_over_fp64_speedup"],
         "roofline": head["roofline"], "gpu_launches": head["gpu_launches"],
-        "fp64": fp64, "mixed": mixed, "peaks": peaks,
-        "e2e": e2e, "cpu_baseline": cpu, "clocks": ck, "clocks_fp64_arm": ck64 if run64 else None,
+        "fp64": main["fp64"], "mixed": main["mixed"], "peaks": peaks,
+        "e2e": main["e2e"], "cpu_baseline": cpu, "clocks": main["clocks"], "clocks_fp64_arm": main["clocks_fp64_arm"],
     }
+    out.update(extras)
     print(json.dumps(out), flush=True)
 
 
 # ---- other configurations (one JSON line each; the default run is the one above) -------------------
 
-def run_c3(args):
-    """n = 32768, 1 and 64 RHS, Householder spectra kappa in {1e2, 1e4, 1e6}: mixed precision +
-    FP64 refinement (each precision) against the plain FP64 GPU factor+solve on the same input."""
-    import torch
-    import gbllt as G
-    n = args.n or 32768
-    s = torch.cuda.current_stream().cuda_stream
-    out = {"metric": METRIC, "config": {"workload": f"C3: n={n}, Householder spectrum, 1 and 64 RHS", "n": n},
-           "unit": "s", "higher_is_better": False, "data": "synthetic", "results": []}
-    fp64_s = {}
-    for kappa in (1e2, 1e4, 1e6):
-        cfg = {"n": n, "nrhs": 64, "kappa": kappa}
-        A0, B64 = make_inputs_gpu(cfg, seed=3)
-        for k in (1, 64):
-            B0 = B64[:k].contiguous()
-            X = torch.zeros_like(B0)
-            if k not in fp64_s and kappa == 1e6:  # the FP64 time does not depend on kappa
-                A = A0.clone()
-                B = B0.clone()
-                info = torch.zeros(1, dtype=torch.int64, device="cuda")
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                G.potrf_dev(A, n, n, info, "L", s)
-                G.potrs_dev(A, n, n, B, k, n, "L", s)
-                torch.cuda.synchronize()
-                fp64_s[k] = time.perf_counter() - t0
-                R = A0 @ B.T - B0.T
-                be = float(torch.linalg.norm(R) / (torch.linalg.norm(A0) * torch.linalg.norm(B)))
-                out["results"].append({"path": "fp64", "nrhs": k, "kappa": kappa, "seconds": fp64_s[k],
-                                       "backward_error": be})
-                del A, B
-            for prec in args.c3_precisions.split(","):
-                G.posv_mixed_dev(A0, n, n, B0, n, X, n, k, G.mixed_opts(prec, 10, 1e-14, False), "L", s,
-                                 raise_on_error=False)  # warm-up
-                X.zero_()  # a failed low-precision factorisation leaves X untouched
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                rc, rep = G.posv_mixed_dev(A0, n, n, B0, n, X, n, k, G.mixed_opts(prec, 10, 1e-14, False), "L", s,
-                                           raise_on_error=False)
-                torch.cuda.synchronize()
-                dt = time.perf_counter() - t0
-                R = A0 @ X.T - B0.T
-                be = float(torch.linalg.norm(R) / (torch.linalg.norm(A0) * torch.linalg.norm(X)))
-                out["results"].append({"path": "mixed", "precision": prec, "nrhs": k, "kappa": kappa, "seconds": dt,
-                                       "reached_1e-14": bool(rc == 0 and rep["info"] == 0 and rep["converged"]
-                                                             and be <= 1e-14), "steps": rep["steps"],
-                                       "info": rep["info"], "backward_error": be, "factor_ms": rep["factor_ms"],
-                                       "refine_ms": rep["refine_ms"]})
-                print(json.dumps(out["results"][-1]), file=sys.stderr, flush=True)
-        del A0, B64
-        torch.cuda.empty_cache()
-    print(json.dumps(out), flush=True)
-
-
-def run_c4(args, ws: int = 1, rank: int = 0):
+def run_c4(args, ws: int = 1, rank: int = 0, steps: int | None = None) -> dict:
     """20000 SPD systems, n_i ~ U{4..256}, one RHS each, FP64 and FP32, one graph-replayed launch.
     With N ranks the systems are sharded by cost (shard.partition, no data-path collective): each
     rank solves its share, the step time is the maximum over ranks, and the value counts all
@@ -574,6 +644,7 @@ def run_c4(args, ws: int = 1, rank: int = 0):
     import gbllt as G
     import shard
     count_all = 20000
+    steps = steps or args.steps
     rng = torch.Generator(device="cpu").manual_seed(21)
     sizes_all = torch.randint(4, 257, (count_all,), generator=rng).numpy().astype(np.int64)
     sizes = sizes_all[shard.partition(sizes_all, ws)[rank]] if ws > 1 else sizes_all
@@ -608,7 +679,7 @@ def run_c4(args, ws: int = 1, rank: int = 0):
         G.profile_enable(True)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         tot = 0.0
-        for _ in range(args.steps):
+        for _ in range(steps):
             a.copy_(a0)
             b.copy_(b0)
             barrier(ws)
@@ -622,7 +693,7 @@ def run_c4(args, ws: int = 1, rank: int = 0):
         G.profile_enable(False)
         assert int(info.max()) == 0
         st = prof[f"batched_posv_{name}"]
-        ms = tot / args.steps
+        ms = tot / steps
         gbs = st["bytes"] / st["ms"] / 1e6
         tfs = st["flops"] / st["ms"] / 1e9
         out["results"].append({"dtype": name, "ms": ms, "solves_per_s": count_all / (ms * 1e-3),
@@ -631,11 +702,12 @@ def run_c4(args, ws: int = 1, rank: int = 0):
                                "variant": plan.variant(), "launches_per_step": 1,
                                "per_rank_note": "achieved_* are rank 0's kernel on its shard" if ws > 1 else None})
     out["peaks"] = peaks
-    if rank == 0:
-        print(json.dumps(out), flush=True)
+    out["steps"] = steps
+    out["timing"] = "CUDA events around each graph-replayed launch (max over ranks), inputs restored between steps"
+    return out
 
 
-def run_c5(args):
+def run_c5(args, passes: int = 2) -> dict:
     """64 RBF kernel matrices, n = 2048 (x ~ U[0,1]^3, lengthscale 0.2, variance 1, noise 1e-2),
     y ~ N(0,1): f = logdet A + y^T A^{-1} y forward and the hand-written adjoint (dA, dy), FP64;
     the mixed-precision forward solves A alpha = y with the tensor-core factorisation + refinement."""
@@ -654,7 +726,7 @@ def run_c5(args):
     streams = [torch.cuda.Stream() for _ in range(nstream)]
     infos = [torch.zeros(1, dtype=torch.int64, device="cuda") for _ in range(nstream)]
     res = {}
-    for it in range(2):  # first pass warms up
+    for it in range(max(passes, 2)):  # the first pass warms up, the last one is reported
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         Ls, alphas, fs = [None] * nmat, [None] * nmat, [None] * nmat
@@ -721,8 +793,9 @@ def run_c5(args):
     out = {"metric": "GP likelihood logdet+quad forward and adjoint (s)", "config": {
         "workload": "C5: 64 RBF matrices n=2048, lengthscale 0.2, noise 1e-2", "nmat": nmat, "n": n},
         "unit": "s", "higher_is_better": False, "data": "synthetic", "results": res,
-        "forward_tflops": fl_fwd / res["forward_s"] / 1e12, "backward_tflops_equiv": fl_fwd / res["backward_s"] / 1e12}
-    print(json.dumps(out), flush=True)
+        "forward_tflops": fl_fwd / res["forward_s"] / 1e12, "backward_tflops_equiv": fl_fwd / res["backward_s"] / 1e12,
+        "timing": "wall clock around all 64 problems on 8 streams, after a warm-up pass"}
+    return out
 
 
 def main():
@@ -731,25 +804,30 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=sorted(CONFIGS) + ["c3", "c4", "c5"], default="c2")
-    ap.add_argument("--c3-precisions", default="bf16x6,tf32x3,bf16x3,tf32,bf16")
+    ap.add_argument("--config", choices=sorted(CONFIGS) + ["c3-sweep", "c4", "c5"], default=DEFAULT_CONFIG)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mixed-precision", default="bf16x6", choices=["fp32", "tf32", "tf32x3", "bf16", "bf16x3", "bf16x6"])
+    ap.add_argument("--no-extras", action="store_true", help="the default configuration's line without the "
+                    "kappa sweep and the C1 / C4 / C5 keys")
+    ap.add_argument("--mixed-precision", default="bf16x6", choices=sorted(SPLIT_PRODUCTS))
     ap.add_argument("--n", type=int, default=0, help="override the order n (profiling a smaller case)")
-    ap.add_argument("--arms", default="both", choices=["both", "fp64", "mixed"])
     args = ap.parse_args()
     if args.impl == "reference":
         # CPU only: under torchrun rank 0 alone runs it, the other ranks exit without work
         run_reference(args, int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")))
         return
     ws, rank, local = dist_setup()
-    if args.config in ("c3", "c4", "c5"):
+    if args.config in ("c3-sweep", "c4", "c5"):
         import torch
         torch.cuda.set_device(local)
         if args.config == "c4":
-            run_c4(args, ws, rank)
+            out = run_c4(args, ws, rank)
+        elif args.config == "c5":
+            out = run_c5(args)
         else:
-            {"c3": run_c3, "c5": run_c5}[args.config](args)
+            out = {"metric": METRIC, "config": {"workload": "n=32768 sweep: kappa in {1e2,1e4,1e6}, 1 and 64 RHS"},
+                   **c3_sweep(args, args.n or CONFIGS["c3"]["n"], None)}
+        if rank == 0:
+            print(json.dumps(out), flush=True)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

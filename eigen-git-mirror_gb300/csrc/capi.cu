@@ -14,7 +14,8 @@ namespace gbllt {
 namespace {
 thread_local std::string g_last_error;
 std::mutex g_dev_mutex;
-int g_dev_ok[64];  // 0 = unchecked, 1 = ok, -1 = unusable
+int g_dev_ok[64];              // 0 = unchecked, 1 = ok, -1 = unusable
+cudaMemPool_t g_pool[64] = {};  // the library's own stream-ordered pool per device (null: default pool)
 }  // namespace
 
 void set_last_error(cudaError_t e, const char* what, const char* file, int line) {
@@ -38,6 +39,9 @@ cudaError_t dev_malloc_async(void** p, size_t bytes, cudaStream_t s) {
     *p = nullptr;
     return cudaErrorMemoryAllocation;
   }
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && g_pool[dev])
+    return cudaMallocFromPoolAsync(p, bytes, g_pool[dev], s);
   return cudaMallocAsync(p, bytes, s);
 }
 
@@ -64,14 +68,23 @@ int ensure_device() {
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     g_dev_ok[dev] = (major == 10 && minor == 3) ? 1 : -1;
     if (g_dev_ok[dev] > 0) {
-      // the library's workspaces come from the device's default stream-ordered pool; by default it
-      // returns freed memory to the system at every synchronisation, and the next call maps it
-      // again (gigabytes for a large solve).  Keep it cached in this process instead;
-      // gbllt_release_cached_memory() gives it back.
-      cudaMemPool_t pool;
-      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      // The library's workspaces come from a stream-ordered pool of its own on each device, which
+      // keeps freed memory cached in the process: a pool that returns it at every synchronisation
+      // makes the next call map it again (gigabytes for a large solve).  The device's default pool,
+      // which other code in the process may use, keeps its own settings.
+      // gbllt_release_cached_memory() gives the cached memory back.  If the pool cannot be created,
+      // allocations fall back to the default pool with its settings unchanged.
+      cudaMemPoolProps props;
+      memset(&props, 0, sizeof props);
+      props.allocType = cudaMemAllocationTypePinned;
+      props.handleTypes = cudaMemHandleTypeNone;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      cudaMemPool_t pool = nullptr;
+      if (cudaMemPoolCreate(&pool, &props) == cudaSuccess) {
         uint64_t thr = UINT64_MAX;
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        g_pool[dev] = pool;
       }
       cudaGetLastError();
     }
@@ -208,7 +221,8 @@ int host_posv(bool do_factor, bool do_solve, int layout, char uplo, int64_t n, i
     if (info) *info = h_info;
   }
   if (do_solve && nrhs > 0 && h_info == 0) {
-    if ((rc = potrs_dev<T>(upper, n, nrhs, d_a, n, d_b, n, s))) return rc;
+    int herr = 0;
+    if ((rc = potrs_dev<T>(upper, n, nrhs, d_a, n, d_b, n, s, &herr))) return rc;
     if (!rowmajor) {
       GB_CUDA_TRY(copy2d_async(b, ldb * es, d_b, n * es, n * es, nrhs, cudaMemcpyDeviceToHost, s));
     } else {
@@ -216,6 +230,10 @@ int host_posv(bool do_factor, bool do_solve, int layout, char uplo, int64_t n, i
       GB_CUDA_TRY(copy2d_async(b, ldb * es, d_bt, nrhs * es, nrhs * es, n, cudaMemcpyDeviceToHost, s));
     }
     GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (herr) {
+      g_last_error = "a bounded wait of the triangular sweeps ran out";
+      return GBLLT_ERR_TIMEOUT;
+    }
   }
   return GBLLT_SUCCESS;
 }
@@ -359,11 +377,19 @@ int gbllt_release_cached_memory(void) {
     cudaGetLastError();
     return GBLLT_ERR_NO_DEVICE;
   }
-  cudaMemPool_t pool;
-  GB_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, dev));
+  if (dev < 0 || dev >= 64 || !g_pool[dev]) return GBLLT_SUCCESS;  // nothing cached by the library
   GB_CUDA_TRY(cudaDeviceSynchronize());
-  GB_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
+  GB_CUDA_TRY(cudaMemPoolTrimTo(g_pool[dev], 0));
   return GBLLT_SUCCESS;
+}
+
+int gbllt_selftest_wait_timeout(int64_t wait_us, int* observed) {
+  if (wait_us < 1000 || wait_us > 2000000) return -1;
+  if (!observed) return -2;
+  *observed = GBLLT_SUCCESS;
+  int rc = ensure_device();
+  if (rc) return rc;
+  return sweep_wait_selftest((unsigned long long)wait_us * 1000ull, lib_stream(), observed);
 }
 
 int gbllt_dpotrf(int layout, char uplo, int64_t n, double* a, int64_t lda, int64_t* info) {

@@ -222,7 +222,15 @@ int inv_l1_estimate(bool upper, int64_t n, const T* d_l, int64_t ldl, double* es
     int diff;
   } h{};
 
-  auto solve = [&](T* x) { return potrs_ws<T>(upper, n, 1, d_l, ldl, x, n, ws, s); };
+  // each solve's error word is read back (the estimate synchronises after every solve anyway)
+  auto solve = [&](T* x) -> int {
+    int r2 = potrs_ws<T>(upper, n, 1, d_l, ldl, x, n, ws, s);
+    if (r2) return r2;
+    int herr = 0;
+    GB_CUDA_TRY(cudaMemcpyAsync(&herr, potrs_ws_error_word(n, sizeof(T), ws), sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return herr ? GBLLT_ERR_TIMEOUT : GBLLT_SUCCESS;
+  };
   auto read_l1 = [&](double* out) -> int {
     l1_kernel<T><<<1, 1024, 0, s>>>(n, v, d_l1);
     GB_CUDA_TRY(cudaMemcpyAsync(&h.l1, d_l1, sizeof(double), cudaMemcpyDeviceToHost, s));

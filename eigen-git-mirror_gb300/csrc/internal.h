@@ -65,9 +65,11 @@ int finalize_info_dev(const DevStatus* st, int64_t* d_info, cudaStream_t s);
 
 // Stream-ordered solve L L^T X = B (upper == false; L lower column-major at d_a) or
 // U^T U X = B (upper == true; U upper column-major), B column-major n x nrhs, in place.
+// host_err (optional): receives the solve's error word (copied in stream order; valid once the
+// caller has synchronised s).
 template <typename T>
 int potrs_dev(bool upper, int64_t n, int64_t nrhs, const T* d_a, int64_t lda, T* d_b, int64_t ldb,
-              cudaStream_t s);
+              cudaStream_t s, int* host_err = nullptr);
 
 // Brackets one kernel launch with profiling events when gbllt_profile_enable(1) is in effect.
 struct ProfScope {
@@ -83,6 +85,14 @@ template <typename T>
 constexpr const char* tname() {
   return sizeof(T) == 8 ? "f64" : "f32";
 }
+
+// The device error word of a solve on the workspace ws (elem = the solve's element size): 0, or 1
+// when a bounded wait of one of its sweeps ran out (the rows it could not solve are then NaN).
+// Cleared by each call; a caller that synchronises reads it to report GBLLT_ERR_TIMEOUT.
+int* potrs_ws_error_word(int64_t n, size_t elem, void* ws);
+// Failure-detection self-test of the sweeps' bounded waits (potrs_lookback.cu); *observed = the
+// code the waits reported.
+int sweep_wait_selftest(unsigned long long wait_ns, cudaStream_t s, int* observed);
 
 // The same solve on a caller-supplied workspace of potrs_ws_bytes(n, sizeof(T)) bytes (allocates
 // nothing).

@@ -600,7 +600,8 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   // from A alone (||A||_F and the tensor-core residual's slices of A): its blocks take only the slots
   // the factorisation leaves free.
   struct Streams {
-    cudaStream_t caller = nullptr;
+    cudaStream_t caller = nullptr;  // may be 0, the legacy default stream
+    bool armed = false;             // caller is set and must wait for the internal streams
     cudaStream_t fs = nullptr, side = nullptr, aux = nullptr, low = nullptr;
     cudaEvent_t lev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t in = nullptr, out = nullptr, pre = nullptr;
@@ -608,8 +609,9 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
       // The caller's stream waits for everything issued on these streams before anything it orders
       // later (the release of the workspace they use): on an early error return the factorisation's
       // or the low-priority stream's kernels may still be running.  Work already issued completes.
+      // The internal streams are non-blocking, so even the legacy default stream needs the wait.
       for (cudaStream_t q : {fs, side, aux, low}) {
-        if (!q || !caller) continue;
+        if (!q || !armed) continue;
         cudaEvent_t e = nullptr;
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) {
           if (cudaEventRecord(e, q) == cudaSuccess) cudaStreamWaitEvent(caller, e, 0);
@@ -629,6 +631,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   bool pre_ready = false;  // ||A||^2 (and A's slices) are being formed on the low-priority stream
   if (may_allocate) {
     xs.caller = s;
+    xs.armed = true;
     int least = 0, greatest = 0;
     GB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     GB_CUDA_TRY(cudaStreamCreateWithPriority(&xs.fs, cudaStreamNonBlocking, greatest));
@@ -643,6 +646,10 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     sumsq_on(a, lda, n, n, upper ? 2 : 1, &norms[0], xs.low);
     if (use_oz) {
       const int rc2 = oz.setup(upper, n, nrhs, a, lda, xs.low);
+      // A's slices are released in the caller's stream order: xs (declared after oz, so destroyed
+      // first) makes the caller's stream wait for the low-priority stream on every exit, while the
+      // low-priority stream itself is destroyed by then
+      if (oz.buf) oz.stream = s;
       if (rc2 == GBLLT_ERR_ALLOC) use_oz = false;  // not enough device memory: the FP64 residual
       else if (rc2) return rc2;
     }
@@ -661,7 +668,6 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   if ((rc = stamp(1))) return rc;
   if (pre_ready) {  // everything after this point (norms, residuals, fallback) may use the low stream's results
     GB_CUDA_TRY(cudaStreamWaitEvent(s, xs.pre, 0));
-    if (oz.buf) oz.stream = s;  // freed in the caller's stream order, after the last residual
   }
   DevStatus hst;
   GB_CUDA_TRY(cudaMemcpyAsync(&hst, st, sizeof hst, cudaMemcpyDeviceToHost, s));
@@ -685,11 +691,14 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
       sumsq(R, n, n, nrhs, 0, &norms[1]);
       sumsq(x, ldx, n, nrhs, 0, &norms[2]);
       double hn[3];
+      int serr = 0;  // the FP32 sweeps' error word: a bounded wait ran out
       GB_CUDA_TRY(cudaMemcpyAsync(hn, norms, sizeof hn, cudaMemcpyDeviceToHost, s));
+      GB_CUDA_TRY(cudaMemcpyAsync(&serr, potrs_ws_error_word(n, sizeof(float), solve_ws), sizeof(int),
+                                  cudaMemcpyDeviceToHost, s));
       GB_CUDA_TRY(cudaStreamSynchronize(s));
       bool tmo = false;
       if ((rc = residual_timed_out(&tmo))) return rc;
-      if (tmo) return GBLLT_ERR_TIMEOUT;
+      if (tmo || serr) return GBLLT_ERR_TIMEOUT;
       const double be =
           (hn[0] > 0 && hn[2] > 0) ? sqrt(hn[1]) / (sqrt(hn[0]) * sqrt(hn[2])) : (hn[1] > 0 ? INFINITY : 0.0);
       r.steps = step + 1;
@@ -742,8 +751,12 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
       sumsq(x, ldx, n, nrhs, 0, &norms[2]);
       sumsq(a, lda, n, n, upper ? 2 : 1, &norms[0]);
       double hn[3];
+      int serr = 0;
       GB_CUDA_TRY(cudaMemcpyAsync(hn, norms, sizeof hn, cudaMemcpyDeviceToHost, s));
+      GB_CUDA_TRY(cudaMemcpyAsync(&serr, potrs_ws_error_word(n, sizeof(double), solve_ws), sizeof(int),
+                                  cudaMemcpyDeviceToHost, s));
       GB_CUDA_TRY(cudaStreamSynchronize(s));
+      if (serr) return GBLLT_ERR_TIMEOUT;
       r.backward_error = sqrt(hn[1]) / (sqrt(hn[0]) * sqrt(hn[2]));
       r.converged = r.backward_error <= o.tol;
       ok = true;

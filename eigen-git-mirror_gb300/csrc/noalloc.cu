@@ -3,11 +3,11 @@
 // gbllt_dposv_mixed_dev needs scratch memory next to its inputs and outputs: the rounded FP32
 // working matrix, the BF16/TF32 panel operands, residuals, partial sums and a status word.  It
 // takes that memory from the stream-ordered pool with cudaMallocAsync.  Some callers cannot let a
-// library allocate: an application whose memory is owned by its own allocator or budget, code
-// that must not create allocations while a stream is being captured, or a plug-in that is handed
-// only the buffers it works on.  For them this entry point runs the same solve on a fixed scratch
-// area that is part of the library image: a file-scope __device__ array of kScratchBytes, which
-// every GPU that loads the library keeps until the process exits.
+// library allocate: an application whose device memory is owned by its own caching allocator or a
+// fixed budget (a second allocator in the same process fragments it and escapes its accounting), or
+// a plug-in that is handed only the buffers it works on.  For them this entry point runs the same
+// solve on a fixed scratch area that is part of the library image: a file-scope __device__ array of
+// kScratchBytes, which every GPU that loads the library keeps until the process exits.
 //
 // Host code cannot use the array's name as a device address (in host code it names a host-side
 // stand-in), so the device address is looked up once per device with cudaGetSymbolAddress, with
@@ -26,7 +26,9 @@
 namespace gbllt {
 namespace {
 
-constexpr size_t kScratchBytes = 64ull << 20;  // 64 MiB: n <= 2048 with 64 right-hand sides and the FP64 fallback
+// 64 MiB: n <= 2048 with 64 right-hand sides and the FP64 fallback, at the default panel width of 256
+// (a wider panel widens the panel operands and can push a problem of that size over the limit)
+constexpr size_t kScratchBytes = 64ull << 20;
 __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 std::mutex g_mu;

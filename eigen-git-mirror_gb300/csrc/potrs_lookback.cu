@@ -22,8 +22,10 @@
 // backward sweep applies D's pseudo-inverse to each block's right-hand sides as it loads them
 // (DSCALE: divide where |d| > the smallest normal number, else 0, LDLT.h:587-600).
 #include <cfloat>
+#include <cmath>
 #include <cstdint>
 #include <type_traits>
+#include <vector>
 
 #include "internal.h"
 
@@ -100,7 +102,7 @@ template <typename T, bool UP, bool BWD, int RCT, bool DSCALE>
 __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, long long lda, long long n,
                                                     T* __restrict__ b, long long ldb, int nrhs, const T* __restrict__ inv,
                                                     int* __restrict__ flags, int* __restrict__ counter,
-                                                    int* __restrict__ err) {
+                                                    int* __restrict__ err, unsigned long long wait_ns) {
   constexpr int CPT = RCT / 4;
   // right-hand-side chunk: an independent chain with its own tickets and flags
   {
@@ -156,7 +158,11 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
       const volatile int* f = flags + J;
       const unsigned long long t0 = gtimer();
       while (*f == 0) {
-        if (gtimer() - t0 > WAIT_NS) {
+        if (*(volatile int*)err) {  // another block's wait already ran out: this chain is broken
+          s_abort = 1;
+          break;
+        }
+        if (gtimer() - t0 > wait_ns) {
           s_abort = 1;
           atomicExch(err, 1);
           break;
@@ -165,7 +171,15 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
       __threadfence();
     }
     __syncthreads();
-    if (s_abort) return;
+    if (s_abort) {
+      // the block's solution cannot be formed: its rows become NaN, so a stream-ordered caller
+      // that never reads the error word still sees that the result is invalid
+      for (int idx = tid; idx < RB * RCT; idx += 256) {
+        const int p = idx & 63, c = idx >> 6;
+        if (I0 + p < n && c < nrhs) b[(long long)c * ldb + I0 + p] = T(NAN);
+      }
+      return;
+    }
     for (int idx = tid; idx < RB * RCT; idx += 256) {
       const int p = idx & 63, c = idx >> 6;
       sm.Ys[p][c] = (J0 + p < n && c < nrhs) ? __ldcg(b + (long long)c * ldb + J0 + p) : T(0);
@@ -204,14 +218,18 @@ __global__ void __launch_bounds__(256) sweep_kernel(const T* __restrict__ a, lon
   if (tid == 0) atomicExch(flags + I, 1);
 }
 
+// grid_blocks (0: all nb): CTAs launched per chain; the self-test launches fewer, behind a preset
+// ticket counter, so that one block's predecessor never publishes.
 template <typename T, bool UP, bool BWD, int RCT, bool DSCALE>
 void launch_sweep_rc(int nb, const T* a, long long lda, long long n, T* b, long long ldb, int nrhs, const T* inv,
-                     int* flags, int* counter, int* err, cudaStream_t s) {
+                     int* flags, int* counter, int* err, cudaStream_t s, unsigned long long wait_ns = WAIT_NS,
+                     int grid_blocks = 0) {
   // set on every launch: cheap, and correct for every device and host thread
   const int smem = (int)sizeof(SweepSmem<T, RCT>);
   cudaFuncSetAttribute(sweep_kernel<T, UP, BWD, RCT, DSCALE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  dim3 grid((unsigned)nb, (unsigned)((nrhs + RCT - 1) / RCT));
-  sweep_kernel<T, UP, BWD, RCT, DSCALE><<<grid, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, flags, counter, err);
+  dim3 grid((unsigned)(grid_blocks > 0 ? grid_blocks : nb), (unsigned)((nrhs + RCT - 1) / RCT));
+  sweep_kernel<T, UP, BWD, RCT, DSCALE>
+      <<<grid, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, flags, counter, err, wait_ns);
 }
 
 // One launch per sweep: chunks of RCT right-hand sides run as parallel chains (grid.y); 4 columns
@@ -401,7 +419,8 @@ __device__ __forceinline__ void colmajor_product(const float* S, int pitch, cons
 __device__ __forceinline__ unsigned poll_sleep_ns(int dist) { return dist <= 2 ? 0u : (dist > 6 ? 2000u : 400u * (dist - 2)); }
 
 template <int CPT>
-__device__ __forceinline__ bool ll_wait_block(const unsigned* src, unsigned* w, int dist, int* err) {
+__device__ __forceinline__ bool ll_wait_block(const unsigned* src, unsigned* w, int dist, int* err,
+                                              unsigned long long wait_ns) {
   if (ll_valid<CPT>(w)) return true;
   const unsigned ns = poll_sleep_ns(dist);
   const unsigned long long t0 = gtimer();
@@ -411,11 +430,23 @@ __device__ __forceinline__ bool ll_wait_block(const unsigned* src, unsigned* w, 
     if (ll_valid<CPT>(w)) return true;
     if ((it & 63) == 0) {
       if (*(volatile int*)err) return false;
-      if (gtimer() - t0 > WAIT_NS) {
+      if (gtimer() - t0 > wait_ns) {
         atomicExch(err, 1);
         return false;
       }
     }
+  }
+}
+
+// A block whose wait ran out (or whose chain is broken) writes NaN into its rows of the solution,
+// so that a stream-ordered caller that never reads the error word still sees an invalid result.
+template <int CPT>
+__device__ __forceinline__ void ll_fill_nan(float* b, long long ldb, long long n, int nrhs, long long I0, int r,
+                                            int cq) {
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    const int c = cq * CPT + q;
+    if (I0 + r < n && c < nrhs) b[(long long)c * ldb + I0 + r] = NAN;
   }
 }
 
@@ -425,7 +456,8 @@ template <bool UP, bool BWD, int CPT, bool DSCALE, bool VEC>
 __global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__ a, long long lda, long long n,
                                                        float* __restrict__ b, long long ldb, int nrhs,
                                                        const float* __restrict__ inv, unsigned* __restrict__ ll,
-                                                       int nch, int* __restrict__ counter, int* __restrict__ err) {
+                                                       int nch, int* __restrict__ counter, int* __restrict__ err,
+                                                       unsigned long long wait_ns) {
   constexpr int RCT = 4 * CPT;
   constexpr bool RFAST = (!BWD && !UP) || (BWD && UP);
   extern __shared__ __align__(16) unsigned char ll_raw[];
@@ -514,12 +546,13 @@ __global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__
     if (k + 1 < nloop) load_tile<RFAST, VEC>(sm.Lb[k & 1], a, lda, n, I0, (long long)(J + step) * RB, tid);
     cp_commit();
     const bool ok =
-        ll_wait_block<CPT>(llc + (size_t)J * RB * RCT + tid * CPT, w, BWD ? J - I : I - J, err);
+        ll_wait_block<CPT>(llc + (size_t)J * RB * RCT + tid * CPT, w, BWD ? J - I : I - J, err, wait_ns);
 #pragma unroll
     for (int q = 0; q < CPT; ++q) sm.Ys[tid * CPT + q] = __uint_as_float(w[q]);
     cp_wait1();
     if (__syncthreads_or(!ok)) {
       asm volatile("cp.async.wait_all;" ::: "memory");
+      ll_fill_nan<CPT>(b, ldb, n, nrhs, I0, r, cq);
       return;
     }
     // request the next awaited block's words before this product
@@ -538,10 +571,13 @@ __global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__
   colmajor_product<CPT>(sm.Ds, RB + 1, sm.Ys, r, cq, x);
   if (has_prev) {
     float* yl = sm.Lb[0];  // both tile buffers are idle now
-    const bool ok = ll_wait_block<CPT>(llc + (size_t)Jlast * RB * RCT + tid * CPT, w, 1, err);
+    const bool ok = ll_wait_block<CPT>(llc + (size_t)Jlast * RB * RCT + tid * CPT, w, 1, err, wait_ns);
 #pragma unroll
     for (int q = 0; q < CPT; ++q) yl[tid * CPT + q] = __uint_as_float(w[q]);
-    if (__syncthreads_or(!ok)) return;
+    if (__syncthreads_or(!ok)) {
+      ll_fill_nan<CPT>(b, ldb, n, nrhs, I0, r, cq);
+      return;
+    }
     float mv[CPT];
 #pragma unroll
     for (int q = 0; q < CPT; ++q) mv[q] = 0.f;
@@ -557,22 +593,24 @@ __global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__
   }
 }
 
+// grid_blocks (0: all nb): row blocks launched per chain (the self-test launches fewer).
 template <bool UP, bool BWD, int CPT, bool DSCALE>
 void launch_sweep_ll_cpt(int nb, int nch, const float* a, long long lda, long long n, float* b, long long ldb,
                          int nrhs, const float* inv, unsigned* ll, int* counter, int* err,
-                         cudaStream_t s) {
+                         cudaStream_t s, unsigned long long wait_ns = WAIT_NS, int grid_blocks = 0) {
   const int smem = (int)sizeof(LLSmem);
   const bool vec = ((uintptr_t)a % 16 == 0) && (lda % 4 == 0);
+  const unsigned grid = (unsigned)((grid_blocks > 0 ? grid_blocks : nb) * nch);
   if (vec) {
     cudaFuncSetAttribute(sweep_ll_kernel<UP, BWD, CPT, DSCALE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          smem);
     sweep_ll_kernel<UP, BWD, CPT, DSCALE, true>
-        <<<nb * nch, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, ll, nch, counter, err);
+        <<<grid, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, ll, nch, counter, err, wait_ns);
   } else {
     cudaFuncSetAttribute(sweep_ll_kernel<UP, BWD, CPT, DSCALE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          smem);
     sweep_ll_kernel<UP, BWD, CPT, DSCALE, false>
-        <<<nb * nch, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, ll, nch, counter, err);
+        <<<grid, 256, smem, s>>>(a, lda, n, b, ldb, nrhs, inv, ll, nch, counter, err, wait_ns);
   }
 }
 
@@ -589,17 +627,24 @@ void launch_sweep_ll(int nb, const float* a, long long lda, long long n, float* 
     launch_sweep_ll_cpt<UP, BWD, 4, DSCALE>(nb, nch, a, lda, n, b, ldb, nrhs, inv, ll, counter, err, s);
 }
 
-// Workspace layouts.  FP64: diagonal inverses | flags, tickets, error word (chains of one launch).
-// FP32: diagonal inverses | tickets, error word | published words (LL_RC per row).
+// Workspace layouts.  Both start with the diagonal inverses, then a 256-byte block whose first word
+// is the call's error word (cleared once per call, set by any bounded wait that ran out).
+// FP64: inverses | error word | flags and tickets (chains of one launch).
+// FP32: inverses | error word, tickets | published words (LL_RC per row).
 size_t ws_flags_offset(int64_t nb, size_t elem) { return ((size_t)nb * RB * RB * elem + 255) & ~(size_t)255; }
 size_t ws_words_offset(int64_t nb) { return ws_flags_offset(nb, sizeof(float)) + 256; }
 size_t ws_bytes_f64(int64_t nb) {
   const int64_t nch = RC / 16;  // chains of one launch, at most
-  return ws_flags_offset(nb, sizeof(double)) + (size_t)(2 * nch * nb + 2 * nch + 8) * sizeof(int) + 256;
+  return ws_flags_offset(nb, sizeof(double)) + 256 + (size_t)(2 * nch * nb + 2 * nch + 8) * sizeof(int) + 256;
 }
+constexpr int kWsFlagsSkip = 64;  // ints of the error block before the FP64 flags
 size_t ws_bytes_f32(int64_t nb) { return ws_words_offset(nb) + (size_t)nb * RB * LL_RC * sizeof(unsigned) + 256; }
 
 }  // namespace
+
+int* potrs_ws_error_word(int64_t n, size_t elem, void* ws) {
+  return (int*)((char*)ws + ws_flags_offset((n + RB - 1) / RB, elem));
+}
 
 // A workspace sized for FP64 also serves the FP32 solve of the same order (the mixed-precision
 // driver runs both on one workspace).
@@ -620,7 +665,9 @@ int sweeps_ws(bool upper, bool ldl, int64_t n, int64_t nrhs, const T* a, int64_t
   static const std::string kf = std::string("sweep_") + tname<T>();
   const int nb = (int)ceil_div(n, RB);
   T* inv = (T*)ws;
-  int* base = (int*)((char*)ws + (((size_t)nb * RB * RB * sizeof(T) + 255) & ~(size_t)255));
+  int* base = (int*)((char*)ws + ws_flags_offset(nb, sizeof(T)));
+  int* err = base;  // the call's error word
+  GB_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
   {
     ProfScope ps(ki.c_str(), s, (double)nb * RB * RB * RB / 3.0, (double)n * RB * sizeof(T) * 1.5);
     if (ldl) {
@@ -633,15 +680,14 @@ int sweeps_ws(bool upper, bool ldl, int64_t n, int64_t nrhs, const T* a, int64_t
   }
   if constexpr (std::is_same<T, float>::value) {
     unsigned* words = (unsigned*)((char*)ws + ws_words_offset(nb));
-    int* fctr = base;
-    int* bctr = base + 1;
-    int* err = base + 2;
+    int* fctr = base + 1;
+    int* bctr = base + 2;
     for (int64_t c0 = 0; c0 < nrhs; c0 += LL_RC) {
       const int nc = (int)(nrhs - c0 < LL_RC ? nrhs - c0 : LL_RC);
       const int rct = ll_chain_cols(nc), nch = (nc + rct - 1) / rct;
       const size_t wbytes = (size_t)nch * nb * RB * rct * sizeof(unsigned);
       float* bc = b + c0 * ldb;
-      GB_CUDA_TRY(cudaMemsetAsync(base, 0, 3 * sizeof(int), s));
+      GB_CUDA_TRY(cudaMemsetAsync(fctr, 0, 2 * sizeof(int), s));
       GB_CUDA_TRY(cudaMemsetAsync(words, 0xFF, wbytes, s));
       const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
       {
@@ -665,13 +711,12 @@ int sweeps_ws(bool upper, bool ldl, int64_t n, int64_t nrhs, const T* a, int64_t
     for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
       const int nc = (int)(nrhs - c0 < RC ? nrhs - c0 : RC);
       const int nch = nc <= 4 ? 1 : (nc + 15) / 16;  // chains in this launch
-      int* fflags = base;                 // forward: nch x nb
-      int* bflags = base + nch * nb;      // backward: nch x nb
-      int* fctr = base + 2 * nch * nb;    // nch forward tickets, nch backward tickets, error word
+      int* fflags = base + kWsFlagsSkip;  // forward: nch x nb
+      int* bflags = fflags + nch * nb;    // backward: nch x nb
+      int* fctr = fflags + 2 * nch * nb;  // nch forward tickets, nch backward tickets
       int* bctr = fctr + nch;
-      int* err = bctr + nch;
       T* bc = b + c0 * ldb;
-      GB_CUDA_TRY(cudaMemsetAsync(base, 0, (size_t)(2 * nch * nb + 2 * nch + 1) * sizeof(int), s));
+      GB_CUDA_TRY(cudaMemsetAsync(fflags, 0, (size_t)(2 * nch * nb + 2 * nch) * sizeof(int), s));
       // algorithmic work per sweep: the lower triangle of L read once, 2 flops per entry and RHS
       const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
       {
@@ -709,7 +754,9 @@ int trsm_sweep_ws(bool upper, bool bwd, bool unit, int64_t n, int64_t nrhs, cons
   static const std::string kf = std::string("sweep_") + tname<T>();
   const int nb = (int)ceil_div(n, RB);
   T* inv = (T*)ws;
-  int* base = (int*)((char*)ws + (((size_t)nb * RB * RB * sizeof(T) + 255) & ~(size_t)255));
+  int* base = (int*)((char*)ws + ws_flags_offset(nb, sizeof(T)));
+  int* err = base;  // the call's error word
+  GB_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
   {
     ProfScope ps(ki.c_str(), s, (double)nb * RB * RB * RB / 3.0, (double)n * RB * sizeof(T) * 1.5);
     if (unit) {
@@ -722,13 +769,12 @@ int trsm_sweep_ws(bool upper, bool bwd, bool unit, int64_t n, int64_t nrhs, cons
   }
   if constexpr (std::is_same<T, float>::value) {
     unsigned* words = (unsigned*)((char*)ws + ws_words_offset(nb));
-    int* ctr = base;
-    int* err = base + 1;
+    int* ctr = base + 1;
     for (int64_t c0 = 0; c0 < nrhs; c0 += LL_RC) {
       const int nc = (int)(nrhs - c0 < LL_RC ? nrhs - c0 : LL_RC);
       const int rct = ll_chain_cols(nc), nch = (nc + rct - 1) / rct;
       float* bc = b + c0 * ldb;
-      GB_CUDA_TRY(cudaMemsetAsync(base, 0, 2 * sizeof(int), s));
+      GB_CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(int), s));
       GB_CUDA_TRY(cudaMemsetAsync(words, 0xFF, (size_t)nch * nb * RB * rct * sizeof(unsigned), s));
       const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
       ProfScope ps(kf.c_str(), s, fl, by);
@@ -744,11 +790,10 @@ int trsm_sweep_ws(bool upper, bool bwd, bool unit, int64_t n, int64_t nrhs, cons
     for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
       const int nc = (int)(nrhs - c0 < RC ? nrhs - c0 : RC);
       const int nch = nc <= 4 ? 1 : (nc + 15) / 16;
-      int* flags = base;
-      int* ctr = base + nch * nb;
-      int* err = ctr + nch;
+      int* flags = base + kWsFlagsSkip;
+      int* ctr = flags + nch * nb;
       T* bc = b + c0 * ldb;
-      GB_CUDA_TRY(cudaMemsetAsync(base, 0, (size_t)(nch * nb + nch + 1) * sizeof(int), s));
+      GB_CUDA_TRY(cudaMemsetAsync(flags, 0, (size_t)(nch * nb + nch) * sizeof(int), s));
       const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
       ProfScope ps(kf.c_str(), s, fl, by);
       if (bwd) {
@@ -768,6 +813,78 @@ template <typename T>
 int ldlt_sweeps_ws(bool upper, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b, int64_t ldb, void* ws,
                    cudaStream_t s) {
   return sweeps_ws<T>(upper, true, n, nrhs, a, lda, b, ldb, ws, s);
+}
+
+// Failure-detection self-test: one forward FP64 sweep and one forward FP32 sweep of order 256
+// whose ticket counters start at 1 and whose grids leave block 0 out, so that no CTA ever solves
+// block 0 and every other block waits for a value that is never published.  The first wait gives
+// up after wait_ns and sets the error word; the others see the word (or time out themselves) and
+// give up too, and every block that gave up writes NaN into its rows.  Checked: both error words
+// set, rows 64..255 NaN, rows 0..63 untouched.  Every access stays inside the buffers: the tickets
+// taken are 1..3 of the 4 row blocks, and no kernel goes past its first wait.
+int sweep_wait_selftest(unsigned long long wait_ns, cudaStream_t s, int* observed) {
+  constexpr int64_t n = 256;
+  const int nb = (int)(n / RB);
+  const size_t a_bytes = n * n * 8, af_bytes = n * n * 4, b_bytes = 256 * 8;
+  const size_t ws64 = (potrs_ws_bytes(n, 8) + 255) & ~(size_t)255, ws32 = (potrs_ws_bytes(n, 4) + 255) & ~(size_t)255;
+  char* buf = nullptr;
+  if (dev_malloc_async((void**)&buf, a_bytes + af_bytes + 2 * b_bytes + ws64 + ws32, s) != cudaSuccess) {
+    cudaGetLastError();
+    return GBLLT_ERR_ALLOC;
+  }
+  struct Free {
+    void* p;
+    cudaStream_t s;
+    ~Free() { cudaFreeAsync(p, s); }
+  } guard{buf, s};
+  double* a = (double*)buf;
+  float* af = (float*)(buf + a_bytes);
+  double* b = (double*)(buf + a_bytes + af_bytes);
+  float* bf = (float*)(buf + a_bytes + af_bytes + b_bytes);
+  char* w64 = buf + a_bytes + af_bytes + 2 * b_bytes;
+  char* w32 = w64 + ws64;
+  GB_CUDA_TRY(cudaMemsetAsync(buf, 0, a_bytes + af_bytes + 2 * b_bytes + ws64 + ws32, s));
+  std::vector<double> hb(n, 1.0);
+  std::vector<float> hbf(n, 1.0f);
+  GB_CUDA_TRY(cudaMemcpyAsync(b, hb.data(), n * 8, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(bf, hbf.data(), n * 4, cudaMemcpyHostToDevice, s));
+  // FP64: error word | flags (nb) | ticket counter, preset to 1
+  int* err64 = potrs_ws_error_word(n, 8, w64);
+  int* flags64 = err64 + kWsFlagsSkip;
+  int* ctr64 = flags64 + nb;
+  const int one = 1;
+  GB_CUDA_TRY(cudaMemcpyAsync(ctr64, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+  launch_sweep_rc<double, false, false, 4, false>(nb, a, n, n, b, n, 1, (const double*)w64, flags64, ctr64, err64, s,
+                                                  wait_ns, nb - 1);
+  // FP32: error word, ticket counter (preset to 1) | published words, all not ready
+  int* err32 = potrs_ws_error_word(n, 4, w32);
+  int* ctr32 = err32 + 1;
+  unsigned* words = (unsigned*)(w32 + ws_words_offset(nb));
+  GB_CUDA_TRY(cudaMemsetAsync(words, 0xFF, (size_t)nb * RB * 4 * sizeof(unsigned), s));
+  GB_CUDA_TRY(cudaMemcpyAsync(ctr32, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+  launch_sweep_ll_cpt<false, false, 1, false>(nb, 1, af, n, n, bf, n, 1, (const float*)w32, words, ctr32, err32, s,
+                                              wait_ns, nb - 1);
+  GB_CUDA_TRY(cudaGetLastError());
+  int e64 = 0, e32 = 0;
+  GB_CUDA_TRY(cudaMemcpyAsync(&e64, err64, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(&e32, err32, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(hb.data(), b, n * 8, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(hbf.data(), bf, n * 4, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  bool rows_ok = true;
+  for (int64_t i = 0; i < n; ++i) {
+    if (i < RB) rows_ok = rows_ok && hb[i] == 1.0 && hbf[i] == 1.0f;
+    else rows_ok = rows_ok && std::isnan(hb[i]) && std::isnan(hbf[i]);
+  }
+  *observed = (e64 && e32) ? GBLLT_ERR_TIMEOUT : GBLLT_SUCCESS;
+  if (!(e64 && e32 && rows_ok)) {
+    char msg[160];
+    snprintf(msg, sizeof msg, "wait self-test: error words %d/%d, rows %s", e64, e32,
+             rows_ok ? "as expected" : "not as expected");
+    set_error_message(msg);
+    return GBLLT_ERR_INTERNAL;
+  }
+  return GBLLT_SUCCESS;
 }
 
 template int potrs_ws<double>(bool, int64_t, int64_t, const double*, int64_t, double*, int64_t, void*, cudaStream_t);

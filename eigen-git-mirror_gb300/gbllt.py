@@ -96,6 +96,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_spocon": (_int, [_int, _ch, _i64, _vp, _i64, ctypes.c_float, _fp]),
     "gbllt_profile_enable": (_int, [_int]),
     "gbllt_profile_read": (_int, [_vp, _int, ctypes.POINTER(_int)]),
+    "gbllt_selftest_wait_timeout": (_int, [_i64, ctypes.POINTER(_int)]),
 }
 
 _lib = None
@@ -548,6 +549,13 @@ def lansy_l1_dev(d_a, n: int, lda: int, d_norm, uplo: str = "L", stream=None, dt
     """1-norm of the symmetric matrix stored in one triangle of d_a, written to the device scalar d_norm."""
     fn = lib().gbllt_dlansy_l1_dev if dtype == np.float64 else lib().gbllt_slansy_l1_dev
     check("gbllt_?lansy_l1_dev", fn(uplo.encode(), n, _ptr(d_a), lda, _ptr(d_norm), stream))
+
+
+def selftest_wait_timeout(wait_us: int = 20000) -> tuple[int, int]:
+    """Run the bounded-wait self-test; returns (return code, the code the waits reported)."""
+    obs = _int(0)
+    rc = lib().gbllt_selftest_wait_timeout(wait_us, ctypes.byref(obs))
+    return int(rc), int(obs.value)
 
 
 def profile_read() -> dict[str, dict]:

@@ -61,10 +61,11 @@ GBLLT_API int gbllt_version(void);
 /* Message of the last GBLLT_ERR_CUDA seen by the calling thread ("" if none). */
 GBLLT_API const char* gbllt_last_error(void);
 
-/* Workspaces come from the current device's default stream-ordered memory pool (cudaMallocAsync),
- * which the library sets, on first use of a device, to keep freed memory cached in the process
- * instead of returning it at every synchronisation (a large solve would otherwise map gigabytes
- * again on each call).  This returns the cached memory of the current device to the system. */
+/* Workspaces come from a stream-ordered memory pool that the library creates for itself on first
+ * use of a device (cudaMemPoolCreate; the device's default pool and its settings are left alone).
+ * That pool keeps freed memory cached in the process instead of returning it at every
+ * synchronisation (a large solve would otherwise map gigabytes again on each call).  This returns
+ * the library's cached memory of the current device to the system. */
 GBLLT_API int gbllt_release_cached_memory(void);
 
 /* Factor A = L L^T ('L') or A = U^T U ('U') in place.
@@ -172,16 +173,18 @@ GBLLT_API int gbllt_dposv_mixed(int layout, char uplo, int64_t n, int64_t nrhs, 
                                 gbllt_mixed_report* report);
 
 /* Same solve as gbllt_dposv_mixed_dev, for callers that cannot let the library allocate device
- * memory (their memory is owned by their own allocator or budget, or they must not allocate while
- * a stream is being captured).  No counterpart in the reference: Eigen's LLT allocates on the host
- * as it pleases.  This entry point calls no cudaMalloc / cudaMallocAsync / cudaFree: its scratch is a
- * fixed 64 MiB area inside the library image, held by every GPU that loads the library until the
- * process exits.  That is enough for n <= 2048 with up to 64 right-hand sides including the FP64
- * fallback; larger problems are rejected with GBLLT_ERR_SCRATCH_LIMIT (gbllt_last_error() says how
- * much scratch they need).  The first call on a device looks up the area's device address; make
- * that first call before any stream capture.  All calls share the area: calls whose GPU work
- * overlaps race and must be serialised by the caller.  No device times are reported
- * (factor_ms = refine_ms = 0). */
+ * memory: their device memory is owned by their own caching allocator or a fixed budget, or they are
+ * plug-ins handed only the buffers they work on.  No counterpart in the reference: Eigen's LLT
+ * allocates on the host as it pleases.  This entry point calls no cudaMalloc / cudaMallocAsync /
+ * cudaFree: its scratch is a fixed 64 MiB area inside the library image, held by every GPU that
+ * loads the library until the process exits.  That is enough for n <= 2048 with up to 64
+ * right-hand sides including the FP64 fallback, at the default panel width (opts->panel = 256; a
+ * wider panel needs more); larger problems are rejected with GBLLT_ERR_SCRATCH_LIMIT
+ * (gbllt_last_error() says how much scratch they need).  The first call on a device looks up the
+ * area's device address; make that first call before any stream capture.  Like
+ * gbllt_dposv_mixed_dev it synchronises `stream` once per refinement step.  All calls share the
+ * area: calls whose GPU work overlaps race and must be serialised by the caller.  No device times
+ * are reported (factor_ms = refine_ms = 0). */
 #define GBLLT_ERR_SCRATCH_LIMIT (-1007)
 GBLLT_API int gbllt_dposv_mixed_dev_noalloc(char uplo, int64_t n, int64_t nrhs, const double* d_a, int64_t lda,
                                             const double* d_b, int64_t ldb, double* d_x, int64_t ldx,
@@ -362,6 +365,19 @@ GBLLT_API int gbllt_strsm_dev(char side, char uplo, char transa, char diag, int6
 GBLLT_API int gbllt_profile_enable(int on);
 /* Wait for the recorded launches and return up to max_entries classes; *n_entries = classes seen. */
 GBLLT_API int gbllt_profile_read(gbllt_kernel_stat* out, int max_entries, int* n_entries);
+
+/* Failure-detection self-test of the device-side bounded waits.  No counterpart in the reference
+ * (Eigen's LLT runs on one CPU thread and never waits on another).  Every wait of the library's
+ * kernels (the solve's look-back flags, the tensor-core pipelines' mbarriers, the rank update's
+ * block flags) gives up after a time limit, sets an error word and returns, so that a lost signal
+ * ends in GBLLT_ERR_TIMEOUT instead of a hung GPU; host-pointer entries then return that code, and
+ * a triangular sweep that gave up writes NaN into the rows it could not solve.  This runs one
+ * FP64 and one FP32 sweep of order 256 in which block 0 is never solved, with the wait limited to
+ * wait_us microseconds (1000 .. 2000000), on the calling thread's library stream.  *observed
+ * receives the code the waits reported (GBLLT_ERR_TIMEOUT); the return value is GBLLT_SUCCESS when
+ * every wait gave up as designed, both error words were set, the unsolved rows are NaN and the
+ * solved ones untouched, and GBLLT_ERR_INTERNAL otherwise.  The device stays usable. */
+GBLLT_API int gbllt_selftest_wait_timeout(int64_t wait_us, int* observed);
 
 #ifdef __cplusplus
 }

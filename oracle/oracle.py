@@ -72,19 +72,34 @@ _lib = None
 _ref = None
 
 
-def build(ref: bool = True) -> None:
-    """Compile liboracle.so; also Eigen's own LLT when the reference headers are present.
-    Same commands as oracle/Makefile, issued directly so that `make` is not required.  No FMA
-    contraction: every product and sum is rounded, as in Eigen's SSE2 build, on x86-64 and aarch64
-    alike."""
+SRC_RECORD = ORACLE_DIR / "_ref" / "eigen_src.txt"  # where the last `ref` build found the Eigen sources
+
+
+def eigen_src() -> Path | None:
+    """The Eigen source tree: $EIGEN_REF, else the one the last `ref` build used; None if neither."""
+    env = os.environ.get("EIGEN_REF")
+    if env:
+        return Path(env)
+    if SRC_RECORD.exists():
+        return Path(SRC_RECORD.read_text().strip())
+    return None
+
+
+def build(ref: bool = True, eigen: str | None = None) -> None:
+    """Compile liboracle.so; with ref, also Eigen's own LLT and BLAS from the Eigen source tree
+    given by `eigen` or $EIGEN_REF, when one is given and holds the sources (nothing else is
+    assumed about where they lie).  Same commands as oracle/Makefile, issued directly so that
+    `make` is not required.  No FMA contraction: every product and sum is rounded, as in Eigen's
+    SSE2 build, on x86-64 and aarch64 alike."""
     src = ORACLE_DIR / "llt_oracle.c"
     deps = [src, ORACLE_DIR / "llt_oracle_body.h"]
     if not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < max(d.stat().st_mtime for d in deps):
         subprocess.run(["gcc", "-O3", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-Wall", "-o",
                         str(LIB_PATH), str(src), "-lm"], check=True)
-    eigen = os.environ.get("EIGEN_REF", "/root/reference")
-    if ref and Path(eigen, "Eigen").is_dir():
+    eigen = eigen or os.environ.get("EIGEN_REF")
+    if ref and eigen and Path(eigen, "Eigen").is_dir():
         REF_PATH.parent.mkdir(exist_ok=True)
+        SRC_RECORD.write_text(str(Path(eigen).resolve()) + "\n")
         cpp = ORACLE_DIR / "eigen_ref.cpp"
         if not REF_PATH.exists() or REF_PATH.stat().st_mtime < cpp.stat().st_mtime:
             subprocess.run(["g++", "-O3", "-DNDEBUG", "-fopenmp", "-fPIC", "-shared", f"-I{eigen}", "-o",

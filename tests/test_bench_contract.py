@@ -38,20 +38,38 @@ def test_ncu_traffic_scaling_laws(bench):
     assert bench.ncu_traffic("sweep_f32", n0, 8) is None  # below one 16-column chunk: not captured
 
 
-@pytest.mark.parametrize("name,bound,peak,scale", [
-    ("tc_update_bf16", "tensor", 2000.0, 1.0),
-    ("tc_update_tf32", "tensor", 1000.0, 1.0),
-    ("syrk_tc_f64", "tensor", 2000.0, 36.0),
-    ("residual_tc", "tensor", 2000.0, 36.0),
-    ("syrk_lower_f64", "tensor", 1.0, 1.0),
+# profiled flops: tc_update_* counts every split product (nseg per algorithmic product); the ozaki
+# kernels count the FP64 product once.  `achieved` is always the algorithmic rate; the executed
+# split-product rate is reported beside it.
+@pytest.mark.parametrize("name,nseg,bound,peak,algo_scale,products", [
+    ("tc_update_bf16", 6, "tensor", 2000.0, 1 / 6, 6),
+    ("tc_update_bf16", 1, "tensor", 2000.0, 1.0, 1),
+    ("tc_update_tf32", 3, "tensor", 1000.0, 1 / 3, 3),
+    ("syrk_tc_f64", 1, "tensor", 2000.0, 1.0, 36),
+    ("residual_tc", 1, "tensor", 2000.0, 1.0, 36),
+    ("syrk_lower_f64", 1, "tensor", 1.0, 1.0, 1),
 ])
-def test_roofline_flop_bound_kernels(bench, name, bound, peak, scale):
+def test_roofline_flop_bound_kernels(bench, name, nseg, bound, peak, algo_scale, products):
     st = {"ms": 2.0, "flops": 4e12, "bytes": 1e9, "launches": 4}
-    r = bench.roofline_for(name, st, PEAKS, 16384, 64)
+    r = bench.roofline_for(name, st, PEAKS, 16384, 64, nseg)
     assert r["bound"] == bound and r["unit"] == "TFLOP/s" and r["peak"] == peak
-    assert r["achieved"] == pytest.approx(scale * 4e12 / 2e-3 / 1e12)
+    assert r["achieved"] == pytest.approx(algo_scale * 4e12 / 2e-3 / 1e12)
     assert r["frac"] == pytest.approx(r["achieved"] / peak)
-    assert r["per_launch_flops"] == pytest.approx(1e12)
+    assert r["per_launch_flops"] == pytest.approx(algo_scale * 1e12)
+    if products > 1:
+        sp = r["split_products"]
+        assert sp["products_per_algorithmic_product"] == products
+        assert sp["tensor_achieved"] == pytest.approx(r["achieved"] * products)
+        assert sp["tensor_frac"] == pytest.approx(sp["tensor_achieved"] / peak)
+    else:
+        assert "split_products" not in r
+
+
+def test_default_config_is_the_metric_config(bench):
+    # the metric (FP64 vs mixed + refinement at backward error <= 1e-14) is quoted on n = 32768
+    c = bench.CONFIGS[bench.DEFAULT_CONFIG]
+    assert (c["n"], c["nrhs"], c["kappa"]) == (32768, 64, 1e6)
+    assert bench.SPLIT_PRODUCTS["bf16x6"] == 6 and bench.SPLIT_PRODUCTS["tf32x3"] == 3
 
 
 def test_roofline_bandwidth_bound_kernel(bench):

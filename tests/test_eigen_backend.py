@@ -7,19 +7,25 @@ and counts it.  The tests' own assertions (VERIFY_IS_APPROX at 1e-6 / 1e-3, the 
 checks, the in-place semantics of LLT<Ref<MatrixXd>>) must all hold, and the call counts prove
 the specialisations were selected.  This checks the header's plumbing (layout, uplo, info mapping,
 leading dimensions, the solve hooks) on the CPU; the GPU kernels behind the C ABI are checked by
-the gpu-marked tests.  Needs the Eigen sources (EIGEN_REF, default /root/reference) and g++.
+the gpu-marked tests.  Needs the Eigen sources ($EIGEN_REF, or the tree the oracle's `ref` build
+used) and g++.
 """
 import os
 import re
 import shutil
 import subprocess
+import sys
 from pathlib import Path
 
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
-EIGEN = Path(os.environ.get("EIGEN_REF", "/root/reference"))
-pytestmark = pytest.mark.skipif(not (EIGEN / "Eigen" / "Cholesky").exists() or shutil.which("g++") is None,
+sys.path.insert(0, str(ROOT / "oracle"))
+import oracle as _oracle  # noqa: E402
+
+EIGEN = _oracle.eigen_src()
+pytestmark = pytest.mark.skipif(EIGEN is None or not (EIGEN / "Eigen" / "Cholesky").exists() or
+                                shutil.which("g++") is None,
                                 reason="Eigen sources or g++ not available")
 
 
