@@ -80,6 +80,17 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
+// The same for 64-byte rows: K-major, 64-byte swizzle, 8-row groups 512 B apart.
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                   // leading-dimension byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;          // stride-dimension byte offset
+  d |= (uint64_t)1 << 46;                   // descriptor version (sm_100 family)
+  d |= (uint64_t)4 << 61;                   // 64-byte swizzle
+  return d;
+}
+
 // Instruction descriptor: fp32 accumulate, A/B K-major, M x N tile.
 // fmt: 1 = BF16 (kind::f16), 2 = TF32 (kind::tf32).
 __host__ __device__ constexpr uint32_t instr_desc_mn(uint32_t fmt, int m, int n) {
@@ -151,18 +162,19 @@ inline PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 2-D K-major map: `rows` rows of `k` elements, `ld` elements apart; box = box_k x box_rows, 128-byte
-// swizzle (box_k * element size must be 128 bytes).  Returns false if the encoder is unavailable or
-// rejects the map.
+// swizzle (box_k * element size must be 128 bytes) or 64-byte swizzle (64 bytes).  Returns false if
+// the encoder is unavailable or rejects the map.
 inline bool make_map_2d(CUtensorMap* m, const void* base, CUtensorMapDataType dt, int es, int64_t rows, int64_t k,
-                        int64_t ld, int box_k, int box_rows) {
+                        int64_t ld, int box_k, int box_rows,
+                        CUtensorMapSwizzle swz = CU_TENSOR_MAP_SWIZZLE_128B) {
   auto fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)(ld * es)};
   cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(m, dt, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult r = fn(m, dt, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
 
