@@ -375,7 +375,7 @@ def measure_config(args, cfg, ws, rank, local, peaks, steps, warmup, profile_ste
     info = torch.zeros(1, dtype=torch.int64, device="cuda")
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
-    opts = G.mixed_opts(args.mixed_precision, 10, 1e-14, fallback=False)
+    opts = G.mixed_opts(args.mixed_precision, 10, 1e-14, fallback=False, reserve_sms=args.reserve_sms)
     nseg = SPLIT_PRODUCTS[args.mixed_precision]
     reports = []
 
@@ -810,6 +810,8 @@ def main():
                     "kappa sweep and the C1 / C4 / C5 keys")
     ap.add_argument("--mixed-precision", default="bf16x6", choices=sorted(SPLIT_PRODUCTS))
     ap.add_argument("--n", type=int, default=0, help="override the order n (profiling a smaller case)")
+    ap.add_argument("--reserve-sms", type=int, default=0, help="SMs left to the panel factorisation while the "
+                    "look-ahead update runs (0: the library's default)")
     args = ap.parse_args()
     if args.impl == "reference":
         # CPU only: under torchrun rank 0 alone runs it, the other ranks exit without work

@@ -263,14 +263,17 @@ void launch_sweep(int nb, const T* a, long long lda, long long n, T* b, long lon
 // of every chain.
 // ---------------------------------------------------------------------------------------------
 
-constexpr int LL_RC = 64;     // right-hand sides per launch: up to 4 chains of 16
+constexpr int LL_RC = 64;     // right-hand sides per launch: one chain of 64, or chains of 16 or 4
 constexpr int PF_PITCH = 68;  // row pitch (floats) of a tile stored with p contiguous
 
+constexpr int LL_NT = 4;      // tile slots: the last-delivered tile, then a ring of look-back tiles
+
+template <int RCT>
 struct LLSmem {
-  float Lb[2][RB * PF_PITCH];  // off-diagonal tiles (double-buffered)
+  float Lb[LL_NT][RB * PF_PITCH];  // off-diagonal tiles: three loads in flight behind the one in use
   float Ds[RB * (RB + 1)];     // Ds[i * 65 + r] = D(r, i)
   float Ms[RB * RB];           // Ms[p * 64 + r] = M(r, p)
-  float Ys[RB * 16];           // staged 64 x RCT block; flat index = word index
+  float Ys[RB * RCT];          // staged 64 x RCT block; flat index = word index
 };
 
 __device__ __forceinline__ uint32_t sptr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -282,7 +285,10 @@ __device__ __forceinline__ void cp_async4(void* dst, const void* src, int bytes)
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(sptr(dst)), "l"(src), "r"(bytes) : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 // Tile G(rr, p) of the sweep for row block I0 and column block J0.  RFAST: element (rr, p) at
 // a[(J0 + p) lda + I0 + rr], kept as lb[p * 64 + rr]; otherwise at a[(I0 + rr) lda + J0 + p], kept as
@@ -319,11 +325,13 @@ constexpr unsigned CANON_NAN = 0x7FC00000u;
 
 template <int CPT>
 __device__ __forceinline__ void ll_load(const unsigned* src, unsigned* w) {
-  if (CPT == 4) {
-    asm volatile("ld.volatile.global.v4.u32 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3])
-                 : "l"(src)
-                 : "memory");
+  if (CPT % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < CPT; k += 4)
+      asm volatile("ld.volatile.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                   : "=r"(w[k]), "=r"(w[k + 1]), "=r"(w[k + 2]), "=r"(w[k + 3])
+                   : "l"(src + k)
+                   : "memory");
   } else {
     asm volatile("ld.volatile.global.u32 %0, [%1];" : "=r"(w[0]) : "l"(src) : "memory");
   }
@@ -345,10 +353,12 @@ __device__ __forceinline__ void ll_store(unsigned* dst, const float* x) {
     const unsigned u = __float_as_uint(x[k]);
     w[k] = u == NOT_READY ? CANON_NAN : u;
   }
-  if (CPT == 4) {
-    asm volatile("st.volatile.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "r"(w[0]), "r"(w[1]), "r"(w[2]),
-                 "r"(w[3])
-                 : "memory");
+  if (CPT % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < CPT; k += 4)
+      asm volatile("st.volatile.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(dst + k), "r"(w[k]), "r"(w[k + 1]),
+                   "r"(w[k + 2]), "r"(w[k + 3])
+                   : "memory");
   } else {
     asm volatile("st.volatile.global.u32 [%0], %1;" ::"l"(dst), "r"(w[0]) : "memory");
   }
@@ -361,12 +371,15 @@ __device__ __forceinline__ void tile_product(const float* lb, const float* ys, i
 #pragma unroll 8
     for (int p = 0; p < RB; ++p) {
       const float l = lb[p * 64 + r];
-      if (CPT == 4) {
-        const float4 y = *reinterpret_cast<const float4*>(ys + p * RCT + cq * 4);
-        acc[0] = fmaf(l, y.x, acc[0]);
-        acc[1] = fmaf(l, y.y, acc[1]);
-        acc[2] = fmaf(l, y.z, acc[2]);
-        acc[3] = fmaf(l, y.w, acc[3]);
+      if (CPT % 4 == 0) {
+#pragma unroll
+        for (int k = 0; k < CPT; k += 4) {
+          const float4 y = *reinterpret_cast<const float4*>(ys + p * RCT + cq * CPT + k);
+          acc[k] = fmaf(l, y.x, acc[k]);
+          acc[k + 1] = fmaf(l, y.y, acc[k + 1]);
+          acc[k + 2] = fmaf(l, y.z, acc[k + 2]);
+          acc[k + 3] = fmaf(l, y.w, acc[k + 3]);
+        }
       } else {
         acc[0] = fmaf(l, ys[p * RCT + cq], acc[0]);
       }
@@ -378,12 +391,15 @@ __device__ __forceinline__ void tile_product(const float* lb, const float* ys, i
       const float lv[4] = {l4.x, l4.y, l4.z, l4.w};
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        if (CPT == 4) {
-          const float4 y = *reinterpret_cast<const float4*>(ys + (p + u) * RCT + cq * 4);
-          acc[0] = fmaf(lv[u], y.x, acc[0]);
-          acc[1] = fmaf(lv[u], y.y, acc[1]);
-          acc[2] = fmaf(lv[u], y.z, acc[2]);
-          acc[3] = fmaf(lv[u], y.w, acc[3]);
+        if (CPT % 4 == 0) {
+#pragma unroll
+          for (int k = 0; k < CPT; k += 4) {
+            const float4 y = *reinterpret_cast<const float4*>(ys + (p + u) * RCT + cq * CPT + k);
+            acc[k] = fmaf(lv[u], y.x, acc[k]);
+            acc[k + 1] = fmaf(lv[u], y.y, acc[k + 1]);
+            acc[k + 2] = fmaf(lv[u], y.z, acc[k + 2]);
+            acc[k + 3] = fmaf(lv[u], y.w, acc[k + 3]);
+          }
         } else {
           acc[0] = fmaf(lv[u], ys[(p + u) * RCT + cq], acc[0]);
         }
@@ -401,12 +417,15 @@ __device__ __forceinline__ void colmajor_product(const float* S, int pitch, cons
 #pragma unroll 8
   for (int p = 0; p < RB; ++p) {
     const float s = S[p * pitch + r];
-    if (CPT == 4) {
-      const float4 y = *reinterpret_cast<const float4*>(ys + p * RCT + cq * 4);
-      out[0] = fmaf(s, y.x, out[0]);
-      out[1] = fmaf(s, y.y, out[1]);
-      out[2] = fmaf(s, y.z, out[2]);
-      out[3] = fmaf(s, y.w, out[3]);
+    if (CPT % 4 == 0) {
+#pragma unroll
+      for (int k = 0; k < CPT; k += 4) {
+        const float4 y = *reinterpret_cast<const float4*>(ys + p * RCT + cq * CPT + k);
+        out[k] = fmaf(s, y.x, out[k]);
+        out[k + 1] = fmaf(s, y.y, out[k + 1]);
+        out[k + 2] = fmaf(s, y.z, out[k + 2]);
+        out[k + 3] = fmaf(s, y.w, out[k + 3]);
+      }
     } else {
       out[0] = fmaf(s, ys[p * RCT + cq], out[0]);
     }
@@ -453,7 +472,7 @@ __device__ __forceinline__ void ll_fill_nan(float* b, long long ldb, long long n
 // One CTA per (row block, right-hand-side chain); 256 threads, thread (r, cq) owns row r and
 // right-hand sides cq * CPT .. cq * CPT + CPT - 1 of its chain (RCT = 4 CPT columns per chain).
 template <bool UP, bool BWD, int CPT, bool DSCALE, bool VEC>
-__global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__ a, long long lda, long long n,
+__global__ void __launch_bounds__(256, 2) sweep_ll_kernel(const float* __restrict__ a, long long lda, long long n,
                                                        float* __restrict__ b, long long ldb, int nrhs,
                                                        const float* __restrict__ inv, unsigned* __restrict__ ll,
                                                        int nch, int* __restrict__ counter, int* __restrict__ err,
@@ -461,7 +480,7 @@ __global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__
   constexpr int RCT = 4 * CPT;
   constexpr bool RFAST = (!BWD && !UP) || (BWD && UP);
   extern __shared__ __align__(16) unsigned char ll_raw[];
-  LLSmem& sm = *reinterpret_cast<LLSmem*>(ll_raw);
+  LLSmem<RCT>& sm = *reinterpret_cast<LLSmem<RCT>*>(ll_raw);
   __shared__ int s_ticket;
   const int tid = threadIdx.x, r = tid & 63, cq = tid >> 6;
   const int nb = (int)((n + RB - 1) / RB);
@@ -479,12 +498,16 @@ __global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__
   const int Jfirst = BWD ? nb - 1 : 0;
   const int nloop = has_prev ? (BWD ? nb - 2 - I : I - 1) : 0;  // blocks before Jlast
 
-  // 1. inputs that depend on no other block: the last-delivered tile (group 0), the first loop
-  //    tile (group 1), the diagonal inverse and this block's right-hand sides
+  // 1. inputs that depend on no other block: the last-delivered tile (group 0, slot 0), the first
+  //    LL_NT - 1 loop tiles (groups 1 .. LL_NT - 1, slots 1 .. LL_NT - 1), the diagonal inverse and
+  //    this block's right-hand sides.  Loop tile k lives in slot (k + 1) % LL_NT and group k + 1.
   if (has_prev) load_tile<RFAST, VEC>(sm.Lb[0], a, lda, n, I0, (long long)Jlast * RB, tid);
   cp_commit();
-  if (nloop > 0) load_tile<RFAST, VEC>(sm.Lb[1], a, lda, n, I0, (long long)Jfirst * RB, tid);
-  cp_commit();
+#pragma unroll
+  for (int k = 0; k < LL_NT - 1; ++k) {
+    if (k < nloop) load_tile<RFAST, VEC>(sm.Lb[1 + k], a, lda, n, I0, (long long)(Jfirst + k * step) * RB, tid);
+    cp_commit();
+  }
   const float* Dinv = inv + (long long)I * RB * RB;  // column-major Linv of block I
   for (int idx = tid; idx < RB * RB; idx += 256) {
     const int lo = idx & 63, hi = idx >> 6;
@@ -509,7 +532,7 @@ __global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__
 
   // 2. M = D G_last, kept column by column (Ms[p * 64 + r] = M(r, p)); thread (r, cq) forms
   //    columns cq * 16 .. cq * 16 + 15
-  cp_wait1();
+  cp_wait<LL_NT - 1>();  // group 0 has landed
   __syncthreads();
   if (has_prev) {
     float m[16];
@@ -535,21 +558,24 @@ __global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__
 #pragma unroll
     for (int j = 0; j < 16; ++j) sm.Ms[(cq * 16 + j) * 64 + r] = m[j];
   }
-  __syncthreads();  // Lb[0] is free for the first prefetch
+  __syncthreads();  // slot 0 is free for the first prefetch
 
-  // 3. the blocks before Jlast, in the order the chain delivers them; tile k sits in Lb[(k+1) & 1]
+  // 3. the blocks before Jlast, in the order the chain delivers them.  Iteration k loads tile
+  //    k + LL_NT - 1 into slot k % LL_NT (freed by tile k - 1, or by G_last for k = 0) and uses tile
+  //    k from slot (k + 1) % LL_NT; its group is complete once at most LL_NT - 1 newer ones are pending.
   float acc[CPT];
 #pragma unroll
   for (int q = 0; q < CPT; ++q) acc[q] = 0.f;
   for (int k = 0; k < nloop; ++k) {
     const int J = Jfirst + k * step;
-    if (k + 1 < nloop) load_tile<RFAST, VEC>(sm.Lb[k & 1], a, lda, n, I0, (long long)(J + step) * RB, tid);
+    if (k + LL_NT - 1 < nloop)
+      load_tile<RFAST, VEC>(sm.Lb[k % LL_NT], a, lda, n, I0, (long long)(J + (LL_NT - 1) * step) * RB, tid);
     cp_commit();
     const bool ok =
         ll_wait_block<CPT>(llc + (size_t)J * RB * RCT + tid * CPT, w, BWD ? J - I : I - J, err, wait_ns);
 #pragma unroll
     for (int q = 0; q < CPT; ++q) sm.Ys[tid * CPT + q] = __uint_as_float(w[q]);
-    cp_wait1();
+    cp_wait<LL_NT - 1>();
     if (__syncthreads_or(!ok)) {
       asm volatile("cp.async.wait_all;" ::: "memory");
       ll_fill_nan<CPT>(b, ldb, n, nrhs, I0, r, cq);
@@ -557,7 +583,7 @@ __global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__
     }
     // request the next awaited block's words before this product
     ll_load<CPT>(llc + (size_t)(k + 1 < nloop ? J + step : Jlast) * RB * RCT + tid * CPT, w);
-    tile_product<RFAST, CPT>(sm.Lb[(k + 1) & 1], sm.Ys, r, cq, acc);
+    tile_product<RFAST, CPT>(sm.Lb[(k + 1) % LL_NT], sm.Ys, r, cq, acc);
     __syncthreads();
   }
 
@@ -570,7 +596,7 @@ __global__ void __launch_bounds__(256) sweep_ll_kernel(const float* __restrict__
   for (int q = 0; q < CPT; ++q) x[q] = 0.f;
   colmajor_product<CPT>(sm.Ds, RB + 1, sm.Ys, r, cq, x);
   if (has_prev) {
-    float* yl = sm.Lb[0];  // both tile buffers are idle now
+    float* yl = sm.Lb[0];  // every tile slot is idle now
     const bool ok = ll_wait_block<CPT>(llc + (size_t)Jlast * RB * RCT + tid * CPT, w, 1, err, wait_ns);
 #pragma unroll
     for (int q = 0; q < CPT; ++q) yl[tid * CPT + q] = __uint_as_float(w[q]);
@@ -598,7 +624,7 @@ template <bool UP, bool BWD, int CPT, bool DSCALE>
 void launch_sweep_ll_cpt(int nb, int nch, const float* a, long long lda, long long n, float* b, long long ldb,
                          int nrhs, const float* inv, unsigned* ll, int* counter, int* err,
                          cudaStream_t s, unsigned long long wait_ns = WAIT_NS, int grid_blocks = 0) {
-  const int smem = (int)sizeof(LLSmem);
+  const int smem = (int)sizeof(LLSmem<4 * CPT>);
   const bool vec = ((uintptr_t)a % 16 == 0) && (lda % 4 == 0);
   const unsigned grid = (unsigned)((grid_blocks > 0 ? grid_blocks : nb) * nch);
   if (vec) {
@@ -615,7 +641,12 @@ void launch_sweep_ll_cpt(int nb, int nch, const float* a, long long lda, long lo
 }
 
 // Chains of 4 right-hand sides for nrhs <= 4, else of 16 (nrhs <= LL_RC per launch).
-inline int ll_chain_cols(int nrhs) { return nrhs <= 4 ? 4 : 16; }
+// Chains of 4 right-hand sides for nrhs <= 4, of 16 up to 16, else of 32.  Every CTA of a chain
+// streams all the tiles left of its block, and a CTA that starts once earlier ones have finished
+// must catch up with the chain at the rate of its tile products: wider chains mean fewer CTAs and
+// fewer re-reads of L, but a longer product on the chain's critical path.  32 columns measured best
+// for 64 right-hand sides (64 was slower: its link carries a 64 x 64 x 64 product).
+inline int ll_chain_cols(int nrhs) { return nrhs <= 4 ? 4 : (nrhs <= 16 ? 16 : 32); }
 
 template <bool UP, bool BWD, bool DSCALE = false>
 void launch_sweep_ll(int nb, const float* a, long long lda, long long n, float* b, long long ldb, int nrhs,
@@ -623,8 +654,10 @@ void launch_sweep_ll(int nb, const float* a, long long lda, long long n, float* 
   const int rct = ll_chain_cols(nrhs), nch = (nrhs + rct - 1) / rct;
   if (rct == 4)
     launch_sweep_ll_cpt<UP, BWD, 1, DSCALE>(nb, nch, a, lda, n, b, ldb, nrhs, inv, ll, counter, err, s);
-  else
+  else if (rct == 16)
     launch_sweep_ll_cpt<UP, BWD, 4, DSCALE>(nb, nch, a, lda, n, b, ldb, nrhs, inv, ll, counter, err, s);
+  else
+    launch_sweep_ll_cpt<UP, BWD, 8, DSCALE>(nb, nch, a, lda, n, b, ldb, nrhs, inv, ll, counter, err, s);
 }
 
 // Workspace layouts.  Both start with the diagonal inverses, then a 256-byte block whose first word
