@@ -22,11 +22,18 @@
 //   - LDLT<MatrixXd|MatrixXf> (and LDLT<Ref<...>>): the pivoted factorisation, through explicit
 //     specialisations of internal::ldlt_inplace<Lower>::unblocked (LDLT.h:297-403) that call
 //     gbllt_?ldlt; ldlt.solve(b) through Solve<LDLT<...>> specialisations calling gbllt_?ldlt_solve.
-// What stays on Eigen's CPU code: LLT::solveInPlace (LLT.h:514-522) calls the triangular views
-// directly and bypasses Solve<>; the L1 norm that LLT::compute keeps for rcond
+//   - triangular solves with a dynamic number of right-hand sides, triangularView<Mode>()
+//     .solveInPlace(B) and .solve(B) (SolveTriangular.h:49-104): partial specialisations of
+//     internal::triangular_solve_matrix for double and float, the hook that
+//     TriangularSolverMatrix_BLAS.h:41-161 uses for ?trsm_, call gbllt_?trsm; and
+//     internal::triangular_solve_vector for a single right-hand-side vector.  LLT::solveInPlace
+//     (LLT.h:514-522), which calls the two triangular views directly, therefore runs on the GPU too.
+// What stays on Eigen's CPU code: the L1 norm that LLT::compute keeps for rcond
 // (LLT.h:443-453; gbllt_?lansy_l1_dev is its device form for callers outside Eigen); fixed-size
 // LDLTs; LDLT::rankUpdate (ldlt_inplace::update, LDLT.h:405-456); LDLT::rcond, whose estimator
-// (ConditionEstimator.h) runs its solves through the GPU solve above.
+// (ConditionEstimator.h) runs its solves through the GPU solve above; triangular solves of complex
+// scalars, of right-hand sides with an inner stride, and of fixed-size vectors of at most 8
+// entries (SolveTriangular.h's compile-time unrolled path).
 //
 // Errors: a failing library call (no usable GPU, CUDA error) trips eigen_assert; with assertions
 // disabled the factorisation reports NumericalIssue and a solve leaves NaN in its result.
@@ -342,6 +349,23 @@ EIGEN_GB300_LDLT_SOLVE(double)
 EIGEN_GB300_LDLT_SOLVE(float)
 
 #undef EIGEN_GB300_LDLT_SOLVE
+
+// ---- triangular solves --------------------------------------------------------------------------
+// SolveTriangular.h:85-104 hands a matrix right-hand side to triangular_solve_matrix<Scalar, Index,
+// Side, Mode, Conjugate, TriStorageOrder, OtherStorageOrder, OtherInnerStride>; a row-major right-hand
+// side is first turned into the transposed problem on the other side
+// (TriangularSolverMatrix.h:17-34), so the column-major cases below see every layout.  As in
+// TriangularSolverMatrix_BLAS.h, a row-major triangle is the transpose of a column-major one with
+// the other uplo, and Conjugate is immaterial for real scalars.
+template <typename Scalar>
+struct gb300_trsm;
+
+#define EIGEN_GB300_TRSM(EIGTYPE, TRSM)                                                                    template <>                                                                                            struct gb300_trsm<EIGTYPE> {                                                                             /* B (m x n, column-major, leading dimension ldb) <- op(T)^-1 B (side 'L') or B op(T)^-1 ('R') */      static void run(char side, int mode, bool tri_rowmajor, int64_t m, int64_t n, const EIGTYPE* tri,                       int64_t ldt, EIGTYPE* b, int64_t ldb) {                                                  if (m == 0 || n == 0) return;                                                                          const bool lower = (mode & Lower) == Lower;                                                            const char uplo = (lower != tri_rowmajor) ? 'L' : 'U';                                                 const char trans = tri_rowmajor ? 'T' : 'N';                                                           const char diag = (mode & UnitDiag) ? 'U' : 'N';                                                       const int rc = TRSM(GBLLT_COL_MAJOR, side, uplo, trans, diag, m, n, EIGTYPE(1), tri, ldt, b, ldb);       if (!gb300_check(#TRSM, rc))                                                                             for (int64_t j = 0; j < n; ++j)                                                                          for (int64_t i = 0; i < m; ++i) b[i + j * ldb] = std::numeric_limits<EIGTYPE>::quiet_NaN();      }                                                                                                    };                                                                                                     /* op(T)^-1 B, B column-major with unit inner stride */                                               template <typename Index, int Mode, bool Conjugate, int TriStorageOrder>                               struct triangular_solve_matrix<EIGTYPE, Index, OnTheLeft, Mode, Conjugate, TriStorageOrder, ColMajor, 1> {     static void run(Index size, Index otherSize, const EIGTYPE* tri, Index triStride, EIGTYPE* other,                      Index otherIncr, Index otherStride, level3_blocking<EIGTYPE, EIGTYPE>&) {                EIGEN_ONLY_USED_FOR_DEBUG(otherIncr);                                                                  eigen_assert(otherIncr == 1);                                                                          gb300_trsm<EIGTYPE>::run('L', Mode, TriStorageOrder == RowMajor, (int64_t)size, (int64_t)otherSize,                                tri, (int64_t)triStride, other, (int64_t)otherStride);                      }                                                                                                    };                                                                                                     /* B op(T)^-1 */                                                                                       template <typename Index, int Mode, bool Conjugate, int TriStorageOrder>                               struct triangular_solve_matrix<EIGTYPE, Index, OnTheRight, Mode, Conjugate, TriStorageOrder, ColMajor, 1> {     static void run(Index size, Index otherSize, const EIGTYPE* tri, Index triStride, EIGTYPE* other,                      Index otherIncr, Index otherStride, level3_blocking<EIGTYPE, EIGTYPE>&) {                EIGEN_ONLY_USED_FOR_DEBUG(otherIncr);                                                                  eigen_assert(otherIncr == 1);                                                                          gb300_trsm<EIGTYPE>::run('R', Mode, TriStorageOrder == RowMajor, (int64_t)otherSize, (int64_t)size,                                tri, (int64_t)triStride, other, (int64_t)otherStride);                      }                                                                                                    };                                                                                                     /* one right-hand-side vector (TriangularSolverVector.h:30-142); OnTheRight reduces to these */        template <typename Index, int Mode, bool Conjugate>                                                    struct triangular_solve_vector<EIGTYPE, EIGTYPE, Index, OnTheLeft, Mode, Conjugate, ColMajor> {          static void run(Index size, const EIGTYPE* lhs, Index lhsStride, EIGTYPE* rhs) {                         gb300_trsm<EIGTYPE>::run('L', Mode, false, (int64_t)size, 1, lhs, (int64_t)lhsStride, rhs,                                       (int64_t)(size > 0 ? size : 1));                                            }                                                                                                    };                                                                                                     template <typename Index, int Mode, bool Conjugate>                                                    struct triangular_solve_vector<EIGTYPE, EIGTYPE, Index, OnTheLeft, Mode, Conjugate, RowMajor> {          static void run(Index size, const EIGTYPE* lhs, Index lhsStride, EIGTYPE* rhs) {                         gb300_trsm<EIGTYPE>::run('L', Mode, true, (int64_t)size, 1, lhs, (int64_t)lhsStride, rhs,                                        (int64_t)(size > 0 ? size : 1));                                            }                                                                                                    };
+
+EIGEN_GB300_TRSM(double, gbllt_dtrsm)
+EIGEN_GB300_TRSM(float, gbllt_strsm)
+
+#undef EIGEN_GB300_TRSM
 
 }  // namespace internal
 }  // namespace Eigen

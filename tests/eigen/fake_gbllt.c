@@ -24,7 +24,12 @@ void oracle_dldlt_solve(char uplo, int64_t n, int64_t nrhs, const double* a, int
 void oracle_sldlt_solve(char uplo, int64_t n, int64_t nrhs, const float* a, int64_t lda, const int* transp, float* b,
                         int64_t ldb);
 
-long fake_calls[12];
+void oracle_dtrsm(char side, char uplo, char op, char diag, int64_t m, int64_t n, double alpha, const double* a,
+                  int64_t lda, double* b, int64_t ldb);
+void oracle_strsm(char side, char uplo, char op, char diag, int64_t m, int64_t n, float alpha, const float* a,
+                  int64_t lda, float* b, int64_t ldb);
+
+long fake_calls[14];
 
 static char eff_uplo(int layout, char uplo) {
   const int up = uplo == 'U' || uplo == 'u';
@@ -104,11 +109,27 @@ int gbllt_sldlt_solve(int layout, char uplo, int64_t n, int64_t nrhs, const floa
   return 0;
 }
 
+int gbllt_dtrsm(int layout, char side, char uplo, char transa, char diag, int64_t m, int64_t n, double alpha,
+                const double* a, int64_t lda, double* b, int64_t ldb) {
+  ++fake_calls[12];
+  if (layout != GBLLT_COL_MAJOR) return -1;
+  oracle_dtrsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb);
+  return 0;
+}
+int gbllt_strsm(int layout, char side, char uplo, char transa, char diag, int64_t m, int64_t n, float alpha,
+                const float* a, int64_t lda, float* b, int64_t ldb) {
+  ++fake_calls[13];
+  if (layout != GBLLT_COL_MAJOR) return -1;
+  oracle_strsm(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb);
+  return 0;
+}
+
 /* Prints the call counts at exit so that the test can check the backend was used. */
 __attribute__((destructor)) static void fake_report(void) {
   fprintf(stderr,
           "fake_gbllt calls: dpotrf=%ld spotrf=%ld dpotrs=%ld spotrs=%ld dpocon=%ld spocon=%ld drankupd=%ld "
-          "srankupd=%ld dldlt=%ld sldlt=%ld dldlts=%ld sldlts=%ld\n",
+          "srankupd=%ld dldlt=%ld sldlt=%ld dldlts=%ld sldlts=%ld dtrsm=%ld strsm=%ld\n",
           fake_calls[0], fake_calls[1], fake_calls[2], fake_calls[3], fake_calls[4], fake_calls[5], fake_calls[6],
-          fake_calls[7], fake_calls[8], fake_calls[9], fake_calls[10], fake_calls[11]);
+          fake_calls[7], fake_calls[8], fake_calls[9], fake_calls[10], fake_calls[11], fake_calls[12],
+          fake_calls[13]);
 }
