@@ -131,10 +131,19 @@ int ldlt_sweeps_ws(bool upper, int64_t n, int64_t nrhs, const T* d_a, int64_t ld
 
 // One triangular sweep in place on b (n x nrhs): L X = B (forward) or L^T X = B (bwd), L lower
 // column-major (upper == false) or stored as its transpose in an upper triangle (upper == true);
-// unit: L's diagonal is 1 and not read.  Workspace of potrs_ws_bytes(n, sizeof(T)) bytes.
+// unit: L's diagonal is 1 and not read.  Workspace of potrs_ws_bytes(n, sizeof(T)) bytes.  ext_err
+// (optional): the device word the sweep's bounded waits report to, instead of the workspace's own
+// (which each call clears); a caller chaining several sweeps keeps one word for all of them.
+// pre_inv (optional, not with unit): the 64 x 64 inverses of L's diagonal blocks, as trinv_all
+// leaves them; the sweep then forms none and runs chains of 4 right-hand sides (a panel of a
+// blocked solve).
 template <typename T>
 int trsm_sweep_ws(bool upper, bool bwd, bool unit, int64_t n, int64_t nrhs, const T* d_a, int64_t lda, T* d_b,
-                  int64_t ldb, void* ws, cudaStream_t s);
+                  int64_t ldb, void* ws, cudaStream_t s, int* ext_err = nullptr, const T* pre_inv = nullptr);
+// The inverses of the 64 x 64 diagonal blocks of the n x n triangle (block b at inv + b * 4096,
+// column-major), one CTA per block.
+template <typename T>
+int trinv_all(bool upper, int64_t n, const T* d_a, int64_t lda, T* inv, cudaStream_t s);
 
 // Pivoted LDL^T (LDLT::compute) of the symmetric matrix in the `upper ? upper : lower` triangle of
 // the column-major device matrix d_a; transpositions, sign and info (0 Success, 1 NumericalIssue)
@@ -201,6 +210,26 @@ struct OzakiSyrk {
   int update_pq(double* a, int64_t lda, int64_t k0, int pw, int64_t rs, const double* q, int64_t ldq, DevStatus* st,
                 cudaStream_t s);
   void release_maps();
+};
+
+// C (m x n, FP64, column-major ldc) -= 2^scale P Q^T on the BF16 tensor cores, exact to FP64 rounding of
+// the result (ozaki.cu: the residual's error-free slicing in a rectangle mode).  P is m x k and Q is
+// n x k; element (i, kk) of each lies at base[i * rstride + kk * kstride] (a column-major array has
+// rstride 1 and kstride = its leading dimension; the transpose of one has rstride = the leading
+// dimension and kstride 1).  attach() places the slices of both operands in a caller-supplied
+// workspace of bytes(mmax, nmax, kmax); run() forms them and the product, stream-ordered.  A bounded
+// wait that runs out sets *err.
+struct OzakiGemm {
+  int64_t mmax = 0, nmax = 0, kmax = 0;
+  int sms = 0;
+  void* pslices = nullptr;
+  void* qslices = nullptr;
+  int* pexp = nullptr;
+  int* qexp = nullptr;
+  static size_t bytes(int64_t mmax, int64_t nmax, int64_t kmax);
+  int attach(void* ws, int64_t mmax, int64_t nmax, int64_t kmax);
+  int run(double* c, int64_t ldc, int64_t m, int64_t n, int64_t k, const double* p, int64_t p_rs, int64_t p_ks,
+          const double* q, int64_t q_rs, int64_t q_ks, int scale, int* err, cudaStream_t s);
 };
 
 // Rank-1 update / downdate of the factor at l (device), L L^T + sigma v v^T; *d_info (device)

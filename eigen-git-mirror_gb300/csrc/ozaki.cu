@@ -271,15 +271,21 @@ struct OzParams {
   long long ldb;
   double* r;
   long long ldr;
-  // trailing update C -= P Q^T (lower; P = Q = L21 for a Cholesky update, Q = L21 D for LDL^T)
+  // update C -= 2^scale P Q^T (lower part only in the lower mode: P = Q = L21 for a Cholesky update,
+  // Q = L21 D for LDL^T; every entry of the rs x ncols rectangle in the rectangle mode)
   double* c;
   long long ldc;
   long long rs;                    // rows of the updated block
   long long ncols;                 // its columns (ncols = rs: the whole trailing lower triangle)
   const int* pexp;                 // per-row scale exponents of P (the M operand)
   const int* pexp_b;               // per-row scale exponents of Q (the N operand)
-  const DevStatus* st;
+  int scale;                       // power of two applied to the product (rectangle mode)
+  const DevStatus* st;             // lower mode: skip the update after a failed pivot
 };
+
+// Kernel modes: the refinement residual R = B - A X, the trailing update C -= P Q^T on the lower
+// part of a block, and the general update C -= 2^scale P Q^T of a rectangle.
+constexpr int OZ_RESIDUAL = 0, OZ_LOWER = 1, OZ_RECT = 2;
 
 // round((hi 2^28 + lo) 2^(e - 63)) to FP64, to nearest even, in integer arithmetic (the FP64 pipe
 // of GB300 retires two operations per SM clock, too few for a per-element conversion); the value is
@@ -318,18 +324,18 @@ __device__ __forceinline__ double fixed_to_double(long long hi, long long lo, in
 
 // Tile t of the list: the residual walks row tiles fastest; the trailing update walks the same
 // 128 x 64 grid over its rs x ncols block and skips the tiles strictly above the diagonal.
-template <bool SYRK>
+template <int MODE>
 __device__ __forceinline__ bool oz_tile(const OzParams& p, long long t, long long& row0, long long& col0) {
   row0 = (t % p.nrt) * BM;
   col0 = (t / p.nrt) * BN;
-  if (!SYRK) return true;
+  if (MODE != OZ_LOWER) return true;
   return col0 < p.ncols && col0 <= row0 + BM - 1;
 }
 
 // Persistent: each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The producer runs up to
 // two K blocks (of any tile) ahead of the MMA warp, so the next tile's loads overlap this tile's
 // products and epilogue; the TMEM accumulators (all 512 columns) are released chunk by chunk.
-template <bool SYRK>
+template <int MODE>
 __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ OzMaps maps, const OzParams p) {
   extern __shared__ uint8_t oz_smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)oz_smem_raw + 1023) & ~(uintptr_t)1023);
@@ -341,7 +347,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
   __shared__ uint32_t tmem_base_s;
   __shared__ volatile int abort_s;
 
-  if (SYRK && p.st->fail_col >= 0) return;  // an earlier pivot failed: nothing to update
+  if (MODE == OZ_LOWER && p.st->fail_col >= 0) return;  // an earlier pivot failed: nothing to update
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nkb = (int)((p.kdim + KB - 1) / KB);
   const int nchunks = (nkb + KC_BLOCKS - 1) / KC_BLOCKS;
@@ -377,7 +383,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
     bool ok = true;
     for (long long t = blockIdx.x; t < p.tiles && ok && !abort_s; t += gridDim.x) {
       long long row0, col0;
-      if (!oz_tile<SYRK>(p, t, row0, col0)) continue;
+      if (!oz_tile<MODE>(p, t, row0, col0)) continue;
       for (int kb = 0; kb < nkb && ok; ++kb, ++kbg) {
         const int xb = (int)(kbg & 1);
         if (!mbar_wait(&xempty[xb], ((uint32_t)(kbg >> 1) & 1u) ^ 1u, &abort_s)) { ok = false; break; }
@@ -409,7 +415,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
     bool ok = true;
     for (long long t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
       long long row0, col0;
-      if (!oz_tile<SYRK>(p, t, row0, col0)) continue;
+      if (!oz_tile<MODE>(p, t, row0, col0)) continue;
       for (int kb = 0; kb < nkb && ok; ++kb, ++kbg) {
         const bool first = (kb % KC_BLOCKS) == 0;
         if (first && chunkg > 0) {  // the epilogue has taken the previous chunk's sums out of TMEM
@@ -452,7 +458,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
     bool ok = true;
     for (long long t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
       long long row0, col0;
-      if (!oz_tile<SYRK>(p, t, row0, col0)) continue;
+      if (!oz_tile<MODE>(p, t, row0, col0)) continue;
       long long hi[16], lo[16];
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
@@ -480,7 +486,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
       }
       if (!ok) break;
       const long long i = row0 + r;
-      if (SYRK) {
+      if (MODE == OZ_LOWER) {
         if (i < p.rs) {
           const int ei = p.pexp[i];
 #pragma unroll
@@ -489,6 +495,15 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
             if (j <= i) {
               p.c[j * p.ldc + i] -= fixed_to_double(hi[c], lo[c], ei + p.pexp_b[j]);
             }
+          }
+        }
+      } else if (MODE == OZ_RECT) {
+        if (i < p.rs) {
+          const int ei = p.pexp[i] + p.scale;
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const long long j = col0 + part * 16 + c;
+            if (j < p.ncols) p.c[j * p.ldc + i] -= fixed_to_double(hi[c], lo[c], ei + p.pexp_b[j]);
           }
         }
       } else if (i < p.n) {
@@ -532,8 +547,9 @@ int oz_prepare_device(int* sms) {
   }
   std::lock_guard<std::mutex> lk(mu);
   if (!nsm[dev]) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(oz_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    GB_CUDA_TRY(cudaFuncSetAttribute(oz_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    GB_CUDA_TRY(cudaFuncSetAttribute(oz_kernel<OZ_RESIDUAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    GB_CUDA_TRY(cudaFuncSetAttribute(oz_kernel<OZ_LOWER>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    GB_CUDA_TRY(cudaFuncSetAttribute(oz_kernel<OZ_RECT>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     int v = 0;
     GB_CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
     nsm[dev] = v > 0 ? v : 1;
@@ -646,7 +662,7 @@ int OzakiResidual::residual(const double* x, int64_t ldx, const double* b, int64
     // X slices, B read and R written
     ProfScope ps(kg.c_str(), s, 2.0 * n * n * nrhs,
                  (double)S * n * n * 2.0 * p.nct + (double)S * n * nrhs * 2.0 + 2.0 * n * nrhs * 8.0);
-    oz_kernel<false><<<grid, THREADS, SMEM_BYTES, s>>>(maps, p);
+    oz_kernel<OZ_RESIDUAL><<<grid, THREADS, SMEM_BYTES, s>>>(maps, p);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
@@ -806,7 +822,7 @@ int OzakiSyrk::update(double* a, int64_t lda, int64_t k0, int pw, int64_t rs, in
     const double c = (double)(ncols < rs ? ncols : rs);
     const double entries = c * (double)rs - c * (c - 1) / 2.0;
     ProfScope ps(ks.c_str(), s, 2.0 * entries * pw, 2.0 * entries * 8.0 + (double)S * rs * w * 2.0);
-    oz_kernel<true><<<grid, THREADS, SMEM_BYTES, s>>>(((const OzMaps*)maps)[wide ? 1 : 0], p);
+    oz_kernel<OZ_LOWER><<<grid, THREADS, SMEM_BYTES, s>>>(((const OzMaps*)maps)[wide ? 1 : 0], p);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
@@ -847,7 +863,190 @@ int OzakiSyrk::update_pq(double* a, int64_t lda, int64_t k0, int pw, int64_t rs,
   {
     const double entries = (double)rs * (rs + 1) / 2.0;
     ProfScope ps(ks.c_str(), s, 2.0 * entries * pw, 2.0 * entries * 8.0 + 2.0 * S * rs * PK * 2.0);
-    oz_kernel<true><<<grid, THREADS, SMEM_BYTES, s>>>(((const OzMaps*)maps)[2], p);
+    oz_kernel<OZ_LOWER><<<grid, THREADS, SMEM_BYTES, s>>>(((const OzMaps*)maps)[2], p);
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+}  // namespace gbllt
+
+// ---- the general FP64-exact product C -= 2^scale P Q^T of a rectangle ----------------------------
+//
+// The blocked triangular solves and the blocked adjoint are made of products of panels with
+// rectangles.  Both operands are sliced like the residual's (one exponent per row, its maximum over
+// k), each from any strided layout, and the product runs in the kernel's rectangle mode: exact
+// 256-deep FP32 chunks, int64 combination across chunks, one rounding into FP64.
+
+namespace gbllt {
+
+namespace {
+
+// Slices of a rows x k operand whose element (i, kk) lies at src[i * rstride + kk * kstride], as
+// K-major rows of w >= k elements (zero past k): row i of slice q at slices + q * sstride + i * w;
+// pexp[i] = the scale exponent of row i.  One thread per row; with kstride = 1 each thread reads its
+// row contiguously, with rstride = 1 a warp reads 32 consecutive rows of each column.
+__global__ void __launch_bounds__(128) oz_rows_slice_kernel(const double* __restrict__ src, long long rstride,
+                                                            long long kstride, long long rows, long long k, long long w,
+                                                            __nv_bfloat16* __restrict__ slices, long long sstride,
+                                                            int* __restrict__ pexp) {
+  const long long i = (long long)blockIdx.x * 128 + threadIdx.x;
+  if (i >= rows) return;
+  const double* row = src + i * rstride;
+  unsigned long long mb = 0;
+  for (long long kk = 0; kk < k; ++kk) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(row[kk * kstride]) & ~(1ull << 63);
+    mb = b > mb ? b : mb;
+  }
+  const int e = scale_exp(__longlong_as_double((long long)mb));
+  pexp[i] = e;
+#pragma unroll 1
+  for (long long p0 = 0; p0 < w; p0 += 8) {
+    uint32_t packed[S][4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const long long pa = p0 + 2 * h, pb = pa + 1;
+      float lo[S], hi[S];
+      split8(pa < k ? row[pa * kstride] : 0.0, e, lo);
+      split8(pb < k ? row[pb * kstride] : 0.0, e, hi);
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        const __nv_bfloat162 v2 = __floats2bfloat162_rn(lo[q], hi[q]);
+        packed[q][h] = *reinterpret_cast<const uint32_t*>(&v2);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < S; ++q)
+      *reinterpret_cast<uint4*>(slices + q * sstride + i * w + p0) =
+          make_uint4(packed[q][0], packed[q][1], packed[q][2], packed[q][3]);
+  }
+}
+
+// The same slices for an operand whose rows are contiguous (kstride 1): one warp per row, lanes
+// along k, so that the reads (8 consecutive values per lane) and the 16-byte slice stores are
+// coalesced.  Four rows per warp, eight warps per CTA.
+__global__ void __launch_bounds__(256) oz_rows_slice_contig_kernel(const double* __restrict__ src, long long rstride,
+                                                                   long long rows, long long k, long long w,
+                                                                   __nv_bfloat16* __restrict__ slices,
+                                                                   long long sstride, int* __restrict__ pexp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int rr = 0; rr < 4; ++rr) {
+    const long long i = (long long)blockIdx.x * 32 + warp * 4 + rr;
+    if (i >= rows) return;
+    const double* row = src + i * rstride;
+    unsigned long long mb = 0;
+    for (long long kk = lane; kk < k; kk += 32) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(row[kk]) & ~(1ull << 63);
+      mb = b > mb ? b : mb;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long other = __shfl_xor_sync(0xffffffffu, mb, o);
+      mb = other > mb ? other : mb;
+    }
+    const int e = scale_exp(__longlong_as_double((long long)mb));
+    if (lane == 0) pexp[i] = e;
+    for (long long p0 = (long long)lane * 8; p0 < w; p0 += 256) {
+      uint32_t packed[S][4];
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const long long pa = p0 + 2 * h, pb = pa + 1;
+        float lo[S], hi[S];
+        split8(pa < k ? row[pa] : 0.0, e, lo);
+        split8(pb < k ? row[pb] : 0.0, e, hi);
+#pragma unroll
+        for (int q = 0; q < S; ++q) {
+          const __nv_bfloat162 v2 = __floats2bfloat162_rn(lo[q], hi[q]);
+          packed[q][h] = *reinterpret_cast<const uint32_t*>(&v2);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < S; ++q)
+        *reinterpret_cast<uint4*>(slices + q * sstride + i * w + p0) =
+            make_uint4(packed[q][0], packed[q][1], packed[q][2], packed[q][3]);
+    }
+  }
+}
+
+// Slices of one operand: the row-contiguous kernel when kstride is 1, else one thread per row.
+void oz_slice_rows(const double* src, long long rstride, long long kstride, long long rows, long long k, long long w,
+                   __nv_bfloat16* slices, long long sstride, int* pexp, cudaStream_t s) {
+  if (kstride == 1)
+    oz_rows_slice_contig_kernel<<<(unsigned)ceil_div(rows, 32), 256, 0, s>>>(src, rstride, rows, k, w, slices, sstride,
+                                                                           pexp);
+  else
+    oz_rows_slice_kernel<<<(unsigned)ceil_div(rows, 128), 128, 0, s>>>(src, rstride, kstride, rows, k, w, slices,
+                                                                      sstride, pexp);
+}
+
+inline int64_t oz_kpad(int64_t k) { return (k + KB - 1) / KB * KB; }
+
+}  // namespace
+
+size_t OzakiGemm::bytes(int64_t mmax, int64_t nmax, int64_t kmax) {
+  const size_t w = (size_t)oz_kpad(kmax);
+  return oz_up256((size_t)S * mmax * w * 2) + oz_up256((size_t)S * nmax * w * 2) + oz_up256((size_t)mmax * 4) +
+         oz_up256((size_t)nmax * 4);
+}
+
+int OzakiGemm::attach(void* ws, int64_t mmax_, int64_t nmax_, int64_t kmax_) {
+  int rc = oz_prepare_device(&sms);
+  if (rc) return rc;
+  mmax = mmax_;
+  nmax = nmax_;
+  kmax = kmax_;
+  const size_t w = (size_t)oz_kpad(kmax);
+  char* q = (char*)ws;
+  pslices = q;
+  q += oz_up256((size_t)S * mmax * w * 2);
+  qslices = q;
+  q += oz_up256((size_t)S * nmax * w * 2);
+  pexp = (int*)q;
+  q += oz_up256((size_t)mmax * 4);
+  qexp = (int*)q;
+  return GBLLT_SUCCESS;
+}
+
+int OzakiGemm::run(double* c, int64_t ldc, int64_t m, int64_t n, int64_t k, const double* pa, int64_t p_rs,
+                   int64_t p_ks, const double* qa, int64_t q_rs, int64_t q_ks, int scale, int* err, cudaStream_t s) {
+  if (m <= 0 || n <= 0 || k <= 0) return GBLLT_SUCCESS;
+  if (!pslices || m > mmax || n > nmax || k > kmax) return GBLLT_ERR_INTERNAL;
+  static const std::string kp = "gemm_slices_f64";
+  static const std::string kg = "gemm_tc_f64";
+  const int64_t w = oz_kpad(k);
+  __nv_bfloat16* ps = (__nv_bfloat16*)pslices;
+  __nv_bfloat16* qs = (__nv_bfloat16*)qslices;
+  {
+    ProfScope pr(kp.c_str(), s, 0.0, (double)(m + n) * k * 8.0 + (double)S * (m + n) * w * 2.0);
+    oz_slice_rows(pa, p_rs, p_ks, m, k, w, ps, (long long)m * w, pexp, s);
+    oz_slice_rows(qa, q_rs, q_ks, n, k, w, qs, (long long)n * w, qexp, s);
+  }
+  OzMaps maps;
+  for (int q = 0; q < S; ++q) {
+    if (!make_map_2d(&maps.a[q], ps + (size_t)q * m * w, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, m, w, w, KB, BM) ||
+        !make_map_2d(&maps.x[q], qs + (size_t)q * n * w, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, n, w, w, KB, BN)) {
+      set_error_message("cuTensorMapEncodeTiled failed (tensor-core FP64 product)");
+      return GBLLT_ERR_INTERNAL;
+    }
+  }
+  OzParams p;
+  memset(&p, 0, sizeof p);
+  p.kdim = k;
+  p.nrt = (int)ceil_div(m, BM);
+  p.nct = (int)ceil_div(n, BN);
+  p.tiles = (long long)p.nrt * p.nct;
+  p.c = c;
+  p.ldc = ldc;
+  p.rs = m;
+  p.ncols = n;
+  p.pexp = pexp;
+  p.pexp_b = qexp;
+  p.scale = scale;
+  p.err = err;
+  const unsigned grid = (unsigned)(p.tiles < sms ? p.tiles : sms);
+  {
+    ProfScope pr(kg.c_str(), s, 2.0 * m * n * k, 2.0 * m * n * 8.0 + (double)S * (m + n) * w * 2.0);
+    oz_kernel<OZ_RECT><<<grid, THREADS, SMEM_BYTES, s>>>(maps, p);
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;

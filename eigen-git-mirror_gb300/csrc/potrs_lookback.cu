@@ -235,10 +235,12 @@ void launch_sweep_rc(int nb, const T* a, long long lda, long long n, T* b, long 
 // One launch per sweep: chunks of RCT right-hand sides run as parallel chains (grid.y); 4 columns
 // per chunk for a single right-hand side, 16 otherwise (more chains spread the FP64 work of the
 // last row blocks over more SMs).
+// narrow: chains of 4 whatever nrhs (more CTAs, each with a quarter of the FP64 work per link).
 template <typename T, bool UP, bool BWD, bool DSCALE = false>
 void launch_sweep(int nb, const T* a, long long lda, long long n, T* b, long long ldb, int nrhs, const T* inv,
-                  int* flags, int* counter, int* err, cudaStream_t s) {
-  if (nrhs <= 4) launch_sweep_rc<T, UP, BWD, 4, DSCALE>(nb, a, lda, n, b, ldb, nrhs, inv, flags, counter, err, s);
+                  int* flags, int* counter, int* err, cudaStream_t s, bool narrow = false) {
+  if (nrhs <= 4 || narrow)
+    launch_sweep_rc<T, UP, BWD, 4, DSCALE>(nb, a, lda, n, b, ldb, nrhs, inv, flags, counter, err, s);
   else launch_sweep_rc<T, UP, BWD, 16, DSCALE>(nb, a, lda, n, b, ldb, nrhs, inv, flags, counter, err, s);
 }
 
@@ -780,24 +782,39 @@ int potrs_ws(bool upper, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b,
 }
 
 template <typename T>
+int trinv_all(bool upper, int64_t n, const T* a, int64_t lda, T* inv, cudaStream_t s) {
+  if (n <= 0) return GBLLT_SUCCESS;
+  static const std::string ki = std::string("trinv_diag_") + tname<T>();
+  const int nb = (int)ceil_div(n, RB);
+  ProfScope ps(ki.c_str(), s, (double)nb * RB * RB * RB / 3.0, (double)n * RB * sizeof(T) * 1.5);
+  if (upper) trinv_kernel<T, true, false><<<nb, 128, 0, s>>>(a, lda, n, inv);
+  else trinv_kernel<T, false, false><<<nb, 128, 0, s>>>(a, lda, n, inv);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+template int trinv_all<double>(bool, int64_t, const double*, int64_t, double*, cudaStream_t);
+
+template <typename T>
 int trsm_sweep_ws(bool upper, bool bwd, bool unit, int64_t n, int64_t nrhs, const T* a, int64_t lda, T* b,
-                  int64_t ldb, void* ws, cudaStream_t s) {
+                  int64_t ldb, void* ws, cudaStream_t s, int* ext_err, const T* pre_inv) {
   if (n <= 0 || nrhs <= 0) return GBLLT_SUCCESS;
   static const std::string ki = std::string("trinv_diag_") + tname<T>();
   static const std::string kf = std::string("sweep_") + tname<T>();
   const int nb = (int)ceil_div(n, RB);
-  T* inv = (T*)ws;
+  // the inverses: the caller's, or formed here in the workspace
+  const T* inv = pre_inv ? pre_inv : (const T*)ws;
   int* base = (int*)((char*)ws + ws_flags_offset(nb, sizeof(T)));
-  int* err = base;  // the call's error word
-  GB_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
-  {
+  int* err = ext_err ? ext_err : base;  // the call's error word, or the caller's (not cleared here)
+  if (!ext_err) GB_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+  if (!pre_inv) {
+    T* winv = (T*)ws;
     ProfScope ps(ki.c_str(), s, (double)nb * RB * RB * RB / 3.0, (double)n * RB * sizeof(T) * 1.5);
     if (unit) {
-      if (upper) trinv_kernel<T, true, true><<<nb, 128, 0, s>>>(a, lda, n, inv);
-      else trinv_kernel<T, false, true><<<nb, 128, 0, s>>>(a, lda, n, inv);
+      if (upper) trinv_kernel<T, true, true><<<nb, 128, 0, s>>>(a, lda, n, winv);
+      else trinv_kernel<T, false, true><<<nb, 128, 0, s>>>(a, lda, n, winv);
     } else {
-      if (upper) trinv_kernel<T, true, false><<<nb, 128, 0, s>>>(a, lda, n, inv);
-      else trinv_kernel<T, false, false><<<nb, 128, 0, s>>>(a, lda, n, inv);
+      if (upper) trinv_kernel<T, true, false><<<nb, 128, 0, s>>>(a, lda, n, winv);
+      else trinv_kernel<T, false, false><<<nb, 128, 0, s>>>(a, lda, n, winv);
     }
   }
   if constexpr (std::is_same<T, float>::value) {
@@ -820,21 +837,27 @@ int trsm_sweep_ws(bool upper, bool bwd, bool unit, int64_t n, int64_t nrhs, cons
       }
     }
   } else {
-    for (int64_t c0 = 0; c0 < nrhs; c0 += RC) {
-      const int nc = (int)(nrhs - c0 < RC ? nrhs - c0 : RC);
-      const int nch = nc <= 4 ? 1 : (nc + 15) / 16;
+    // chains per launch stay within the RC / 16 the workspace holds flags for: 16-wide chains up to
+    // RC right-hand sides, or (panel sub-solves) 4-wide chains up to 64
+    const int step = pre_inv ? 64 : RC;
+    for (int64_t c0 = 0; c0 < nrhs; c0 += step) {
+      const int nc = (int)(nrhs - c0 < step ? nrhs - c0 : step);
+      const int nch = (nc <= 4 || pre_inv) ? (nc + 3) / 4 : (nc + 15) / 16;
       int* flags = base + kWsFlagsSkip;
       int* ctr = flags + nch * nb;
       T* bc = b + c0 * ldb;
       GB_CUDA_TRY(cudaMemsetAsync(flags, 0, (size_t)(nch * nb + nch) * sizeof(int), s));
       const double fl = (double)n * (n + 1) * nc, by = (double)n * (n + 1) / 2.0 * sizeof(T) + 2.0 * n * nc * sizeof(T);
       ProfScope ps(kf.c_str(), s, fl, by);
+      // a caller that supplies the inverses solves one panel of a blocked solve: chains of 4 spread
+      // its few row blocks' FP64 work over more SMs
+      const bool narrow = pre_inv != nullptr;
       if (bwd) {
-        if (upper) launch_sweep<T, true, true>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
-        else launch_sweep<T, false, true>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
+        if (upper) launch_sweep<T, true, true>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s, narrow);
+        else launch_sweep<T, false, true>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s, narrow);
       } else {
-        if (upper) launch_sweep<T, true, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
-        else launch_sweep<T, false, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s);
+        if (upper) launch_sweep<T, true, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s, narrow);
+        else launch_sweep<T, false, false>(nb, a, lda, n, bc, ldb, nc, inv, flags, ctr, err, s, narrow);
       }
     }
   }
@@ -926,8 +949,8 @@ template int ldlt_sweeps_ws<double>(bool, int64_t, int64_t, const double*, int64
                                     cudaStream_t);
 template int ldlt_sweeps_ws<float>(bool, int64_t, int64_t, const float*, int64_t, float*, int64_t, void*, cudaStream_t);
 template int trsm_sweep_ws<double>(bool, bool, bool, int64_t, int64_t, const double*, int64_t, double*, int64_t, void*,
-                                   cudaStream_t);
+                                   cudaStream_t, int*, const double*);
 template int trsm_sweep_ws<float>(bool, bool, bool, int64_t, int64_t, const float*, int64_t, float*, int64_t, void*,
-                                  cudaStream_t);
+                                  cudaStream_t, int*, const float*);
 
 }  // namespace gbllt

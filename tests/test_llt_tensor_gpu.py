@@ -152,6 +152,24 @@ def test_tensor_path_column_graded_reconstruction(oracle, gbllt):
     assert r_gpu <= max(10 * r_ref, 1e-16) and r_gpu <= 4 * n * U
 
 
+@pytest.mark.parametrize("n,k", [(2048, 16), (2100, 70), (4097, 33)])
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_tensor_path_blocked_solve(oracle, gbllt, n, k, uplo):
+    # from n = 2048 and 16 right-hand sides the FP64 solve runs in 256-row panels: the look-back sweep
+    # on each diagonal block and FP64-exact tensor-core products for the rest of the right-hand sides
+    a = oracle.gen_householder(n, 1e4)
+    f = np.array(a, order="F", copy=True)
+    assert oracle.potrf(f, uplo) == 0  # the oracle's factor: the solves are compared on the same L
+    b = np.asfortranarray(oracle.normal(40, n * k).reshape(n, k, order="F"))
+    x = np.array(b, order="F", copy=True)
+    gbllt.potrs(f, x, uplo)
+    xr = np.array(b, order="F", copy=True)
+    oracle.potrs(f, xr, uplo)
+    assert rel(x, xr) <= 1e-12
+    cols = [0, k // 2, k - 1]
+    assert oracle.backward_error(a, np.asfortranarray(x[:, cols]), np.asfortranarray(b[:, cols]), uplo) <= 1e-15
+
+
 @pytest.mark.slow
 def test_tensor_path_full_size_config2_factor(oracle, gbllt):
     """n = 16384, 64 RHS, Householder spectrum with kappa = 1e6 (full size): the factor against the
