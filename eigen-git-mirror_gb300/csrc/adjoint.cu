@@ -252,48 +252,124 @@ __global__ void sym_rank_update_kernel(long long n, long long nrhs, const double
   Ab[j * ldab + i] -= 0.5 * s;
 }
 
+// W (jb x (n - j0), row a contiguous over r, leading dimension ldw) = [sym(M_JJ); M_IJ]^T for the panel
+// at j0: for r < jb the symmetric matrix whose lower triangle is M_JJ's, below it M_IJ.
+__global__ void build_panel_w_kernel(const double* __restrict__ M, long long ldm, long long j0, int jb, long long n,
+                                     double* __restrict__ W, long long ldw) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int a = blockIdx.y;
+  if (r >= n - j0 || a >= jb) return;
+  double v;
+  if (r < jb) v = r >= a ? M[(j0 + a) * ldm + j0 + r] : M[(j0 + r) * ldm + j0 + a];
+  else v = M[(j0 + a) * ldm + j0 + r];
+  W[(long long)a * ldw + r] = v;
+}
+
+// A bounded wait of a tensor-core product ran out: the gradient is invalid, and its lower triangle
+// becomes NaN so that a stream-ordered caller sees it.
+__global__ void nan_if_error_kernel(const int* __restrict__ err, long long n, double* __restrict__ M, long long ldm) {
+  if (*(volatile const int*)err == 0) return;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * n) return;
+  const long long i = idx % n, j = idx / n;
+  if (i >= j) M[j * ldm + i] = __longlong_as_double(0x7ff8000000000000ll);
+}
+
+constexpr int APW = 64;      // panel width of the reverse sweep (two 32-wide blocks)
+constexpr int64_t KC2 = 2048;  // rows of L per product of the panel-row update (bounds the slices)
+
 }  // namespace
 
-int potrf_adjoint_dev(int64_t n, const double* L, int64_t ldl, double* M, int64_t ldm, cudaStream_t s) {
+// The reverse sweep in 64-wide panels, last to first.  Inside a panel the 32-wide blocks run the
+// per-block recurrences above with their column range K restricted to the panel; what each block
+// would add into the columns left of the panel is linear in the panel's final values, and is added
+// after the panel as two products on the tensor cores (OzakiGemm; nsl = 8: FP64-exact, nsl = 4: the
+// 28-bit products of the mixed-precision adjoint):
+//     M_IK -= 2 M_IJ L_JK                      (rows I below the panel; M_IJ holds Cbar / 2)
+//     M_JK -= 2 W^T L_RK,  W = [sym(M_JJ); M_IJ] (the panel's rows; R = the rows from the panel down)
+// where sym(M_JJ) collects, through the symmetric matrix whose lower triangle M_JJ holds, the
+// products with the panel's own blocks: Cbar^T of the blocks below, Dbar on the diagonal, Cbar of the
+// blocks above.  The in-panel work stays on the FP64 pipe (about 2 n^2 * 64 flops); the products with
+// the panel (2 n^3 / 3) run on the tensor cores.
+int potrf_adjoint_dev(int64_t n, const double* L, int64_t ldl, double* M, int64_t ldm, cudaStream_t s, int nsl) {
   static const std::string kt = "adjoint_trsm_f64", kd = "adjoint_diag_f64";
-  // split-K partials of the long, narrow products (stream-ordered, from the pool)
-  double* part = nullptr;
-  if (dev_malloc_async((void**)&part, (size_t)kSplitElems * sizeof(double), s) != cudaSuccess) {
+  const size_t pb = (size_t)kSplitElems * sizeof(double);
+  const size_t g1b = (OzakiGemm::bytes(n, n, APW) + 255) & ~(size_t)255;
+  const int64_t kc2 = n < KC2 ? n : KC2;
+  const size_t g2b = (OzakiGemm::bytes(APW, n, kc2) + 255) & ~(size_t)255;
+  const int64_t ldw = (n + 31) / 32 * 32;
+  const size_t wb = (size_t)APW * ldw * sizeof(double);
+  char* ws = nullptr;
+  if (dev_malloc_async((void**)&ws, pb + g1b + g2b + wb + 256, s) != cudaSuccess) {
     cudaGetLastError();
-    set_error_message("gbllt_dpotrf_adjoint_dev: cudaMallocAsync of the split-K scratch failed");
+    set_error_message("gbllt_dpotrf_adjoint_dev: cudaMallocAsync of the workspace failed");
     return GBLLT_ERR_ALLOC;
   }
-  const int64_t last = ((n - 1) / ANB) * ANB;
-  for (int64_t j0 = last; j0 >= 0; j0 -= ANB) {
-    const int jb = (int)(n - j0 < ANB ? n - j0 : ANB);
-    const int64_t i0 = j0 + jb, ni = n - i0;  // rows below the block
-    const double* Ljj = L + j0 * ldl + j0;
-    const double* Lij = L + j0 * ldl + i0;
-    const double* Ljk = L + j0;               // rows J, columns 0..j0
-    const double* Lik = L + i0;               // rows I, columns 0..j0
-    double* Mjj = M + j0 * ldm + j0;
-    double* Mij = M + j0 * ldm + i0;
-    double* Mjk = M + j0;
-    double* Mik = M + i0;
-    if (ni > 0) {
+  struct Free {
+    void* p;
+    cudaStream_t s;
+    ~Free() { cudaFreeAsync(p, s); }
+  } guard{ws, s};
+  double* part = (double*)ws;  // split-K partials of the long, narrow in-panel products
+  OzakiGemm g1, g2;
+  int rc;
+  if ((rc = g1.attach(ws + pb, n, n, APW)) || (rc = g2.attach(ws + pb + g1b, APW, n, kc2))) return rc;
+  double* W = (double*)(ws + pb + g1b + g2b);
+  int* err = (int*)(ws + pb + g1b + g2b + wb);
+  GB_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+  const int64_t last = ((n - 1) / APW) * APW;
+  for (int64_t p0 = last; p0 >= 0; p0 -= APW) {
+    const int pw = (int)(n - p0 < APW ? n - p0 : APW);
+    // ---- the panel's blocks, last to first, columns K restricted to [p0, j0)
+    for (int64_t j0 = p0 + ((pw - 1) / ANB) * ANB; j0 >= p0; j0 -= ANB) {
+      const int jb = (int)(n - j0 < ANB ? n - j0 : ANB);
+      const int64_t i0 = j0 + jb, ni = n - i0;  // rows below the block
+      const int64_t kw = j0 - p0;               // columns of the panel left of the block
+      const double* Ljj = L + j0 * ldl + j0;
+      const double* Lij = L + j0 * ldl + i0;
+      const double* Ljk = L + p0 * ldl + j0;   // rows J, columns p0 .. j0
+      const double* Lik = L + p0 * ldl + i0;   // rows I, columns p0 .. j0
+      double* Mjj = M + j0 * ldm + j0;
+      double* Mij = M + j0 * ldm + i0;
+      double* Mjk = M + p0 * ldm + j0;
+      double* Mik = M + p0 * ldm + i0;
+      if (ni > 0) {
+        {
+          ProfScope ps(kt.c_str(), s, (double)ni * jb * jb, 16.0 * ni * jb);
+          trsm_right_lower_kernel<<<(unsigned)ceil_div(ni, 64), 64, 0, s>>>(Ljj, ldl, jb, Mij, ldm, ni);  // Cbar/2
+        }
+        // M_IJ now holds Cbar / 2 (its final, symmetric-convention value); the updates use Cbar = 2 M_IJ
+        gemm<1, 0>(jb, jb, ni, -2.0, Mij, ldm, Lij, ldl, Mjj, ldm, true, part, s);        // M_JJ -= tril(Cbar^T L_IJ)
+        if (kw > 0) {
+          gemm<0, 0>(ni, kw, jb, -2.0, Mij, ldm, Ljk, ldl, Mik, ldm, false, part, s);     // M_IK -= Cbar L_JK
+          gemm<1, 0>(jb, kw, ni, -2.0, Mij, ldm, Lik, ldl, Mjk, ldm, false, part, s);     // M_JK -= Cbar^T L_IK
+        }
+      }
       {
-        ProfScope ps(kt.c_str(), s, (double)ni * jb * jb, 16.0 * ni * jb);
-        trsm_right_lower_kernel<<<(unsigned)ceil_div(ni, 64), 64, 0, s>>>(Ljj, ldl, jb, Mij, ldm, ni);  // Cbar/2
+        ProfScope ps(kd.c_str(), s, 4.0 * jb * jb * jb, 24.0 * jb * jb);
+        chol_adjoint_diag_kernel<<<1, 256, 0, s>>>(Ljj, ldl, jb, Mjj, ldm);          // Dbar
       }
-      // M_IJ now holds Cbar / 2 (its final, symmetric-convention value); the updates use Cbar = 2 M_IJ
-      gemm<1, 0>(jb, jb, ni, -2.0, Mij, ldm, Lij, ldl, Mjj, ldm, true, part, s);        // M_JJ -= tril(Cbar^T L_IJ)
-      if (j0 > 0) {
-        gemm<0, 0>(ni, j0, jb, -2.0, Mij, ldm, Ljk, ldl, Mik, ldm, false, part, s);     // M_IK -= Cbar L_JK
-        gemm<1, 0>(jb, j0, ni, -2.0, Mij, ldm, Lik, ldl, Mjk, ldm, false, part, s);     // M_JK -= Cbar^T L_IK
-      }
+      if (kw > 0) gemm<2, 0>(jb, kw, jb, -2.0, Mjj, ldm, Ljk, ldl, Mjk, ldm, false, part, s);  // M_JK -= 2 Dbar L_JK
     }
+    if (p0 == 0) break;
+    // ---- the columns left of the panel, on the tensor cores
+    const int64_t r0 = p0 + pw, nr = n - r0;  // rows below the panel
+    // M_IK -= 2 M_IJ L_JK: P = M_IJ (element (i, a) = M(r0 + i, p0 + a)), Q = L_JK^T (element
+    // (k, a) = L(p0 + a, k))
+    if (nr > 0 && (rc = g1.run(M + r0, ldm, nr, p0, pw, M + p0 * ldm + r0, 1, ldm, L + p0, ldl, 1, 1, err, s, nsl)))
+      return rc;
+    // M_JK -= 2 W^T L_RK in chunks of rows of R: P = W^T (element (a, r) = W[a ldw + r]), Q = L_RK^T
+    // (element (k, r) = L(p0 + r, k))
     {
-      ProfScope ps(kd.c_str(), s, 4.0 * jb * jb * jb, 24.0 * jb * jb);
-      chol_adjoint_diag_kernel<<<1, 256, 0, s>>>(Ljj, ldl, jb, Mjj, ldm);          // Dbar
+      const dim3 g((unsigned)ceil_div(n - p0, 256), (unsigned)pw);
+      build_panel_w_kernel<<<g, 256, 0, s>>>(M, ldm, p0, pw, n, W, ldw);
     }
-    if (j0 > 0) gemm<2, 0>(jb, j0, jb, -2.0, Mjj, ldm, Ljk, ldl, Mjk, ldm, false, part, s);  // M_JK -= 2 Dbar L_JK
+    for (int64_t c0 = 0; c0 < n - p0; c0 += kc2) {
+      const int64_t kc = n - p0 - c0 < kc2 ? n - p0 - c0 : kc2;
+      if ((rc = g2.run(M + p0, ldm, pw, p0, kc, W + c0, ldw, 1, L + p0 + c0, ldl, 1, 1, err, s, nsl))) return rc;
+    }
   }
-  cudaFreeAsync(part, s);
+  nan_if_error_kernel<<<(unsigned)ceil_div(n * n, 256), 256, 0, s>>>(err, n, M, ldm);
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
 }
@@ -329,7 +405,20 @@ int gbllt_dpotrf_adjoint_dev(int64_t n, const double* d_l, int64_t ldl, double* 
   if (n == 0) return GBLLT_SUCCESS;
   int rc = ensure_device();
   if (rc) return rc;
-  return potrf_adjoint_dev(n, d_l, ldl, d_lbar, ldlb, (cudaStream_t)stream);
+  return potrf_adjoint_dev(n, d_l, ldl, d_lbar, ldlb, (cudaStream_t)stream, 8);
+}
+
+int gbllt_dpotrf_adjoint_mixed_dev(int64_t n, const double* d_l, int64_t ldl, double* d_lbar, int64_t ldlb,
+                                   void* stream) {
+  if (n < 0) return -1;
+  if (n > 0 && !d_l) return -2;
+  if (ldl < (n > 1 ? n : 1)) return -3;
+  if (n > 0 && !d_lbar) return -4;
+  if (ldlb < (n > 1 ? n : 1)) return -5;
+  if (n == 0) return GBLLT_SUCCESS;
+  int rc = ensure_device();
+  if (rc) return rc;
+  return potrf_adjoint_dev(n, d_l, ldl, d_lbar, ldlb, (cudaStream_t)stream, 4);
 }
 
 int gbllt_dpotrs_adjoint_dev(int64_t n, int64_t nrhs, const double* d_l, int64_t ldl, const double* d_x, int64_t ldx,

@@ -218,7 +218,9 @@ struct OzakiSyrk {
 // rstride 1 and kstride = its leading dimension; the transpose of one has rstride = the leading
 // dimension and kstride 1).  attach() places the slices of both operands in a caller-supplied
 // workspace of bytes(mmax, nmax, kmax); run() forms them and the product, stream-ordered.  A bounded
-// wait that runs out sets *err.
+// wait that runs out sets *err.  nsl < 8 uses only the first nsl 7-bit slices of each operand and the
+// slice pairs of weight below nsl: the product then carries about 7 nsl bits (nsl = 4: FP32 level)
+// for (nsl (nsl + 1) / 2) / 36 of the tensor-core work.
 struct OzakiGemm {
   int64_t mmax = 0, nmax = 0, kmax = 0;
   int sms = 0;
@@ -229,7 +231,7 @@ struct OzakiGemm {
   static size_t bytes(int64_t mmax, int64_t nmax, int64_t kmax);
   int attach(void* ws, int64_t mmax, int64_t nmax, int64_t kmax);
   int run(double* c, int64_t ldc, int64_t m, int64_t n, int64_t k, const double* p, int64_t p_rs, int64_t p_ks,
-          const double* q, int64_t q_rs, int64_t q_ks, int scale, int* err, cudaStream_t s);
+          const double* q, int64_t q_rs, int64_t q_ks, int scale, int* err, cudaStream_t s, int nsl = 8);
 };
 
 // Rank-1 update / downdate of the factor at l (device), L L^T + sigma v v^T; *d_info (device)

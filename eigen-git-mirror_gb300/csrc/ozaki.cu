@@ -280,6 +280,7 @@ struct OzParams {
   const int* pexp;                 // per-row scale exponents of P (the M operand)
   const int* pexp_b;               // per-row scale exponents of Q (the N operand)
   int scale;                       // power of two applied to the product (rectangle mode)
+  int nsl;                         // slices used per operand (S: FP64-exact; fewer: 7 nsl bits)
   const DevStatus* st;             // lower mode: skip the update after a failed pivot
 };
 
@@ -387,11 +388,11 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
       for (int kb = 0; kb < nkb && ok; ++kb, ++kbg) {
         const int xb = (int)(kbg & 1);
         if (!mbar_wait(&xempty[xb], ((uint32_t)(kbg >> 1) & 1u) ^ 1u, &abort_s)) { ok = false; break; }
-        mbar_expect_tx(&xfull[xb], X_SET);
-        for (int q = 0; q < S; ++q)
+        mbar_expect_tx(&xfull[xb], p.nsl * X_BYTES);
+        for (int q = 0; q < p.nsl; ++q)
           tma_load_2d(x_buf + xb * X_SET + q * X_BYTES, &maps.x[q], &xfull[xb], kb * KB, (int)col0);
         issued_x = kbg + 1;
-        for (int sp = 0; sp < S; ++sp, ++it) {
+        for (int sp = 0; sp < p.nsl; ++sp, ++it) {
           const int st = (int)(it % A_STAGES);
           if (!mbar_wait(&aempty[st], ((uint32_t)(it / A_STAGES) & 1u) ^ 1u, &abort_s)) { ok = false; break; }
           mbar_expect_tx(&afull[st], A_BYTES);
@@ -426,12 +427,12 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
         if (!mbar_wait(&xfull[xb], (uint32_t)(kbg >> 1) & 1u, &abort_s)) { ok = false; break; }
         tc_fence_after();
         const uint32_t xs0 = smem_u32(x_buf + xb * X_SET);
-        for (int sp = 0; sp < S; ++sp, ++it) {
+        for (int sp = 0; sp < p.nsl; ++sp, ++it) {
           const int st = (int)(it % A_STAGES);
           if (!mbar_wait(&afull[st], (uint32_t)(it / A_STAGES) & 1u, &abort_s)) { ok = false; break; }
           tc_fence_after();
           const uint64_t ad = sw128_desc(smem_u32(a_ring + st * A_BYTES));
-          for (int q = 0; q + sp < S; ++q) {
+          for (int q = 0; q + sp < p.nsl; ++q) {
             const uint64_t bd = sw128_desc(xs0 + q * X_BYTES);
             const uint32_t d = tmem + (uint32_t)((sp + q) * BN);
 #pragma unroll
@@ -471,6 +472,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
         const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(part * 16);
 #pragma unroll
         for (int w = 0; w < S; ++w) {
+          if (w >= p.nsl) break;  // weights past the slices used hold nothing
           float v[16];
           tmem_ld16(base + (uint32_t)(w * BN), v);
 #pragma unroll
@@ -642,6 +644,7 @@ int OzakiResidual::residual(const double* x, int64_t ldx, const double* b, int64
   if (rc) return rc;
   OzParams p;
   memset(&p, 0, sizeof p);
+  p.nsl = S;
   p.kdim = n;
   p.nrt = (int)ceil_div(n, BM);
   p.nct = (int)ceil_div(nrhs, BN);
@@ -804,6 +807,7 @@ int OzakiSyrk::update(double* a, int64_t lda, int64_t k0, int pw, int64_t rs, in
   }
   OzParams p;
   memset(&p, 0, sizeof p);
+  p.nsl = S;
   p.kdim = w;
   p.nrt = (int)ceil_div(rs, BM);
   p.nct = (int)ceil_div(ncols, BN);
@@ -847,6 +851,7 @@ int OzakiSyrk::update_pq(double* a, int64_t lda, int64_t k0, int pw, int64_t rs,
   }
   OzParams p;
   memset(&p, 0, sizeof p);
+  p.nsl = S;
   p.kdim = PK;
   p.nrt = (int)ceil_div(rs, BM);
   p.nct = (int)ceil_div(rs, BN);
@@ -1008,11 +1013,13 @@ int OzakiGemm::attach(void* ws, int64_t mmax_, int64_t nmax_, int64_t kmax_) {
 }
 
 int OzakiGemm::run(double* c, int64_t ldc, int64_t m, int64_t n, int64_t k, const double* pa, int64_t p_rs,
-                   int64_t p_ks, const double* qa, int64_t q_rs, int64_t q_ks, int scale, int* err, cudaStream_t s) {
+                   int64_t p_ks, const double* qa, int64_t q_rs, int64_t q_ks, int scale, int* err, cudaStream_t s,
+                   int nsl) {
   if (m <= 0 || n <= 0 || k <= 0) return GBLLT_SUCCESS;
-  if (!pslices || m > mmax || n > nmax || k > kmax) return GBLLT_ERR_INTERNAL;
+  if (!pslices || m > mmax || n > nmax || k > kmax || nsl < 1 || nsl > S) return GBLLT_ERR_INTERNAL;
   static const std::string kp = "gemm_slices_f64";
   static const std::string kg = "gemm_tc_f64";
+  static const std::string kg28 = "gemm_tc_28bit";
   const int64_t w = oz_kpad(k);
   __nv_bfloat16* ps = (__nv_bfloat16*)pslices;
   __nv_bfloat16* qs = (__nv_bfloat16*)qslices;
@@ -1031,6 +1038,7 @@ int OzakiGemm::run(double* c, int64_t ldc, int64_t m, int64_t n, int64_t k, cons
   }
   OzParams p;
   memset(&p, 0, sizeof p);
+  p.nsl = S;
   p.kdim = k;
   p.nrt = (int)ceil_div(m, BM);
   p.nct = (int)ceil_div(n, BN);
@@ -1042,10 +1050,12 @@ int OzakiGemm::run(double* c, int64_t ldc, int64_t m, int64_t n, int64_t k, cons
   p.pexp = pexp;
   p.pexp_b = qexp;
   p.scale = scale;
+  p.nsl = nsl;
   p.err = err;
   const unsigned grid = (unsigned)(p.tiles < sms ? p.tiles : sms);
   {
-    ProfScope pr(kg.c_str(), s, 2.0 * m * n * k, 2.0 * m * n * 8.0 + (double)S * (m + n) * w * 2.0);
+    ProfScope pr(nsl == S ? kg.c_str() : kg28.c_str(), s, 2.0 * m * n * k,
+                 2.0 * m * n * 8.0 + (double)nsl * (m + n) * w * 2.0);
     oz_kernel<OZ_RECT><<<grid, THREADS, SMEM_BYTES, s>>>(maps, p);
   }
   GB_CUDA_TRY(cudaGetLastError());

@@ -64,6 +64,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_dposv_batched": (_int, [_vp, _vp, _vp, _vp]),
     "gbllt_sposv_batched": (_int, [_vp, _vp, _vp, _vp]),
     "gbllt_dpotrf_adjoint_dev": (_int, [_i64, _vp, _i64, _vp, _i64, _vp]),
+    "gbllt_dpotrf_adjoint_mixed_dev": (_int, [_i64, _vp, _i64, _vp, _i64, _vp]),
     "gbllt_dpotrs_adjoint_dev": (_int, [_i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _vp]),
     "gbllt_drank_update": (_int, [_int, _ch, _i64, _vp, _i64, _vp, ctypes.c_double, _i64p]),
     "gbllt_srank_update": (_int, [_int, _ch, _i64, _vp, _i64, _vp, ctypes.c_float, _i64p]),
@@ -358,9 +359,11 @@ def posv_mixed(a: np.ndarray, b: np.ndarray, opts: MixedOpts | None = None, uplo
     return x, rc, rep.as_dict()
 
 
-def potrf_adjoint_dev(l_cm, n: int, ldl: int, lbar_cm, ldlb: int, stream: int = 0) -> None:
-    """In place: lbar (df/dL, lower) becomes df/dA (lower triangle of the symmetric gradient)."""
-    check("gbllt_dpotrf_adjoint_dev", lib().gbllt_dpotrf_adjoint_dev(n, _ptr(l_cm), ldl, _ptr(lbar_cm), ldlb, stream))
+def potrf_adjoint_dev(l_cm, n: int, ldl: int, lbar_cm, ldlb: int, stream: int = 0, mixed: bool = False) -> None:
+    """In place: lbar (df/dL, lower) becomes df/dA (lower triangle of the symmetric gradient); mixed:
+    the panel products at 28 bits (gbllt_dpotrf_adjoint_mixed_dev)."""
+    fn = "gbllt_dpotrf_adjoint_mixed_dev" if mixed else "gbllt_dpotrf_adjoint_dev"
+    check(fn, getattr(lib(), fn)(n, _ptr(l_cm), ldl, _ptr(lbar_cm), ldlb, stream))
 
 
 def potrs_adjoint_dev(l_cm, n: int, ldl: int, x_cm, ldx: int, xbar_cm, ldxb: int, bbar_cm, ldbb: int, nrhs: int,

@@ -234,9 +234,17 @@ GBLLT_API int gbllt_sposv_batched(gbllt_batch_plan* plan, float* a, float* b, in
  * Gradients with respect to A are symmetric matrices G with df = sum_ij G_ij dA_ij for symmetric
  * dA; their lower triangle is stored. */
 /* d_lbar holds Lbar = df/dL (lower triangle) on entry and Abar = df/dA on return.  Blocked, in
- * place, from L only (no stored intermediates): n^3/3 flops, like the factorisation itself. */
+ * place, from L only (no stored intermediates): about 2 n^3 / 3 flops, twice the factorisation's;
+ * the products with each 64-wide panel run FP64-exact on the tensor cores, the rest on the FP64
+ * pipe.  A bounded wait that runs out leaves NaN in the gradient. */
 GBLLT_API int gbllt_dpotrf_adjoint_dev(int64_t n, const double* d_l, int64_t ldl, double* d_lbar, int64_t ldlb,
                                        void* stream);
+/* The same reverse sweep in mixed precision: the products with each panel carry 28 bits (four of
+ * the eight 7-bit slices of each operand, 10 of the 36 slice products), everything else stays FP64.
+ * The gradient is accurate to about FP32 level (relative error ~1e-7 or better on well-conditioned
+ * problems). */
+GBLLT_API int gbllt_dpotrf_adjoint_mixed_dev(int64_t n, const double* d_l, int64_t ldl, double* d_lbar,
+                                             int64_t ldlb, void* stream);
 /* For X = A^{-1} B (n x nrhs) with its adjoint Xbar: writes Bbar = A^{-1} Xbar and, when d_abar is
  * not NULL, accumulates Abar -= sym(Bbar X^T) into its lower triangle. */
 GBLLT_API int gbllt_dpotrs_adjoint_dev(int64_t n, int64_t nrhs, const double* d_l, int64_t ldl, const double* d_x,

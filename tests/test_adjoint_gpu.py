@@ -36,19 +36,22 @@ def gpu_factor(gbllt, a):
     return d
 
 
-@pytest.mark.parametrize("n", [1, 5, 31, 32, 33, 100, 257])
-def test_chol_adjoint_matches_reference(oracle, gbllt, n):
+@pytest.mark.parametrize("n", [1, 5, 31, 32, 33, 63, 64, 65, 100, 129, 257, 700])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_chol_adjoint_matches_reference(oracle, gbllt, n, mixed):
+    # FP64 adjoint within 1e-10 of the symbolic reference; the mixed-precision adjoint (28-bit panel
+    # products) within 1e-6
     a = oracle.gen_gram(n, seed=80 + n)
     dL = gpu_factor(gbllt, a)
     L = np.tril(_np(dL))
     rng = np.random.default_rng(n)
     Lbar = np.tril(rng.standard_normal((n, n)))
     M = _cm(Lbar)
-    gbllt.potrf_adjoint_dev(dL, n, n, M, n, _stream())
+    gbllt.potrf_adjoint_dev(dL, n, n, M, n, _stream(), mixed=mixed)
     torch.cuda.synchronize()
     got = np.tril(_np(M))
     ref = np.tril(oracle.chol_adjoint_ref(L, Lbar))
-    assert np.linalg.norm(got - ref) <= 1e-10 * np.linalg.norm(ref)
+    assert np.linalg.norm(got - ref) <= (1e-6 if mixed else 1e-10) * np.linalg.norm(ref)
 
 
 def _f_weights(gbllt, a, W):
@@ -74,6 +77,61 @@ def test_chol_adjoint_finite_differences(oracle, gbllt, n):
         fd = (_f_weights(gbllt, a + h * E, W) - _f_weights(gbllt, a - h * E, W)) / (2 * h)
         an = float(np.sum(G * E))
         assert abs(fd - an) <= 1e-6 * max(abs(an), 1.0), (fd, an)
+
+
+def _gp_gradient(gbllt, a, y, mixed):
+    """The GP objective's gradient through the hand-written adjoints: (dA lower, symmetric
+    convention, as a full symmetric matrix; dy)."""
+    n = a.shape[0]
+    s = _stream()
+    L = gpu_factor(gbllt, a)
+    alpha = torch.from_numpy(y.copy()).cuda().reshape(1, n)
+    gbllt.potrs_dev(L, n, n, alpha, 1, n, "L", s)
+    M = torch.zeros_like(L)
+    M.diagonal().copy_(2.0 / torch.diagonal(L))
+    gbllt.potrf_adjoint_dev(L, n, n, M, n, s, mixed=mixed)
+    bbar = torch.empty_like(alpha)
+    yt = torch.from_numpy(y.copy()).cuda().reshape(1, n)
+    gbllt.potrs_adjoint_dev(L, n, n, alpha, n, yt, n, bbar, n, 1, M, n, s)
+    torch.cuda.synchronize()
+    G = np.tril(_np(M))
+    return G + np.tril(G, -1).T, (alpha + bbar).cpu().numpy().reshape(n)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_gp_gradient_full_size_rbf(oracle, gbllt, mixed):
+    # the C5 problem size: an RBF kernel matrix of n = 2048 points (lengthscale 0.2, noise 1e-2).  The
+    # gradient of logdet A + y^T A^-1 y is A^-1 - a a^T (a = A^-1 y) in the symmetric convention, and
+    # 2 a for y: checked against that closed form (an FP64 cuSOLVER inverse), and the FP64 gradient
+    # against central finite differences (h = 1e-6) along three random symmetric directions.  Stated
+    # errors (relative, Frobenius): FP64 1e-8; mixed precision (28-bit panel products, amplified by the
+    # condition number, about 1e5 here) 1e-4.
+    n = 2048
+    a = oracle.gen_rbf(n, seed=31, ell=0.2, sigma2=1.0, noise=1e-2)
+    y = oracle.normal(32, n)
+    G, gy = _gp_gradient(gbllt, a, y, mixed)
+    A = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    Ainv = torch.cholesky_inverse(torch.linalg.cholesky(A)).cpu().numpy()
+    al = np.linalg.solve(a, y)
+    want = Ainv - np.outer(al, al)
+    tol = 1e-4 if mixed else 1e-8
+    assert np.linalg.norm(G - want) <= tol * np.linalg.norm(want)
+    assert np.linalg.norm(gy - 2.0 * al) <= 1e-10 * np.linalg.norm(al)
+    if mixed:
+        return
+
+    def f(ap):
+        Lp = np.linalg.cholesky(ap)
+        return 2.0 * np.sum(np.log(np.diag(Lp))) + float(y @ np.linalg.solve(ap, y))
+
+    rng = np.random.default_rng(5)
+    for _ in range(3):
+        E = rng.standard_normal((n, n)) * 1e-3
+        E = E + E.T
+        h = 1e-6
+        fd = (f(a + h * E) - f(a - h * E)) / (2 * h)
+        an = float(np.sum(G * E))
+        assert abs(fd - an) <= 1e-5 * max(abs(an), 1.0), (fd, an)
 
 
 class GPObjective(torch.autograd.Function):
