@@ -202,7 +202,8 @@ int host_posv(bool do_factor, bool do_solve, int layout, char uplo, int64_t n, i
   DevStatus* st = (DevStatus*)((char*)d_bt + ((bbytes + 255) / 256) * 256);
   int64_t* dinfo = (int64_t*)((char*)st + 256);  // the allocation reserves 2 x 256 B past d_bt
 
-  GB_CUDA_TRY(copy2d_async(d_a, n * es, a, lda * es, n * es, n, cudaMemcpyHostToDevice, s));
+  // only the stored triangle is read (and written) on the device
+  GB_CUDA_TRY(copy_triangle_async(upper, n, d_a, n, a, lda, es, cudaMemcpyHostToDevice, s));
   if (do_solve && nrhs > 0) {
     if (!rowmajor) {
       GB_CUDA_TRY(copy2d_async(d_b, n * es, b, ldb * es, n * es, nrhs, cudaMemcpyHostToDevice, s));
@@ -214,7 +215,7 @@ int host_posv(bool do_factor, bool do_solve, int layout, char uplo, int64_t n, i
   int64_t h_info = 0;
   if (do_factor) {
     if ((rc = factor_dev<T>(upper, n, d_a, n, st, dinfo, s))) return rc;
-    GB_CUDA_TRY(copy2d_async(a, lda * es, d_a, n * es, n * es, n, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(copy_triangle_async(upper, n, a, lda, d_a, n, es, cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaMemcpyAsync(&h_info, dinfo, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     if (h_info == GBLLT_ERR_TIMEOUT) return GBLLT_ERR_TIMEOUT;
@@ -344,7 +345,8 @@ extern "C" int gbllt_dposv_mixed(int layout, char uplo, int64_t n, int64_t nrhs,
   double* d_b = (double*)((char*)work.p + abytes);
   double* d_x = (double*)((char*)d_b + bbytes);
   double* d_t = (double*)((char*)d_x + bbytes);
-  GB_CUDA_TRY(copy2d_async(d_a, n * es, a, lda * es, n * es, n, cudaMemcpyHostToDevice, s));
+  // the solve reads only the stored triangle of A
+  GB_CUDA_TRY(copy_triangle_async(upper, n, d_a, n, a, lda, es, cudaMemcpyHostToDevice, s));
   if (!rowmajor) {
     GB_CUDA_TRY(copy2d_async(d_b, n * es, b, ldb * es, n * es, nrhs, cudaMemcpyHostToDevice, s));
   } else {

@@ -14,6 +14,23 @@ inline cudaError_t copy2d_async(void* dst, size_t dpitch, const void* src, size_
   return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, s);
 }
 
+// Copies the `upper ? upper : lower` triangle of a column-major n x n matrix (leading dimensions
+// dld / sld in elements of es bytes) in column panels of 256: each panel is one 2-D copy of its
+// diagonal block and the rows below it (above it for upper), so about half of the matrix moves.  The
+// other triangle of dst is left as it was.
+inline cudaError_t copy_triangle_async(bool upper, int64_t n, void* dst, size_t dld, const void* src, size_t sld,
+                                       size_t es, cudaMemcpyKind kind, cudaStream_t s) {
+  for (int64_t j0 = 0; j0 < n; j0 += 256) {
+    const int64_t jb = n - j0 < 256 ? n - j0 : 256;
+    const int64_t r0 = upper ? 0 : j0, rows = upper ? j0 + jb : n - j0;
+    const cudaError_t e =
+        cudaMemcpy2DAsync((char*)dst + ((size_t)j0 * dld + r0) * es, dld * es, (const char*)src + ((size_t)j0 * sld + r0) * es,
+                          sld * es, (size_t)rows * es, (size_t)jb, kind, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 // Plain-path panel width: the diagonal block factored by one CTA and the depth of each
 // trailing update.
 constexpr int kNB = 64;
@@ -175,6 +192,8 @@ struct OzakiResidual {
   OzakiResidual& operator=(const OzakiResidual&) = delete;
   ~OzakiResidual();
   static size_t bytes(int64_t n, int64_t nrhs);
+  // The device memory alone, stream-ordered on s (setup() reserves it itself when this was not called).
+  int reserve(int64_t n, int64_t nrhs, cudaStream_t s);
   int setup(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, cudaStream_t s);
   int residual(const double* x, int64_t ldx, const double* b, int64_t ldb, double* r, int64_t ldr, cudaStream_t s);
   // copies the device timeout word (1 if a bounded wait of the product kernel ran out) to host memory
@@ -228,6 +247,7 @@ struct OzakiGemm {
   void* qslices = nullptr;
   int* pexp = nullptr;
   int* qexp = nullptr;
+  unsigned long long* rmax = nullptr;  // row maxima of a column-major operand being sliced
   static size_t bytes(int64_t mmax, int64_t nmax, int64_t kmax);
   int attach(void* ws, int64_t mmax, int64_t nmax, int64_t kmax);
   int run(double* c, int64_t ldc, int64_t m, int64_t n, int64_t k, const double* p, int64_t p_rs, int64_t p_ks,

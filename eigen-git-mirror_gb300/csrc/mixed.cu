@@ -632,6 +632,14 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   if (may_allocate) {
     xs.caller = s;
     xs.armed = true;
+    // A's slices are reserved on the caller's stream, before the fork below, so that every call makes
+    // the same allocations on the same stream in the same order and the pool hands back the same
+    // blocks (an allocation on a fresh internal stream does not always reuse them)
+    if (use_oz) {
+      const int rc2 = oz.reserve(n, nrhs, s);
+      if (rc2 == GBLLT_ERR_ALLOC) use_oz = false;  // not enough device memory: the FP64 residual
+      else if (rc2) return rc2;
+    }
     int least = 0, greatest = 0;
     GB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     GB_CUDA_TRY(cudaStreamCreateWithPriority(&xs.fs, cudaStreamNonBlocking, greatest));

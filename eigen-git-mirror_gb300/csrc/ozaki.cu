@@ -574,10 +574,8 @@ size_t OzakiResidual::bytes(int64_t n, int64_t nrhs) {
          oz_up256((size_t)n * 4) + oz_up256((size_t)nrhs * 4) + 256 + 256;
 }
 
-int OzakiResidual::setup(bool upper, int64_t n_, int64_t nrhs_, const double* a, int64_t lda, cudaStream_t s) {
-  int sms = 0;
-  int rc = oz_prepare_device(&sms);
-  if (rc) return rc;
+int OzakiResidual::reserve(int64_t n_, int64_t nrhs_, cudaStream_t s) {
+  if (buf) return GBLLT_SUCCESS;
   n = n_;
   nrhs = nrhs_;
   stream = s;
@@ -587,6 +585,18 @@ int OzakiResidual::setup(bool upper, int64_t n_, int64_t nrhs_, const double* a,
     buf = nullptr;
     set_error_message("cudaMallocAsync failed (tensor-core residual slices)");
     return GBLLT_ERR_ALLOC;
+  }
+  return GBLLT_SUCCESS;
+}
+
+int OzakiResidual::setup(bool upper, int64_t n_, int64_t nrhs_, const double* a, int64_t lda, cudaStream_t s) {
+  int sms = 0;
+  int rc = oz_prepare_device(&sms);
+  if (rc) return rc;
+  if (!buf) {
+    if ((rc = reserve(n_, nrhs_, s))) return rc;
+  } else if (n_ != n || nrhs_ != nrhs) {
+    return GBLLT_ERR_INTERNAL;
   }
   char* q = (char*)buf;
   aslices = q;
@@ -973,15 +983,73 @@ __global__ void __launch_bounds__(256) oz_rows_slice_contig_kernel(const double*
   }
 }
 
-// Slices of one operand: the row-contiguous kernel when kstride is 1, else one thread per row.
-void oz_slice_rows(const double* src, long long rstride, long long kstride, long long rows, long long k, long long w,
-                   __nv_bfloat16* slices, long long sstride, int* pexp, cudaStream_t s) {
-  if (kstride == 1)
+// A column-major operand (rstride 1) in two passes spread over both dimensions: the row maxima by
+// 256-column chunks (atomicMax on the bit patterns of |v|, which order like the values), then the
+// slices of 64-column blocks, one thread per row and block.
+__global__ void __launch_bounds__(256) oz_colmajor_max_kernel(const double* __restrict__ src, long long kstride,
+                                                              long long rows, long long k,
+                                                              unsigned long long* __restrict__ rmax) {
+  const long long i = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (i >= rows) return;
+  const long long k0 = (long long)blockIdx.y * 256, k1 = k0 + 256 < k ? k0 + 256 : k;
+  unsigned long long mb = 0;
+  for (long long kk = k0; kk < k1; ++kk) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(src[i + kk * kstride]) & ~(1ull << 63);
+    mb = b > mb ? b : mb;
+  }
+  atomicMax(rmax + i, mb);
+}
+
+__global__ void __launch_bounds__(128) oz_colmajor_slice_kernel(const double* __restrict__ src, long long kstride,
+                                                                long long rows, long long k, long long w,
+                                                                const unsigned long long* __restrict__ rmax,
+                                                                __nv_bfloat16* __restrict__ slices, long long sstride,
+                                                                int* __restrict__ pexp) {
+  const long long i = (long long)blockIdx.x * 128 + threadIdx.x;
+  if (i >= rows) return;
+  const int e = scale_exp(__longlong_as_double((long long)rmax[i]));
+  if (blockIdx.y == 0) pexp[i] = e;
+  const long long pbeg = (long long)blockIdx.y * 64;
+#pragma unroll 1
+  for (long long p0 = pbeg; p0 < pbeg + 64 && p0 < w; p0 += 8) {
+    uint32_t packed[S][4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const long long pa = p0 + 2 * h, pb = pa + 1;
+      float lo[S], hi[S];
+      split8(pa < k ? src[i + pa * kstride] : 0.0, e, lo);
+      split8(pb < k ? src[i + pb * kstride] : 0.0, e, hi);
+#pragma unroll
+      for (int q = 0; q < S; ++q) {
+        const __nv_bfloat162 v2 = __floats2bfloat162_rn(lo[q], hi[q]);
+        packed[q][h] = *reinterpret_cast<const uint32_t*>(&v2);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < S; ++q)
+      *reinterpret_cast<uint4*>(slices + q * sstride + i * w + p0) =
+          make_uint4(packed[q][0], packed[q][1], packed[q][2], packed[q][3]);
+  }
+}
+
+// Slices of one operand: the row-contiguous kernel when kstride is 1, the two-pass column-major one
+// when rstride is 1 (rmax: rows words of scratch), else one thread per row.
+int oz_slice_rows(const double* src, long long rstride, long long kstride, long long rows, long long k, long long w,
+                  __nv_bfloat16* slices, long long sstride, int* pexp, unsigned long long* rmax, cudaStream_t s) {
+  if (kstride == 1) {
     oz_rows_slice_contig_kernel<<<(unsigned)ceil_div(rows, 32), 256, 0, s>>>(src, rstride, rows, k, w, slices, sstride,
                                                                            pexp);
-  else
+  } else if (rstride == 1 && rmax) {
+    GB_CUDA_TRY(cudaMemsetAsync(rmax, 0, (size_t)rows * 8, s));
+    oz_colmajor_max_kernel<<<dim3((unsigned)ceil_div(rows, 256), (unsigned)ceil_div(k, 256)), 256, 0, s>>>(
+        src, kstride, rows, k, rmax);
+    oz_colmajor_slice_kernel<<<dim3((unsigned)ceil_div(rows, 128), (unsigned)(w / 64)), 128, 0, s>>>(
+        src, kstride, rows, k, w, rmax, slices, sstride, pexp);
+  } else {
     oz_rows_slice_kernel<<<(unsigned)ceil_div(rows, 128), 128, 0, s>>>(src, rstride, kstride, rows, k, w, slices,
                                                                       sstride, pexp);
+  }
+  return GBLLT_SUCCESS;
 }
 
 inline int64_t oz_kpad(int64_t k) { return (k + KB - 1) / KB * KB; }
@@ -991,7 +1059,7 @@ inline int64_t oz_kpad(int64_t k) { return (k + KB - 1) / KB * KB; }
 size_t OzakiGemm::bytes(int64_t mmax, int64_t nmax, int64_t kmax) {
   const size_t w = (size_t)oz_kpad(kmax);
   return oz_up256((size_t)S * mmax * w * 2) + oz_up256((size_t)S * nmax * w * 2) + oz_up256((size_t)mmax * 4) +
-         oz_up256((size_t)nmax * 4);
+         oz_up256((size_t)nmax * 4) + oz_up256((size_t)(mmax > nmax ? mmax : nmax) * 8);
 }
 
 int OzakiGemm::attach(void* ws, int64_t mmax_, int64_t nmax_, int64_t kmax_) {
@@ -1009,6 +1077,8 @@ int OzakiGemm::attach(void* ws, int64_t mmax_, int64_t nmax_, int64_t kmax_) {
   pexp = (int*)q;
   q += oz_up256((size_t)mmax * 4);
   qexp = (int*)q;
+  q += oz_up256((size_t)nmax * 4);
+  rmax = (unsigned long long*)q;
   return GBLLT_SUCCESS;
 }
 
@@ -1025,8 +1095,9 @@ int OzakiGemm::run(double* c, int64_t ldc, int64_t m, int64_t n, int64_t k, cons
   __nv_bfloat16* qs = (__nv_bfloat16*)qslices;
   {
     ProfScope pr(kp.c_str(), s, 0.0, (double)(m + n) * k * 8.0 + (double)S * (m + n) * w * 2.0);
-    oz_slice_rows(pa, p_rs, p_ks, m, k, w, ps, (long long)m * w, pexp, s);
-    oz_slice_rows(qa, q_rs, q_ks, n, k, w, qs, (long long)n * w, qexp, s);
+    int rc = oz_slice_rows(pa, p_rs, p_ks, m, k, w, ps, (long long)m * w, pexp, rmax, s);
+    if (!rc) rc = oz_slice_rows(qa, q_rs, q_ks, n, k, w, qs, (long long)n * w, qexp, rmax, s);
+    if (rc) return rc;
   }
   OzMaps maps;
   for (int q = 0; q < S; ++q) {
