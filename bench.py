@@ -288,20 +288,27 @@ def measured_peaks() -> dict:
 # law that scales them to this run's launch (profiles/ holds the summaries with the commands):
 #   symm_residual_f64 (NR = 16 kernel): 1.628 GB at n = 8192, 64 RHS; A's stored tiles are read
 #     once per 16-column chunk of right-hand sides, so traffic grows as n^2 * ceil(k / 16).
-#   sweep_f32 (16-column chains): 143.9 MB at n = 8192, 64 RHS (mean of the forward and backward
-#     launch); the triangle of L is read once whatever k is, so traffic grows as n^2.
-#   tc_update_bf16: 15.3 MB per launch at n = 8192, the mean over the 158 launches of one BF16x6
-#     factorisation (in-panel, strip and look-ahead updates); the C traffic of a factorisation
-#     grows as n^3 and its launches as n, so the mean per launch grows as n^2.
+#   sweep_f32 (chains of 32 columns): 578 MB at n = 16384, 64 RHS (mean of the forward and backward
+#     launch); the triangle of L is read about once whatever k is, so traffic grows as n^2.
+#   tc_update_bf16: the look-ahead launch at n = 8192 moved 0.75 of its algorithmic bytes (C read and
+#     written once in FP32, the operand parts once; part of C stays in L2): the launch's algorithmic
+#     bytes times that ratio.
 NCU_TRAFFIC = {"symm_residual_f64": (8192, 64, 1.628e9, "n2_kchunks"),
-               "sweep_f32": (8192, 64, 1.439e8, "n2"),
-               "tc_update_bf16": (8192, 64, 1.530e7, "n2")}
+               "sweep_f32": (16384, 64, 5.78e8, "n2"),
+               "tc_update_bf16": (8192, 64, 0.75, "ratio")}
+TRAFFIC_SOURCE = {"n2_kchunks": "ncu dram__bytes_read.sum + dram__bytes_write.sum at n={n0}, {k0} RHS, scaled by "
+                                "n^2 ceil(k/16)",
+                  "n2": "ncu dram__bytes_read.sum + dram__bytes_write.sum at n={n0}, {k0} RHS, scaled by n^2",
+                  "ratio": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a look-ahead launch at n={n0}: "
+                           "{by} of its algorithmic bytes, applied to this launch's algorithmic bytes"}
 
 
-def ncu_traffic(name: str, n: int, k: int):
+def ncu_traffic(name: str, n: int, k: int, per_launch_bytes: float | None = None):
     if name not in NCU_TRAFFIC or k < 16:
         return None
     n0, k0, by, law = NCU_TRAFFIC[name]
+    if law == "ratio":
+        return by * per_launch_bytes if per_launch_bytes else None
     scale = (n / n0) ** 2
     if law == "n2_kchunks":
         scale *= (-(-k // 16)) / (-(-k0 // 16))
@@ -338,13 +345,14 @@ def roofline_for(name: str, st: dict, peaks: dict, n: int = 0, k: int = 0, nseg:
     else:
         bound, unit, peak, src = "hbm", "GB/s", peaks["hbm_gbs"], peaks["source"]["hbm_gbs"]
         ach = st["bytes"] / ms / 1e6
-    traffic = ncu_traffic(name, n, k)
+    traffic = ncu_traffic(name, n, k, st["bytes"] / st["launches"])
     per_launch = st["flops"] / st["launches"] / (products if name not in OZAKI_KERNELS else 1)
+    src_fmt = NCU_TRAFFIC[name] if name in NCU_TRAFFIC else None
     out = {"kernel": name, "bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
            "work": "algorithmic flops (one product per output and depth step)" if unit == "TFLOP/s"
            else "algorithmic bytes",
-           "traffic": traffic, "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at n=8192, "
-           f"64 RHS, scaled by {'n^2 ceil(k/16)' if NCU_TRAFFIC[name][3] == 'n2_kchunks' else 'n^2'}"
+           "traffic": traffic,
+           "traffic_source": TRAFFIC_SOURCE[src_fmt[3]].format(n0=src_fmt[0], k0=src_fmt[1], by=src_fmt[2])
            if traffic else None, "launches": st["launches"],
            "per_launch_flops": per_launch, "per_launch_bytes": st["bytes"] / st["launches"],
            "peak_source": src,

@@ -27,6 +27,9 @@ def test_llt_flops(bench):
 
 
 def test_ncu_traffic_scaling_laws(bench):
+    n0, k0, ratio, law = bench.NCU_TRAFFIC["tc_update_bf16"]
+    assert law == "ratio" and bench.ncu_traffic("tc_update_bf16", 32768, 64, 1e9) == pytest.approx(ratio * 1e9)
+    assert bench.ncu_traffic("tc_update_bf16", 32768, 64, None) is None
     n0, k0, by, _ = bench.NCU_TRAFFIC["sweep_f32"]
     assert bench.ncu_traffic("sweep_f32", n0, k0) == pytest.approx(by)
     assert bench.ncu_traffic("sweep_f32", 2 * n0, k0) == pytest.approx(4 * by)
