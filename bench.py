@@ -455,15 +455,21 @@ def measure_config(args, cfg, ws, rank, local, peaks, steps, warmup, profile_ste
         R = A0 @ Xs.T - B0.T
         return float(torch.linalg.norm(R) / (torch.linalg.norm(A0) * torch.linalg.norm(Xs)))
 
-    ms64, prof64, ck64 = timed(step_fp64, profile_steps[0])
-    assert int(info.item()) == 0, f"factorisation failed, info={int(info.item())}"
-    be64 = backward_error(B)
-    reports.clear()
-    msmx, profmx, ckmx = timed(step_mixed, profile_steps[1])
-    rcs = {rc for rc, _ in reports}
-    rep = reports[-1][1]
-    bemx = backward_error(X)
-    mixed_ok = rcs == {G.SUCCESS} and rep["converged"] and bemx <= 1e-14
+    # --arms fp64 / mixed (profiling a smaller case) times one arm only; that arm is then the headline
+    run64, runmx = args.arms != "mixed", args.arms != "fp64"
+    ms64 = prof64 = ck64 = be64 = msmx = profmx = ckmx = bemx = None
+    mixed_ok = False
+    if run64:
+        ms64, prof64, ck64 = timed(step_fp64, profile_steps[0])
+        assert int(info.item()) == 0, f"factorisation failed, info={int(info.item())}"
+        be64 = backward_error(B)
+    if runmx:
+        reports.clear()
+        msmx, profmx, ckmx = timed(step_mixed, profile_steps[1])
+        rcs = {rc for rc, _ in reports}
+        rep = reports[-1][1]
+        bemx = backward_error(X)
+        mixed_ok = rcs == {G.SUCCESS} and rep["converged"] and bemx <= 1e-14
 
     def arm(ms, prof, be, nprof, extra, seg=1):
         d = {"seconds_per_solve": ms / steps / 1e3, "tflops": ws * flops * steps / (ms * 1e-3) / 1e12,
@@ -480,14 +486,19 @@ def measure_config(args, cfg, ws, rank, local, peaks, steps, warmup, profile_ste
         d.update(extra)
         return d
 
-    fp64 = arm(ms64, prof64, be64, profile_steps[0], {"path": "plain FP64: gbllt_dpotrf_dev + gbllt_dpotrs_dev"})
-    mixed = arm(msmx, profmx, bemx, profile_steps[1],
-                {"path": f"gbllt_dposv_mixed_dev precision={args.mixed_precision}, FP64 residuals, tol 1e-14, "
-                         f"no fallback", "precision": args.mixed_precision, "reached_1e-14": mixed_ok,
-                 "steps": rep["steps"], "history": rep["history"], "factor_ms": rep["factor_ms"],
-                 "refine_ms": rep["refine_ms"]}, nseg)
-    use_mixed = mixed_ok and mixed["seconds_per_solve"] < fp64["seconds_per_solve"]
+    fp64 = mixed = None
+    if run64:
+        fp64 = arm(ms64, prof64, be64, profile_steps[0],
+                   {"path": "plain FP64: gbllt_dpotrf_dev + gbllt_dpotrs_dev"})
+    if runmx:
+        mixed = arm(msmx, profmx, bemx, profile_steps[1],
+                    {"path": f"gbllt_dposv_mixed_dev precision={args.mixed_precision}, FP64 residuals, tol 1e-14, "
+                             f"no fallback", "precision": args.mixed_precision, "reached_1e-14": mixed_ok,
+                     "steps": rep["steps"], "history": rep["history"], "factor_ms": rep["factor_ms"],
+                     "refine_ms": rep["refine_ms"]}, nseg)
+    use_mixed = mixed_ok and (fp64 is None or mixed["seconds_per_solve"] < fp64["seconds_per_solve"])
     head = mixed if use_mixed else fp64
+    assert head is not None, "the mixed arm alone did not reach backward error 1e-14"
     del A, B
     torch.cuda.empty_cache()
 
@@ -532,7 +543,8 @@ def measure_config(args, cfg, ws, rank, local, peaks, steps, warmup, profile_ste
     res = {"n": n, "nrhs": k, "kappa": cfg["kappa"], "fp64": fp64, "mixed": mixed, "use_mixed": use_mixed,
            "head": head, "ms_head": msmx if use_mixed else ms64, "clocks": ckmx if use_mixed else ck64,
            "clocks_fp64_arm": ck64, "e2e": e2e, "l2": l2_note, "flops": flops,
-           "mixed_over_fp64_speedup": fp64["seconds_per_solve"] / mixed["seconds_per_solve"] if mixed_ok else None}
+           "mixed_over_fp64_speedup": (fp64["seconds_per_solve"] / mixed["seconds_per_solve"]
+                                       if mixed_ok and fp64 is not None else None)}
     del A0, B0, X
     torch.cuda.empty_cache()
     return res
@@ -607,7 +619,7 @@ def run_ours(args, ws, rank, local):
     main = measure_config(args, cfg, ws, rank, local, peaks, K, W, (min(K, 5), K), max(3, min(K, 10)))
     head = main["head"]
     extras = {}
-    if args.config == DEFAULT_CONFIG and not args.no_extras:
+    if args.config == DEFAULT_CONFIG and not args.no_extras and args.arms == "both":
         extras["c3_sweep"] = c3_sweep(args, cfg["n"], main["fp64"]["seconds_per_solve"])
         c1 = measure_config(args, CONFIGS["c1"], ws, rank, local, peaks, max(K, 10), max(W, 3), (0, 0), 5,
                             clocks_on=False)
@@ -827,6 +839,8 @@ def main():
                     "kappa sweep and the C1 / C4 / C5 keys")
     ap.add_argument("--mixed-precision", default="bf16x6", choices=sorted(SPLIT_PRODUCTS))
     ap.add_argument("--n", type=int, default=0, help="override the order n (profiling a smaller case)")
+    ap.add_argument("--arms", choices=["both", "fp64", "mixed"], default="both",
+                    help="time one arm only (profiling); that arm is then the line's headline, without extras")
     ap.add_argument("--reserve-sms", type=int, default=0, help="SMs left to the panel factorisation while the "
                     "look-ahead update runs (0: the library's default)")
     args = ap.parse_args()

@@ -127,7 +127,7 @@ struct MixedLayout {
   int nb, zc, nparts, jpc, nsq;
   size_t es_k, bytes, fallback_bytes;
 };
-int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* out);  // defaults; -1 if invalid
+int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* out, int64_t n);  // defaults; -1 if invalid
 // lookahead: room for the second set of panel operands that the two-stream schedule uses.
 MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o, bool lookahead);
 // The solve on a caller-supplied workspace of ws_bytes (>= mixed_layout(.., may_allocate).bytes).

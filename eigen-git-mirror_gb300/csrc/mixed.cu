@@ -448,19 +448,24 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
 // SMs left to the panel factorisation while the look-ahead update of the previous panel runs.
 constexpr int kDefaultReserveSms = 24;
 
-int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o) {
+// Default outer panel width.  A wider panel makes each trailing update deeper (fewer passes of C
+// through HBM per flop) at the price of a longer panel factorisation; from n = 16384 on, 384 is the
+// faster width (n = 32768, BF16x6: 87 ms per factorisation against 93 ms at 256).
+int default_panel(int64_t n) { return n >= 16384 ? 384 : 256; }
+
+int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o, int64_t n) {
   memset(o, 0, sizeof *o);
   o->precision = GBLLT_PREC_TF32X3;
   o->max_steps = 10;
   o->tol = 1e-14;
   o->fallback_fp64 = 1;
-  o->panel = 256;
+  o->panel = default_panel(n);
   if (in) {
     *o = *in;
     if (o->max_steps <= 0) o->max_steps = 10;
     if (o->max_steps > 16) o->max_steps = 16;
     if (!(o->tol > 0)) o->tol = 1e-14;
-    if (o->panel <= 0) o->panel = 256;
+    if (o->panel <= 0) o->panel = default_panel(n);
   }
   if (o->reserve_sms == 0) o->reserve_sms = kDefaultReserveSms;
   if (o->precision < GBLLT_PREC_FP32 || o->precision > GBLLT_PREC_BF16X6) return -1;
@@ -779,7 +784,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
 int posv_mixed_dev(bool upper, int64_t n, int64_t nrhs, const double* a, int64_t lda, const double* b, int64_t ldb,
                    double* x, int64_t ldx, const gbllt_mixed_opts* opts, gbllt_mixed_report* rep, cudaStream_t s) {
   gbllt_mixed_opts o;
-  if (resolve_mixed_opts(opts, &o)) return -10;
+  if (resolve_mixed_opts(opts, &o, n)) return -10;
   const MixedLayout Ly = mixed_layout(n, nrhs, o, true);
   void* raw = nullptr;
   if (dev_malloc_async((void**)&raw, Ly.bytes, s) != cudaSuccess) {

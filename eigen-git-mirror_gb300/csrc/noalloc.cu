@@ -68,7 +68,7 @@ extern "C" int gbllt_dposv_mixed_dev_noalloc(char uplo, int64_t n, int64_t nrhs,
   if (n > 0 && nrhs > 0 && !d_x) return -8;
   if (ldx < (n > 1 ? n : 1)) return -9;
   gbllt_mixed_opts o;
-  if (resolve_mixed_opts(opts, &o)) return -10;
+  if (resolve_mixed_opts(opts, &o, n)) return -10;
   if (report) memset(report, 0, sizeof *report);
   if (n == 0 || nrhs == 0) return GBLLT_SUCCESS;
   const MixedLayout ly = mixed_layout(n, nrhs, o, false);

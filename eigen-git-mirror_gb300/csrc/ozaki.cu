@@ -24,8 +24,9 @@
 //
 // oz_kernel: persistent CTAs walking a list of 128-row x 64-column output tiles, 576 threads: a TMA
 // producer warp (A slice tiles through a 4-stage ring, the 8 X slice tiles of a 64-wide K block
-// double-buffered, running ahead across tiles), an MMA warp (tcgen05.mma M = 128, N = 64, K = 16,
-// 144 per K block) and 16 epilogue warps (four per TMEM lane quadrant, 16 columns each).  The same
+// double-buffered, running ahead across tiles), an MMA warp (tcgen05.mma M = 128, K = 16, N = 64 to
+// 256: the pairs of one A slice with up to four X slices in one instruction, 48 per K block) and 16
+// epilogue warps (four per TMEM lane quadrant, 16 columns each).  The same
 // kernel forms the residual (K = n, chunks of 256) and the trailing update of the FP64 factorisation
 // (K = one 64-wide panel, one chunk, C -= product on the lower tiles).  Every mbarrier wait is bounded.
 // A non-finite value in A or X makes the whole residual NaN, which the refinement reports as
@@ -410,8 +411,11 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
         mbar_wait(&xfull[k & 1], (uint32_t)(k >> 1) & 1u, &dummy);
     }
   } else if (warp == 1 && lane == 0) {
-    // ---- MMA issuer: pairs (p, q) with p + q <= S - 1 (0-based) into accumulator w = p + q
-    constexpr uint32_t idesc = instr_desc_mn(1u, BM, BN);
+    // ---- MMA issuer: pairs (p, q) with p + q <= S - 1 (0-based) into accumulator w = p + q.  The X
+    // slices of a K block sit back to back in shared memory (64 rows each, whole 1024-byte swizzle
+    // atoms) and the accumulators of q = 0, 1, ... in consecutive TMEM columns, so one MMA with
+    // N = 64 * (number of slices) covers up to four pairs of the same A slice: the A tile is read
+    // once per 256 columns instead of once per 64.
     long long kbg = 0, it = 0, chunkg = 0;
     bool ok = true;
     for (long long t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
@@ -432,9 +436,11 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
           if (!mbar_wait(&afull[st], (uint32_t)(it / A_STAGES) & 1u, &abort_s)) { ok = false; break; }
           tc_fence_after();
           const uint64_t ad = sw128_desc(smem_u32(a_ring + st * A_BYTES));
-          for (int q = 0; q + sp < p.nsl; ++q) {
-            const uint64_t bd = sw128_desc(xs0 + q * X_BYTES);
-            const uint32_t d = tmem + (uint32_t)((sp + q) * BN);
+          for (int q0 = 0; q0 + sp < p.nsl; q0 += 4) {
+            const int nq = p.nsl - sp - q0 < 4 ? p.nsl - sp - q0 : 4;
+            const uint32_t idesc = instr_desc_mn(1u, BM, nq * BN);
+            const uint64_t bd = sw128_desc(xs0 + q0 * X_BYTES);
+            const uint32_t d = tmem + (uint32_t)((sp + q0) * BN);
 #pragma unroll
             for (int j = 0; j < KB / 16; ++j)  // 32 bytes along K per MMA: +2 in the (addr >> 4) field
               mma<0>(d, ad + 2 * j, bd + 2 * j, idesc, (first && sp == 0 && j == 0) ? 0u : 1u);

@@ -76,6 +76,32 @@ def test_mixed_sizes(oracle, gbllt, n, nrhs, residual):
     assert oracle.backward_error(a, x, b) <= 1e-14
 
 
+@pytest.mark.parametrize("panel", [64, 128, 192, 320, 384, 512])
+@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3", "bf16x6"])
+def test_mixed_panel_widths(oracle, gbllt, spectra, panel, prec):
+    # outer panels of any multiple of 64 (the default is 256 below n = 16384 and 384 from there on):
+    # a ragged last panel (1536 = 4 * 384 = 3 * 512), the look-ahead split and the in-panel updates
+    pytest.importorskip("torch")
+    a = spectra[1e4]
+    n = a.shape[0]
+    b = np.asfortranarray(oracle.normal(13, n * 5).reshape(n, 5, order="F"))
+    rc, rep, x = _dev_solve(gbllt, a, b, gbllt.mixed_opts(prec, 10, 1e-14, fallback=False, panel=panel))
+    assert rc == gbllt.SUCCESS and rep["converged"] and not rep["used_fallback"], rep
+    assert oracle.backward_error(a, x, b) <= 1e-14
+    assert rep["history"][0] <= 1e-5
+
+
+def test_mixed_panel_width_checked(gbllt):
+    import torch
+    n = 100
+    A = torch.eye(n, dtype=torch.float64, device="cuda")
+    B = torch.ones(1, n, dtype=torch.float64, device="cuda")
+    X = torch.zeros_like(B)
+    rc, _ = gbllt.posv_mixed_dev(A, n, n, B, n, X, n, 1, gbllt.mixed_opts("bf16x6", panel=100), "L", 0,
+                                 raise_on_error=False)
+    assert rc == -10  # LAPACK-style: argument 10 (opts) is invalid
+
+
 @pytest.mark.parametrize("prec", ["tf32x3", "bf16x3"])
 def test_mixed_upper_and_host_api(oracle, gbllt, prec):
     n, k = 900, 2
