@@ -23,8 +23,10 @@
 // accumulation aligns each step's products to the running sum, so small terms added to a large
 // sum lose low bits.  A tile therefore runs two passes over K when the last segment is hi*hi: the
 // cross terms of every K-block first (the sum stays small), then hi*hi with only the hi parts
-// loaded.  A 128 x 256 tile of a 3-part split then performs 128 flops per byte it loads (170 in
-// one pass), against 64 for a 128 x 128 tile that loads one part pair per product.
+// loaded, NP K-blocks to a stage (one K-block's hi parts would feed too few MMAs to cover the
+// copies' latency with the ring's few stages).  A 128 x 256 tile of a 3-part split then performs
+// 128 flops per byte it loads (170 in one pass), against 64 for a 128 x 128 tile that loads one
+// part pair per product.
 //
 // Every mbarrier wait is bounded; on timeout the kernel raises an error flag, waits (bounded)
 // for its own TMA copies, frees its TMEM and returns.
@@ -123,7 +125,10 @@ __global__ void __launch_bounds__(THREADS, 1) tc_update_kernel(const __grid_cons
   constexpr int KI = KIND == 0 ? 16 : 8;               // K of one MMA instruction
   constexpr int MMAS = KE / KI;                        // MMAs per K-block and segment (2)
   const int nk = (p.k + KE - 1) / KE;                  // K-blocks
-  const int nkt = p.two_pass ? 2 * nk : nk;            // stages per tile (two passes: nk each)
+  // stages per tile: one per K-block; in a second (hi*hi) pass each stage carries the hi parts of
+  // NP K-blocks in its NP part slots, so that pass keeps as many MMAs in flight per stage
+  const int nk2 = p.two_pass ? (nk + NP - 1) / NP : 0;
+  const int nkt = nk + nk2;
 
   if (threadIdx.x == 0) {
     abort_s = 0;
@@ -159,15 +164,24 @@ __global__ void __launch_bounds__(THREADS, 1) tc_update_kernel(const __grid_cons
         const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
         if (!mbar_wait(&empty_bar[s], ph ^ 1u, &abort_s)) break;
         uint8_t* st = smem + s * S::STAGE;
-        const bool hi_only = kt >= nk;  // second pass: the hi parts only
-        const int kk = hi_only ? kt - nk : kt;
-        const int nq = hi_only ? 1 : NP;
-        mbar_expect_tx(&full_bar[s], nq * (S::A_PART + S::B_PART));
+        if (kt < nk) {  // all NP parts of K-block kt, part q in slot q
+          mbar_expect_tx(&full_bar[s], NP * (S::A_PART + S::B_PART));
 #pragma unroll
-        for (int q = 0; q < NP; ++q) {
-          if (q < nq) {
-            tma_load_2d(st + q * S::A_PART, &maps.a[q], &full_bar[s], kk * KE, p.a_row0 + row0);
-            tma_load_2d(st + NP * S::A_PART + q * S::B_PART, &maps.b[q], &full_bar[s], kk * KE, p.b_row0 + col0);
+          for (int q = 0; q < NP; ++q) {
+            tma_load_2d(st + q * S::A_PART, &maps.a[q], &full_bar[s], kt * KE, p.a_row0 + row0);
+            tma_load_2d(st + NP * S::A_PART + q * S::B_PART, &maps.b[q], &full_bar[s], kt * KE, p.b_row0 + col0);
+          }
+        } else {  // second pass: the hi parts of K-blocks kb0 .. kb0 + nq - 1, K-block kb0 + q in slot q
+          const int kb0 = (kt - nk) * NP;
+          const int nq = nk - kb0 < NP ? nk - kb0 : NP;
+          mbar_expect_tx(&full_bar[s], nq * (S::A_PART + S::B_PART));
+#pragma unroll
+          for (int q = 0; q < NP; ++q) {
+            if (q < nq) {
+              tma_load_2d(st + q * S::A_PART, &maps.a[0], &full_bar[s], (kb0 + q) * KE, p.a_row0 + row0);
+              tma_load_2d(st + NP * S::A_PART + q * S::B_PART, &maps.b[0], &full_bar[s], (kb0 + q) * KE,
+                          p.b_row0 + col0);
+            }
           }
         }
         issued = it + 1;
@@ -198,17 +212,27 @@ __global__ void __launch_bounds__(THREADS, 1) tc_update_kernel(const __grid_cons
         if (!mbar_wait(&full_bar[s], ph, &abort_s)) { ok = false; break; }
         tc_fence_after();
         const uint32_t st = smem_u32(smem + s * S::STAGE);
-        // one pass: every segment; two passes: segments 0 .. nseg-2, then the last one (hi*hi)
-        const int seg0 = (p.two_pass && kt >= nk) ? p.nseg - 1 : 0;
-        const int seg1 = (p.two_pass && kt < nk) ? p.nseg - 1 : p.nseg;
-        for (int seg = seg0; seg < seg1; ++seg) {
-          const uint32_t code = (p.seg_code >> (4 * seg)) & 0xFu;
-          const uint64_t ad = sw64_desc(st + (code & 3u) * S::A_PART);
-          const uint64_t bd = sw64_desc(st + NP * S::A_PART + (code >> 2) * S::B_PART);
+        if (kt < nk) {
+          // one pass: every segment; two passes: segments 0 .. nseg-2 here, the last one (hi*hi) below
+          const int seg1 = p.two_pass ? p.nseg - 1 : p.nseg;
+          for (int seg = 0; seg < seg1; ++seg) {
+            const uint32_t code = (p.seg_code >> (4 * seg)) & 0xFu;
+            const uint64_t ad = sw64_desc(st + (code & 3u) * S::A_PART);
+            const uint64_t bd = sw64_desc(st + NP * S::A_PART + (code >> 2) * S::B_PART);
 #pragma unroll
-          for (int j = 0; j < MMAS; ++j) {
-            // advance 32 bytes along K inside the 64-byte swizzle row: +2 in the (addr >> 4) field
-            mma<KIND>(d_tmem, ad + 2 * j, bd + 2 * j, idesc, (kt > 0 || seg > seg0 || j > 0) ? 1u : 0u);
+            for (int j = 0; j < MMAS; ++j) {
+              // advance 32 bytes along K inside the 64-byte swizzle row: +2 in the (addr >> 4) field
+              mma<KIND>(d_tmem, ad + 2 * j, bd + 2 * j, idesc, (kt > 0 || seg > 0 || j > 0) ? 1u : 0u);
+            }
+          }
+        } else {  // second pass: hi*hi of the K-blocks held in the stage's slots
+          const int kb0 = (kt - nk) * NP;
+          const int nq = nk - kb0 < NP ? nk - kb0 : NP;
+          for (int q = 0; q < nq; ++q) {
+            const uint64_t ad = sw64_desc(st + q * S::A_PART);
+            const uint64_t bd = sw64_desc(st + NP * S::A_PART + q * S::B_PART);
+#pragma unroll
+            for (int j = 0; j < MMAS; ++j) mma<KIND>(d_tmem, ad + 2 * j, bd + 2 * j, idesc, 1u);
           }
         }
         mma_commit(&empty_bar[s]);
