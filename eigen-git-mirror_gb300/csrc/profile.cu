@@ -22,6 +22,7 @@ struct Rec {
   int kind;
   cudaEvent_t e0, e1;
   double flops, bytes;
+  cudaStream_t stream;
 };
 std::vector<Rec> g_recs;
 std::vector<std::string> g_kinds;
@@ -55,6 +56,7 @@ ProfScope::ProfScope(const char* kind, cudaStream_t s, double flops, double byte
   r.e1 = take_event();
   r.flops = flops;
   r.bytes = bytes;
+  r.stream = s;
   cudaEventRecord(r.e0, s);
   g_recs.push_back(r);
   slot = (int)g_recs.size() - 1;
@@ -111,6 +113,33 @@ int gbllt_profile_read(gbllt_kernel_stat* out, int max_entries, int* n_entries) 
       if (cnt < max_entries) out[cnt] = a;
       ++cnt;
     }
+  *n_entries = cnt;
+  return GBLLT_SUCCESS;
+}
+
+int gbllt_profile_trace(gbllt_launch_record* out, int max_entries, int* n_entries) {
+  if (!out && max_entries > 0) return -1;
+  if (!n_entries) return -3;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  const int cnt = (int)g_recs.size();
+  for (int i = 0; i < cnt && i < max_entries; ++i) {
+    const Rec& r = g_recs[i];
+    if (cudaEventSynchronize(r.e1) != cudaSuccess) {
+      cudaGetLastError();
+      return GBLLT_ERR_CUDA;
+    }
+    gbllt_launch_record& o = out[i];
+    memset(&o, 0, sizeof o);
+    strncpy(o.name, g_kinds[r.kind].c_str(), sizeof(o.name) - 1);
+    o.stream = (uint64_t)(uintptr_t)r.stream;
+    float t0 = 0.f, t1 = 0.f;
+    cudaEventElapsedTime(&t0, g_recs[0].e0, r.e0);
+    cudaEventElapsedTime(&t1, g_recs[0].e0, r.e1);
+    o.start_ms = t0;
+    o.end_ms = t1;
+    o.flops = r.flops;
+    o.bytes = r.bytes;
+  }
   *n_entries = cnt;
   return GBLLT_SUCCESS;
 }

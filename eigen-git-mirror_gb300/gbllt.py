@@ -97,6 +97,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_spocon": (_int, [_int, _ch, _i64, _vp, _i64, ctypes.c_float, _fp]),
     "gbllt_profile_enable": (_int, [_int]),
     "gbllt_profile_read": (_int, [_vp, _int, ctypes.POINTER(_int)]),
+    "gbllt_profile_trace": (_int, [_vp, _int, ctypes.POINTER(_int)]),
     "gbllt_selftest_wait_timeout": (_int, [_i64, ctypes.POINTER(_int)]),
 }
 
@@ -109,6 +110,11 @@ class KernelStat(ctypes.Structure):
 
 
 PREC = {"fp32": 0, "tf32": 1, "tf32x3": 2, "bf16": 3, "bf16x3": 4, "bf16x6": 5}
+
+
+class LaunchRecord(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 40), ("stream", ctypes.c_uint64), ("start_ms", ctypes.c_double),
+                ("end_ms", ctypes.c_double), ("flops", ctypes.c_double), ("bytes", ctypes.c_double)]
 
 
 class MixedOpts(ctypes.Structure):
@@ -575,3 +581,16 @@ def profile_read() -> dict[str, dict]:
         out[s.name.decode()] = dict(launches=int(s.launches), ms=float(s.ms), flops=float(s.flops),
                                     bytes=float(s.bytes))
     return out
+
+
+def profile_trace(cap: int = 1 << 20) -> list[dict]:
+    """Every launch recorded since profile_enable, in launch order: kernel class, stream, device
+    start / end (ms after the first recorded launch), algorithmic flops and bytes."""
+    cnt = _int(0)
+    check("gbllt_profile_trace", lib().gbllt_profile_trace(None, 0, ctypes.byref(cnt)))
+    n = min(cnt.value, cap)
+    arr = (LaunchRecord * max(n, 1))()
+    check("gbllt_profile_trace", lib().gbllt_profile_trace(ctypes.cast(arr, _vp), n, ctypes.byref(cnt)))
+    return [dict(name=arr[i].name.decode(), stream=int(arr[i].stream), start_ms=float(arr[i].start_ms),
+                 end_ms=float(arr[i].end_ms), flops=float(arr[i].flops), bytes=float(arr[i].bytes))
+            for i in range(n)]

@@ -375,6 +375,21 @@ GBLLT_API int gbllt_profile_enable(int on);
 /* Wait for the recorded launches and return up to max_entries classes; *n_entries = classes seen. */
 GBLLT_API int gbllt_profile_read(gbllt_kernel_stat* out, int max_entries, int* n_entries);
 
+/* One recorded launch: its kernel class, the stream it ran on, and its start and end on the device,
+ * in ms after the first launch recorded since gbllt_profile_enable (events on the launch's stream,
+ * so concurrent launches on different streams overlap in time). */
+typedef struct {
+  char name[40];
+  uint64_t stream;
+  double start_ms;
+  double end_ms;
+  double flops;
+  double bytes;
+} gbllt_launch_record;
+/* Wait for the recorded launches and return the first max_entries of them in launch order;
+ * *n_entries = launches recorded.  No counterpart in the reference (a tracing aid). */
+GBLLT_API int gbllt_profile_trace(gbllt_launch_record* out, int max_entries, int* n_entries);
+
 /* Failure-detection self-test of the device-side bounded waits.  No counterpart in the reference
  * (Eigen's LLT runs on one CPU thread and never waits on another).  Every wait of the library's
  * kernels (the solve's look-back flags, the tensor-core pipelines' mbarriers, the rank update's

@@ -93,6 +93,19 @@ def test_tensor_path_failing_column(oracle, gbllt, k, uplo):
     assert gbllt.potrf(f, uplo) == k + 1
 
 
+@pytest.mark.parametrize("k", [300, 1000, 4400])
+def test_tensor_path_failing_column_lookahead(oracle, gbllt, k):
+    # from n = 4096 the trailing updates run one panel ahead on a side stream: a failing pivot there
+    # stops the updates still queued and reports the oracle's column
+    n = 4500
+    a = oracle.gen_gram(n, seed=6)
+    a[k, k] = -1.0
+    assert oracle.blocked(np.array(a, order="F")) == k
+    for uplo in ("L", "U"):
+        f = np.array(a, order="F")
+        assert gbllt.potrf(f, uplo) == k + 1
+
+
 def test_tensor_path_loses_definiteness_mid_factorisation(oracle, gbllt):
     # A = G G^T/n + s I with s just below -lambda_min(G G^T/n) at a late column: the failure comes
     # from the accumulated trailing updates, not from an input diagonal entry
