@@ -224,19 +224,29 @@ void symm_residual_fp64(bool upper, int64_t n, int64_t nrhs, const double* a, in
 
 // ---- deterministic sums of squares ------------------------------------------------------------
 
-// mode 0: column-major m x k block (ld);  mode 1/2: symmetric matrix from its lower/upper triangle
+// mode 0: column-major m x k block (ld);  mode 1/2: symmetric matrix from its lower/upper triangle.
+// The work is cut into tasks of SUMSQ_ROWS rows of one column; block b takes the tasks b,
+// b + gridDim.x, ... and thread t the rows t, t + 256, ... of each: a fixed order, so the sum does not
+// depend on timing, and one index division per task instead of one per element (with a division per
+// element the pass over A took milliseconds and crowded the first panel of the factorisation that
+// runs beside it).
+constexpr long long SUMSQ_ROWS = 2048;
 __global__ void __launch_bounds__(256) sumsq_kernel(const double* __restrict__ a, long long ld, long long m, long long k,
                                                     int mode, double* __restrict__ part) {
   __shared__ double red[256];
   double s = 0.0;
-  const long long total = m * k;
-  for (long long idx = (long long)blockIdx.x * 256 + threadIdx.x; idx < total; idx += (long long)gridDim.x * 256) {
-    const long long j = idx / m, i = idx % m;
+  const long long per_col = (m + SUMSQ_ROWS - 1) / SUMSQ_ROWS;
+  for (long long t = blockIdx.x; t < k * per_col; t += gridDim.x) {
+    const long long j = t / per_col, c = t - j * per_col;
+    long long i0 = c * SUMSQ_ROWS, i1 = i0 + SUMSQ_ROWS < m ? i0 + SUMSQ_ROWS : m;
     // the triangle that is not stored is never read (it may hold anything, NaN included)
-    const bool in = mode == 0 || (mode == 1 ? i >= j : i <= j);
-    if (!in) continue;
-    const double v = a[j * ld + i];
-    s += (mode == 0 || i == j ? 1.0 : 2.0) * v * v;
+    if (mode == 1 && i0 < j) i0 = j;
+    if (mode == 2 && i1 > j + 1) i1 = j + 1;
+    const double* col = a + j * ld;
+    for (long long i = i0 + threadIdx.x; i < i1; i += 256) {
+      const double v = col[i];
+      s += (mode == 0 || i == j ? 1.0 : 2.0) * v * v;
+    }
   }
   red[threadIdx.x] = s;
   __syncthreads();
@@ -403,9 +413,10 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
     }
     if (rs > 0 && prec != GBLLT_PREC_FP32) {
       void* const* pp = (lookahead && (iter & 1)) ? parts2 : parts;
-      // the operand buffers about to be overwritten were last read by the side update two panels ago,
-      // and the columns of the next panel were last written by the previous side update
-      if (lookahead && side_pending) GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[2 + ((iter + 1) & 1)], 0));
+      // the operand buffers about to be overwritten were last read by the side update two panels ago
+      // (waited for here), and the columns of the next panel were last written by the previous side
+      // update (waited for before the strip below, so that the split overlaps that update)
+      if (lookahead && iter >= 2) GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[2 + (iter & 1)], 0));
       {
         ProfScope ps(ksplit.c_str(), s, 0.0, (double)rs * bs * 4.0 + (double)rs * ldk * (kind == kTcBF16 ? 2 : 4) * np);
         dim3 grid((unsigned)ceil_div(rs, TS), (unsigned)ceil_div(ldk, TS));
@@ -414,6 +425,7 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
         else
           split_panel_kernel<1><<<grid, 256, 0, s>>>(af, ldf, k0 + bs, k0, rs, bs, np, pp[0], pp[1], pp[2], ldk);
       }
+      if (lookahead && side_pending) GB_CUDA_TRY(cudaStreamWaitEvent(s, ev[2 + ((iter + 1) & 1)], 0));
       TcOperand op{{pp[0], pp[1], pp[2]}, rs, bs, ldk, 0};
       float* c0 = af + (k0 + bs) * ldf + (k0 + bs);
       int rc;
@@ -553,8 +565,9 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   };
 
   auto sumsq_on = [&](const double* p, int64_t ld, int64_t m, int64_t k, int mode, double* out, cudaStream_t st_) {
-    int blocks = (int)((m * k + 255) / 256);
-    blocks = blocks < 1 ? 1 : (blocks > nsq ? nsq : blocks);
+    const int64_t tasks = k * ((m + SUMSQ_ROWS - 1) / SUMSQ_ROWS);
+    int blocks = (int)(tasks < nsq ? tasks : nsq);
+    blocks = blocks < 1 ? 1 : blocks;
     sumsq_kernel<<<blocks, 256, 0, st_>>>(p, ld, m, k, mode, sq);
     sum_parts_kernel<<<1, 256, 0, st_>>>(sq, blocks, out);
   };
