@@ -497,6 +497,9 @@ struct BatchPlan {
   int grid = 0;
   size_t smem = 0;
   double tuned_ms[kNumVariants] = {};
+  // the FP32 plan of the same sizes that the mixed-precision solve factors with (made and tuned on
+  // its first call)
+  BatchPlan* f32 = nullptr;
   // cached graph
   cudaGraphExec_t exec = nullptr;
   void* g_a = nullptr;
@@ -609,6 +612,7 @@ int batch_plan_create(int64_t count, const int64_t* n, int elem, BatchPlan** out
 
 void batch_plan_destroy(BatchPlan* p) {
   if (!p) return;
+  batch_plan_destroy(p->f32);
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->dev) cudaFree(p->dev);
   delete p;
@@ -725,6 +729,363 @@ int batch_run(BatchPlan* p, T* a, T* b, int64_t* info, bool use_graph, cudaStrea
 
 template int batch_run<double>(BatchPlan*, double*, double*, int64_t*, bool, cudaStream_t);
 template int batch_run<float>(BatchPlan*, float*, float*, int64_t*, bool, cudaStream_t);
+
+// ---- batched mixed precision: FP32 factorisation, FP64 refinement --------------------------------
+//
+// Each FP64 system is rounded to FP32 and factored, with its first solve, by the FP32 batched kernel
+// (dsposv's scheme per system, as gbllt_dposv_mixed_dev does for one large system).  The refinement
+// then runs one launch per step for the whole batch, CTAs pulling systems from the largest-first
+// queue: r = b - A x in FP64 from A's lower triangle, the normwise backward error
+// ||r||_F / (||A||_F ||x||_F) against tol, and while it is above, x += L^{-T} L^{-1} r with the FP32
+// factor (r scaled by its largest entry before the rounding).  A system leaves the queue's work once
+// it converged, its FP32 factorisation failed, or the last step checked it.
+
+namespace {
+
+enum : int { kMxActive = 0, kMxDone = 1, kMxFailed = 2, kMxStalled = 3 };
+
+// The lower triangle of every system rounded to FP32 (same packed layout), and b.  A warp per column.
+__global__ void __launch_bounds__(256) round_lower_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                                                          float* __restrict__ af, float* __restrict__ bf,
+                                                          const int* __restrict__ nv, const int64_t* __restrict__ aoff,
+                                                          const int64_t* __restrict__ boff, int count) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int s = blockIdx.x; s < count; s += gridDim.x) {
+    const int n = nv[s];
+    const double* A = a + aoff[s];
+    float* F = af + aoff[s];
+    for (int j = warp; j < n; j += 8)
+      for (int i = j + lane; i < n; i += 32) F[(long long)j * n + i] = (float)A[(long long)j * n + i];
+    for (int i = threadIdx.x; i < n; i += 256) bf[boff[s] + i] = (float)b[boff[s] + i];
+  }
+}
+
+struct RefineArgs {
+  const double* a;       // FP64 systems (lower triangles read)
+  const double* b;
+  double* x;             // iterates, laid out like b
+  const float* lf;       // FP32 factors (lower), laid out like a
+  const float* xf;       // FP32 first solutions, laid out like b
+  const int64_t* info32; // FP32 factorisation info
+  int64_t* info;
+  int* state;            // kMx* per system
+  double* anorm2;        // ||A||_F^2 per system (formed at step 0)
+  const int* order;
+  const int* n;
+  const int64_t* aoff;
+  const int64_t* boff;
+  int count;
+  int* counter;          // queue ticket, zeroed before each launch
+  int* active;           // systems corrected by this launch
+  int* done;             // systems converged so far
+  unsigned long long* maxbe;  // the largest backward error at the systems' last checks (bit pattern)
+  int step, last;
+  double tol;
+};
+
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) refine_batch_kernel(RefineArgs p) {
+  constexpr int NW = THREADS / 32;
+  __shared__ double xs[kMaxBatchN];
+  __shared__ double rs[kMaxBatchN];
+  __shared__ __align__(16) float rf[kMaxBatchN];
+  __shared__ __align__(16) float Dg[32 * kDgLd];
+  __shared__ double red[4][NW];
+  __shared__ int s_ticket;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (;;) {
+    if (tid == 0) s_ticket = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int t = s_ticket;
+    __syncthreads();
+    if (t >= p.count) break;
+    const int sys = p.order[t];
+    const int n = p.n[sys];
+    int st = p.state[sys];
+    if (p.step == 0) {
+      st = p.info32[sys] != 0 ? kMxFailed : kMxActive;
+      if (tid == 0) {
+        p.state[sys] = st;
+        if (st == kMxFailed) p.info[sys] = p.info32[sys];
+      }
+    }
+    if (st != kMxActive) continue;  // uniform over the CTA
+    const double* A = p.a + p.aoff[sys];
+    const double* B = p.b + p.boff[sys];
+    double* X = p.x + p.boff[sys];
+    for (int i = tid; i < n; i += THREADS) xs[i] = p.step == 0 ? (double)p.xf[p.boff[sys] + i] : X[i];
+    __syncthreads();
+    // r = b - A x.  Rows over the threads for the part on and left of the diagonal (a column of the
+    // lower triangle at a time, coalesced); then a warp per column for the part right of it.
+    double a2 = 0.0;
+    for (int i = tid; i < n; i += THREADS) {
+      double r = B[i];
+      for (int j = 0; j <= i; ++j) {
+        const double v = A[(long long)j * n + i];
+        r = fma(-v, xs[j], r);
+        if (p.step == 0) a2 += (i == j ? 1.0 : 2.0) * v * v;
+      }
+      rs[i] = r;
+    }
+    __syncthreads();
+    for (int j = warp; j < n; j += NW) {
+      double sacc = 0.0;
+      for (int i = j + 1 + lane; i < n; i += 32) sacc = fma(A[(long long)j * n + i], xs[i], sacc);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) sacc += __shfl_down_sync(0xffffffffu, sacc, off);
+      if (lane == 0) rs[j] -= sacc;
+    }
+    __syncthreads();
+    double rr = 0.0, xx = 0.0, rm = 0.0;
+    for (int i = tid; i < n; i += THREADS) {
+      rr = fma(rs[i], rs[i], rr);
+      xx = fma(xs[i], xs[i], xx);
+      rm = fmax(rm, fabs(rs[i]));
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      rr += __shfl_down_sync(0xffffffffu, rr, off);
+      xx += __shfl_down_sync(0xffffffffu, xx, off);
+      a2 += __shfl_down_sync(0xffffffffu, a2, off);
+      rm = fmax(rm, __shfl_down_sync(0xffffffffu, rm, off));
+    }
+    if (lane == 0) {
+      red[0][warp] = rr;
+      red[1][warp] = xx;
+      red[2][warp] = a2;
+      red[3][warp] = rm;
+    }
+    __syncthreads();
+    rr = xx = a2 = rm = 0.0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      rr += red[0][w];
+      xx += red[1][w];
+      a2 += red[2][w];
+      rm = fmax(rm, red[3][w]);
+    }
+    if (p.step == 0) {
+      if (tid == 0) p.anorm2[sys] = a2;
+    } else {
+      a2 = p.anorm2[sys];
+    }
+    const double be = rr == 0.0 ? 0.0 : sqrt(rr) / (sqrt(a2) * sqrt(xx));
+    const bool ok = be <= p.tol;  // false for NaN
+    if (ok || p.step == p.last) {
+      if (p.step == 0)
+        for (int i = tid; i < n; i += THREADS) X[i] = xs[i];
+      if (tid == 0) {
+        p.state[sys] = ok ? kMxDone : kMxStalled;
+        p.info[sys] = ok ? 0 : GBLLT_BATCH_NOT_CONVERGED;
+        if (ok) atomicAdd(p.done, 1);
+        atomicMax(p.maxbe, (unsigned long long)__double_as_longlong(be));
+      }
+      __syncthreads();  // xs, rs are reused by the next system
+      continue;
+    }
+    // the correction with the FP32 factor, r scaled by its largest entry
+    for (int i = tid; i < n; i += THREADS) rf[i] = (float)(rs[i] / rm);
+    __syncthreads();
+    solve_sweeps<float, THREADS>(p.lf + p.aoff[sys], n, n, rf, Dg);
+    for (int i = tid; i < n; i += THREADS) X[i] = fma(rm, (double)rf[i], xs[i]);
+    if (tid == 0) atomicAdd(p.active, 1);
+    __syncthreads();
+  }
+}
+
+// Systems left to the FP64 fallback (FP32 factorisation failed or tol not reached).
+__global__ void list_unsolved_kernel(const int* __restrict__ state, int count, int* __restrict__ list,
+                                     int* __restrict__ nlist) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < count; s += gridDim.x * blockDim.x)
+    if (state[s] == kMxFailed || state[s] == kMxStalled) list[atomicAdd(nlist, 1)] = s;
+}
+
+// Copy systems list[k] of a packed batch to system k of another (dir 0), or the right-hand sides
+// back (dir 1: x of system k of the small batch to list[k] of the large one).  A CTA per system.
+__global__ void __launch_bounds__(256) gather_systems_kernel(const int* __restrict__ list, int nlist,
+                                                             const int* __restrict__ nv,
+                                                             const int64_t* __restrict__ aoff,
+                                                             const int64_t* __restrict__ boff, const double* __restrict__ a,
+                                                             const double* __restrict__ b, const int64_t* __restrict__ aoff2,
+                                                             const int64_t* __restrict__ boff2, double* __restrict__ a2,
+                                                             double* __restrict__ b2) {
+  for (int k = blockIdx.x; k < nlist; k += gridDim.x) {
+    const int s = list[k], n = nv[s];
+    for (long long e = threadIdx.x; e < (long long)n * n; e += 256) a2[aoff2[k] + e] = a[aoff[s] + e];
+    for (int i = threadIdx.x; i < n; i += 256) b2[boff2[k] + i] = b[boff[s] + i];
+  }
+}
+
+__global__ void __launch_bounds__(256) scatter_solutions_kernel(const int* __restrict__ list, int nlist,
+                                                                const int* __restrict__ nv,
+                                                                const int64_t* __restrict__ boff,
+                                                                const int64_t* __restrict__ boff2,
+                                                                const double* __restrict__ x2,
+                                                                const int64_t* __restrict__ info2,
+                                                                double* __restrict__ x, int64_t* __restrict__ info) {
+  for (int k = blockIdx.x; k < nlist; k += gridDim.x) {
+    const int s = list[k], n = nv[s];
+    if (info2[k] == 0)
+      for (int i = threadIdx.x; i < n; i += 256) x[boff[s] + i] = x2[boff2[k] + i];
+    if (threadIdx.x == 0) info[s] = info2[k];
+  }
+}
+
+constexpr int kRefineThreads = 128;
+
+}  // namespace
+
+int batch_posv_mixed(BatchPlan* p, const double* a, const double* b, double* x, int64_t* info,
+                     const gbllt_mixed_opts& o, gbllt_batch_mixed_report* rep, cudaStream_t s) {
+  gbllt_batch_mixed_report r;
+  memset(&r, 0, sizeof r);
+  if (rep) *rep = r;
+  if (p->count == 0) return GBLLT_SUCCESS;
+  const int count = (int)p->count;
+  // the FP32 plan of the same sizes, tuned once
+  {
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (!p->f32) {
+      std::vector<int64_t> sizes(p->h_n.begin(), p->h_n.end());
+      BatchPlan* f = nullptr;
+      int rc = batch_plan_create(p->count, sizes.data(), 4, &f);
+      if (rc) return rc;
+      if ((rc = batch_plan_tune(f, s)) < 0) {
+        batch_plan_destroy(f);
+        return rc;
+      }
+      p->f32 = f;
+    }
+  }
+  BatchPlan* f = p->f32;
+  // workspace: FP32 factors and first solutions, per-system state, counters
+  auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  const size_t o_af = 0, o_bf = o_af + up((size_t)p->a_elems * 4), o_i32 = o_bf + up((size_t)p->b_elems * 4),
+               o_st = o_i32 + up((size_t)count * 8), o_an = o_st + up((size_t)count * 4),
+               o_list = o_an + up((size_t)count * 8), o_cnt = o_list + up((size_t)count * 4), total = o_cnt + 256;
+  char* ws = nullptr;
+  if (dev_malloc_async((void**)&ws, total, s) != cudaSuccess) {
+    cudaGetLastError();
+    set_error_message("gbllt_batch_dposv_mixed_dev: allocation of the workspace failed");
+    return GBLLT_ERR_ALLOC;
+  }
+  struct Free {
+    void* p;
+    cudaStream_t s;
+    ~Free() { cudaFreeAsync(p, s); }
+  } ws_free{ws, s};
+  float* af = (float*)(ws + o_af);
+  float* bf = (float*)(ws + o_bf);
+  int64_t* info32 = (int64_t*)(ws + o_i32);
+  int* state = (int*)(ws + o_st);
+  double* anorm2 = (double*)(ws + o_an);
+  int* list = (int*)(ws + o_list);
+  int* cnt = (int*)(ws + o_cnt);  // [0] ticket, [1] active, [2] done, [3] unsolved; [4..5] max backward error
+  unsigned long long* maxbe = (unsigned long long*)(cnt + 4);
+  GB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 64, s));
+  {
+    static const std::string kr = "batched_round_f32";
+    double by = 0;
+    for (int v : p->h_n) by += (double)v * (v + 1) / 2.0 * 12.0 + (double)v * 12.0;
+    ProfScope ps(kr.c_str(), s, 0.0, by);
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    round_lower_kernel<<<(unsigned)std::max(1, std::min(count, 8 * std::max(sms, 1))), 256, 0, s>>>(
+        a, b, af, bf, p->d_n, p->d_aoff, p->d_boff, count);
+    GB_CUDA_TRY(cudaGetLastError());
+  }
+  {
+    std::lock_guard<std::mutex> lk(f->mu);
+    int rc = run_plan<float>(f, af, bf, info32, s, true);
+    if (rc) return rc;
+  }
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned grid = (unsigned)std::max(1, std::min(count, 8 * std::max(sms, 1)));
+  RefineArgs ra{a,      b,      x,          af,         bf,        info32, info,   state,
+                anorm2, p->d_order, p->d_n, p->d_aoff, p->d_boff, count, cnt,    cnt + 1,
+                cnt + 2, maxbe, 0,          o.max_steps, o.tol};
+  static const std::string kf = "batched_refine_f64";
+  double fl = 0, by = 0;
+  for (int v : p->h_n) {
+    fl += 2.0 * v * v + 2.0 * v * v;  // the FP64 residual and the FP32 solve
+    by += (double)v * (v + 1) / 2.0 * 12.0 + (double)v * 32.0;
+  }
+  for (int step = 0; step <= o.max_steps; ++step) {
+    ra.step = step;
+    GB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 8, s));  // ticket and active count
+    {
+      ProfScope ps(kf.c_str(), s, fl, by);
+      refine_batch_kernel<kRefineThreads><<<grid, kRefineThreads, 0, s>>>(ra);
+      GB_CUDA_TRY(cudaGetLastError());
+    }
+    int act = 0;
+    GB_CUDA_TRY(cudaMemcpyAsync(&act, cnt + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (act == 0) break;
+    r.steps = step + 1;
+  }
+  int host_cnt[4] = {0, 0, 0, 0};
+  unsigned long long hbe = 0;
+  // the systems left to the FP64 fallback
+  list_unsolved_kernel<<<(unsigned)std::max(1, std::min((count + 255) / 256, 1024)), 256, 0, s>>>(state, count, list,
+                                                                                                   cnt + 3);
+  GB_CUDA_TRY(cudaGetLastError());
+  GB_CUDA_TRY(cudaMemcpyAsync(host_cnt, cnt, 16, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(&hbe, maxbe, 8, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  r.converged = host_cnt[2];
+  double mbe = 0;
+  memcpy(&mbe, &hbe, 8);
+  r.max_backward_error = mbe;
+  const int nf = host_cnt[3];
+  if (nf > 0 && o.fallback_fp64) {
+    // the unsolved systems, in index order, as a batch of their own solved by the FP64 kernel
+    std::vector<int> h_list(nf);
+    GB_CUDA_TRY(cudaMemcpy(h_list.data(), list, (size_t)nf * 4, cudaMemcpyDeviceToHost));
+    std::sort(h_list.begin(), h_list.end());
+    GB_CUDA_TRY(cudaMemcpyAsync(list, h_list.data(), (size_t)nf * 4, cudaMemcpyHostToDevice, s));
+    std::vector<int64_t> sizes(nf);
+    for (int k = 0; k < nf; ++k) sizes[k] = p->h_n[h_list[k]];
+    BatchPlan* t = nullptr;
+    int rc = batch_plan_create(nf, sizes.data(), 8, &t);
+    if (rc) return rc;
+    struct PlanFree {
+      BatchPlan* t;
+      ~PlanFree() { batch_plan_destroy(t); }
+    } t_free{t};
+    t->variant = p->variant;
+    configure<double>(t);
+    char* tw = nullptr;
+    const size_t ta = up((size_t)t->a_elems * 8), tb = up((size_t)t->b_elems * 8);
+    if (dev_malloc_async((void**)&tw, ta + tb + (size_t)nf * 8, s) != cudaSuccess) {
+      cudaGetLastError();
+      set_error_message("gbllt_batch_dposv_mixed_dev: allocation of the fallback's workspace failed");
+      return GBLLT_ERR_ALLOC;
+    }
+    struct Free2 {
+      void* p;
+      cudaStream_t s;
+      ~Free2() { cudaFreeAsync(p, s); }
+    } tw_free{tw, s};
+    double* ta_p = (double*)tw;
+    double* tb_p = (double*)(tw + ta);
+    int64_t* tinfo = (int64_t*)(tw + ta + tb);
+    const unsigned g2 = (unsigned)std::min(nf, 4096);
+    gather_systems_kernel<<<g2, 256, 0, s>>>(list, nf, p->d_n, p->d_aoff, p->d_boff, a, b, t->d_aoff, t->d_boff, ta_p,
+                                             tb_p);
+    GB_CUDA_TRY(cudaGetLastError());
+    if ((rc = run_plan<double>(t, ta_p, tb_p, tinfo, s, true))) return rc;
+    scatter_solutions_kernel<<<g2, 256, 0, s>>>(list, nf, p->d_n, p->d_boff, t->d_boff, tb_p, tinfo, x, info);
+    GB_CUDA_TRY(cudaGetLastError());
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    r.fallback = nf;
+  }
+  if (rep) *rep = r;
+  return GBLLT_SUCCESS;
+}
 
 }  // namespace gbllt
 
@@ -919,6 +1280,22 @@ int gbllt_dposv_batched(gbllt_batch_plan* plan, double* a, double* b, int64_t* i
 
 int gbllt_sposv_batched(gbllt_batch_plan* plan, float* a, float* b, int64_t* info) {
   return host_batched(plan, a, b, info, 4);
+}
+
+int gbllt_batch_dposv_mixed_dev(gbllt_batch_plan* plan, const double* d_a, const double* d_b, double* d_x,
+                                int64_t* d_info, const gbllt_mixed_opts* opts, gbllt_batch_mixed_report* report,
+                                void* stream) {
+  if (!plan) return -1;
+  BatchPlan* p = (BatchPlan*)plan;
+  if (p->elem != 8) return -1;
+  if (p->count > 0 && (!d_a || !d_b)) return -2;
+  if (p->count > 0 && !d_x) return -4;
+  if (p->count > 0 && !d_info) return -5;
+  gbllt_mixed_opts o;
+  if (resolve_mixed_opts(opts, &o, 0)) return -6;
+  int rc = ensure_device();
+  if (rc) return rc;
+  return batch_posv_mixed(p, d_a, d_b, d_x, d_info, o, report, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -60,6 +60,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_batch_plan_set_variant": (_int, [_vp, _int]),
     "gbllt_batch_plan_variant": (_int, [_vp, ctypes.POINTER(_int), ctypes.POINTER(_int), ctypes.POINTER(_int)]),
     "gbllt_dposv_batched_dev": (_int, [_vp, _vp, _vp, _vp, _vp]),
+    "gbllt_batch_dposv_mixed_dev": (_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbllt_sposv_batched_dev": (_int, [_vp, _vp, _vp, _vp, _vp]),
     "gbllt_dposv_batched": (_int, [_vp, _vp, _vp, _vp]),
     "gbllt_sposv_batched": (_int, [_vp, _vp, _vp, _vp]),
@@ -110,6 +111,18 @@ class KernelStat(ctypes.Structure):
 
 
 PREC = {"fp32": 0, "tf32": 1, "tf32x3": 2, "bf16": 3, "bf16x3": 4, "bf16x6": 5}
+
+
+class BatchMixedReport(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int), ("converged", ctypes.c_int64), ("fallback", ctypes.c_int64),
+                ("max_backward_error", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {"steps": int(self.steps), "converged": int(self.converged), "fallback": int(self.fallback),
+                "max_backward_error": float(self.max_backward_error)}
+
+
+BATCH_NOT_CONVERGED = -1
 
 
 class LaunchRecord(ctypes.Structure):
@@ -416,6 +429,16 @@ class BatchPlan:
     def solve_dev(self, a, b, info, stream: int = 0) -> None:
         fn = "gbllt_dposv_batched_dev" if self.elem == 8 else "gbllt_sposv_batched_dev"
         check(fn, getattr(lib(), fn)(self.handle, _ptr(a), _ptr(b), _ptr(info), stream))
+
+    def solve_mixed_dev(self, a, b, x, info, opts: "MixedOpts | None" = None, stream: int = 0) -> dict:
+        """gbllt_batch_dposv_mixed_dev: FP64 systems solved with FP32 factors and FP64 refinement;
+        a and b are read only, x receives the solutions.  Returns the report."""
+        rep = BatchMixedReport()
+        check("gbllt_batch_dposv_mixed_dev",
+              lib().gbllt_batch_dposv_mixed_dev(self.handle, _ptr(a), _ptr(b), _ptr(x), _ptr(info),
+                                                ctypes.byref(opts) if opts is not None else None,
+                                                ctypes.byref(rep), stream))
+        return rep.as_dict()
 
     def solve(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
         info = np.zeros(len(self.sizes), dtype=np.int64)

@@ -229,6 +229,29 @@ GBLLT_API int gbllt_sposv_batched_dev(gbllt_batch_plan* plan, float* d_a, float*
 GBLLT_API int gbllt_dposv_batched(gbllt_batch_plan* plan, double* a, double* b, int64_t* info);
 GBLLT_API int gbllt_sposv_batched(gbllt_batch_plan* plan, float* a, float* b, int64_t* info);
 
+/* Batched mixed-precision solve: every FP64 system of a plan (elem_bytes 8) solved to FP64
+ * accuracy with an FP32 factorisation and FP64 iterative refinement -- the batched counterpart of
+ * gbllt_dposv_mixed_dev, with no counterpart in the reference (Eigen solves each system in FP64).
+ * A and b are read only (A's lower triangle); x receives the solutions, laid out like b.
+ * Per system: A is rounded to FP32 and factored (the FP32 batched kernel, whose variant is tuned on
+ * the first call), then x is refined with r = b - A x in FP64 until ||r||_F <= tol ||A||_F ||x||_F
+ * or max_steps corrections were made; one launch per step for the whole batch.  Uses
+ * opts->max_steps, ->tol and ->fallback_fp64 (precision, panel, reserve_sms and residual are not
+ * used).  info[s]: 0 solved; k > 0: the FP64 factorisation (fallback) or, without fallback, the FP32
+ * one failed at column k; GBLLT_BATCH_NOT_CONVERGED: no fallback and tol not reached (x holds the
+ * last iterate).  With fallback_fp64, the systems that the FP32 factorisation or the refinement
+ * failed are solved again by the FP64 batched kernel.  Synchronises `stream` once per step. */
+#define GBLLT_BATCH_NOT_CONVERGED (-1)
+typedef struct {
+  int steps;                 /* refinement steps made (corrections of the slowest system) */
+  int64_t converged;         /* systems that reached tol in mixed precision */
+  int64_t fallback;          /* systems solved again in FP64 */
+  double max_backward_error; /* the largest ||r||_F / (||A||_F ||x||_F) at the last check */
+} gbllt_batch_mixed_report;
+GBLLT_API int gbllt_batch_dposv_mixed_dev(gbllt_batch_plan* plan, const double* d_a, const double* d_b, double* d_x,
+                                          int64_t* d_info, const gbllt_mixed_opts* opts,
+                                          gbllt_batch_mixed_report* report, void* stream);
+
 /* ---- Reverse mode (adjoints) of the factorisation and the solve, FP64, device pointers -------
  * Eigen has no derivative of LLT; these give the gradients of any scalar function of the factor
  * or of the solution, for A symmetric positive definite with A = L L^T (lower, column-major).

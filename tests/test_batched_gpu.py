@@ -113,3 +113,96 @@ def test_batched_autotuner_cache(oracle, gbllt, tmp_path):
     a2, b2 = a.copy(), b.copy()
     info = plan2.solve(a2, b2)
     _check(oracle, sizes, a, b, a2, b2, info, np.float32)
+
+
+def _systems(a, b, sizes):
+    off = boff = 0
+    for n in sizes:
+        n = int(n)
+        yield a[off:off + n * n].reshape(n, n, order="F"), b[boff:boff + n], boff
+        off += n * n
+        boff += n
+
+
+def _mixed(gbllt, plan, a, b, opts):
+    torch = pytest.importorskip("torch")
+    da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    dx = torch.zeros_like(db)
+    di = torch.full((len(plan.sizes),), -7, dtype=torch.int64, device="cuda")
+    rep = plan.solve_mixed_dev(da, db, dx, di, opts, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    # A and b are read only
+    assert np.array_equal(da.cpu().numpy(), a) and np.array_equal(db.cpu().numpy(), b)
+    return rep, dx.cpu().numpy(), di.cpu().numpy()
+
+
+def test_batched_mixed_refines_every_system(oracle, gbllt):
+    # FP32 factors + FP64 refinement: every system to backward error 1e-14 (the oracle's
+    # double-double residual), within 1e-12 of the oracle's FP64 solution (kappa < 100 here)
+    sizes = list(oracle.batch_sizes(300, seed=23, lo=4, hi=256)) + EDGE
+    mats, a, b = _batch(oracle, sizes, np.float64, seed=500)
+    plan = gbllt.BatchPlan(sizes, np.float64)
+    rep, x, info = _mixed(gbllt, plan, a, b, gbllt.mixed_opts("fp32", 10, 1e-14, fallback=False))
+    assert np.all(info == 0)
+    assert rep["converged"] == len(sizes) and rep["fallback"] == 0
+    assert 1 <= rep["steps"] <= 4 and rep["max_backward_error"] <= 1e-14
+    ref_a, ref_b = a.copy(), b.copy()
+    assert np.all(oracle.batched_posv(np.asarray(sizes, dtype=np.int64), ref_a, ref_b) == 0)
+    for (m, bs, off), n in zip(_systems(a, b, sizes), sizes):
+        if not n:
+            continue
+        xs = x[off:off + n]
+        assert oracle.backward_error(np.asfortranarray(m), xs.reshape(n, 1), bs.reshape(n, 1)) <= 1e-14, n
+        xr = ref_b[off:off + n]
+        assert np.linalg.norm(xs - xr) <= 1e-12 * np.linalg.norm(xr), n
+
+
+def test_batched_mixed_fallback_and_failures(oracle, gbllt):
+    # ill-conditioned systems (kappa 1e10: the FP32 factorisation fails or the refinement stalls) and
+    # a system that is not positive definite, among well-conditioned ones
+    good = [40, 130, 7, 256]
+    ill = [(64, 1e10), (200, 1e10)]
+    sizes = good[:2] + [n for n, _ in ill] + good[2:] + [150]
+    mats = [oracle.gen_gram(40, seed=1), oracle.gen_gram(130, seed=2), oracle.gen_householder(64, 1e10),
+            oracle.gen_householder(200, 1e10), oracle.gen_gram(7, seed=3), oracle.gen_gram(256, seed=4)]
+    bad = np.array(oracle.gen_gram(150, seed=5), order="F")
+    bad[77, 77] = -1.0
+    mats.append(bad)
+    a = np.concatenate([m.ravel(order="F") for m in mats])
+    b = np.concatenate([oracle.normal(600 + i, n) for i, n in enumerate(sizes)])
+    plan = gbllt.BatchPlan(sizes, np.float64)
+    # without fallback: the ill systems report a failed FP32 column or no convergence, the
+    # indefinite one its FP32 failing column
+    rep, x, info = _mixed(gbllt, plan, a, b, gbllt.mixed_opts("fp32", 10, 1e-14, fallback=False))
+    assert list(info[[0, 1, 4, 5]]) == [0, 0, 0, 0]
+    assert all(v == gbllt.BATCH_NOT_CONVERGED or v > 0 for v in info[[2, 3]])
+    assert info[6] > 0 and rep["converged"] == 4
+    # with fallback: the ill systems are solved in FP64 (backward error 1e-15), the indefinite one
+    # reports the FP64 failing column of the oracle
+    rep, x, info = _mixed(gbllt, plan, a, b, gbllt.mixed_opts("fp32", 10, 1e-14, fallback=True))
+    want = oracle.blocked(np.array(bad, order="F"))
+    assert list(info) == [0, 0, 0, 0, 0, 0, want + 1]
+    assert rep["fallback"] == 3 and rep["converged"] == 4
+    for k, ((m, bs, off), n) in enumerate(zip(_systems(a, b, sizes), sizes)):
+        if k == 6:
+            continue
+        assert oracle.backward_error(np.asfortranarray(m), x[off:off + n].reshape(n, 1),
+                                     bs.reshape(n, 1)) <= 1e-14, k
+
+
+def test_batched_mixed_arguments(gbllt):
+    torch = pytest.importorskip("torch")
+    empty = gbllt.BatchPlan([], np.float64)
+    t = torch.zeros(1, dtype=torch.float64, device="cuda")
+    i = torch.zeros(1, dtype=torch.int64, device="cuda")
+    assert empty.solve_mixed_dev(t, t, t, i)["converged"] == 0
+    f32 = gbllt.BatchPlan([3], np.float32)
+    rep = gbllt.BatchMixedReport()
+    rc = gbllt.lib().gbllt_batch_dposv_mixed_dev(f32.handle, t.data_ptr(), t.data_ptr(), t.data_ptr(), i.data_ptr(),
+                                                 None, None, 0)
+    assert rc == -1  # an FP32 plan
+    plan = gbllt.BatchPlan([3], np.float64)
+    rc = gbllt.lib().gbllt_batch_dposv_mixed_dev(plan.handle, None, t.data_ptr(), t.data_ptr(), i.data_ptr(), None,
+                                                 None, 0)
+    assert rc == -2
+    del rep
