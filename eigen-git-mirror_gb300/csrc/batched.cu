@@ -744,19 +744,38 @@ namespace {
 
 enum : int { kMxActive = 0, kMxDone = 1, kMxFailed = 2, kMxStalled = 3 };
 
-// The lower triangle of every system rounded to FP32 (same packed layout), and b.  A warp per column.
+// The lower triangle of every system rounded to FP32 (same packed layout), and b; also ||A||_F^2 of
+// each system from the rounded entries (the backward-error test needs it to a few digits only, and
+// FP32 keeps it off the FP64 pipe).  A warp per column.
 __global__ void __launch_bounds__(256) round_lower_kernel(const double* __restrict__ a, const double* __restrict__ b,
                                                           float* __restrict__ af, float* __restrict__ bf,
-                                                          const int* __restrict__ nv, const int64_t* __restrict__ aoff,
+                                                          double* __restrict__ anorm2, const int* __restrict__ nv,
+                                                          const int64_t* __restrict__ aoff,
                                                           const int64_t* __restrict__ boff, int count) {
+  __shared__ float red[8];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int s = blockIdx.x; s < count; s += gridDim.x) {
     const int n = nv[s];
     const double* A = a + aoff[s];
     float* F = af + aoff[s];
+    float q = 0.f;
     for (int j = warp; j < n; j += 8)
-      for (int i = j + lane; i < n; i += 32) F[(long long)j * n + i] = (float)A[(long long)j * n + i];
+      for (int i = j + lane; i < n; i += 32) {
+        const float v = (float)A[(long long)j * n + i];
+        F[(long long)j * n + i] = v;
+        q = fmaf(i == j ? v : 2.f * v, v, q);
+      }
     for (int i = threadIdx.x; i < n; i += 256) bf[boff[s] + i] = (float)b[boff[s] + i];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) q += __shfl_down_sync(0xffffffffu, q, off);
+    if (lane == 0) red[warp] = q;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.f;
+      for (int w = 0; w < 8; ++w) t += red[w];
+      anorm2[s] = (double)t;
+    }
+    __syncthreads();
   }
 }
 
@@ -769,28 +788,35 @@ struct RefineArgs {
   const int64_t* info32; // FP32 factorisation info
   int64_t* info;
   int* state;            // kMx* per system
-  double* anorm2;        // ||A||_F^2 per system (formed at step 0)
+  const double* anorm2;  // ||A||_F^2 per system
   const int* order;
   const int* n;
   const int64_t* aoff;
   const int64_t* boff;
   int count;
-  int* counter;          // queue ticket, zeroed before each launch
-  int* active;           // systems corrected by this launch
+  float* rsc;            // residuals scaled by their largest entry, FP32, laid out like b
+  double* rmax;          // that scale per system
+  int* counter;          // queue ticket of the residual launch, zeroed before each step
+  int* counter2;         // queue ticket of the correction launch, zeroed before each step
+  int* active;           // systems left for a correction by this step
   int* done;             // systems converged so far
   unsigned long long* maxbe;  // the largest backward error at the systems' last checks (bit pattern)
   int step, last;
   double tol;
 };
 
+constexpr int kRefRows = 64;   // rows of a staged tile of A (one per thread)
+constexpr int kTileLd = 33;    // its row pitch in doubles (odd: column reads across rows avoid bank conflicts)
+
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) refine_batch_kernel(RefineArgs p) {
   constexpr int NW = THREADS / 32;
+  static_assert(THREADS == kRefRows, "one thread per row of a staged tile");
   __shared__ double xs[kMaxBatchN];
   __shared__ double rs[kMaxBatchN];
-  __shared__ __align__(16) float rf[kMaxBatchN];
-  __shared__ __align__(16) float Dg[32 * kDgLd];
-  __shared__ double red[4][NW];
+  __shared__ double tile[kRefRows * kTileLd];
+  __shared__ double part[NW][32];
+  __shared__ double red[3][NW];
   __shared__ int s_ticket;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (;;) {
@@ -813,29 +839,55 @@ __global__ void __launch_bounds__(THREADS) refine_batch_kernel(RefineArgs p) {
     const double* A = p.a + p.aoff[sys];
     const double* B = p.b + p.boff[sys];
     double* X = p.x + p.boff[sys];
-    for (int i = tid; i < n; i += THREADS) xs[i] = p.step == 0 ? (double)p.xf[p.boff[sys] + i] : X[i];
-    __syncthreads();
-    // r = b - A x.  Rows over the threads for the part on and left of the diagonal (a column of the
-    // lower triangle at a time, coalesced); then a warp per column for the part right of it.
-    double a2 = 0.0;
     for (int i = tid; i < n; i += THREADS) {
-      double r = B[i];
-      for (int j = 0; j <= i; ++j) {
-        const double v = A[(long long)j * n + i];
-        r = fma(-v, xs[j], r);
-        if (p.step == 0) a2 += (i == j ? 1.0 : 2.0) * v * v;
-      }
-      rs[i] = r;
+      xs[i] = p.step == 0 ? (double)p.xf[p.boff[sys] + i] : X[i];
+      rs[i] = B[i];
     }
     __syncthreads();
-    for (int j = warp; j < n; j += NW) {
-      double sacc = 0.0;
-      for (int i = j + 1 + lane; i < n; i += 32) sacc = fma(A[(long long)j * n + i], xs[i], sacc);
+    // r = b - A x with A's lower triangle read once per step, coalesced: the triangle goes through
+    // shared memory in tiles of kRefRows rows x 32 columns (column by column, kRefRows consecutive
+    // doubles each).  From a tile at rows R0.., columns J0..: thread t adds row R0 + t's products with
+    // x(J0..) to r (its own row), and lane c of warp w the products of column J0 + c over the warp's
+    // rows with x(R0..) to a partial sum of r(J0 + c) (its own column): every FP64 instruction with all
+    // lanes busy, no shuffles; the warps' partials are added once per tile.
+    for (int J0 = 0; J0 < n; J0 += 32) {
+      const int jb = n - J0 < 32 ? n - J0 : 32;
+      for (int R0 = J0; R0 < n; R0 += kRefRows) {
+        const int rb = n - R0 < kRefRows ? n - R0 : kRefRows;
+        for (int c = 0; c < jb; ++c)
+          for (int r = tid; r < rb; r += THREADS) tile[r * kTileLd + c] = A[(long long)(J0 + c) * n + R0 + r];
+        __syncthreads();
+        {  // rows: r(i) -= sum_{j <= i} A(i, j) x(j) over this tile's columns
+          const int r = tid;
+          if (r < rb) {
+            const int i = R0 + r;
+            double acc = 0.0;
+#pragma unroll 8
+            for (int c = 0; c < 32; ++c)
+              if (c < jb && J0 + c <= i) acc = fma(tile[r * kTileLd + c], xs[J0 + c], acc);
+            rs[i] -= acc;
+          }
+        }
+        {  // columns: r(j) -= sum_{i > j} A(i, j) x(i), lane = column, this warp's rows
+          double acc = 0.0;
+          const int j = J0 + lane;
+#pragma unroll 8
+          for (int rr = 0; rr < kRefRows / NW; ++rr) {
+            const int r = warp * (kRefRows / NW) + rr;
+            if (r < rb && lane < jb && R0 + r > j) acc = fma(tile[r * kTileLd + lane], xs[R0 + r], acc);
+          }
+          part[warp][lane] = acc;
+        }
+        __syncthreads();
+        if (tid < jb) {
+          double sum = 0.0;
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) sacc += __shfl_down_sync(0xffffffffu, sacc, off);
-      if (lane == 0) rs[j] -= sacc;
+          for (int w = 0; w < NW; ++w) sum += part[w][tid];
+          rs[J0 + tid] -= sum;
+        }
+        __syncthreads();
+      }
     }
-    __syncthreads();
     double rr = 0.0, xx = 0.0, rm = 0.0;
     for (int i = tid; i < n; i += THREADS) {
       rr = fma(rs[i], rs[i], rr);
@@ -846,34 +898,27 @@ __global__ void __launch_bounds__(THREADS) refine_batch_kernel(RefineArgs p) {
     for (int off = 16; off > 0; off >>= 1) {
       rr += __shfl_down_sync(0xffffffffu, rr, off);
       xx += __shfl_down_sync(0xffffffffu, xx, off);
-      a2 += __shfl_down_sync(0xffffffffu, a2, off);
       rm = fmax(rm, __shfl_down_sync(0xffffffffu, rm, off));
     }
     if (lane == 0) {
       red[0][warp] = rr;
       red[1][warp] = xx;
-      red[2][warp] = a2;
-      red[3][warp] = rm;
+      red[2][warp] = rm;
     }
     __syncthreads();
-    rr = xx = a2 = rm = 0.0;
+    rr = xx = rm = 0.0;
 #pragma unroll
     for (int w = 0; w < NW; ++w) {
       rr += red[0][w];
       xx += red[1][w];
-      a2 += red[2][w];
-      rm = fmax(rm, red[3][w]);
+      rm = fmax(rm, red[2][w]);
     }
-    if (p.step == 0) {
-      if (tid == 0) p.anorm2[sys] = a2;
-    } else {
-      a2 = p.anorm2[sys];
-    }
+    const double a2 = p.anorm2[sys];
     const double be = rr == 0.0 ? 0.0 : sqrt(rr) / (sqrt(a2) * sqrt(xx));
     const bool ok = be <= p.tol;  // false for NaN
+    if (p.step == 0)
+      for (int i = tid; i < n; i += THREADS) X[i] = xs[i];
     if (ok || p.step == p.last) {
-      if (p.step == 0)
-        for (int i = tid; i < n; i += THREADS) X[i] = xs[i];
       if (tid == 0) {
         p.state[sys] = ok ? kMxDone : kMxStalled;
         p.info[sys] = ok ? 0 : GBLLT_BATCH_NOT_CONVERGED;
@@ -883,12 +928,40 @@ __global__ void __launch_bounds__(THREADS) refine_batch_kernel(RefineArgs p) {
       __syncthreads();  // xs, rs are reused by the next system
       continue;
     }
-    // the correction with the FP32 factor, r scaled by its largest entry
-    for (int i = tid; i < n; i += THREADS) rf[i] = (float)(rs[i] / rm);
+    // left for the correction launch: r scaled by its largest entry, rounded to FP32
+    const double rinv = 1.0 / rm;
+    for (int i = tid; i < n; i += THREADS) p.rsc[p.boff[sys] + i] = (float)(rs[i] * rinv);
+    if (tid == 0) {
+      p.rmax[sys] = rm;
+      atomicAdd(p.active, 1);
+    }
+    __syncthreads();
+  }
+}
+
+// The correction of every system the residual launch left active: x += L^{-T} L^{-1} r with the FP32
+// factor (the solve's 32-row blocks want more threads than the residual's tiles).
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) correct_batch_kernel(RefineArgs p) {
+  __shared__ __align__(16) float rf[kMaxBatchN];
+  __shared__ __align__(16) float Dg[32 * kDgLd];
+  __shared__ int s_ticket;
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) s_ticket = atomicAdd(p.counter2, 1);
+    __syncthreads();
+    const int t = s_ticket;
+    __syncthreads();
+    if (t >= p.count) break;
+    const int sys = p.order[t];
+    if (p.state[sys] != kMxActive) continue;  // uniform over the CTA
+    const int n = p.n[sys];
+    double* X = p.x + p.boff[sys];
+    for (int i = tid; i < n; i += THREADS) rf[i] = p.rsc[p.boff[sys] + i];
     __syncthreads();
     solve_sweeps<float, THREADS>(p.lf + p.aoff[sys], n, n, rf, Dg);
-    for (int i = tid; i < n; i += THREADS) X[i] = fma(rm, (double)rf[i], xs[i]);
-    if (tid == 0) atomicAdd(p.active, 1);
+    const double rm = p.rmax[sys];
+    for (int i = tid; i < n; i += THREADS) X[i] = fma(rm, (double)rf[i], X[i]);
     __syncthreads();
   }
 }
@@ -931,7 +1004,8 @@ __global__ void __launch_bounds__(256) scatter_solutions_kernel(const int* __res
   }
 }
 
-constexpr int kRefineThreads = 128;
+constexpr int kRefineThreads = kRefRows;
+constexpr int kCorrectThreads = 128;
 
 }  // namespace
 
@@ -962,7 +1036,8 @@ int batch_posv_mixed(BatchPlan* p, const double* a, const double* b, double* x, 
   auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
   const size_t o_af = 0, o_bf = o_af + up((size_t)p->a_elems * 4), o_i32 = o_bf + up((size_t)p->b_elems * 4),
                o_st = o_i32 + up((size_t)count * 8), o_an = o_st + up((size_t)count * 4),
-               o_list = o_an + up((size_t)count * 8), o_cnt = o_list + up((size_t)count * 4), total = o_cnt + 256;
+               o_list = o_an + up((size_t)count * 8), o_rsc = o_list + up((size_t)count * 4),
+               o_rm = o_rsc + up((size_t)p->b_elems * 4), o_cnt = o_rm + up((size_t)count * 8), total = o_cnt + 256;
   char* ws = nullptr;
   if (dev_malloc_async((void**)&ws, total, s) != cudaSuccess) {
     cudaGetLastError();
@@ -980,8 +1055,11 @@ int batch_posv_mixed(BatchPlan* p, const double* a, const double* b, double* x, 
   int* state = (int*)(ws + o_st);
   double* anorm2 = (double*)(ws + o_an);
   int* list = (int*)(ws + o_list);
-  int* cnt = (int*)(ws + o_cnt);  // [0] ticket, [1] active, [2] done, [3] unsolved; [4..5] max backward error
-  unsigned long long* maxbe = (unsigned long long*)(cnt + 4);
+  float* rsc = (float*)(ws + o_rsc);
+  double* rmax = (double*)(ws + o_rm);
+  // [0] residual ticket, [1] active, [2] correction ticket, [3] done, [4] unsolved; [6..7] max backward error
+  int* cnt = (int*)(ws + o_cnt);
+  unsigned long long* maxbe = (unsigned long long*)(cnt + 6);
   GB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 64, s));
   {
     static const std::string kr = "batched_round_f32";
@@ -992,7 +1070,7 @@ int batch_posv_mixed(BatchPlan* p, const double* a, const double* b, double* x, 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     round_lower_kernel<<<(unsigned)std::max(1, std::min(count, 8 * std::max(sms, 1))), 256, 0, s>>>(
-        a, b, af, bf, p->d_n, p->d_aoff, p->d_boff, count);
+        a, b, af, bf, anorm2, p->d_n, p->d_aoff, p->d_boff, count);
     GB_CUDA_TRY(cudaGetLastError());
   }
   {
@@ -1004,21 +1082,32 @@ int batch_posv_mixed(BatchPlan* p, const double* a, const double* b, double* x, 
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const unsigned grid = (unsigned)std::max(1, std::min(count, 8 * std::max(sms, 1)));
-  RefineArgs ra{a,      b,      x,          af,         bf,        info32, info,   state,
-                anorm2, p->d_order, p->d_n, p->d_aoff, p->d_boff, count, cnt,    cnt + 1,
-                cnt + 2, maxbe, 0,          o.max_steps, o.tol};
+  RefineArgs ra{a,     b,          x,      af,        bf,        info32, info,    state,   anorm2,
+                p->d_order, p->d_n, p->d_aoff, p->d_boff, count, rsc, rmax, cnt, cnt + 2, cnt + 1,
+                cnt + 3, maxbe, 0,      o.max_steps, o.tol};
   static const std::string kf = "batched_refine_f64";
   double fl = 0, by = 0;
   for (int v : p->h_n) {
-    fl += 2.0 * v * v + 2.0 * v * v;  // the FP64 residual and the FP32 solve
-    by += (double)v * (v + 1) / 2.0 * 12.0 + (double)v * 32.0;
+    fl += 2.0 * v * v;  // the FP64 residual
+    by += (double)v * (v + 1) / 2.0 * 8.0 + (double)v * 28.0;
+  }
+  static const std::string kc = "batched_correct_f32";
+  double flc = 0, byc = 0;
+  for (int v : p->h_n) {
+    flc += 2.0 * v * v;
+    byc += (double)v * (v + 1) / 2.0 * 4.0 + (double)v * 20.0;
   }
   for (int step = 0; step <= o.max_steps; ++step) {
     ra.step = step;
-    GB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 8, s));  // ticket and active count
+    GB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 12, s));  // the two tickets and the active count
     {
       ProfScope ps(kf.c_str(), s, fl, by);
       refine_batch_kernel<kRefineThreads><<<grid, kRefineThreads, 0, s>>>(ra);
+      GB_CUDA_TRY(cudaGetLastError());
+    }
+    {
+      ProfScope ps(kc.c_str(), s, flc, byc);
+      correct_batch_kernel<kCorrectThreads><<<grid, kCorrectThreads, 0, s>>>(ra);
       GB_CUDA_TRY(cudaGetLastError());
     }
     int act = 0;
@@ -1027,20 +1116,20 @@ int batch_posv_mixed(BatchPlan* p, const double* a, const double* b, double* x, 
     if (act == 0) break;
     r.steps = step + 1;
   }
-  int host_cnt[4] = {0, 0, 0, 0};
+  int host_cnt[5] = {0, 0, 0, 0, 0};
   unsigned long long hbe = 0;
   // the systems left to the FP64 fallback
   list_unsolved_kernel<<<(unsigned)std::max(1, std::min((count + 255) / 256, 1024)), 256, 0, s>>>(state, count, list,
-                                                                                                   cnt + 3);
+                                                                                                   cnt + 4);
   GB_CUDA_TRY(cudaGetLastError());
-  GB_CUDA_TRY(cudaMemcpyAsync(host_cnt, cnt, 16, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(host_cnt, cnt, 20, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaMemcpyAsync(&hbe, maxbe, 8, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
-  r.converged = host_cnt[2];
+  r.converged = host_cnt[3];
   double mbe = 0;
   memcpy(&mbe, &hbe, 8);
   r.max_backward_error = mbe;
-  const int nf = host_cnt[3];
+  const int nf = host_cnt[4];
   if (nf > 0 && o.fallback_fp64) {
     // the unsolved systems, in index order, as a batch of their own solved by the FP64 kernel
     std::vector<int> h_list(nf);
