@@ -176,3 +176,24 @@ def test_mixed_concurrent_host_threads(oracle, gbllt):
         assert torch.equal(x_p, x_s)
         x = np.asfortranarray(x_p.cpu().numpy().T)
         assert oracle.backward_error(mats[i], x, rhs[i]) <= 1e-14
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("prec", ["bf16x6", "bf16x3"])
+def test_mixed_full_size_default_panel(oracle, gbllt, prec):
+    """n = 16384, 64 right-hand sides, Householder spectrum with kappa = 1e6: the default schedule at
+    this order (outer panel 384, look-ahead, tensor-core residual) reaches backward error 1e-14 without
+    the FP64 fallback, checked by an independent FP64 residual (cuBLAS through torch)."""
+    torch = pytest.importorskip("torch")
+    n, k = 16384, 64
+    A = torch.from_numpy(np.ascontiguousarray(oracle.gen_householder(n, 1e6))).cuda()  # symmetric
+    g = torch.Generator(device="cuda").manual_seed(5)
+    B = torch.randn(k, n, generator=g, dtype=torch.float64, device="cuda")  # column-major n x k
+    X = torch.zeros_like(B)
+    rc, rep = gbllt.posv_mixed_dev(A, n, n, B, n, X, n, k, gbllt.mixed_opts(prec, 10, 1e-14, fallback=False), "L",
+                                   torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert rc == gbllt.SUCCESS and rep["converged"] and not rep["used_fallback"], rep
+    assert rep["steps"] <= 6
+    be = float(torch.linalg.norm(A @ X.T - B.T) / (torch.linalg.norm(A) * torch.linalg.norm(X)))
+    assert be <= 1e-14
