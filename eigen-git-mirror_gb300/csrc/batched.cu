@@ -973,8 +973,7 @@ __global__ void list_unsolved_kernel(const int* __restrict__ state, int count, i
     if (state[s] == kMxFailed || state[s] == kMxStalled) list[atomicAdd(nlist, 1)] = s;
 }
 
-// Copy systems list[k] of a packed batch to system k of another (dir 0), or the right-hand sides
-// back (dir 1: x of system k of the small batch to list[k] of the large one).  A CTA per system.
+// Copy system list[k] (A and b) of a packed batch to system k of another.  A CTA per system.
 __global__ void __launch_bounds__(256) gather_systems_kernel(const int* __restrict__ list, int nlist,
                                                              const int* __restrict__ nv,
                                                              const int64_t* __restrict__ aoff,
@@ -989,6 +988,8 @@ __global__ void __launch_bounds__(256) gather_systems_kernel(const int* __restri
   }
 }
 
+// The other way: the solution and info of system k of the small batch to system list[k] of the large
+// one (the solution only where that system's factorisation succeeded).
 __global__ void __launch_bounds__(256) scatter_solutions_kernel(const int* __restrict__ list, int nlist,
                                                                 const int* __restrict__ nv,
                                                                 const int64_t* __restrict__ boff,
