@@ -187,6 +187,7 @@ struct OzakiResidual {
   int* rexp = nullptr;
   int* xexp = nullptr;
   int* flags = nullptr;
+  long long* part = nullptr;  // the K-split product's int64 sums
   OzakiResidual() = default;
   OzakiResidual(const OzakiResidual&) = delete;
   OzakiResidual& operator=(const OzakiResidual&) = delete;

@@ -49,6 +49,7 @@ constexpr int S = 8;          // slices per operand
 constexpr int BETA = 7;       // bits per slice
 constexpr int KB = 64;        // K elements per 128-byte row (BF16)
 constexpr int KC_BLOCKS = 4;  // K blocks per exact chunk (KC = 256)
+constexpr int kMaxKParts = 8;  // K ranges of the residual's K-split (at most)
 constexpr int BM = 128;
 constexpr int BN = 64;
 constexpr int A_STAGES = 4;
@@ -283,6 +284,11 @@ struct OzParams {
   int scale;                       // power of two applied to the product (rectangle mode)
   int nsl;                         // slices used per operand (S: FP64-exact; fewer: 7 nsl bits)
   const DevStatus* st;             // lower mode: skip the update after a failed pivot
+  // residual mode with kparts > 1: K is cut into kparts ranges of whole chunks, the tile list holds
+  // every (tile, range) pair, and each writes its two int64 sums per output to part
+  // ([range][0 / 1][column][row]); oz_residual_sum_kernel adds them and forms R
+  int kparts;
+  long long* part;
 };
 
 // Kernel modes: the refinement residual R = B - A X, the trailing update C -= P Q^T on the lower
@@ -328,10 +334,26 @@ __device__ __forceinline__ double fixed_to_double(long long hi, long long lo, in
 // 128 x 64 grid over its rs x ncols block and skips the tiles strictly above the diagonal.
 template <int MODE>
 __device__ __forceinline__ bool oz_tile(const OzParams& p, long long t, long long& row0, long long& col0) {
+  if (MODE == OZ_RESIDUAL && p.kparts > 1) t %= (long long)p.nrt * p.nct;
   row0 = (t % p.nrt) * BM;
   col0 = (t / p.nrt) * BN;
   if (MODE != OZ_LOWER) return true;
   return col0 < p.ncols && col0 <= row0 + BM - 1;
+}
+
+// The K blocks [kb0, kb1) of list entry t and its K range index: all of K, or in the residual's
+// K-split the range t / (tiles per range), whole 256-deep chunks each.
+template <int MODE>
+__device__ __forceinline__ int oz_krange(const OzParams& p, long long t, int nkb, int& kb0, int& kb1) {
+  kb0 = 0;
+  kb1 = nkb;
+  if (MODE != OZ_RESIDUAL || p.kparts <= 1) return 0;
+  const int kp = (int)(t / ((long long)p.nrt * p.nct));
+  const int nch = (nkb + KC_BLOCKS - 1) / KC_BLOCKS;
+  const int c0 = (int)((long long)kp * nch / p.kparts), c1 = (int)((long long)(kp + 1) * nch / p.kparts);
+  kb0 = c0 * KC_BLOCKS;
+  kb1 = c1 * KC_BLOCKS < nkb ? c1 * KC_BLOCKS : nkb;
+  return kp;
 }
 
 // Persistent: each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The producer runs up to
@@ -352,7 +374,6 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
   if (MODE == OZ_LOWER && p.st->fail_col >= 0) return;  // an earlier pivot failed: nothing to update
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nkb = (int)((p.kdim + KB - 1) / KB);
-  const int nchunks = (nkb + KC_BLOCKS - 1) / KC_BLOCKS;
 
   if (threadIdx.x == 0) {
     abort_s = 0;
@@ -386,7 +407,9 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
     for (long long t = blockIdx.x; t < p.tiles && ok && !abort_s; t += gridDim.x) {
       long long row0, col0;
       if (!oz_tile<MODE>(p, t, row0, col0)) continue;
-      for (int kb = 0; kb < nkb && ok; ++kb, ++kbg) {
+      int kb0, kb1;
+      oz_krange<MODE>(p, t, nkb, kb0, kb1);
+      for (int kb = kb0; kb < kb1 && ok; ++kb, ++kbg) {
         const int xb = (int)(kbg & 1);
         if (!mbar_wait(&xempty[xb], ((uint32_t)(kbg >> 1) & 1u) ^ 1u, &abort_s)) { ok = false; break; }
         mbar_expect_tx(&xfull[xb], p.nsl * X_BYTES);
@@ -421,8 +444,10 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
     for (long long t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
       long long row0, col0;
       if (!oz_tile<MODE>(p, t, row0, col0)) continue;
-      for (int kb = 0; kb < nkb && ok; ++kb, ++kbg) {
-        const bool first = (kb % KC_BLOCKS) == 0;
+      int kb0, kb1;
+      oz_krange<MODE>(p, t, nkb, kb0, kb1);
+      for (int kb = kb0; kb < kb1 && ok; ++kb, ++kbg) {
+        const bool first = ((kb - kb0) % KC_BLOCKS) == 0;
         if (first && chunkg > 0) {  // the epilogue has taken the previous chunk's sums out of TMEM
           if (!mbar_wait(&tempty, (uint32_t)(chunkg - 1) & 1u, &abort_s)) { ok = false; break; }
           tc_fence_after();
@@ -449,7 +474,7 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
         }
         if (!ok) break;
         mma_commit(&xempty[xb]);
-        if ((kb % KC_BLOCKS) == KC_BLOCKS - 1 || kb == nkb - 1) {
+        if (((kb - kb0) % KC_BLOCKS) == KC_BLOCKS - 1 || kb == kb1 - 1) {
           mma_commit(&tfull);
           ++chunkg;
         }
@@ -466,6 +491,9 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
     for (long long t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
       long long row0, col0;
       if (!oz_tile<MODE>(p, t, row0, col0)) continue;
+      int kb0, kb1;
+      const int kp = oz_krange<MODE>(p, t, nkb, kb0, kb1);
+      const int nchunks = (kb1 - kb0 + KC_BLOCKS - 1) / KC_BLOCKS;
       long long hi[16], lo[16];
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
@@ -514,6 +542,17 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
             if (j < p.ncols) p.c[j * p.ldc + i] -= fixed_to_double(hi[c], lo[c], ei + p.pexp_b[j]);
           }
         }
+      } else if (p.kparts > 1) {  // residual, one K range: its sums for oz_residual_sum_kernel
+        if (i < p.n) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const long long j = col0 + part * 16 + c;
+            if (j < p.nrhs) {
+              p.part[((long long)(kp * 2) * p.nrhs + j) * p.n + i] = hi[c];
+              p.part[((long long)(kp * 2 + 1) * p.nrhs + j) * p.n + i] = lo[c];
+            }
+          }
+        }
       } else if (i < p.n) {
         const int e = p.rexp[i];
         const bool bad = (p.flag[0] | p.flag[1]) != 0;
@@ -534,6 +573,28 @@ __global__ void __launch_bounds__(THREADS, 1) oz_kernel(const __grid_constant__ 
   if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+// The residual from a K-split product: the kparts ranges' int64 sums added (exactly), rounded once to
+// FP64, R = B - A X (NaN everywhere when A or X held a non-finite value).
+__global__ void __launch_bounds__(256) oz_residual_sum_kernel(const long long* __restrict__ part, int kparts,
+                                                              long long n, long long nrhs,
+                                                              const int* __restrict__ rexp,
+                                                              const int* __restrict__ xexp,
+                                                              const int* __restrict__ flag,
+                                                              const double* __restrict__ b, long long ldb,
+                                                              double* __restrict__ r, long long ldr) {
+  const bool bad = (flag[0] | flag[1]) != 0;
+  for (long long idx = (long long)blockIdx.x * 256 + threadIdx.x; idx < n * nrhs; idx += (long long)gridDim.x * 256) {
+    const long long j = idx / n, i = idx - j * n;
+    long long hi = 0, lo = 0;
+    for (int kp = 0; kp < kparts; ++kp) {
+      hi += part[((long long)(kp * 2) * nrhs + j) * n + i];
+      lo += part[((long long)(kp * 2 + 1) * nrhs + j) * n + i];
+    }
+    const double ax = fixed_to_double(hi, lo, rexp[i] + xexp[j]);
+    r[j * ldr + i] = bad ? __longlong_as_double(0x7ff8000000000000ll) : b[j * ldb + i] - ax;
   }
 }
 
@@ -577,7 +638,8 @@ OzakiResidual::~OzakiResidual() {
 size_t OzakiResidual::bytes(int64_t n, int64_t nrhs) {
   const int64_t lds = (n + 7) / 8 * 8;  // 16-byte row pitch for TMA
   return oz_up256((size_t)S * n * lds * 2) + oz_up256((size_t)S * nrhs * lds * 2) + oz_up256((size_t)n * 8) +
-         oz_up256((size_t)n * 4) + oz_up256((size_t)nrhs * 4) + 256 + 256;
+         oz_up256((size_t)n * 4) + oz_up256((size_t)nrhs * 4) + 256 + oz_up256((size_t)kMaxKParts * 2 * nrhs * n * 8) +
+         256;
 }
 
 int OzakiResidual::reserve(int64_t n_, int64_t nrhs_, cudaStream_t s) {
@@ -616,6 +678,8 @@ int OzakiResidual::setup(bool upper, int64_t n_, int64_t nrhs_, const double* a,
   xexp = (int*)q;
   q += oz_up256((size_t)nrhs * 4);
   flags = (int*)q;  // [0] A non-finite, [1] X non-finite, [2] timeout
+  q += 256;
+  part = (long long*)q;  // the K-split's sums: kMaxKParts x 2 x nrhs x n
   GB_CUDA_TRY(cudaMemsetAsync(rmax, 0, (size_t)n * 8, s));
   GB_CUDA_TRY(cudaMemsetAsync(flags, 0, 16, s));
   const int64_t t = ceil_div(n, 64);
@@ -675,6 +739,28 @@ int OzakiResidual::residual(const double* x, int64_t ldx, const double* b, int64
   p.r = r;
   p.ldr = ldr;
   p.err = flags + 2;
+  // With fewer tiles than a few per SM the last wave of the tile list runs part-empty (n = 32768,
+  // 64 RHS: 256 tiles on 152 SMs fill 84 % of two waves).  K is then cut into kparts ranges of whole
+  // chunks, at least 4 chunks each, so that the (tile, range) list fills its waves to >= 95 %; the
+  // ranges' exact int64 sums are added by a second kernel.
+  const long long base_tiles = p.tiles;
+  const int nch = (int)ceil_div(ceil_div(n, KB), KC_BLOCKS);
+  int kparts = 1;
+  {
+    auto fill = [&](int kp) {
+      const long long u = base_tiles * kp, waves = (u + sms - 1) / sms;
+      return (double)u / (double)(waves * sms);
+    };
+    double best = fill(1);
+    for (int kp = 2; kp <= kMaxKParts && nch / kp >= 4 && best < 0.95; ++kp)
+      if (fill(kp) > best + 0.02) {
+        best = fill(kp);
+        kparts = kp;
+      }
+  }
+  p.kparts = kparts;
+  p.part = part;
+  p.tiles = base_tiles * kparts;
   const unsigned grid = (unsigned)(p.tiles < sms ? p.tiles : sms);
   {
     // algorithmic work: the FP64 product 2 n^2 nrhs; bytes: the 8 A slices read once per column tile,
@@ -684,6 +770,14 @@ int OzakiResidual::residual(const double* x, int64_t ldx, const double* b, int64
     oz_kernel<OZ_RESIDUAL><<<grid, THREADS, SMEM_BYTES, s>>>(maps, p);
   }
   GB_CUDA_TRY(cudaGetLastError());
+  if (kparts > 1) {
+    static const std::string kr = "residual_sum";
+    ProfScope ps(kr.c_str(), s, 0.0, (double)kparts * 2 * n * nrhs * 8.0 + 2.0 * n * nrhs * 8.0);
+    const long long tot = n * nrhs;
+    const unsigned g = (unsigned)std::min<long long>((tot + 255) / 256, 8LL * sms);
+    oz_residual_sum_kernel<<<g, 256, 0, s>>>(part, kparts, n, nrhs, rexp, xexp, flags, b, ldb, r, ldr);
+    GB_CUDA_TRY(cudaGetLastError());
+  }
   return GBLLT_SUCCESS;
 }
 

@@ -60,7 +60,8 @@ def test_residual_argument_errors():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n,k", [(1, 1), (63, 5), (300, 64), (1000, 70), (2049, 3)])
+# from n = 2048 the product runs K-split (2 to 8 ranges of whole chunks, summed exactly in int64)
+@pytest.mark.parametrize("n,k", [(1, 1), (63, 5), (300, 64), (1000, 70), (2049, 3), (4096, 16), (8192, 64)])
 @pytest.mark.parametrize("uplo", ["L", "U"])
 def test_tensor_residual_exact_on_integers(oracle, n, k, uplo):
     torch = pytest.importorskip("torch")
@@ -111,9 +112,10 @@ def test_tensor_residual_wide_scales(oracle):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("where", ["a", "x"])
-def test_tensor_residual_nonfinite_gives_nan(oracle, where):
+@pytest.mark.parametrize("n", [130, 4100])
+def test_tensor_residual_nonfinite_gives_nan(oracle, where, n):
     torch = pytest.importorskip("torch")
-    n, k = 130, 3
+    k = 3
     g = oracle.normal(8, n * n).reshape(n, n)
     af = g + g.T
     x = oracle.normal(9, n * k).reshape(n, k)
