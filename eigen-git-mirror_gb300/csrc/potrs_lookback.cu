@@ -21,6 +21,8 @@
 // L has a unit diagonal (trinv_kernel<UNIT>) and the diagonal of the stored factor holds D; the
 // backward sweep applies D's pseudo-inverse to each block's right-hand sides as it loads them
 // (DSCALE: divide where |d| > the smallest normal number, else 0, LDLT.h:587-600).
+#include <cuda_bf16.h>
+
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -275,7 +277,9 @@ struct LLSmem {
   float Lb[LL_NT][RB * PF_PITCH];  // off-diagonal tiles: three loads in flight behind the one in use
   float Ds[RB * (RB + 1)];     // Ds[i * 65 + r] = D(r, i)
   float Ms[RB * RB];           // Ms[p * 64 + r] = M(r, p)
-  float Ys[RB * RCT];          // staged 64 x RCT block; flat index = word index
+  // staged 64 x RCT block; flat index = word index, or (32-column chains, whose look-back products
+  // run on the tensor cores) column by column with row pitch PF_PITCH: Ys[c * 68 + p] = Y(p, c)
+  float Ys[RB * RCT > RCT * PF_PITCH ? RB * RCT : RCT * PF_PITCH];
 };
 
 __device__ __forceinline__ uint32_t sptr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -293,8 +297,9 @@ __device__ __forceinline__ void cp_wait() {
 }
 
 // Tile G(rr, p) of the sweep for row block I0 and column block J0.  RFAST: element (rr, p) at
-// a[(J0 + p) lda + I0 + rr], kept as lb[p * 64 + rr]; otherwise at a[(I0 + rr) lda + J0 + p], kept as
-// lb[rr * 68 + p].  Entries beyond n are zero-filled.  VEC: 16-byte copies (a 16-byte aligned,
+// a[(J0 + p) lda + I0 + rr], kept as lb[p * 68 + rr]; otherwise at a[(I0 + rr) lda + J0 + p], kept as
+// lb[rr * 68 + p] (the pitch of 68 keeps the tensor-core fragment reads of either layout within two
+// banks' conflicts).  Entries beyond n are zero-filled.  VEC: 16-byte copies (a 16-byte aligned,
 // lda a multiple of 4).
 template <bool RFAST, bool VEC>
 __device__ __forceinline__ void load_tile(float* lb, const float* __restrict__ a, long long lda, long long n,
@@ -307,7 +312,7 @@ __device__ __forceinline__ void load_tile(float* lb, const float* __restrict__ a
       const long long fg = (RFAST ? I0 : J0) + f, sg = (RFAST ? J0 : I0) + s;
       const int bytes = (fg < n && sg < n) ? (int)(n - fg < 4 ? n - fg : 4) * 4 : 0;
       const float* src = bytes ? a + sg * lda + fg : a;
-      cp_async16(RFAST ? lb + s * 64 + f : lb + s * PF_PITCH + f, src, bytes);
+      cp_async16(lb + s * PF_PITCH + f, src, bytes);
     }
   } else {
 #pragma unroll 4
@@ -317,7 +322,7 @@ __device__ __forceinline__ void load_tile(float* lb, const float* __restrict__ a
       const long long fg = (RFAST ? I0 : J0) + f, sg = (RFAST ? J0 : I0) + s;
       const int bytes = (fg < n && sg < n) ? 4 : 0;
       const float* src = bytes ? a + sg * lda + fg : a;
-      cp_async4(RFAST ? lb + s * 64 + f : lb + s * PF_PITCH + f, src, bytes);
+      cp_async4(lb + s * PF_PITCH + f, src, bytes);
     }
   }
 }
@@ -372,7 +377,7 @@ __device__ __forceinline__ void tile_product(const float* lb, const float* ys, i
   if (RFAST) {
 #pragma unroll 8
     for (int p = 0; p < RB; ++p) {
-      const float l = lb[p * 64 + r];
+      const float l = lb[p * PF_PITCH + r];
       if (CPT % 4 == 0) {
 #pragma unroll
         for (int k = 0; k < CPT; k += 4) {
@@ -408,6 +413,90 @@ __device__ __forceinline__ void tile_product(const float* lb, const float* ys, i
       }
     }
   }
+}
+
+// The look-back product of a 32-column chain on the tensor cores: acc (64 x 32) += G (64 x 64) Y
+// (64 x 32) with mma.sync m16n8k16 BF16.  Each FP32 operand is split into three BF16 parts
+// (x = x0 + x1 + x2, 24 bits, exact for FP32), and the six part products of one 64 x 64 tile are
+// accumulated, the small ones first, in registers that start at zero; the tile's sum is then added
+// to acc with an FP32 add.  The tensor cores' FP32 accumulation truncates, and adding every product
+// straight into acc's long running sum biased it: the solve's error grew 40-fold and cost the
+// refinement one to two steps.  Per tile, the error is below the CUDA-core product's (2.4e-7 vs
+// 8.1e-7 relative at n = 32768, 64 RHS).  The CUDA-core product reads three shared-memory wavefronts
+// per eight multiply-adds and bounds how fast a CTA that starts behind the chain catches up.  Warp w
+// computes rows 16 (w % 4) .. + 16 and columns 16 (w / 4) .. + 16 (two 8-column tiles); c[n][i] is
+// the m16n8 accumulator fragment of its n-th tile: rows g (i < 2) and g + 8, columns 2 t + (i & 1),
+// with g = lane / 4, t = lane % 4.  G: lb (RFAST: lb[p * 68 + rr], else lb[rr * 68 + p]); Y:
+// ysT[c * 68 + p].
+
+// x (a pair of FP32 values) as three packed BF16x2 parts, the low k in the low half.
+__device__ __forceinline__ void split3_bf16x2(float x0, float x1, uint32_t* part) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(x0, x1);
+    part[i] = *reinterpret_cast<const uint32_t*>(&v);
+    x0 -= __low2float(v);
+    x1 -= __high2float(v);
+  }
+}
+
+__device__ __forceinline__ void mma_bf16(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+template <bool RFAST>
+__device__ __forceinline__ void tile_product_tc(const float* lb, const float* ysT, int tid, float (*c)[4]) {
+  const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+  const int m0 = 16 * (warp & 3), n0 = 16 * (warp >> 2);
+  float s[2][4] = {};  // this tile's product, added to c once at the end
+#pragma unroll 1
+  for (int k0 = 0; k0 < RB; k0 += 16) {
+    // A fragment: rows m0 + g (+8), k columns k0 + 2t, +1 (regs 0, 1) and k0 + 2t + 8, +9 (regs 2, 3)
+    float av[8];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {      // k half: +0 / +8
+#pragma unroll
+      for (int rr = 0; rr < 2; ++rr) {  // row: g / g + 8
+        const int row = m0 + g + 8 * rr, k = k0 + 2 * t + 8 * h;
+        if (RFAST) {
+          av[4 * h + 2 * rr] = lb[k * PF_PITCH + row];
+          av[4 * h + 2 * rr + 1] = lb[(k + 1) * PF_PITCH + row];
+        } else {
+          const float2 v = *reinterpret_cast<const float2*>(lb + row * PF_PITCH + k);
+          av[4 * h + 2 * rr] = v.x;
+          av[4 * h + 2 * rr + 1] = v.y;
+        }
+      }
+    }
+    uint32_t ap[4][3];  // register i of the fragment (rows g, g+8, g, g+8 for i = 0..3), part
+#pragma unroll
+    for (int i = 0; i < 4; ++i) split3_bf16x2(av[2 * i], av[2 * i + 1], ap[i]);
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt) {
+      const int col = n0 + 8 * nt + g;
+      const float2 y0 = *reinterpret_cast<const float2*>(ysT + col * PF_PITCH + k0 + 2 * t);
+      const float2 y1 = *reinterpret_cast<const float2*>(ysT + col * PF_PITCH + k0 + 2 * t + 8);
+      uint32_t bp0[3], bp1[3];
+      split3_bf16x2(y0.x, y0.y, bp0);
+      split3_bf16x2(y1.x, y1.y, bp1);
+      // parts (p, q) with p + q = 2, then 1, then 0
+      mma_bf16(s[nt], ap[0][2], ap[1][2], ap[2][2], ap[3][2], bp0[0], bp1[0]);
+      mma_bf16(s[nt], ap[0][1], ap[1][1], ap[2][1], ap[3][1], bp0[1], bp1[1]);
+      mma_bf16(s[nt], ap[0][0], ap[1][0], ap[2][0], ap[3][0], bp0[2], bp1[2]);
+      mma_bf16(s[nt], ap[0][1], ap[1][1], ap[2][1], ap[3][1], bp0[0], bp1[0]);
+      mma_bf16(s[nt], ap[0][0], ap[1][0], ap[2][0], ap[3][0], bp0[1], bp1[1]);
+      mma_bf16(s[nt], ap[0][0], ap[1][0], ap[2][0], ap[3][0], bp0[0], bp1[0]);
+    }
+  }
+#pragma unroll
+  for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) c[nt][i] += s[nt][i];
 }
 
 // out[q] (+)= sum_p S[p * pitch + r] * ys[p][cq * CPT + q]: the product of a shared 64 x 64 matrix
@@ -545,7 +634,7 @@ __global__ void __launch_bounds__(256, 2) sweep_ll_kernel(const float* __restric
       const float d = sm.Ds[i * 65 + r];
       if (RFAST) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) m[j] = fmaf(d, sm.Lb[0][(cq * 16 + j) * 64 + i], m[j]);
+        for (int j = 0; j < 16; ++j) m[j] = fmaf(d, sm.Lb[0][(cq * 16 + j) * PF_PITCH + i], m[j]);
       } else {
 #pragma unroll
         for (int k4 = 0; k4 < 4; ++k4) {
@@ -565,9 +654,13 @@ __global__ void __launch_bounds__(256, 2) sweep_ll_kernel(const float* __restric
   // 3. the blocks before Jlast, in the order the chain delivers them.  Iteration k loads tile
   //    k + LL_NT - 1 into slot k % LL_NT (freed by tile k - 1, or by G_last for k = 0) and uses tile
   //    k from slot (k + 1) % LL_NT; its group is complete once at most LL_NT - 1 newer ones are pending.
+  constexpr bool TC = CPT == 8;  // 32-column chains: the look-back products on the tensor cores
   float acc[CPT];
 #pragma unroll
   for (int q = 0; q < CPT; ++q) acc[q] = 0.f;
+  float cf[2][4];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) cf[i >> 2][i & 3] = 0.f;
   for (int k = 0; k < nloop; ++k) {
     const int J = Jfirst + k * step;
     if (k + LL_NT - 1 < nloop)
@@ -575,8 +668,13 @@ __global__ void __launch_bounds__(256, 2) sweep_ll_kernel(const float* __restric
     cp_commit();
     const bool ok =
         ll_wait_block<CPT>(llc + (size_t)J * RB * RCT + tid * CPT, w, BWD ? J - I : I - J, err, wait_ns);
+    if (TC) {  // word tid * 8 + q is Y(tid / 4, (tid % 4) * 8 + q)
 #pragma unroll
-    for (int q = 0; q < CPT; ++q) sm.Ys[tid * CPT + q] = __uint_as_float(w[q]);
+      for (int q = 0; q < CPT; ++q) sm.Ys[((tid & 3) * 8 + q) * PF_PITCH + (tid >> 2)] = __uint_as_float(w[q]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < CPT; ++q) sm.Ys[tid * CPT + q] = __uint_as_float(w[q]);
+    }
     cp_wait<LL_NT - 1>();
     if (__syncthreads_or(!ok)) {
       asm volatile("cp.async.wait_all;" ::: "memory");
@@ -585,7 +683,21 @@ __global__ void __launch_bounds__(256, 2) sweep_ll_kernel(const float* __restric
     }
     // request the next awaited block's words before this product
     ll_load<CPT>(llc + (size_t)(k + 1 < nloop ? J + step : Jlast) * RB * RCT + tid * CPT, w);
-    tile_product<RFAST, CPT>(sm.Lb[(k + 1) % LL_NT], sm.Ys, r, cq, acc);
+    if (TC) tile_product_tc<RFAST>(sm.Lb[(k + 1) % LL_NT], sm.Ys, tid, cf);
+    else tile_product<RFAST, CPT>(sm.Lb[(k + 1) % LL_NT], sm.Ys, r, cq, acc);
+    __syncthreads();
+  }
+  if (TC) {  // the accumulator fragments back to thread (r, cq)'s row and columns, through Ys
+    const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    const int m0 = 16 * (warp & 3), n0 = 16 * (warp >> 2);
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        sm.Ys[(m0 + g + (i >> 1) * 8) * RCT + n0 + 8 * nt + 2 * t + (i & 1)] = cf[nt][i];
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) acc[q] = sm.Ys[r * RCT + cq * CPT + q];
     __syncthreads();
   }
 
