@@ -51,15 +51,19 @@ void launch_potrf_diag(T* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cud
 // factorisation).
 // pk > 0: the block first receives A11 -= P P^T with P the pk columns from column pk0 in the block's
 // rows (one panel step whose trailing update left the block out).
+// linv: also write L11^{-1} there (64 x 64 FP32, row-major, identity beyond bs) for
+// launch_trsm_panel_tc.
 void launch_potrf_diag_f32s(float* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s,
-                            int64_t pk0 = 0, int pk = 0);
+                            int64_t pk0 = 0, int pk = 0, float* linv = nullptr);
 // Rows below the block: A(k0+bs.., k0..k0+bs) <- A(...) L11^{-T}, rs rows.
 template <typename T>
 void launch_trsm_panel(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, cudaStream_t s);
-// The same FP32 solve, also writing the solved rows as np split parts (BF16, or TF32 when tf32 is
-// set), K-major with 64 columns per row: the operand of the mixed-precision in-panel update.
-void launch_trsm_panel_split(float* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, int tf32, int np,
-                             void* const* parts, cudaStream_t s);
+// The same FP32 solve as the product A21 L11^{-T} with the inverse from launch_potrf_diag_f32s, on
+// the tensor cores (mma.sync, three-part BF16 split: FP32-accurate), also writing the solved rows as
+// np split parts (BF16, or TF32 when tf32 is set; np = 0: none), K-major with 64 columns per row: the
+// operand of the mixed-precision in-panel update.
+void launch_trsm_panel_tc(float* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, const float* linv,
+                          int tf32, int np, void* const* parts, cudaStream_t s);
 // Lower update of the first ncols columns of the rs x rs trailing matrix by the bs-wide panel:
 // A22 -= A21 A21^T, or A22 -= A21 B^T with B the rs x bs array at bsrc (leading dimension ldb).
 template <typename T>

@@ -344,7 +344,7 @@ int split_parts(int prec) {
 //   ev[4]: the step's panel solve finished (aux waits before the in-panel update)
 //   ev[5]: the in-panel update finished (main waits before the next panel solve)
 int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int reserve_sms, void* const* parts,
-                    void* const* parts2, void* const* ipparts, int64_t ldk, DevStatus* st, int* d_err,
+                    void* const* parts2, void* const* ipparts, float* linv, int64_t ldk, DevStatus* st, int* d_err,
                     cudaStream_t s, cudaStream_t side, cudaEvent_t* ev, cudaStream_t aux) {
   static const std::string ksplit = "split_panel";
   const int kind = (prec == GBLLT_PREC_BF16 || prec == GBLLT_PREC_BF16X3 || prec == GBLLT_PREC_BF16X6) ? kTcBF16
@@ -365,8 +365,10 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
       const int jb = (int)(k0 + bs - j0 < kNB ? k0 + bs - j0 : kNB);
       const int64_t below = n - j0 - jb;
       const int64_t cols_left = k0 + bs - (j0 + jb);
+      // the split precisions solve the panel on the tensor cores with the block's inverse
+      float* const li = prec == GBLLT_PREC_FP32 ? nullptr : linv;
       if (diag_ready) diag_ready = false;
-      else launch_potrf_diag_f32s(af, ldf, j0, jb, st, s);
+      else launch_potrf_diag_f32s(af, ldf, j0, jb, st, s, 0, 0, li);
       if (prec == GBLLT_PREC_FP32) {
         launch_trsm_panel<float>(af, ldf, j0, jb, below, st, s);
         if (cols_left > 0 || rs > 0) launch_syrk_lower<float>(af, ldf, j0, jb, below, below, st, s);
@@ -377,11 +379,11 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
         u_pending = false;
       }
       if (cols_left == 0) {
-        launch_trsm_panel<float>(af, ldf, j0, jb, below, st, s);
+        launch_trsm_panel_tc(af, ldf, j0, jb, below, st, li, 0, 0, nullptr, s);
         continue;
       }
       // the solve writes the step's split operand too (K-major, 64 wide)
-      launch_trsm_panel_split(af, ldf, j0, jb, below, st, kind == kTcBF16 ? 0 : 1, np, ipparts, s);
+      launch_trsm_panel_tc(af, ldf, j0, jb, below, st, li, kind == kTcBF16 ? 0 : 1, np, ipparts, s);
       int64_t skip = 0;  // rows of the next diagonal block, left out of the in-panel update
       cudaStream_t us = s;
       if (aux) {
@@ -389,7 +391,7 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
         // itself) while the rest of the in-panel update runs on aux
         skip = cols_left < kNB ? cols_left : kNB;
         GB_CUDA_TRY(cudaEventRecord(ev[4], s));
-        launch_potrf_diag_f32s(af, ldf, j0 + jb, (int)skip, st, s, j0, jb);
+        launch_potrf_diag_f32s(af, ldf, j0 + jb, (int)skip, st, s, j0, jb, li);
         diag_ready = true;
         GB_CUDA_TRY(cudaStreamWaitEvent(aux, ev[4], 0));
         us = aux;
@@ -502,7 +504,7 @@ MixedLayout mixed_layout(int64_t n, int64_t nrhs, const gbllt_mixed_opts& o, boo
                ? 2 : 4;
   L.bytes = (size_t)L.ldf * n * 4 + (size_t)n * 8 + (size_t)n * nrhs * (8 + 4) + (size_t)L.nparts * n * nrhs * 8 +
             (size_t)L.nsq * 8 + 64 + (size_t)split_parts(o.precision) * (lookahead ? 2 : 1) * n * L.ldk * L.es_k +
-            (size_t)split_parts(o.precision) * (n * kNB * L.es_k + 256) +
+            (size_t)split_parts(o.precision) * (n * kNB * L.es_k + 256) + kNB * kNB * 4 + 256 +
             sizeof(DevStatus) + 16 * 256 + potrs_ws_bytes(n, 8);
   L.fallback_bytes = (size_t)n * n * 8 + 256;
   return L;
@@ -540,6 +542,7 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     for (int i = 0; i < split_parts(o.precision); ++i) parts2[i] = ar.take<char>((size_t)n * ldk * es_k);
   void* ipparts[3] = {nullptr, nullptr, nullptr};  // one 64-column step's operands for the in-panel update
   for (int i = 0; i < split_parts(o.precision); ++i) ipparts[i] = ar.take<char>((size_t)n * kNB * es_k);
+  float* linv = ar.take<float>(kNB * kNB);  // the current 64-column step's L11^{-1}
   DevStatus* st = ar.take<DevStatus>(1);
   int* d_err = (int*)&st->timeout;
   void* solve_ws = ar.take<char>(potrs_ws_bytes(n, 8));  // sized for the FP64 fallback solve too
@@ -683,13 +686,13 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
     }
     GB_CUDA_TRY(cudaEventRecord(xs.pre, xs.low));
     pre_ready = true;
-    rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, o.reserve_sms, parts, parts2, ipparts, ldk, st, d_err,
+    rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, o.reserve_sms, parts, parts2, ipparts, linv, ldk, st, d_err,
                          xs.fs, xs.side, xs.lev, xs.aux);
     if (rc) return rc;
     GB_CUDA_TRY(cudaEventRecord(xs.out, xs.fs));
     GB_CUDA_TRY(cudaStreamWaitEvent(s, xs.out, 0));
   } else {
-    rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, o.reserve_sms, parts, parts2, ipparts, ldk, st, d_err, s,
+    rc = potrf_mixed_f32(n, af, ldf, o.precision, o.panel, o.reserve_sms, parts, parts2, ipparts, linv, ldk, st, d_err, s,
                          nullptr, xs.lev, nullptr);
     if (rc) return rc;
   }

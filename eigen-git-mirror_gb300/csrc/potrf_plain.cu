@@ -12,7 +12,9 @@
 //                       FP64 pipe (balanced lanes, pivots off the critical path);
 //   trsm_panel_kernel   A21 <- A21 L11^{-T}: four threads per row of A21, the row held in
 //                       registers, L11 from shared memory (the OnTheRight solve that
-//                       LLT.h:364 issues, TriangularSolverMatrix.h:188-329);
+//                       LLT.h:364 issues, TriangularSolverMatrix.h:188-329).  The mixed-precision
+//                       factorisation's FP32 panels use trsm_panel_tc_kernel instead: the product
+//                       with L11^{-1} (formed by the FP32 diagonal kernel) on the tensor cores;
 //   syrk_lower_kernel   A22 -= A21 A21^T on 64 x 64 tiles of the lower triangle only (the rank
 //                       update of LLT.h:365 -> GeneralMatrixMatrixTriangular.h:57-194), each
 //                       thread accumulating a 4 x 4 register block over the panel depth.
@@ -23,6 +25,7 @@
 #include <cuda_bf16.h>
 
 #include "internal.h"
+#include "mma_split.cuh"
 
 namespace gbllt {
 
@@ -40,11 +43,16 @@ constexpr int NB = kNB;
 // pk columns pk0 .. pk0+pk-1 of the block's rows (the step's panel); the caller leaves the block out
 // of that step's own trailing update, so this factorisation does not wait for it.
 constexpr int DIAG_THREADS = 512;
-template <bool PRE>
+// LINV: the kernel also writes L11^{-1} (64 x 64, row-major, identity beyond bs) to linv, for the
+// tensor-core panel solve.  Warp w forms columns j = w, w + 16, w + 32, w + 48 of X = L11^{-1} by
+// right-looking substitution on the identity, lane l holding rows l and l + 32: at step k the lane of
+// row k divides by the pivot, one shuffle hands X(k, j) to the warp, and every lane updates its rows
+// below k.  Rows above a column's start stay exactly zero, so all four columns run one loop.
+template <bool PRE, bool LINV>
 __global__ void __launch_bounds__(DIAG_THREADS) potrf_diag_f32s_kernel(float* __restrict__ a, long long lda,
                                                                        long long k0, int bs,
                                                                        DevStatus* __restrict__ st, long long pk0,
-                                                                       int pk) {
+                                                                       int pk, float* __restrict__ linv) {
   if (st->fail_col >= 0) return;
   constexpr int G = DIAG_THREADS / NB;  // column groups
   __shared__ float s[NB][NB + 1];         // s[c][r] = A(r, c), lower part; L once column c is done
@@ -188,6 +196,39 @@ __global__ void __launch_bounds__(DIAG_THREADS) potrf_diag_f32s_kernel(float* __
     if (c < done && r < bs && r >= c) blk[(long long)c * lda + r] = s[c][r];
   }
   if (tid == 0 && done < bs) st->fail_col = k0 + done;
+  if constexpr (LINV) {
+    static_assert(DIAG_THREADS == 16 * 32, "sixteen warps, four columns of the inverse each");
+    if (done < bs) return;  // failed: the panel solve does not run
+    const int w = tid >> 5, l = tid & 31;
+    // s holds L (zero above the diagonal and beyond bs); the identity continues past bs
+    const float r0 = l < bs ? 1.f / s[l][l] : 1.f, r1 = l + 32 < bs ? 1.f / s[l + 32][l + 32] : 1.f;
+    float x0[4], x1[4];  // X(l, j_q), X(l + 32, j_q) with j_q = w + 16 q
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      x0[q] = l == w + 16 * q ? 1.f : 0.f;
+      x1[q] = l + 32 == w + 16 * q ? 1.f : 0.f;
+    }
+    for (int k = w; k < NB; ++k) {
+      const bool hi = k >= 32;  // warp-uniform
+      const int src = k & 31;
+      const float lk0 = l > k ? s[k][l] : 0.f, lk1 = l + 32 > k ? s[k][l + 32] : 0.f;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float xk = __shfl_sync(0xffffffffu, hi ? x1[q] * r1 : x0[q] * r0, src);
+        if (l == src) {
+          if (hi) x1[q] = xk;
+          else x0[q] = xk;
+        }
+        x0[q] = fmaf(-lk0, xk, x0[q]);
+        x1[q] = fmaf(-lk1, xk, x1[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      linv[l * NB + w + 16 * q] = x0[q];
+      linv[(l + 32) * NB + w + 16 * q] = x1[q];
+    }
+  }
 }
 
 // T = storage type, TC = arithmetic type (the mixed-precision path stores float and factors the
@@ -363,15 +404,12 @@ __device__ __forceinline__ void ld4(const T* p, T* v) {
 // updates its later columns x_p -= x_j L11(p, j), which are independent of each other.  L11 is kept
 // per sub-lane (Lq[s][j][m] = L11(4m + s, j)), so a thread's reads are 16-byte vectors; the
 // sub-lane blocks are 16 bytes apart in bank order.  Compared with one thread per row, the code is
-// a third as long and four times as many warps share it.
-// SPLIT (FP32 only): the solved row is also written as the K-major tensor-core operand of the
-// in-panel update, np successive roundings (SPLIT 1: BF16, 2: TF32) at parts[k][r * 64 + p].
+// a third as long and four times as many warps share it.  (The split precisions of the mixed
+// factorisation use trsm_panel_tc_kernel below instead.)
 constexpr int TRSM_ROWS = 32;  // rows per CTA of 128 threads
-template <typename T, int SPLIT>
+template <typename T>
 __global__ void __launch_bounds__(128) trsm_panel_kernel(T* __restrict__ a, long long lda, long long k0, int bs,
-                                                         long long rs, const DevStatus* __restrict__ st, int np,
-                                                         void* __restrict__ p0, void* __restrict__ p1,
-                                                         void* __restrict__ p2) {
+                                                         long long rs, const DevStatus* __restrict__ st) {
   if (st->fail_col >= 0) return;
   constexpr int QS = NB * 16 + 16 / (int)sizeof(T);  // sub-lane block stride
   __shared__ __align__(16) T Lq[4 * QS];
@@ -413,42 +451,149 @@ __global__ void __launch_bounds__(128) trsm_panel_kernel(T* __restrict__ a, long
     for (int m = 0; m < 16; ++m)
       if (4 * m + sl < bs) row[(long long)(4 * m + sl) * lda] = x[m];
   }
+}
+
+// A21 <- A21 L11^{-T} as a product with the inverse that the diagonal kernel wrote (linv[c * 64 + p]
+// = L11^{-1}(c, p)), on the tensor cores: mma.sync m16n8k16 with the three-part BF16 split of
+// mma_split.cuh (FP32-accurate; the six products of each output go into a zeroed accumulator, 64
+// deep).  The substitution kernel above is a chain of 64 dependent steps per row with a shuffle
+// each; this is one 64-deep product per row, the rows independent.  Linv's zero upper triangle is
+// skipped (8-column tiles left of the k16 step).
+// CTA: 128 threads, 64 rows (TT_ROWS).  The A21 tile is staged column by column (As[p * 68 + r],
+// coalesced 16-byte loads) and the inverse's parts as rows (Lp[part][c * 72 + p]); both pitches make
+// the fragment reads conflict-free.  Warp w owns rows 16 w .. 16 w + 15 and all 64 columns (eight
+// n8 tiles).  X goes back through As: column-major to A21, and as np split parts (K-major, 64 per
+// row) for the in-panel update.
+constexpr int TT_ROWS = 64, TT_PITCH = 68, TL_PITCH = 72;
+template <int SPLIT>
+__global__ void __launch_bounds__(128) trsm_panel_tc_kernel(float* __restrict__ a, long long lda, long long k0, int bs,
+                                                            long long rs, const DevStatus* __restrict__ st,
+                                                            const float* __restrict__ linv, int np,
+                                                            void* __restrict__ p0, void* __restrict__ p1,
+                                                            void* __restrict__ p2) {
+  if (st->fail_col >= 0) return;
+  __shared__ __align__(16) float As[NB * TT_PITCH];
+  __shared__ __align__(16) __nv_bfloat16 Lp[3][NB * TL_PITCH];
+  const int tid = threadIdx.x;
+  const long long row0 = (long long)blockIdx.x * TT_ROWS;
+  float* const src = a + k0 * lda + (k0 + bs) + row0;  // element (r, p) at src[p * lda + r]
+  const int nrow = rs - row0 < TT_ROWS ? (int)(rs - row0) : TT_ROWS;
+  const bool vec = (lda & 3) == 0 && ((k0 + bs + row0) & 3) == 0 && nrow == TT_ROWS;
+  // the A21 tile (zero beyond bs columns and nrow rows)
+  if (vec) {
+    float4 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = tid + 128 * u, p = idx >> 4, r4 = (idx & 15) * 4;
+      v[u] = p < bs ? *reinterpret_cast<const float4*>(src + (long long)p * lda + r4) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = tid + 128 * u, p = idx >> 4, r4 = (idx & 15) * 4;
+      *reinterpret_cast<float4*>(As + p * TT_PITCH + r4) = v[u];
+    }
+  } else {
+    for (int idx = tid; idx < NB * TT_ROWS; idx += 128) {
+      const int p = idx >> 6, r = idx & 63;
+      As[p * TT_PITCH + r] = (p < bs && r < nrow) ? src[(long long)p * lda + r] : 0.f;
+    }
+  }
+  // the inverse's three parts, row c of Linv at Lp[part][c * 72 ..]
+  {
+    float4 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = reinterpret_cast<const float4*>(linv)[tid + 128 * u];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = (tid + 128 * u) * 4, c = idx >> 6, p = idx & 63;
+      uint32_t lo[3], hi[3];
+      split3_bf16x2(v[u].x, v[u].y, lo);
+      split3_bf16x2(v[u].z, v[u].w, hi);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        *reinterpret_cast<uint2*>(&Lp[k][c * TL_PITCH + p]) = make_uint2(lo[k], hi[k]);
+    }
+  }
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+  const int m0 = 16 * warp;
+  float c[8][4];
+#pragma unroll
+  for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) c[nt][i] = 0.f;
+#pragma unroll
+  for (int ks = 0; ks < NB; ks += 16) {
+    uint32_t ap[4][3];  // A fragment register i (rows g, g + 8, g, g + 8; k 2t / 2t + 8), part
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int row = m0 + g + 8 * (i & 1), k = ks + 2 * t + 8 * (i >> 1);
+      split3_bf16x2(As[k * TT_PITCH + row], As[(k + 1) * TT_PITCH + row], ap[i]);
+    }
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      if (ks > 8 * nt + 7) continue;  // Linv(c, p) = 0 for p > c: the whole k16 x n8 block
+      const int col = 8 * nt + g;
+      uint32_t b0[3], b1[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        b0[k] = *reinterpret_cast<const uint32_t*>(&Lp[k][col * TL_PITCH + ks + 2 * t]);
+        b1[k] = *reinterpret_cast<const uint32_t*>(&Lp[k][col * TL_PITCH + ks + 2 * t + 8]);
+      }
+      mma_split6(c[nt], ap, b0, b1);
+    }
+  }
+  // X back into the warp's own rows of As (no other warp reads them), then out
+  __syncwarp();
+#pragma unroll
+  for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) As[(8 * nt + 2 * t + (i & 1)) * TT_PITCH + m0 + g + 8 * (i >> 1)] = c[nt][i];
+  __syncthreads();
+  if (vec) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = tid + 128 * u, p = idx >> 4, r4 = (idx & 15) * 4;
+      if (p < bs)
+        *reinterpret_cast<float4*>(src + (long long)p * lda + r4) = *reinterpret_cast<const float4*>(As + p * TT_PITCH + r4);
+    }
+  } else {
+    for (int idx = tid; idx < NB * TT_ROWS; idx += 128) {
+      const int p = idx >> 6, r = idx & 63;
+      if (p < bs && r < nrow) src[(long long)p * lda + r] = As[p * TT_PITCH + r];
+    }
+  }
   if constexpr (SPLIT != 0) {
-    static_assert(sizeof(T) == 4, "split operands are made from FP32 panels");
-    __shared__ float xs[TRSM_ROWS][NB + 1];  // the quad's row, gathered to 16 consecutive columns each
+    // 8 columns of one row per 16-byte BF16 store (two for TF32); consecutive threads, consecutive rows
+    for (int idx = tid; idx < TT_ROWS * (NB / 8); idx += 128) {
+      const int r = idx & 63, pc = (idx >> 6) * 8;
+      if (r >= nrow) continue;
+      float v[8];
 #pragma unroll
-    for (int m = 0; m < 16; ++m) xs[rl][4 * m + sl] = (float)x[m];
-    __syncwarp();
-    if (live) {
+      for (int u = 0; u < 8; ++u) v[u] = As[(pc + u) * TT_PITCH + r];
+      const long long e = (row0 + r) * NB + pc;
+      for (int k = 0; k < np; ++k) {
+        void* part = k == 0 ? p0 : (k == 1 ? p1 : p2);
+        if (SPLIT == 1) {
+          uint32_t w[4];
 #pragma unroll
-      for (int q = 0; q < 16; q += 8) {  // 8 columns: one 16-byte store of BF16, two of TF32
-        const int p = 16 * sl + q;
-        float v[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = xs[rl][p + u];
-        for (int k = 0; k < np; ++k) {
-          void* part = k == 0 ? p0 : (k == 1 ? p1 : p2);
-          if (SPLIT == 1) {
-            uint32_t w[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const __nv_bfloat16 lo = __float2bfloat16_rn(v[2 * u]), hi = __float2bfloat16_rn(v[2 * u + 1]);
-              v[2 * u] -= __bfloat162float(lo);
-              v[2 * u + 1] -= __bfloat162float(hi);
-              w[u] = (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-            }
-            *reinterpret_cast<uint4*>((__nv_bfloat16*)part + r * NB + p) = make_uint4(w[0], w[1], w[2], w[3]);
-          } else {
-            float h[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-              h[u] = to_tf32(v[u]);
-              v[u] -= h[u];
-            }
-            float4* dst = reinterpret_cast<float4*>((float*)part + r * NB + p);
-            dst[0] = make_float4(h[0], h[1], h[2], h[3]);
-            dst[1] = make_float4(h[4], h[5], h[6], h[7]);
+          for (int u = 0; u < 4; ++u) {
+            const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * u], v[2 * u + 1]);
+            w[u] = *reinterpret_cast<const uint32_t*>(&h);
+            v[2 * u] -= __low2float(h);
+            v[2 * u + 1] -= __high2float(h);
           }
+          *reinterpret_cast<uint4*>((__nv_bfloat16*)part + e) = make_uint4(w[0], w[1], w[2], w[3]);
+        } else {
+          float h[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            h[u] = to_tf32(v[u]);
+            v[u] -= h[u];
+          }
+          float4* dst = reinterpret_cast<float4*>((float*)part + e);
+          dst[0] = make_float4(h[0], h[1], h[2], h[3]);
+          dst[1] = make_float4(h[4], h[5], h[6], h[7]);
         }
       }
     }
@@ -582,12 +727,17 @@ void launch_potrf_diag(T* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cud
 }
 
 void launch_potrf_diag_f32s(float* a, int64_t lda, int64_t k0, int bs, DevStatus* st, cudaStream_t s, int64_t pk0,
-                            int pk) {
+                            int pk, float* linv) {
   static const std::string kd = "potrf_diag_f32";
   ProfScope ps(kd.c_str(), s, (double)bs * bs * bs / 3.0 + (double)bs * bs * pk,
                (double)bs * (bs + 1) * sizeof(float) + (double)bs * pk * sizeof(float));
-  if (pk > 0) potrf_diag_f32s_kernel<true><<<1, DIAG_THREADS, 0, s>>>(a, lda, k0, bs, st, pk0, pk);
-  else potrf_diag_f32s_kernel<false><<<1, DIAG_THREADS, 0, s>>>(a, lda, k0, bs, st, 0, 0);
+  if (linv) {
+    if (pk > 0) potrf_diag_f32s_kernel<true, true><<<1, DIAG_THREADS, 0, s>>>(a, lda, k0, bs, st, pk0, pk, linv);
+    else potrf_diag_f32s_kernel<false, true><<<1, DIAG_THREADS, 0, s>>>(a, lda, k0, bs, st, 0, 0, linv);
+  } else {
+    if (pk > 0) potrf_diag_f32s_kernel<true, false><<<1, DIAG_THREADS, 0, s>>>(a, lda, k0, bs, st, pk0, pk, nullptr);
+    else potrf_diag_f32s_kernel<false, false><<<1, DIAG_THREADS, 0, s>>>(a, lda, k0, bs, st, 0, 0, nullptr);
+  }
 }
 
 template <typename T>
@@ -595,19 +745,22 @@ void launch_trsm_panel(T* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevSta
   if (rs <= 0) return;
   static const std::string kt = std::string("trsm_panel_") + tname<T>();
   ProfScope ps(kt.c_str(), s, (double)rs * bs * bs, (2.0 * rs * bs + 0.5 * bs * bs) * sizeof(T));
-  trsm_panel_kernel<T, 0><<<(unsigned)ceil_div(rs, TRSM_ROWS), 128, 0, s>>>(a, lda, k0, bs, rs, st, 0, nullptr,
-                                                                            nullptr, nullptr);
+  trsm_panel_kernel<T><<<(unsigned)ceil_div(rs, TRSM_ROWS), 128, 0, s>>>(a, lda, k0, bs, rs, st);
 }
 
-void launch_trsm_panel_split(float* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, int tf32, int np,
-                             void* const* parts, cudaStream_t s) {
+void launch_trsm_panel_tc(float* a, int64_t lda, int64_t k0, int bs, int64_t rs, DevStatus* st, const float* linv,
+                          int tf32, int np, void* const* parts, cudaStream_t s) {
   if (rs <= 0) return;
   static const std::string kt = "trsm_panel_f32";
   ProfScope ps(kt.c_str(), s, (double)rs * bs * bs,
                (2.0 * rs * bs + 0.5 * bs * bs) * sizeof(float) + (double)rs * NB * np * (tf32 ? 4.0 : 2.0));
-  const unsigned g = (unsigned)ceil_div(rs, TRSM_ROWS);
-  if (tf32) trsm_panel_kernel<float, 2><<<g, 128, 0, s>>>(a, lda, k0, bs, rs, st, np, parts[0], parts[1], parts[2]);
-  else trsm_panel_kernel<float, 1><<<g, 128, 0, s>>>(a, lda, k0, bs, rs, st, np, parts[0], parts[1], parts[2]);
+  const unsigned g = (unsigned)ceil_div(rs, TT_ROWS);
+  void* p0 = np > 0 ? parts[0] : nullptr;
+  void* p1 = np > 1 ? parts[1] : nullptr;
+  void* p2 = np > 2 ? parts[2] : nullptr;
+  if (np == 0) trsm_panel_tc_kernel<0><<<g, 128, 0, s>>>(a, lda, k0, bs, rs, st, linv, 0, p0, p1, p2);
+  else if (tf32) trsm_panel_tc_kernel<2><<<g, 128, 0, s>>>(a, lda, k0, bs, rs, st, linv, np, p0, p1, p2);
+  else trsm_panel_tc_kernel<1><<<g, 128, 0, s>>>(a, lda, k0, bs, rs, st, linv, np, p0, p1, p2);
 }
 
 template <typename T>

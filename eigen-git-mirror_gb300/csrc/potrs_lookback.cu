@@ -21,8 +21,6 @@
 // L has a unit diagonal (trinv_kernel<UNIT>) and the diagonal of the stored factor holds D; the
 // backward sweep applies D's pseudo-inverse to each block's right-hand sides as it loads them
 // (DSCALE: divide where |d| > the smallest normal number, else 0, LDLT.h:587-600).
-#include <cuda_bf16.h>
-
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -30,6 +28,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "mma_split.cuh"
 
 namespace gbllt {
 
@@ -416,10 +415,9 @@ __device__ __forceinline__ void tile_product(const float* lb, const float* ys, i
 }
 
 // The look-back product of a 32-column chain on the tensor cores: acc (64 x 32) += G (64 x 64) Y
-// (64 x 32) with mma.sync m16n8k16 BF16.  Each FP32 operand is split into three BF16 parts
-// (x = x0 + x1 + x2, 24 bits, exact for FP32), and the six part products of one 64 x 64 tile are
-// accumulated, the small ones first, in registers that start at zero; the tile's sum is then added
-// to acc with an FP32 add.  The tensor cores' FP32 accumulation truncates, and adding every product
+// (64 x 32) with mma.sync m16n8k16 BF16 and the three-part split of mma_split.cuh: the six part
+// products of one 64 x 64 tile are accumulated, the small ones first, in registers that start at
+// zero; the tile's sum is then added to acc with an FP32 add.  The tensor cores' FP32 accumulation truncates, and adding every product
 // straight into acc's long running sum biased it: the solve's error grew 40-fold and cost the
 // refinement one to two steps.  Per tile, the error is below the CUDA-core product's (2.4e-7 vs
 // 8.1e-7 relative at n = 32768, 64 RHS).  The CUDA-core product reads three shared-memory wavefronts
@@ -428,26 +426,6 @@ __device__ __forceinline__ void tile_product(const float* lb, const float* ys, i
 // the m16n8 accumulator fragment of its n-th tile: rows g (i < 2) and g + 8, columns 2 t + (i & 1),
 // with g = lane / 4, t = lane % 4.  G: lb (RFAST: lb[p * 68 + rr], else lb[rr * 68 + p]); Y:
 // ysT[c * 68 + p].
-
-// x (a pair of FP32 values) as three packed BF16x2 parts, the low k in the low half.
-__device__ __forceinline__ void split3_bf16x2(float x0, float x1, uint32_t* part) {
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const __nv_bfloat162 v = __floats2bfloat162_rn(x0, x1);
-    part[i] = *reinterpret_cast<const uint32_t*>(&v);
-    x0 -= __low2float(v);
-    x1 -= __high2float(v);
-  }
-}
-
-__device__ __forceinline__ void mma_bf16(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
-                                         uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
-      "{%0, %1, %2, %3};"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
 
 template <bool RFAST>
 __device__ __forceinline__ void tile_product_tc(const float* lb, const float* ysT, int tid, float (*c)[4]) {
@@ -484,13 +462,7 @@ __device__ __forceinline__ void tile_product_tc(const float* lb, const float* ys
       uint32_t bp0[3], bp1[3];
       split3_bf16x2(y0.x, y0.y, bp0);
       split3_bf16x2(y1.x, y1.y, bp1);
-      // parts (p, q) with p + q = 2, then 1, then 0
-      mma_bf16(s[nt], ap[0][2], ap[1][2], ap[2][2], ap[3][2], bp0[0], bp1[0]);
-      mma_bf16(s[nt], ap[0][1], ap[1][1], ap[2][1], ap[3][1], bp0[1], bp1[1]);
-      mma_bf16(s[nt], ap[0][0], ap[1][0], ap[2][0], ap[3][0], bp0[2], bp1[2]);
-      mma_bf16(s[nt], ap[0][1], ap[1][1], ap[2][1], ap[3][1], bp0[0], bp1[0]);
-      mma_bf16(s[nt], ap[0][0], ap[1][0], ap[2][0], ap[3][0], bp0[1], bp1[1]);
-      mma_bf16(s[nt], ap[0][0], ap[1][0], ap[2][0], ap[3][0], bp0[0], bp1[0]);
+      mma_split6(s[nt], ap, bp0, bp1);
     }
   }
 #pragma unroll
