@@ -30,32 +30,50 @@ namespace {
 
 constexpr int TS = 32;  // conversion tile
 
-// Af(i, j) = d_i * A(i, j) * d_j for i >= j (A given by its lower or upper triangle), as float.
-template <bool UP>
-__global__ void __launch_bounds__(256) convert_scaled_kernel(const double* __restrict__ a, long long lda, long long n,
-                                                             const double* __restrict__ d, float* __restrict__ af,
-                                                             long long ldf) {
+// Af(i, j) = d_i * A(i, j) * d_j for i >= j, as float, A given by its upper triangle: element
+// (i, j), i >= j, lives at a[i * lda + j], so each 32 x 32 tile is transposed through shared memory.
+__global__ void __launch_bounds__(256) convert_scaled_upper_kernel(const double* __restrict__ a, long long lda,
+                                                                   long long n, const double* __restrict__ d,
+                                                                   float* __restrict__ af, long long ldf) {
   __shared__ double t[TS][TS + 1];
   int ti, tj;
   lower_tile_coords(blockIdx.x, ti, tj);
   const long long i0 = (long long)ti * TS, j0 = (long long)tj * TS;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  if (!UP) {
-    for (int c = ty; c < TS; c += 8) {
-      const long long i = i0 + tx, j = j0 + c;
-      if (i < n && j < n && i >= j) af[j * ldf + i] = (float)(d[i] * a[j * lda + i] * d[j]);
+  for (int c = ty; c < TS; c += 8) {
+    const long long col = i0 + c, row = j0 + tx;  // a[col * lda + row] = A(row, col) = A(col, row)
+    if (col < n && row < n && col >= row) t[c][tx] = a[col * lda + row];
+  }
+  __syncthreads();
+  for (int c = ty; c < TS; c += 8) {
+    const long long i = i0 + tx, j = j0 + c;
+    if (i < n && j < n && i >= j) af[j * ldf + i] = (float)(d[i] * t[tx][c] * d[j]);
+  }
+}
+
+// The same conversion for a lower-stored A, a column at a time: CTA b takes columns b, b + gridDim.x,
+// ... and its threads stream down each column from the diagonal (coalesced reads and writes, four
+// rows per thread in flight).  One CTA per 32 x 32 tile, as above, spent more time starting tiles
+// than moving bytes (about 1 TB/s at n = 32768); the product is the same, so is the result.
+__global__ void __launch_bounds__(256) convert_scaled_lower_kernel(const double* __restrict__ a, long long lda,
+                                                                   long long n, const double* __restrict__ d,
+                                                                   float* __restrict__ af, long long ldf) {
+  for (long long j = blockIdx.x; j < n; j += gridDim.x) {
+    const double dj = d[j];
+    const double* col = a + j * lda;
+    float* out = af + j * ldf;
+    long long i = j + threadIdx.x;
+    for (; i + 3 * 256 < n; i += 4 * 256) {
+      double v[4], di[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        v[u] = col[i + u * 256];
+        di[u] = d[i + u * 256];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) out[i + u * 256] = (float)(di[u] * v[u] * dj);
     }
-  } else {
-    // element (i, j), i >= j, lives at a[i * lda + j] (upper storage of the transpose)
-    for (int c = ty; c < TS; c += 8) {
-      const long long col = i0 + c, row = j0 + tx;  // a[col * lda + row] = A(row, col) = A(col, row)
-      if (col < n && row < n && col >= row) t[c][tx] = a[col * lda + row];
-    }
-    __syncthreads();
-    for (int c = ty; c < TS; c += 8) {
-      const long long i = i0 + tx, j = j0 + c;
-      if (i < n && j < n && i >= j) af[j * ldf + i] = (float)(d[i] * t[tx][c] * d[j]);
-    }
+    for (; i < n; i += 256) out[i] = (float)(d[i] * col[i] * dj);
   }
 }
 
@@ -613,9 +631,18 @@ int posv_mixed_core(bool upper, int64_t n, int64_t nrhs, const double* a, int64_
   if (upper) diag_scale_kernel<true><<<grid1(n), 256, 0, s>>>(a, lda, n, dsc);
   else diag_scale_kernel<false><<<grid1(n), 256, 0, s>>>(a, lda, n, dsc);
   {
+    static const std::string kc = "convert_scaled";
+    ProfScope ps(kc.c_str(), s, 2.0 * n * (n + 1) / 2, (double)n * (n + 1) / 2 * 12.0);
     const int64_t nt = ceil_div(n, TS);
-    if (upper) convert_scaled_kernel<true><<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(a, lda, n, dsc, af, ldf);
-    else convert_scaled_kernel<false><<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(a, lda, n, dsc, af, ldf);
+    if (upper) {
+      convert_scaled_upper_kernel<<<(unsigned)(nt * (nt + 1) / 2), 256, 0, s>>>(a, lda, n, dsc, af, ldf);
+    } else {
+      int sms = 0, dev = 0;
+      GB_CUDA_TRY(cudaGetDevice(&dev));
+      GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      const int64_t g = (int64_t)sms * 8;
+      convert_scaled_lower_kernel<<<(unsigned)(n < g ? n : g), 256, 0, s>>>(a, lda, n, dsc, af, ldf);
+    }
   }
   // 2. low-precision factorisation.  Where creating streams is allowed it runs on three internal
   // streams of the highest priority (chain, look-ahead update, next diagonal block), fenced to the

@@ -43,11 +43,12 @@ constexpr int NB = kNB;
 // pk columns pk0 .. pk0+pk-1 of the block's rows (the step's panel); the caller leaves the block out
 // of that step's own trailing update, so this factorisation does not wait for it.
 constexpr int DIAG_THREADS = 512;
-// LINV: the kernel also writes L11^{-1} (64 x 64, row-major, identity beyond bs) to linv, for the
-// tensor-core panel solve.  Warp w forms columns j = w, w + 16, w + 32, w + 48 of X = L11^{-1} by
-// right-looking substitution on the identity, lane l holding rows l and l + 32: at step k the lane of
-// row k divides by the pivot, one shuffle hands X(k, j) to the warp, and every lane updates its rows
-// below k.  Rows above a column's start stay exactly zero, so all four columns run one loop.
+// LINV: the kernel also writes X = L11^{-1} (64 x 64, row-major, identity beyond bs) to linv, for the
+// tensor-core panel solve, in 16 x 16 blocks: 64 threads invert the four diagonal blocks (thread
+// (b, j) substitutes column j of block b, unrolled, L read by broadcast), then the blocks below
+// follow by distance from the diagonal, d = 1, 2, 3: T = sum_{k=j}^{i-1} L_ik X_kj, then
+// X_ij = -X_ii T, every entry of a level at once.  Seven barriers; a warp substitution over the
+// whole block issued ten times the instructions.
 template <bool PRE, bool LINV>
 __global__ void __launch_bounds__(DIAG_THREADS) potrf_diag_f32s_kernel(float* __restrict__ a, long long lda,
                                                                        long long k0, int bs,
@@ -70,9 +71,9 @@ __global__ void __launch_bounds__(DIAG_THREADS) potrf_diag_f32s_kernel(float* __
 #pragma unroll
     for (int u = 0; u < NB * NB / DIAG_THREADS; ++u) s[(tid >> 6) + u * G][tid & 63] = v[u];
   }
+  constexpr int PP = NB + 4;                   // row pitch: rows stay 16-byte aligned
+  __shared__ __align__(16) float pr[NB * PP];  // PRE: pr[r * PP + q] = P(r, q), zero beyond pk; LINV: X
   if constexpr (PRE) {
-    constexpr int PP = NB + 4;                // row pitch: rows stay 16-byte aligned
-    __shared__ __align__(16) float pr[NB * PP];  // pr[r * PP + q] = P(r, q), zero beyond pk
     const float* pan = a + pk0 * lda + k0;
     {
       float v[NB * NB / DIAG_THREADS];
@@ -197,36 +198,52 @@ __global__ void __launch_bounds__(DIAG_THREADS) potrf_diag_f32s_kernel(float* __
   }
   if (tid == 0 && done < bs) st->fail_col = k0 + done;
   if constexpr (LINV) {
-    static_assert(DIAG_THREADS == 16 * 32, "sixteen warps, four columns of the inverse each");
-    if (done < bs) return;  // failed: the panel solve does not run
-    const int w = tid >> 5, l = tid & 31;
+    static_assert(DIAG_THREADS >= 3 * 256 / 2 && NB == 64, "four 16 x 16 blocks per side");
+    if (done < bs) return;  // failed: the panel solve does not run (block-uniform)
     // s holds L (zero above the diagonal and beyond bs); the identity continues past bs
-    const float r0 = l < bs ? 1.f / s[l][l] : 1.f, r1 = l + 32 < bs ? 1.f / s[l + 32][l + 32] : 1.f;
-    float x0[4], x1[4];  // X(l, j_q), X(l + 32, j_q) with j_q = w + 16 q
+    float* xs = pr;                  // xs[r * PP + c] = X(r, c)
+    __shared__ float rinv[NB];       // 1 / L(r, r), 1 beyond bs
+    __shared__ float tb[3][16][17];  // T of the blocks of one level
+    if (tid < NB) rinv[tid] = tid < bs ? 1.f / s[tid][tid] : 1.f;
+    __syncthreads();
+    if (tid < NB) {  // diagonal block b, column j: rows i = 0 .. 15 by substitution
+      const int b = tid >> 4, j = tid & 15, o = 16 * b;
+      float x[16];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      x0[q] = l == w + 16 * q ? 1.f : 0.f;
-      x1[q] = l + 32 == w + 16 * q ? 1.f : 0.f;
-    }
-    for (int k = w; k < NB; ++k) {
-      const bool hi = k >= 32;  // warp-uniform
-      const int src = k & 31;
-      const float lk0 = l > k ? s[k][l] : 0.f, lk1 = l + 32 > k ? s[k][l + 32] : 0.f;
+      for (int i = 0; i < 16; ++i) {
+        float acc = i == j ? 1.f : 0.f;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float xk = __shfl_sync(0xffffffffu, hi ? x1[q] * r1 : x0[q] * r0, src);
-        if (l == src) {
-          if (hi) x1[q] = xk;
-          else x0[q] = xk;
-        }
-        x0[q] = fmaf(-lk0, xk, x0[q]);
-        x1[q] = fmaf(-lk1, xk, x1[q]);
+        for (int k = 0; k < i; ++k) acc = fmaf(-s[o + k][o + i], x[k], acc);  // x[k] = 0 for k < j
+        x[i] = acc * rinv[o + i];
       }
-    }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      linv[l * NB + w + 16 * q] = x0[q];
-      linv[(l + 32) * NB + w + 16 * q] = x1[q];
+      for (int i = 0; i < 16; ++i) xs[(o + i) * PP + o + j] = x[i];
+    }
+    __syncthreads();
+    for (int d = 1; d < 4; ++d) {
+      const int cnt = (4 - d) * 256;  // blocks (j + d, j), j = 0 .. 3 - d
+      for (int idx = tid; idx < cnt; idx += DIAG_THREADS) {
+        const int jb = idx >> 8, r = (idx >> 4) & 15, c = idx & 15, ib = jb + d;
+        float t0 = 0.f, t1 = 0.f;
+        for (int q = 16 * jb; q < 16 * ib; q += 2) {
+          t0 = fmaf(s[q][16 * ib + r], xs[q * PP + 16 * jb + c], t0);
+          t1 = fmaf(s[q + 1][16 * ib + r], xs[(q + 1) * PP + 16 * jb + c], t1);
+        }
+        tb[jb][r][c] = t0 + t1;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < cnt; idx += DIAG_THREADS) {
+        const int jb = idx >> 8, r = (idx >> 4) & 15, c = idx & 15, ib = jb + d;
+        float v = 0.f;
+#pragma unroll
+        for (int m = 0; m < 16; ++m) v = fmaf(xs[(16 * ib + r) * PP + 16 * ib + m], tb[jb][m][c], v);
+        xs[(16 * ib + r) * PP + 16 * jb + c] = -v;
+      }
+      __syncthreads();
+    }
+    for (int idx = tid; idx < NB * NB; idx += DIAG_THREADS) {
+      const int r = idx >> 6, c = idx & 63;
+      linv[idx] = (c >> 4) <= (r >> 4) ? xs[r * PP + c] : 0.f;
     }
   }
 }
