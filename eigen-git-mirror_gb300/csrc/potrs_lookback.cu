@@ -276,10 +276,15 @@ struct LLSmem {
   float Lb[LL_NT][RB * PF_PITCH];  // off-diagonal tiles: three loads in flight behind the one in use
   float Ds[RB * (RB + 1)];     // Ds[i * 65 + r] = D(r, i)
   float Ms[RB * RB];           // Ms[p * 64 + r] = M(r, p)
-  // staged 64 x RCT block; flat index = word index, or (32-column chains, whose look-back products
-  // run on the tensor cores) column by column with row pitch PF_PITCH: Ys[c * 68 + p] = Y(p, c)
-  float Ys[RB * RCT > RCT * PF_PITCH ? RB * RCT : RCT * PF_PITCH];
+  // staged 64 x RCT block, flat index = word index; for 32-column chains, whose look-back products
+  // run on the tensor cores, the block's three BF16 parts instead (ys_part_index), 12 KB
+  float Ys[RCT == 32 ? 3 * 32 * 32 : RB * RCT];
 };
+
+// Word of the packed BF16 pair (Y(2 pi, c), Y(2 pi + 1, c)) of part `part` in the staged parts: column c
+// holds its 32 pairs at c * 32, the pair index XOR-swizzled by (c % 8) * 4 so that the eight columns
+// and four pairs that a warp's B-fragment load touches fall in 32 different banks.
+__device__ __forceinline__ int ys_part_index(int part, int c, int pi) { return part * 1024 + c * 32 + (pi ^ ((c & 7) << 2)); }
 
 __device__ __forceinline__ uint32_t sptr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -416,24 +421,25 @@ __device__ __forceinline__ void tile_product(const float* lb, const float* ys, i
 
 // The look-back product of a 32-column chain on the tensor cores: acc (64 x 32) += G (64 x 64) Y
 // (64 x 32) with mma.sync m16n8k16 BF16 and the three-part split of mma_split.cuh: the six part
-// products of one 64 x 64 tile are accumulated, the small ones first, in registers that start at
-// zero; the tile's sum is then added to acc with an FP32 add.  The tensor cores' FP32 accumulation truncates, and adding every product
-// straight into acc's long running sum biased it: the solve's error grew 40-fold and cost the
-// refinement one to two steps.  Per tile, the error is below the CUDA-core product's (2.4e-7 vs
-// 8.1e-7 relative at n = 32768, 64 RHS).  The CUDA-core product reads three shared-memory wavefronts
-// per eight multiply-adds and bounds how fast a CTA that starts behind the chain catches up.  Warp w
-// computes rows 16 (w % 4) .. + 16 and columns 16 (w / 4) .. + 16 (two 8-column tiles); c[n][i] is
-// the m16n8 accumulator fragment of its n-th tile: rows g (i < 2) and g + 8, columns 2 t + (i & 1),
-// with g = lane / 4, t = lane % 4.  G: lb (RFAST: lb[p * 68 + rr], else lb[rr * 68 + p]); Y:
-// ysT[c * 68 + p].
-
+// products of one tile are accumulated, the small ones first, in registers that start at zero; the
+// tile's sum is then added to acc with an FP32 add.  The tensor cores' FP32 accumulation truncates,
+// and adding every product straight into acc's long running sum biased it: the solve's error grew
+// 40-fold and cost the refinement one to two steps.  Per tile, the error is below the CUDA-core
+// product's (2.4e-7 vs 8.1e-7 relative at n = 32768, 64 RHS).
+// Y's parts are split once per tile when the block is staged (stage_y_parts); warp w takes rows
+// 16 (w % 4) .. + 16 and the K half 32 (w / 4) .. + 32 of the tile for all 32 columns, so each G entry
+// is split by one warp.  (Splitting Y in every warp and G in two, the product bounded how fast a CTA
+// that starts behind the chain caught up: two sweeps at n = 32768, 64 RHS, took 6.26 ms, 4.01 ms
+// with no product at all.)  c[n][i] is the m16n8 accumulator fragment of the warp's n-th 8-column
+// tile over its K half: rows g (i < 2) and g + 8, columns 2 t + (i & 1), g = lane / 4, t = lane % 4.
+// G: lb (RFAST: lb[p * 68 + rr], else lb[rr * 68 + p]).
 template <bool RFAST>
-__device__ __forceinline__ void tile_product_tc(const float* lb, const float* ysT, int tid, float (*c)[4]) {
+__device__ __forceinline__ void tile_product_tc(const float* lb, const uint32_t* yp, int tid, float (*c)[4]) {
   const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
-  const int m0 = 16 * (warp & 3), n0 = 16 * (warp >> 2);
-  float s[2][4] = {};  // this tile's product, added to c once at the end
-#pragma unroll 1
-  for (int k0 = 0; k0 < RB; k0 += 16) {
+  const int m0 = 16 * (warp & 3), kh = 32 * (warp >> 2);
+  float s[4][4] = {};  // this tile's product, added to c once at the end
+#pragma unroll
+  for (int k0 = kh; k0 < kh + 32; k0 += 16) {
     // A fragment: rows m0 + g (+8), k columns k0 + 2t, +1 (regs 0, 1) and k0 + 2t + 8, +9 (regs 2, 3)
     float av[8];
 #pragma unroll
@@ -455,20 +461,40 @@ __device__ __forceinline__ void tile_product_tc(const float* lb, const float* ys
 #pragma unroll
     for (int i = 0; i < 4; ++i) split3_bf16x2(av[2 * i], av[2 * i + 1], ap[i]);
 #pragma unroll
-    for (int nt = 0; nt < 2; ++nt) {
-      const int col = n0 + 8 * nt + g;
-      const float2 y0 = *reinterpret_cast<const float2*>(ysT + col * PF_PITCH + k0 + 2 * t);
-      const float2 y1 = *reinterpret_cast<const float2*>(ysT + col * PF_PITCH + k0 + 2 * t + 8);
+    for (int nt = 0; nt < 4; ++nt) {
+      const int col = 8 * nt + g, pi = k0 / 2 + t;
       uint32_t bp0[3], bp1[3];
-      split3_bf16x2(y0.x, y0.y, bp0);
-      split3_bf16x2(y1.x, y1.y, bp1);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        bp0[q] = yp[ys_part_index(q, col, pi)];
+        bp1[q] = yp[ys_part_index(q, col, pi + 4)];
+      }
       mma_split6(s[nt], ap, bp0, bp1);
     }
   }
 #pragma unroll
-  for (int nt = 0; nt < 2; ++nt)
+  for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
     for (int i = 0; i < 4; ++i) c[nt][i] += s[nt][i];
+}
+
+// Stage the awaited block's words (thread tid holds Y(tid / 4, (tid % 4) * 8 + q) in w[q]) as the
+// three BF16 parts of row pairs: a thread and the one holding the neighbouring row (tid ^ 4) swap
+// one word per column, the even row's thread packs and splits columns 0..3 of its eight, the odd
+// row's columns 4..7.
+__device__ __forceinline__ void stage_y_parts(const unsigned* w, uint32_t* yp, int tid) {
+  const int p = tid >> 2, c0 = (tid & 3) * 8;
+  const bool even = (p & 1) == 0;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const unsigned other = __shfl_xor_sync(0xffffffffu, even ? w[u + 4] : w[u], 4);
+    const int q = even ? u : u + 4;
+    const float lo = __uint_as_float(even ? w[u] : other), hi = __uint_as_float(even ? other : w[u + 4]);
+    uint32_t part[3];
+    split3_bf16x2(lo, hi, part);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) yp[ys_part_index(k, c0 + q, p >> 1)] = part[k];
+  }
 }
 
 // out[q] (+)= sum_p S[p * pitch + r] * ys[p][cq * CPT + q]: the product of a shared 64 x 64 matrix
@@ -630,9 +656,10 @@ __global__ void __launch_bounds__(256, 2) sweep_ll_kernel(const float* __restric
   float acc[CPT];
 #pragma unroll
   for (int q = 0; q < CPT; ++q) acc[q] = 0.f;
-  float cf[2][4];
+  float cf[4][4];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) cf[i >> 2][i & 3] = 0.f;
+  for (int i = 0; i < 16; ++i) cf[i >> 2][i & 3] = 0.f;
+  uint32_t* const yp = reinterpret_cast<uint32_t*>(sm.Ys);
   for (int k = 0; k < nloop; ++k) {
     const int J = Jfirst + k * step;
     if (k + LL_NT - 1 < nloop)
@@ -641,8 +668,7 @@ __global__ void __launch_bounds__(256, 2) sweep_ll_kernel(const float* __restric
     const bool ok =
         ll_wait_block<CPT>(llc + (size_t)J * RB * RCT + tid * CPT, w, BWD ? J - I : I - J, err, wait_ns);
     if (TC) {  // word tid * 8 + q is Y(tid / 4, (tid % 4) * 8 + q)
-#pragma unroll
-      for (int q = 0; q < CPT; ++q) sm.Ys[((tid & 3) * 8 + q) * PF_PITCH + (tid >> 2)] = __uint_as_float(w[q]);
+      stage_y_parts(w, yp, tid);
     } else {
 #pragma unroll
       for (int q = 0; q < CPT; ++q) sm.Ys[tid * CPT + q] = __uint_as_float(w[q]);
@@ -655,21 +681,22 @@ __global__ void __launch_bounds__(256, 2) sweep_ll_kernel(const float* __restric
     }
     // request the next awaited block's words before this product
     ll_load<CPT>(llc + (size_t)(k + 1 < nloop ? J + step : Jlast) * RB * RCT + tid * CPT, w);
-    if (TC) tile_product_tc<RFAST>(sm.Lb[(k + 1) % LL_NT], sm.Ys, tid, cf);
+    if (TC) tile_product_tc<RFAST>(sm.Lb[(k + 1) % LL_NT], yp, tid, cf);
     else tile_product<RFAST, CPT>(sm.Lb[(k + 1) % LL_NT], sm.Ys, r, cq, acc);
     __syncthreads();
   }
-  if (TC) {  // the accumulator fragments back to thread (r, cq)'s row and columns, through Ys
+  if (TC) {  // the two K halves' fragments back to thread (r, cq)'s row and columns, through the idle
+             // tile slots 1 and 2 (row pitch 36)
     const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
-    const int m0 = 16 * (warp & 3), n0 = 16 * (warp >> 2);
+    const int m0 = 16 * (warp & 3);
+    float* const half = sm.Lb[1 + (warp >> 2)];
 #pragma unroll
-    for (int nt = 0; nt < 2; ++nt)
+    for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
-        sm.Ys[(m0 + g + (i >> 1) * 8) * RCT + n0 + 8 * nt + 2 * t + (i & 1)] = cf[nt][i];
+      for (int i = 0; i < 4; ++i) half[(m0 + g + (i >> 1) * 8) * 36 + 8 * nt + 2 * t + (i & 1)] = cf[nt][i];
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < CPT; ++q) acc[q] = sm.Ys[r * RCT + cq * CPT + q];
+    for (int q = 0; q < CPT; ++q) acc[q] = sm.Lb[1][r * 36 + cq * CPT + q] + sm.Lb[2][r * 36 + cq * CPT + q];
     __syncthreads();
   }
 
