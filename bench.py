@@ -290,9 +290,9 @@ def measured_peaks() -> dict:
 #     once per 16-column chunk of right-hand sides, so traffic grows as n^2 * ceil(k / 16).
 #   sweep_f32 (chains of 32 columns): 578 MB at n = 16384, 64 RHS (mean of the forward and backward
 #     launch); the triangle of L is read about once whatever k is, so traffic grows as n^2.
-#   tc_update_bf16: the look-ahead launch at n = 8192 moved 0.75 of its algorithmic bytes (C read and
-#     written once in FP32, the operand parts once; part of C stays in L2): the launch's algorithmic
-#     bytes times that ratio.
+#   tc_update_bf16: the look-ahead launch at n = 8192 moved 0.75 of its algorithmic bytes with BF16x6
+#     and 0.755 with BF16x3 (C read and written once in FP32, the operand parts once; part of C stays
+#     in L2): the launch's algorithmic bytes times that ratio.
 NCU_TRAFFIC = {"symm_residual_f64": (8192, 64, 1.628e9, "n2_kchunks"),
                "sweep_f32": (16384, 64, 5.78e8, "n2"),
                "tc_update_bf16": (8192, 64, 0.75, "ratio")}
@@ -383,7 +383,8 @@ def measure_config(args, cfg, ws, rank, local, peaks, steps, warmup, profile_ste
     info = torch.zeros(1, dtype=torch.int64, device="cuda")
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
-    opts = G.mixed_opts(args.mixed_precision, 10, 1e-14, fallback=False, reserve_sms=args.reserve_sms)
+    opts = G.mixed_opts(args.mixed_precision, 10, 1e-14, fallback=False, panel=args.panel,
+                        reserve_sms=args.reserve_sms)
     nseg = SPLIT_PRODUCTS[args.mixed_precision]
     reports = []
 
@@ -864,12 +865,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="the default configuration's line without the "
                     "kappa sweep and the C1 / C4 / C5 keys")
-    ap.add_argument("--mixed-precision", default="bf16x6", choices=sorted(SPLIT_PRODUCTS))
+    ap.add_argument("--mixed-precision", default="bf16x3", choices=sorted(SPLIT_PRODUCTS),
+                    help="split of the mixed factorisation's tensor-core products (bf16x3: two BF16 parts, "
+                    "three products; bf16x6: three parts, six products)")
     ap.add_argument("--n", type=int, default=0, help="override the order n (profiling a smaller case)")
     ap.add_argument("--arms", choices=["both", "fp64", "mixed"], default="both",
                     help="time one arm only (profiling); that arm is then the line's headline, without extras")
     ap.add_argument("--reserve-sms", type=int, default=0, help="SMs left to the panel factorisation while the "
                     "look-ahead update runs (0: the library's default)")
+    ap.add_argument("--panel", type=int, default=0, help="outer panel width of the mixed factorisation "
+                    "(0: the library default)")
     args = ap.parse_args()
     if args.impl == "reference":
         # CPU only: under torchrun rank 0 alone runs it, the other ranks exit without work

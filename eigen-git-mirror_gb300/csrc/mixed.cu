@@ -483,9 +483,17 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
 constexpr int kDefaultReserveSms = 32;
 
 // Default outer panel width.  A wider panel makes each trailing update deeper (fewer passes of C
-// through HBM per flop) at the price of a longer panel factorisation; from n = 16384 on, 384 is the
-// faster width (n = 32768, BF16x6: 87 ms per factorisation against 93 ms at 256).
-int default_panel(int64_t n) { return n >= 16384 ? 384 : 256; }
+// through HBM per flop) at the price of a longer panel factorisation.  Solve times to 1e-14 (64 RHS,
+// kappa = 1e6):
+//   BF16x6, n = 32768: 114 ms at 384, 111 ms at 512, 121 ms at 640 and 768 (a fifth refinement step:
+//     the deeper updates' FP32 accumulation in TMEM costs the factor accuracy); n = 24576: 60.5 ms at
+//     384, 66 ms at 512 (five steps);
+//   BF16x3 (five steps at every width; its error is the two-part split's): n = 32768: 110.2 / 107.5 /
+//     106.6 / 106.1 ms at 384 / 512 / 640 / 768; n = 16384: 31.4 / 31.1 / 31.4 ms at 384 / 512 / 640.
+int default_panel(int64_t n, int precision) {
+  if (precision == GBLLT_PREC_BF16X3) return n >= 32768 ? 640 : n >= 16384 ? 512 : 256;
+  return n >= 16384 ? 384 : 256;
+}
 
 int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o, int64_t n) {
   memset(o, 0, sizeof *o);
@@ -493,14 +501,13 @@ int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o, int64_t 
   o->max_steps = 10;
   o->tol = 1e-14;
   o->fallback_fp64 = 1;
-  o->panel = default_panel(n);
   if (in) {
     *o = *in;
     if (o->max_steps <= 0) o->max_steps = 10;
     if (o->max_steps > 16) o->max_steps = 16;
     if (!(o->tol > 0)) o->tol = 1e-14;
-    if (o->panel <= 0) o->panel = default_panel(n);
   }
+  if (o->panel <= 0) o->panel = default_panel(n, o->precision);
   if (o->reserve_sms == 0) o->reserve_sms = kDefaultReserveSms;
   if (o->precision < GBLLT_PREC_FP32 || o->precision > GBLLT_PREC_BF16X6) return -1;
   if (o->residual != GBLLT_RESIDUAL_AUTO && o->residual != GBLLT_RESIDUAL_TENSOR &&

@@ -125,7 +125,7 @@ typedef struct {
   double tol;        /* target normwise backward error; <= 0 -> 1e-14 */
   int fallback_fp64; /* when refinement fails, solve with the plain FP64 GPU factorisation */
   int panel;         /* outer panel width, a multiple of 64; <= 0 -> 256 below n = 16384, 384 from
-                        there on */
+                        there on (BF16X3: 512 from 16384, 640 from 32768) */
   int reserve_sms;   /* SMs left to the panel factorisation while the look-ahead update runs on the
                         others: 0 -> library default, < 0 -> none (the update may use every SM) */
   int residual;      /* how R = B - A X is formed: GBLLT_RESIDUAL_AUTO (0, default), _FP64 or
