@@ -535,7 +535,10 @@ def measure_config(args, cfg, ws, rank, local, peaks, steps, warmup, profile_ste
             if i > 0:  # the first call warms up
                 tt.append(dt)
         e2e_s = max_over_ranks(ws, sum(tt) / len(tt))
-        bytes_io = int(n * n * 8 + n * k * 8)
+        # the library copies A's stored triangle in 256-column blocks, each from its diagonal row down
+        # (and the FP64 entry copies the factor's back)
+        tri = sum((n - j0) * min(256, n - j0) for j0 in range(0, n, 256)) * 8
+        bytes_io = tri + int(n * k * 8)
         e2e = {"value": ws * flops / e2e_s / 1e12, "unit": "TFLOP/s", "seconds_per_step": e2e_s,
                "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": int(n * k * 8) if use_mixed else bytes_io,
                "calls_timed": len(tt),
