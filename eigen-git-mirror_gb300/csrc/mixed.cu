@@ -346,6 +346,15 @@ int split_parts(int prec) {
   }
 }
 
+// SMs left to the panel factorisation while the look-ahead update of the previous panel runs.  With
+// the library default (reserve_sms = 0) the reservation follows the panels: the update of panel k
+// does about rs^2 panel flops beside the chain of panel k+1 (about rs panel^2 flops, plus a latency
+// floor), so the chain's share grows as rs shrinks: SMs / (1 + kReserveRatio rs / panel), between
+// kDefaultReserveSms (the first panels; BF16x6, 64 RHS: 32 against 24 saved 0.5-1.7 ms at n = 32768,
+// 40 and 48 were slower) and half the SMs.
+constexpr int kDefaultReserveSms = 32;
+constexpr double kReserveRatio = 0.08;
+
 // Factor the scaled FP32 working matrix af (n x n lower, ldf) with tensor-core trailing updates.
 // With a side stream (and the events and second operand set that go with it), one panel of
 // lookahead: panel k's trailing update is split into the strip of panel k+1's columns (main stream,
@@ -371,6 +380,21 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
   const bool lookahead = side != nullptr && prec != GBLLT_PREC_FP32;
   const int nseg = np == 1 ? 1 : np == 2 ? 3 : 6;
   const uint32_t code = np == 1 ? kSegX1 : np == 2 ? kSegX3 : kSegX6;
+  const bool adaptive = reserve_sms == 0;
+  int sms = 0;
+  if (adaptive) {
+    int dev = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  // SMs reserved for the chain of a panel with rs_chain rows below it
+  auto reserve_for = [&](int64_t rs_chain) -> int {
+    if (!adaptive) return reserve_sms;
+    int v = (int)(sms / (1.0 + kReserveRatio * (double)rs_chain / panel));
+    if (v > sms / 2) v = sms / 2;
+    return v < kDefaultReserveSms ? kDefaultReserveSms : v;
+  };
+  int cur_res = adaptive ? kDefaultReserveSms : reserve_sms;  // the reservation of the update in flight
   int iter = 0;
   bool side_pending = false;
   bool diag_ready = false;  // the current step's diagonal block is already factored (previous step)
@@ -417,7 +441,7 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
       TcOperand ipa{{ipparts[0], ipparts[1], ipparts[2]}, below, kNB, kNB, skip};
       TcOperand ipb{{ipparts[0], ipparts[1], ipparts[2]}, below, kNB, kNB, 0};
       // capped to the reserved SMs, one left to the diagonal block
-      int cap = (lookahead && side_pending && reserve_sms > 0) ? reserve_sms : 0;
+      int cap = (lookahead && side_pending && cur_res > 0) ? cur_res : 0;
       if (cap > 1 && aux) --cap;
       const int rc = tc_update(ipa, ipb, kind, nseg, code, af + (j0 + jb) * ldf + (j0 + jb + skip), ldf,
                                below - skip, cols_left, kTcLowerRect, d_err, us, 0, cap, (int)skip);
@@ -461,8 +485,9 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
         // the rest of the trailing matrix on the side stream
         GB_CUDA_TRY(cudaStreamWaitEvent(side, ev[iter & 1], 0));
         TcOperand op2{{pp[0], pp[1], pp[2]}, rs, bs, ldk, nb};
+        cur_res = reserve_for(rs - nb);
         rc = tc_update(op2, op2, kind, nseg, code, c0 + nb * ldf + nb, ldf, rs - nb, rs - nb, kTcLowerTri, d_err,
-                       side, reserve_sms > 0 ? reserve_sms : 0);
+                       side, cur_res > 0 ? cur_res : 0);
         if (rc) return rc;
         GB_CUDA_TRY(cudaEventRecord(ev[2 + (iter & 1)], side));
         side_pending = true;
@@ -476,11 +501,6 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
 }
-
-// SMs left to the panel factorisation while the look-ahead update of the previous panel runs
-// (BF16x6, 64 RHS: 32 against 24 saved 0.1 ms at n = 8192, 0.5 ms at 16384 and 0.5-1.7 ms at 32768;
-// 40 and 48 were slower again).
-constexpr int kDefaultReserveSms = 32;
 
 // Default outer panel width.  A wider panel makes each trailing update deeper (fewer passes of C
 // through HBM per flop) at the price of a longer panel factorisation.  Solve times to 1e-14 (64 RHS,
@@ -508,7 +528,6 @@ int resolve_mixed_opts(const gbllt_mixed_opts* in, gbllt_mixed_opts* o, int64_t 
     if (!(o->tol > 0)) o->tol = 1e-14;
   }
   if (o->panel <= 0) o->panel = default_panel(n, o->precision);
-  if (o->reserve_sms == 0) o->reserve_sms = kDefaultReserveSms;
   if (o->precision < GBLLT_PREC_FP32 || o->precision > GBLLT_PREC_BF16X6) return -1;
   if (o->residual != GBLLT_RESIDUAL_AUTO && o->residual != GBLLT_RESIDUAL_TENSOR &&
       o->residual != GBLLT_RESIDUAL_FP64)

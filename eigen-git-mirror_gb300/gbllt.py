@@ -155,7 +155,8 @@ RESIDUAL = {"auto": 0, "fp64": 1, "tensor": 2}
 def mixed_opts(precision: str = "tf32x3", max_steps: int = 10, tol: float = 1e-14, fallback: bool = True,
                panel: int = 0, reserve_sms: int = 0, residual: str = "auto") -> MixedOpts:
     """gbllt_mixed_opts; panel 0 and reserve_sms 0 take the library defaults (panel 256 below
-    n = 16384, 384 from there on, for bf16x3 512 from 16384 and 640 from 32768; 32 reserved SMs)."""
+    n = 16384, 384 from there on, for bf16x3 512 from 16384 and 640 from 32768; 32 reserved SMs for the
+    first panels, more as the trailing matrix shrinks)."""
     return MixedOpts(PREC[precision], max_steps, tol, 1 if fallback else 0, panel, reserve_sms,
                      RESIDUAL[residual])
 

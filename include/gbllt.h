@@ -127,7 +127,8 @@ typedef struct {
   int panel;         /* outer panel width, a multiple of 64; <= 0 -> 256 below n = 16384, 384 from
                         there on (BF16X3: 512 from 16384, 640 from 32768) */
   int reserve_sms;   /* SMs left to the panel factorisation while the look-ahead update runs on the
-                        others: 0 -> library default, < 0 -> none (the update may use every SM) */
+                        others: 0 -> library default (32 for the first panels, growing to half the
+                        SMs as the trailing matrix shrinks), < 0 -> none (the update may use every SM) */
   int residual;      /* how R = B - A X is formed: GBLLT_RESIDUAL_AUTO (0, default), _FP64 or
                         _TENSOR */
 } gbllt_mixed_opts;
