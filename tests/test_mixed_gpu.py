@@ -76,10 +76,24 @@ def test_mixed_sizes(oracle, gbllt, n, nrhs, residual):
     assert oracle.backward_error(a, x, b) <= 1e-14
 
 
+@pytest.mark.parametrize("n", [257, 700, 1000])
+@pytest.mark.parametrize("prec", ["bf16x3", "bf16x6"])
+def test_mixed_ragged_bf16(oracle, gbllt, n, prec):
+    # orders that leave the tensor-core panel solve a last CTA of fewer than 64 rows, with the BF16
+    # parts of the in-panel operand written from it
+    pytest.importorskip("torch")
+    a = oracle.gen_gram(n, seed=90 + n)
+    b = np.asfortranarray(oracle.normal(91, n * 3).reshape(n, 3, order="F"))
+    rc, rep, x = _dev_solve(gbllt, a, b, gbllt.mixed_opts(prec, 10, 1e-14, fallback=False))
+    assert rc == gbllt.SUCCESS and rep["converged"] and not rep["used_fallback"], rep
+    assert oracle.backward_error(a, x, b) <= 1e-14
+
+
 @pytest.mark.parametrize("panel", [64, 128, 192, 320, 384, 512])
 @pytest.mark.parametrize("prec", ["tf32x3", "bf16x3", "bf16x6"])
 def test_mixed_panel_widths(oracle, gbllt, spectra, panel, prec):
-    # outer panels of any multiple of 64 (the default is 256 below n = 16384 and 384 from there on):
+    # outer panels of any multiple of 64 (the default is 256 below n = 16384; from there on 384, and
+    # 512 / 640 for BF16x3):
     # a ragged last panel (1536 = 4 * 384 = 3 * 512), the look-ahead split and the in-panel updates
     pytest.importorskip("torch")
     a = spectra[1e4]
@@ -182,8 +196,9 @@ def test_mixed_concurrent_host_threads(oracle, gbllt):
 @pytest.mark.parametrize("prec", ["bf16x6", "bf16x3"])
 def test_mixed_full_size_default_panel(oracle, gbllt, prec):
     """n = 16384, 64 right-hand sides, Householder spectrum with kappa = 1e6: the default schedule at
-    this order (outer panel 384, look-ahead, tensor-core residual) reaches backward error 1e-14 without
-    the FP64 fallback, checked by an independent FP64 residual (cuBLAS through torch)."""
+    this order (outer panel 384, 512 for BF16x3, look-ahead with the growing SM reservation,
+    tensor-core residual) reaches backward error 1e-14 without the FP64 fallback, checked by an
+    independent FP64 residual (cuBLAS through torch)."""
     torch = pytest.importorskip("torch")
     n, k = 16384, 64
     A = torch.from_numpy(np.ascontiguousarray(oracle.gen_householder(n, 1e6))).cuda()  # symmetric
