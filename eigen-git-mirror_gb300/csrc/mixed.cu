@@ -509,7 +509,8 @@ int potrf_mixed_f32(int64_t n, float* af, int64_t ldf, int prec, int panel, int 
 //     the deeper updates' FP32 accumulation in TMEM costs the factor accuracy); n = 24576: 60.5 ms at
 //     384, 66 ms at 512 (five steps);
 //   BF16x3 (five steps at every width; its error is the two-part split's): n = 32768: 110.2 / 107.5 /
-//     106.6 / 106.1 ms at 384 / 512 / 640 / 768; n = 16384: 31.4 / 31.1 / 31.4 ms at 384 / 512 / 640.
+//     106.6 / 106.1 ms at 384 / 512 / 640 / 768; n = 24576: 62.0 / 61.1 / 60.8 ms at 384 / 512 / 640;
+//     n = 16384: 31.4 / 31.1 / 31.4 ms at 384 / 512 / 640.
 int default_panel(int64_t n, int precision) {
   if (precision == GBLLT_PREC_BF16X3) return n >= 32768 ? 640 : n >= 16384 ? 512 : 256;
   return n >= 16384 ? 384 : 256;
