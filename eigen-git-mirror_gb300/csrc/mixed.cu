@@ -30,6 +30,25 @@ namespace {
 
 constexpr int TS = 32;  // conversion tile
 
+// x rounded to the nearest float, ties to even (IEEE 754), in integer arithmetic on x's bits where
+// the result is a normal float; zeros, subnormal results, overflow beyond the rounding and
+// non-finite values take the hardware conversion.  On GB300 the FP64-to-FP32 conversion runs on the
+// narrow FP64 pipe: the working copy's conversion was bound by it (84 % busy, DRAM 22 %).
+__device__ __forceinline__ float f64_to_f32_rn(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ef = (int)((b >> 52) & 0x7FF) - 1023 + 127;  // the float's biased exponent
+  if (ef >= 1 && ef <= 254) {
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;  // 52 fraction bits
+    const unsigned int keep = (unsigned int)(m >> 29);    // the top 23
+    const unsigned int rest = (unsigned int)(m & 0x1FFFFFFFu);
+    const unsigned int up = (rest > 0x10000000u || (rest == 0x10000000u && (keep & 1u))) ? 1u : 0u;
+    // a carry out of the fraction raises the exponent (254 + 1 = infinity, as rounding requires)
+    const unsigned int bits = (((unsigned int)ef << 23) | keep) + up;
+    return __uint_as_float(bits | ((unsigned int)(b >> 32) & 0x80000000u));
+  }
+  return __double2float_rn(x);
+}
+
 // Af(i, j) = d_i * A(i, j) * d_j for i >= j, as float, A given by its upper triangle: element
 // (i, j), i >= j, lives at a[i * lda + j], so each 32 x 32 tile is transposed through shared memory.
 __global__ void __launch_bounds__(256) convert_scaled_upper_kernel(const double* __restrict__ a, long long lda,
@@ -47,7 +66,7 @@ __global__ void __launch_bounds__(256) convert_scaled_upper_kernel(const double*
   __syncthreads();
   for (int c = ty; c < TS; c += 8) {
     const long long i = i0 + tx, j = j0 + c;
-    if (i < n && j < n && i >= j) af[j * ldf + i] = (float)(d[i] * t[tx][c] * d[j]);
+    if (i < n && j < n && i >= j) af[j * ldf + i] = f64_to_f32_rn(d[i] * t[tx][c] * d[j]);
   }
 }
 
@@ -55,6 +74,16 @@ __global__ void __launch_bounds__(256) convert_scaled_upper_kernel(const double*
 // ... and its threads stream down each column from the diagonal (coalesced reads and writes, four
 // rows per thread in flight).  One CTA per 32 x 32 tile, as above, spent more time starting tiles
 // than moving bytes (about 1 TB/s at n = 32768); the product is the same, so is the result.
+
+// Self-test of f64_to_f32_rn: out[i] = f64_to_f32_rn(in[i]) and ref[i] = the hardware conversion.
+__global__ void f64_to_f32_selftest_kernel(const double* __restrict__ in, float* __restrict__ out,
+                                           float* __restrict__ ref, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    out[i] = f64_to_f32_rn(in[i]);
+    ref[i] = __double2float_rn(in[i]);
+  }
+}
 __global__ void __launch_bounds__(256) convert_scaled_lower_kernel(const double* __restrict__ a, long long lda,
                                                                    long long n, const double* __restrict__ d,
                                                                    float* __restrict__ af, long long ldf) {
@@ -71,9 +100,9 @@ __global__ void __launch_bounds__(256) convert_scaled_lower_kernel(const double*
         di[u] = d[i + u * 256];
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) out[i + u * 256] = (float)(di[u] * v[u] * dj);
+      for (int u = 0; u < 4; ++u) out[i + u * 256] = f64_to_f32_rn(di[u] * v[u] * dj);
     }
-    for (; i < n; i += 256) out[i] = (float)(d[i] * col[i] * dj);
+    for (; i < n; i += 256) out[i] = f64_to_f32_rn(d[i] * col[i] * dj);
   }
 }
 
@@ -908,6 +937,18 @@ extern "C" int gbllt_dsyresid_dev(char uplo, int64_t n, int64_t nrhs, const doub
   }
   symm_residual_fp64(upper, n, nrhs, d_a, lda, d_x, ldx, d_b, ldb, d_r, ldr, (double*)part, nparts, jpc, s);
   cudaFreeAsync(part, s);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GBLLT_SUCCESS;
+}
+
+extern "C" int gbllt_selftest_f64_to_f32(const double* d_in, float* d_out, float* d_ref, int64_t n, void* stream) {
+  using namespace gbllt;
+  if (n < 0) return -4;
+  if (n > 0 && (!d_in || !d_out || !d_ref)) return -1;
+  if (n == 0) return GBLLT_SUCCESS;
+  const int rc = ensure_device();
+  if (rc) return rc;
+  f64_to_f32_selftest_kernel<<<grid1(n), 256, 0, (cudaStream_t)stream>>>(d_in, d_out, d_ref, n);
   GB_CUDA_TRY(cudaGetLastError());
   return GBLLT_SUCCESS;
 }

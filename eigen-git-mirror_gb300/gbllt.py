@@ -100,6 +100,7 @@ SIGNATURES: dict[str, tuple] = {
     "gbllt_profile_read": (_int, [_vp, _int, ctypes.POINTER(_int)]),
     "gbllt_profile_trace": (_int, [_vp, _int, ctypes.POINTER(_int)]),
     "gbllt_selftest_wait_timeout": (_int, [_i64, ctypes.POINTER(_int)]),
+    "gbllt_selftest_f64_to_f32": (_int, [_vp, _vp, _vp, _i64, _vp]),
 }
 
 _lib = None

@@ -427,6 +427,12 @@ GBLLT_API int gbllt_profile_trace(gbllt_launch_record* out, int max_entries, int
  * solved ones untouched, and GBLLT_ERR_INTERNAL otherwise.  The device stays usable. */
 GBLLT_API int gbllt_selftest_wait_timeout(int64_t wait_us, int* observed);
 
+/* Self-test of the FP64-to-FP32 rounding that forms the mixed solve's FP32 working copy (integer
+ * arithmetic on the bits, round to nearest even; the FP32 conversion of the GPU otherwise runs on
+ * its narrow FP64 pipe): d_out[i] receives that rounding of d_in[i] and d_ref[i] the hardware
+ * conversion, n device values each, stream-ordered on `stream`.  The two agree bit for bit. */
+GBLLT_API int gbllt_selftest_f64_to_f32(const double* d_in, float* d_out, float* d_ref, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
