@@ -49,8 +49,21 @@ __device__ __forceinline__ float f64_to_f32_rn(double x) {
   return __double2float_rn(x);
 }
 
-// Af(i, j) = d_i * A(i, j) * d_j for i >= j, as float, A given by its upper triangle: element
-// (i, j), i >= j, lives at a[i * lda + j], so each 32 x 32 tile is transposed through shared memory.
+// v * 2^p rounded to float: an exponent add on v's bits where v and the product are normal doubles
+// (exact), else ldexp; then f64_to_f32_rn.  Neither step uses the FP64 pipe on the common path.
+__device__ __forceinline__ float scale_pow2_to_f32(double v, int p) {
+  const long long b = __double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e > 0 && e < 0x7FF && e + p > 0 && e + p < 0x7FF) return f64_to_f32_rn(__longlong_as_double(b + ((long long)p << 52)));
+  return f64_to_f32_rn(ldexp(v, p));
+}
+
+// The exponent p of a scale d = 2^p (a normal power of two).
+__device__ __forceinline__ int pow2_exponent(double d) { return (int)((__double_as_longlong(d) >> 52) & 0x7FF) - 1023; }
+
+// Af(i, j) = d_i * A(i, j) * d_j for i >= j, as float (d powers of two: exact scaling, one rounding),
+// A given by its upper triangle: element (i, j), i >= j, lives at a[i * lda + j], so each 32 x 32 tile
+// is transposed through shared memory.
 __global__ void __launch_bounds__(256) convert_scaled_upper_kernel(const double* __restrict__ a, long long lda,
                                                                    long long n, const double* __restrict__ d,
                                                                    float* __restrict__ af, long long ldf) {
@@ -66,7 +79,7 @@ __global__ void __launch_bounds__(256) convert_scaled_upper_kernel(const double*
   __syncthreads();
   for (int c = ty; c < TS; c += 8) {
     const long long i = i0 + tx, j = j0 + c;
-    if (i < n && j < n && i >= j) af[j * ldf + i] = f64_to_f32_rn(d[i] * t[tx][c] * d[j]);
+    if (i < n && j < n && i >= j) af[j * ldf + i] = scale_pow2_to_f32(t[tx][c], pow2_exponent(d[i]) + pow2_exponent(d[j]));
   }
 }
 
@@ -88,7 +101,7 @@ __global__ void __launch_bounds__(256) convert_scaled_lower_kernel(const double*
                                                                    long long n, const double* __restrict__ d,
                                                                    float* __restrict__ af, long long ldf) {
   for (long long j = blockIdx.x; j < n; j += gridDim.x) {
-    const double dj = d[j];
+    const int pj = pow2_exponent(d[j]);
     const double* col = a + j * lda;
     float* out = af + j * ldf;
     long long i = j + threadIdx.x;
@@ -100,9 +113,9 @@ __global__ void __launch_bounds__(256) convert_scaled_lower_kernel(const double*
         di[u] = d[i + u * 256];
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) out[i + u * 256] = f64_to_f32_rn(di[u] * v[u] * dj);
+      for (int u = 0; u < 4; ++u) out[i + u * 256] = scale_pow2_to_f32(v[u], pow2_exponent(di[u]) + pj);
     }
-    for (; i < n; i += 256) out[i] = f64_to_f32_rn(d[i] * col[i] * dj);
+    for (; i < n; i += 256) out[i] = scale_pow2_to_f32(col[i], pow2_exponent(d[i]) + pj);
   }
 }
 
@@ -110,8 +123,13 @@ template <bool UP>
 __global__ void diag_scale_kernel(const double* __restrict__ a, long long lda, long long n, double* __restrict__ d) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
+    // d_i = 2^-floor(e / 2) for a_ii = f 2^e, f in [0.5, 1): d_i^2 a_ii in [0.5, 2) (the power-of-two
+    // equilibration of LAPACK's xPOEQUB; the refinement converged in the same steps as with
+    // 1 / sqrt(a_ii), and the scaling of A, R and X is exact)
     const double v = a[i * lda + i];
-    d[i] = v > 0.0 ? 1.0 / sqrt(v) : 1.0;
+    int e = 0;
+    if (v > 0.0) frexp(v, &e);
+    d[i] = v > 0.0 ? ldexp(1.0, -(e >> 1)) : 1.0;
   }
 }
 
