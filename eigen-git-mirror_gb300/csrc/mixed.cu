@@ -3,12 +3,14 @@
 // Eigen's LLT<MatrixXd> (Eigen/src/Cholesky/LLT.h:430-498) factors and solves entirely in FP64.
 // On GB300 the FP64 pipe delivers ~1 TFLOP/s while the tensor cores deliver ~1 PFLOP/s (TF32) and
 // ~2 PFLOP/s (BF16), so this path:
-//   1. scales A symmetrically to unit diagonal (D A D, D = diag(a_ii)^-1/2, Higham & Pranesh 2021)
-//      and rounds the scaled lower triangle to an FP32 working matrix;
+//   1. scales A symmetrically by powers of two (D A D, D = 2^-floor(e_i / 2) for a_ii = f 2^e_i, so the
+//      diagonal lies in [0.5, 2): exact scaling, as LAPACK's xPOEQUB) and rounds the scaled lower
+//      triangle to an FP32 working matrix;
 //   2. factors it with the blocked right-looking algorithm of llt_inplace::blocked (LLT.h:338-368)
-//      in two levels: panels of width `panel` are factored in 64-column steps (diagonal blocks by
-//      one warp in FP32 registers, the panel TRSM on FP32 cores, its result split into tensor-core
-//      operands for the in-panel update on tcgen05), and the trailing SYRK of each panel
+//      in two levels: panels of width `panel` are factored in 64-column steps (the diagonal block and
+//      its inverse in FP32 by one CTA, the panel solve as the product with that inverse on the tensor
+//      cores, its result split into tensor-core operands for the in-panel update on tcgen05), and the
+//      trailing SYRK of each panel
 //      -- almost all of the n^3/3 flops -- runs on tcgen05 tensor cores in TF32 or BF16 (optionally
 //      as split-precision products) with FP32 accumulation, one panel ahead on a second stream;
 //   3. refines in FP64: r = b - A x (reading only the stored triangle of A; on the FP64 pipe, or for

@@ -106,10 +106,11 @@ GBLLT_API int gbllt_spotrs_dev(char uplo, int64_t n, int64_t nrhs, const float* 
 
 /* ---- Mixed precision with FP64 iterative refinement ---------------------------------------
  * Solves A X = B to FP64 accuracy (normwise backward error <= tol) from a low-precision
- * factorisation: A is scaled to unit diagonal and rounded to FP32, the trailing updates of the
- * blocked factorisation run on tensor cores in the chosen precision with FP32 accumulation, the
- * 64 x 64 diagonal blocks are factored in FP64, and residuals r = B - A X are formed in FP64 from
- * the stored triangle of A.  Replaces LLT<MatrixXd>::compute followed by solve
+ * factorisation: A is scaled by powers of two to a diagonal in [0.5, 2) and rounded to FP32, the
+ * trailing updates of the blocked factorisation run on tensor cores in the chosen precision with
+ * FP32 accumulation, the 64 x 64 diagonal blocks are factored in FP32, and residuals r = B - A X are
+ * formed from the stored triangle of A in FP64 or FP64-exact on the tensor cores (the residual
+ * method).  Replaces LLT<MatrixXd>::compute followed by solve
  * (Eigen/src/Cholesky/LLT.h:430-460, :483-498) for callers that need the solution, not the factor;
  * it is the counterpart of LAPACK's dsposv.  A and B are not modified. */
 #define GBLLT_PREC_FP32 0   /* trailing update on FP32 CUDA cores (no tensor cores) */
